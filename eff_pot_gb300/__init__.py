@@ -1,0 +1,16 @@
+"""eff_pot_gb300: GB300-native Orsay-Trento helium order-parameter evolution.
+
+The package is the host side of libeffpot.so (CUDA, sm_103a): the C ABI in
+include/eff_pot.h does all the work on the GPU; this package binds it with
+ctypes and mirrors the reference's subroutine interface (Solver).
+"""
+from . import _abi
+from .config import make_config, config_dict, morse, null_potential, DEFAULTS, KTOPS, MP_U
+from .solver import Solver, EffPotError, load_library, library_config_defaults, LIBPATH
+from .initial import woods_saxon_psi, grid_axes
+
+__all__ = [
+    "Solver", "EffPotError", "load_library", "library_config_defaults", "make_config",
+    "config_dict", "morse", "null_potential", "woods_saxon_psi", "grid_axes", "DEFAULTS",
+    "KTOPS", "MP_U", "LIBPATH",
+]

@@ -1,0 +1,63 @@
+"""Solver configuration: the reference's module defaults and namelist keys.
+
+Defaults follow modules.f90 (deriva :15,19; grid :75-84; he4 :124-133;
+lenard4 :191-196), V_impur.f90:1-16 and DFT4He3d.f90:78 (n4=300).
+"""
+from . import _abi
+
+DEFAULTS = dict(
+    nx=64, ny=64, nz=64, xmax=64.0, ymax=64.0, zmax=64.0,
+    npd=13, icon=_abi.EP_ICON_ZERO_OUTSIDE, core=_abi.EP_CORE_OT,
+    cp4=-2.41186e4, cpp4=1.85850e6, den4c=0.062, alphas=54.31, l=1.0,
+    den0s=0.04, h2o2m4=6.05969638298, C=3.1577504e4, beta=40.0, den_m=0.37,
+    h4ot=2.190323, h4op=2.359665, eps4=10.22, sigma4=2.556, b4=-718.99,
+    time_mode=_abi.EP_IMAGINARY_TIME, renormalize=1, n4=300.0,
+    impurity=_abi.EP_IMPURITY_NONE, mimpur=0.0, fix_lambda=0, als_p=0.0,
+    ev0=0.0, z_exciplex_exclusion=0.0, precision=_abi.EP_FP64, device=0,
+)
+
+CORES = {"OT": _abi.EP_CORE_OT, "OT ": _abi.EP_CORE_OT, "OTC": _abi.EP_CORE_OTC,
+         "OP": _abi.EP_CORE_OP, "OP ": _abi.EP_CORE_OP}
+
+# Ktops: picoseconds per kelvin^-1 (DFT4He3d.f90:55).
+KTOPS = 7.63822291
+# proton mass in A^-2 K^-1 (modules.f90:333).
+MP_U = 0.0207569277
+
+
+def make_config(**kw):
+    """An EpConfig with the reference defaults overridden by kw.
+
+    ``core`` may be given as the namelist string ('OT ', 'OTC', 'OP ').
+    """
+    vals = dict(DEFAULTS)
+    for k, v in kw.items():
+        if k not in vals:
+            raise KeyError(f"unknown configuration key {k!r}")
+        if k == "core" and isinstance(v, str):
+            v = CORES[v.upper() if len(v) == 3 else v.upper()]
+        vals[k] = v
+    cfg = _abi.EpConfig()
+    for k, v in vals.items():
+        setattr(cfg, k, v)
+    return cfg
+
+
+def config_dict(cfg):
+    return {name: getattr(cfg, name) for name, _ in cfg._fields_}
+
+
+def morse(De=10.0, re=4.5, alpha=1.2, r_cutoff=0.0, umax=1000.0):
+    """The He-X Morse pair potential V = De*(exp(-2a(r-re)) - 2exp(-a(r-re)))."""
+    p = _abi.EpPotential()
+    p.kind = _abi.EP_POT_MORSE
+    p.r_cutoff = r_cutoff
+    p.umax = umax
+    p.par[0], p.par[1], p.par[2], p.par[3] = De, re, alpha, 0.0
+    return p
+
+
+def null_potential():
+    p = _abi.EpPotential()
+    p.kind = _abi.EP_POT_NULL
+    return p

@@ -1,0 +1,385 @@
+// ep_api.cu - the C ABI of include/eff_pot.h.
+//
+// One ep_ctx is one solver instance on one GPU: its own stream, its own
+// device buffers (Engine<double> for the FP64 drop-in path, Engine<float>
+// for the FP32 path) and the small host-side impurity state.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "../../include/eff_pot.h"
+#include "ep_engine.h"
+
+struct ep_ctx {
+  ep_config cfg{};
+  cudaStream_t st = nullptr;
+  Prof prof;
+  ImpState imp;
+  std::string err;
+  Engine<double>* e64 = nullptr;
+  Engine<float>* e32 = nullptr;
+  cudaEvent_t ev[16] = {};
+};
+
+namespace {
+
+thread_local std::string g_create_error;
+
+bool factor235(int n) {
+  if (n < 2) return false;
+  while (n % 2 == 0) n /= 2;
+  while (n % 3 == 0) n /= 3;
+  while (n % 5 == 0) n /= 5;
+  return n == 1;
+}
+
+int fail(ep_ctx* c, int code, const std::string& msg) {
+  if (c) c->err = msg;
+  return code;
+}
+
+// Select_Pot subset (V_impur.f90:87-932) plus the Morse selector.
+double select_pot(const ep_potential& p, double r) {
+  if (p.kind == EP_POT_NULL) return 0.0;
+  if (r < p.r_cutoff) return p.umax;
+  if (p.kind == EP_POT_MORSE) {
+    const double e = std::exp(-p.par[2] * (r - p.par[1]));
+    return p.par[0] * (e * e - 2.0 * e);
+  }
+  return 0.0;
+}
+
+template <class F>
+int dispatch(ep_ctx* c, F f) {
+  if (!c) return EP_ERR_INVALID_ARG;
+  if (c->e64) return f(*c->e64);
+  if (c->e32) return f(*c->e32);
+  return fail(c, EP_ERR_STATE, "context has no engine");
+}
+
+}  // namespace
+
+extern "C" {
+
+int ep_config_init(ep_config* c) {
+  if (!c) return EP_ERR_INVALID_ARG;
+  std::memset(c, 0, sizeof(*c));
+  c->nx = c->ny = c->nz = 64;
+  c->xmax = c->ymax = c->zmax = 64.0;
+  c->npd = 13;
+  c->icon = EP_ICON_ZERO_OUTSIDE;
+  c->core = EP_CORE_OT;
+  c->cp4 = -2.41186e4;
+  c->cpp4 = 1.85850e6;
+  c->den4c = 0.062;
+  c->alphas = 54.31;
+  c->l = 1.0;
+  c->den0s = 0.04;
+  c->h2o2m4 = 6.05969638298;
+  c->C = 3.1577504e4;
+  c->beta = 40.0;
+  c->den_m = 0.37;
+  c->h4ot = 2.190323;
+  c->h4op = 2.359665;
+  c->eps4 = 10.22;
+  c->sigma4 = 2.556;
+  c->b4 = -718.99;
+  c->time_mode = EP_IMAGINARY_TIME;
+  c->renormalize = 1;
+  c->n4 = 300.0;
+  c->impurity = EP_IMPURITY_NONE;
+  c->mimpur = 0.0;
+  c->fix_lambda = 0;
+  c->als_p = 0.0;
+  c->ev0 = 0.0;
+  c->z_exciplex_exclusion = 0.0;
+  c->precision = EP_FP64;
+  c->device = 0;
+  return EP_OK;
+}
+
+const char* ep_create_error(void) { return g_create_error.c_str(); }
+
+int ep_create(const ep_config* cfg, ep_ctx** out) {
+  g_create_error.clear();
+  if (!cfg || !out) { g_create_error = "null argument"; return EP_ERR_INVALID_ARG; }
+  *out = nullptr;
+  const ep_config& c = *cfg;
+  if (c.nx % 2 || c.ny % 2 || c.nz % 2 || !factor235(c.nx) || !factor235(c.ny) || !factor235(c.nz)) {
+    g_create_error = "grid sizes must be even with prime factors 2, 3, 5 only";
+    return EP_ERR_BAD_GRID;
+  }
+  if (c.npd < 3 || c.npd > 25 || c.npd % 2 == 0) { g_create_error = "npd must be odd, 3..25"; return EP_ERR_INVALID_ARG; }
+  if (c.npd > 13) { g_create_error = "stencils wider than 13 points are not built"; return EP_ERR_UNSUPPORTED; }
+  if (c.nx < c.npd || c.ny < c.npd || c.nz < c.npd) { g_create_error = "grid smaller than the stencil"; return EP_ERR_BAD_GRID; }
+  if (c.icon != EP_ICON_PERIODIC && c.icon != EP_ICON_ZERO_OUTSIDE) {
+    g_create_error = "icon must be 8 (periodic) or 13 (zero outside)";
+    return EP_ERR_UNSUPPORTED;
+  }
+  if (c.core != EP_CORE_OT && c.core != EP_CORE_OTC && c.core != EP_CORE_OP) { g_create_error = "unknown core"; return EP_ERR_INVALID_ARG; }
+  if (c.impurity == EP_IMPURITY_MOVING && !(c.mimpur > 0.0)) {
+    g_create_error = "a moving impurity needs mimpur > 0";
+    return EP_ERR_INVALID_ARG;
+  }
+  if (c.precision != EP_FP64 && c.precision != EP_FP32) { g_create_error = "unknown precision"; return EP_ERR_INVALID_ARG; }
+  int ndev = 0;
+  if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) {
+    cudaGetLastError();
+    g_create_error = "no CUDA device visible";
+    return EP_ERR_NO_DEVICE;
+  }
+  if (c.device < 0 || c.device >= ndev) { g_create_error = "device ordinal out of range"; return EP_ERR_INVALID_ARG; }
+  if (cudaSetDevice(c.device) != cudaSuccess) { g_create_error = "cudaSetDevice failed"; return EP_ERR_CUDA; }
+  ep_ctx* x = new ep_ctx();
+  x->cfg = c;
+  if (cudaStreamCreateWithFlags(&x->st, cudaStreamNonBlocking) != cudaSuccess) {
+    g_create_error = "stream creation failed";
+    delete x;
+    return EP_ERR_CUDA;
+  }
+  int r;
+  if (c.precision == EP_FP64) {
+    x->e64 = new Engine<double>();
+    r = x->e64->init(c, x->st, &x->prof, &x->imp, &x->err);
+  } else {
+    x->e32 = new Engine<float>();
+    r = x->e32->init(c, x->st, &x->prof, &x->imp, &x->err);
+  }
+  if (r) {
+    g_create_error = x->err;
+    ep_destroy(x);
+    return r;
+  }
+  *out = x;
+  return EP_OK;
+}
+
+int ep_destroy(ep_ctx* c) {
+  if (!c) return EP_ERR_INVALID_ARG;
+  cudaSetDevice(c->cfg.device);
+  if (c->st) cudaStreamSynchronize(c->st);
+  if (c->e64) { c->e64->release(); delete c->e64; }
+  if (c->e32) { c->e32->release(); delete c->e32; }
+  if (c->imp.d_potpi) cudaFree(c->imp.d_potpi);
+  if (c->imp.d_potdel) cudaFree(c->imp.d_potdel);
+  c->prof.release();
+  for (cudaEvent_t e : c->ev)
+    if (e) cudaEventDestroy(e);
+  if (c->st) cudaStreamDestroy(c->st);
+  delete c;
+  return EP_OK;
+}
+
+const char* ep_last_error(const ep_ctx* c) { return c ? c->err.c_str() : "null context"; }
+
+// potenimpini (potenimpini.f90:11-58), P state.
+int ep_set_impurity_potentials(ep_ctx* c, const ep_potential* pi, const ep_potential* sigma, const ep_potential* plus) {
+  if (!c || !pi || !sigma) return EP_ERR_INVALID_ARG;
+  const ep_config& g = c->cfg;
+  const int npot = 100 * std::max(g.nx, std::max(g.ny, g.nz)) + 1;
+  const double rmax = 4.0 * std::max(g.xmax, std::max(g.ymax, g.zmax));
+  const double del = rmax / (double)(npot - 1);
+  std::vector<double> tp(npot + 2), td(npot + 2);
+  for (int i = 1; i <= npot; ++i) {
+    const double r = (double)(i - 1) * del;
+    const double a = select_pot(*pi, r);
+    tp[i] = a;
+    td[i] = select_pot(*sigma, r) - a;
+  }
+  tp[0] = tp[1]; tp[npot + 1] = tp[npot];
+  td[0] = td[1]; td[npot + 1] = td[npot];
+  if (plus) c->imp.plus = *plus;
+  return ep_set_impurity_tables(c, tp.data(), td.data(), npot, del, sigma->umax);
+}
+
+int ep_set_impurity_tables(ep_ctx* c, const double* potpi, const double* potdel, int npot, double delinter,
+                           double umax_sigma) {
+  if (!c || !potpi || !potdel || npot < 3 || !(delinter > 0)) return EP_ERR_INVALID_ARG;
+  cudaSetDevice(c->cfg.device);
+  if (c->imp.d_potpi) cudaFree(c->imp.d_potpi);
+  if (c->imp.d_potdel) cudaFree(c->imp.d_potdel);
+  c->imp.d_potpi = c->imp.d_potdel = nullptr;
+  const size_t n = (size_t)(npot + 2) * sizeof(double);
+  if (cudaMalloc((void**)&c->imp.d_potpi, n) != cudaSuccess || cudaMalloc((void**)&c->imp.d_potdel, n) != cudaSuccess) {
+    cudaGetLastError();
+    return fail(c, EP_ERR_OOM, "table allocation failed");
+  }
+  cudaMemcpyAsync(c->imp.d_potpi, potpi, n, cudaMemcpyHostToDevice, c->st);
+  cudaMemcpyAsync(c->imp.d_potdel, potdel, n, cudaMemcpyHostToDevice, c->st);
+  if (cudaStreamSynchronize(c->st) != cudaSuccess) return fail(c, EP_ERR_CUDA, "table upload failed");
+  c->imp.npot = npot;
+  c->imp.delinter = delinter;
+  c->imp.umax_sigma = umax_sigma;
+  c->imp.have_tables = true;
+  return EP_OK;
+}
+
+int ep_set_impurity_state(ep_ctx* c, const double* rimp, const double* vimp, const double* invar) {
+  if (!c) return EP_ERR_INVALID_ARG;
+  for (int i = 0; i < 3; ++i) {
+    if (rimp) c->imp.rimp[i] = rimp[i];
+    if (vimp) c->imp.vimp[i] = vimp[i];
+  }
+  if (invar)
+    for (int i = 0; i < 10; ++i) c->imp.invar[i] = std::complex<double>(invar[2 * i], invar[2 * i + 1]);
+  return EP_OK;
+}
+
+int ep_get_impurity_state(ep_ctx* c, double* rimp, double* vimp, double* aimp, double* invar) {
+  if (!c) return EP_ERR_INVALID_ARG;
+  for (int i = 0; i < 3; ++i) {
+    if (rimp) rimp[i] = c->imp.rimp[i];
+    if (vimp) vimp[i] = c->imp.vimp[i];
+    if (aimp) aimp[i] = c->imp.aimp[i];
+  }
+  if (invar)
+    for (int i = 0; i < 10; ++i) { invar[2 * i] = c->imp.invar[i].real(); invar[2 * i + 1] = c->imp.invar[i].imag(); }
+  return EP_OK;
+}
+
+int ep_upload_psi(ep_ctx* c, const double* psi) {
+  if (!c || !psi) return EP_ERR_INVALID_ARG;
+  return dispatch(c, [&](auto& e) -> int { return e.upload_psi(psi); });
+}
+int ep_download_psi(ep_ctx* c, double* psi) {
+  if (!c || !psi) return EP_ERR_INVALID_ARG;
+  return dispatch(c, [&](auto& e) -> int { return e.download_c(EP_CFIELD_PSI, psi); });
+}
+int ep_download_cfield(ep_ctx* c, int which, double* out) {
+  if (!c || !out) return EP_ERR_INVALID_ARG;
+  return dispatch(c, [&](auto& e) -> int { return e.download_c(which, out); });
+}
+int ep_download_field(ep_ctx* c, int which, double* out) {
+  if (!c || !out) return EP_ERR_INVALID_ARG;
+  return dispatch(c, [&](auto& e) -> int { return e.download_r(which, out); });
+}
+
+int ep_potenimp(ep_ctx* c) {
+  return dispatch(c, [&](auto& e) -> int {
+    int r = e.potenimp();
+    return r ? r : e.check_flags();
+  });
+}
+int ep_poten(ep_ctx* c) {
+  return dispatch(c, [&](auto& e) -> int {
+    int r = e.poten();
+    return r ? r : e.check_flags();
+  });
+}
+int ep_energy(ep_ctx* c, ep_energies* out) {
+  if (!out) return EP_ERR_INVALID_ARG;
+  return dispatch(c, [&](auto& e) -> int { return e.energy(out); });
+}
+int ep_forceimp(ep_ctx* c, double* F) {
+  if (!F) return EP_ERR_INVALID_ARG;
+  return dispatch(c, [&](auto& e) -> int { return e.forceimp(F); });
+}
+int ep_potinvar(ep_ctx* c, double* hinvar) {
+  if (!hinvar) return EP_ERR_INVALID_ARG;
+  return dispatch(c, [&](auto& e) -> int {
+    double F[3];
+    int r = e.forceimp(F);
+    if (r) return r;
+    std::complex<double> H[10];
+    r = e.potinvar(H);
+    for (int i = 0; i < 10; ++i) { hinvar[2 * i] = H[i].real(); hinvar[2 * i + 1] = H[i].imag(); }
+    return r;
+  });
+}
+int ep_steprk(ep_ctx* c, double dt) {
+  return dispatch(c, [&](auto& e) -> int { return e.steprk(dt); });
+}
+int ep_steppc(ep_ctx* c, double dt, ep_step_errors* err) {
+  return dispatch(c, [&](auto& e) -> int { return e.steppc(dt, err); });
+}
+
+int ep_run(ep_ctx* c, int nsteps, double dt, ep_run_stats* stats) {
+  if (!c || nsteps < 0) return EP_ERR_INVALID_ARG;
+  const bool renorm = c->cfg.time_mode == EP_IMAGINARY_TIME && c->cfg.renormalize;
+  return dispatch(c, [&](auto& e) -> int {
+    ep_step_errors se{};
+    for (int s = 0; s < nsteps; ++s) {
+      const bool last = (s == nsteps - 1) && stats;
+      int r = e.steppc(dt, last ? &se : nullptr);
+      if (r) return r;
+      if (renorm && (r = e.rescale_pending())) return r;
+    }
+    if (stats) {
+      stats->errHe = se.errHe;
+      stats->mu = e.last_mu;
+      stats->norm = e.last_norm;
+      stats->steps_done = nsteps;
+      return e.check_flags();
+    }
+    return EP_OK;
+  });
+}
+
+int ep_renormalize(ep_ctx* c, double* norm_before) {
+  return dispatch(c, [&](auto& e) -> int { return e.renormalize(norm_before, true); });
+}
+
+int ep_synchronize(ep_ctx* c) {
+  if (!c) return EP_ERR_INVALID_ARG;
+  if (cudaStreamSynchronize(c->st) != cudaSuccess) return fail(c, EP_ERR_CUDA, cudaGetErrorString(cudaGetLastError()));
+  return EP_OK;
+}
+
+void* ep_stream(ep_ctx* c) { return c ? (void*)c->st : nullptr; }
+
+int ep_event_record(ep_ctx* c, int slot) {
+  if (!c || slot < 0 || slot >= 16) return EP_ERR_INVALID_ARG;
+  if (!c->ev[slot] && cudaEventCreate(&c->ev[slot]) != cudaSuccess) return fail(c, EP_ERR_CUDA, "event create");
+  if (cudaEventRecord(c->ev[slot], c->st) != cudaSuccess) return fail(c, EP_ERR_CUDA, "event record");
+  return EP_OK;
+}
+
+int ep_event_elapsed(ep_ctx* c, int a, int b, double* ms) {
+  if (!c || !ms || a < 0 || a >= 16 || b < 0 || b >= 16 || !c->ev[a] || !c->ev[b]) return EP_ERR_INVALID_ARG;
+  if (cudaEventSynchronize(c->ev[b]) != cudaSuccess) return fail(c, EP_ERR_CUDA, "event sync");
+  float t = 0.f;
+  if (cudaEventElapsedTime(&t, c->ev[a], c->ev[b]) != cudaSuccess) return fail(c, EP_ERR_CUDA, "event elapsed");
+  *ms = t;
+  return EP_OK;
+}
+
+long long ep_kernel_launches(const ep_ctx* c) { return c ? c->prof.launches : 0; }
+
+int ep_profile_enable(ep_ctx* c, int on) {
+  if (!c) return EP_ERR_INVALID_ARG;
+  c->prof.collect();
+  c->prof.on = on != 0;
+  return EP_OK;
+}
+
+int ep_profile_read(ep_ctx* c, char* names, int cap, double* ms, long long* launches, int maxn, int* n) {
+  if (!c || !n) return EP_ERR_INVALID_ARG;
+  c->prof.collect();
+  const int k = (int)c->prof.names.size();
+  *n = k;
+  int off = 0;
+  for (int i = 0; i < k && i < maxn; ++i) {
+    if (ms) ms[i] = c->prof.ms[i];
+    if (launches) launches[i] = c->prof.cnt[i];
+    if (names) {
+      const std::string& s = c->prof.names[i];
+      if (off + (int)s.size() + 1 <= cap) {
+        std::memcpy(names + off, s.c_str(), s.size() + 1);
+        off += (int)s.size() + 1;
+      }
+    }
+  }
+  for (int i = 0; i < k; ++i) { c->prof.ms[i] = 0.0; c->prof.cnt[i] = 0; }
+  return EP_OK;
+}
+
+long long ep_device_bytes(const ep_ctx* c) {
+  if (!c) return 0;
+  return (c->e64 ? c->e64->bytes : 0) + (c->e32 ? c->e32->bytes : 0);
+}
+
+}  // extern "C"

@@ -1,0 +1,63 @@
+// ep_common.cuh - shared types and helpers of the eff_pot CUDA library.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#define EP_DEV __device__ __forceinline__
+#define EP_HD __host__ __device__ __forceinline__
+
+// ---------------------------------------------------------------------------
+// Complex numbers as CUDA vector types (x = re, y = im).
+template <class T> struct cpx_traits;
+template <> struct cpx_traits<double> { typedef double2 type; };
+template <> struct cpx_traits<float> { typedef float2 type; };
+template <class T> using C2 = typename cpx_traits<T>::type;
+
+EP_HD double2 operator+(double2 a, double2 b) { return make_double2(a.x + b.x, a.y + b.y); }
+EP_HD double2 operator-(double2 a, double2 b) { return make_double2(a.x - b.x, a.y - b.y); }
+EP_HD double2 operator*(double s, double2 a) { return make_double2(s * a.x, s * a.y); }
+EP_HD float2 operator+(float2 a, float2 b) { return make_float2(a.x + b.x, a.y + b.y); }
+EP_HD float2 operator-(float2 a, float2 b) { return make_float2(a.x - b.x, a.y - b.y); }
+EP_HD float2 operator*(float s, float2 a) { return make_float2(s * a.x, s * a.y); }
+
+template <class T> EP_HD C2<T> cmk(T a, T b) { C2<T> r; r.x = a; r.y = b; return r; }
+template <class T2> EP_HD T2 cmul(T2 a, T2 b) {
+  T2 r; r.x = a.x * b.x - a.y * b.y; r.y = a.x * b.y + a.y * b.x; return r;
+}
+// a * conj(b)
+template <class T2> EP_HD T2 cmulc(T2 a, T2 b) {
+  T2 r; r.x = a.x * b.x + a.y * b.y; r.y = a.y * b.x - a.x * b.y; return r;
+}
+template <class T2> EP_HD T2 conjg(T2 a) { T2 r; r.x = a.x; r.y = -a.y; return r; }
+// i*a
+template <class T2> EP_HD T2 mul_i(T2 a) { T2 r; r.x = -a.y; r.y = a.x; return r; }
+// -i*a
+template <class T2> EP_HD T2 mul_mi(T2 a) { T2 r; r.x = a.y; r.y = -a.x; return r; }
+
+// ---------------------------------------------------------------------------
+// Device-side scalar block shared by all kernels of a context.  Reductions
+// are accumulated in FP64 whatever the field precision.
+struct DevScalars {
+  double sums[32];      // finalize outputs (named by the producing kernel)
+  double scale;         // pending imaginary-time renormalisation factor
+  double errHe, norm, mu;
+  unsigned int flags;   // bit 0: non-finite detected; bit 1: den <= 0
+};
+enum { EP_FLAG_NONFINITE = 1u, EP_FLAG_DEN_NONPOS = 2u };
+
+// ---------------------------------------------------------------------------
+// 1-D FFT plan: length and radix sequence (radices 8,4,2,3,5).
+struct FftPlan {
+  int n;
+  int nst;
+  int rad[12];
+};
+
+// Geometry of a grid (passed by value to kernels).
+struct Geo {
+  int nx, ny, nz, nxh;
+  long long N, Nh;
+};
+
+#define EP_MAX_NPD 25
+#define EP_MAX_R 12

@@ -1,0 +1,128 @@
+// ep_engine.h - host-side engine of one solver instance in one precision.
+#pragma once
+#include <cuda_runtime.h>
+
+#include <complex>
+#include <string>
+#include <vector>
+
+#include "../../include/eff_pot.h"
+#include "ep_common.cuh"
+#include "ep_kernels.cuh"
+
+// Launch accounting and optional per-class event timing.
+struct Prof {
+  long long launches = 0;
+  bool on = false;
+  std::vector<std::string> names;
+  std::vector<double> ms;
+  std::vector<long long> cnt;
+  struct Rec { int cls; cudaEvent_t a, b; };
+  std::vector<Rec> pending;
+  std::vector<cudaEvent_t> pool;
+  int cls(const char* name);
+  cudaEvent_t ev();
+  void begin(cudaStream_t st, const char* name, cudaEvent_t& a, int& c);
+  void end(cudaStream_t st, int c, cudaEvent_t a);
+  void collect();
+  void release();
+};
+
+// Small-vector state of the classical impurity and the internal variables
+// (module classicimp; the steppc/steprk history arrays).
+struct ImpState {
+  double rimp[3] = {0, 0, 0}, vimp[3] = {0, 0, 0}, aimp[3] = {0, 0, 0};
+  std::complex<double> invar[10], hinvar[10];
+  double qr[3] = {0, 0, 0}, qv[3] = {0, 0, 0};
+  double rimpold[3][3] = {}, vimpold[3][3] = {}, aimpold[3][2] = {};
+  int ioldr[3] = {0, 1, 2}, ioldv[3] = {0, 1, 2}, iolda[2] = {0, 1}, ioldiv[3] = {0, 1, 2}, ioldhiv[2] = {0, 1};
+  double pcr[3] = {0, 0, 0}, pcv[3] = {0, 0, 0};
+  std::complex<double> qiv[10], invarold[10][3], hinvarold[10][2], pciv[10];
+  // interpolation tables (module interpol), FP64 on the device
+  int npot = 0;
+  double delinter = 0, umax_sigma = 9.674836e3;
+  double* d_potpi = nullptr;
+  double* d_potdel = nullptr;
+  ep_potential plus{};
+  bool have_tables = false;
+};
+
+template <class T>
+class Engine {
+ public:
+  typedef C2<T> CT;
+  ep_config cfg{};
+  Geo g{};
+  double hx = 0, hy = 0, hz = 0, dxyz = 0;
+  cudaStream_t st = nullptr;
+  Prof* prof = nullptr;
+  ImpState* imp = nullptr;
+  std::string* err = nullptr;
+  int dev_sm = 0;
+  long long bytes = 0;
+  Phys phys{};
+  FdW<T> fd{};
+
+  // state (module rho / rkpc / field)
+  CT* psi = nullptr;
+  CT* spare = nullptr;
+  CT* po[3] = {nullptr, nullptr, nullptr};
+  CT* ph[2] = {nullptr, nullptr};
+  CT* pc = nullptr;
+  CT* q = nullptr;
+  int ioldp[3] = {0, 1, 2}, ioldh[2] = {0, 1};
+  bool have_field = false;
+  // real fields
+  T *den = nullptr, *pot4 = nullptr, *uimp = nullptr, *dencg = nullptr, *delj4 = nullptr;
+  T *dxd = nullptr, *dyd = nullptr, *dzd = nullptr, *falfs = nullptr, *intx = nullptr, *inty = nullptr,
+    *intz = nullptr, *ualphas = nullptr, *gy = nullptr, *gz = nullptr, *dgx = nullptr, *vpi = nullptr,
+    *delta = nullptr;
+  // spectra and kernels
+  CT* S[4] = {nullptr, nullptr, nullptr, nullptr};
+  CT* Tb[4] = {nullptr, nullptr, nullptr, nullptr};
+  T *fvlj4 = nullptr, *wcgk = nullptr, *kalfs = nullptr;
+  CT *twx = nullptr, *twy = nullptr, *twz = nullptr;
+  FftPlan p2{}, pY{}, pZ{};
+  // reductions
+  double* partials = nullptr;
+  long long npartials = 0;
+  DevScalars* sc = nullptr;
+  double last_mu = 0, last_norm = 0;
+
+  int init(const ep_config& c, cudaStream_t s, Prof* p, ImpState* im, std::string* e);
+  void release();
+
+  // sub-steps
+  int poten();
+  int potenimp();
+  int energy(ep_energies* out);
+  int forceimp(double* F);
+  int potinvar(std::complex<double>* H);
+  int steprk(double dt);
+  int steppc(double dt, ep_step_errors* err);
+  int renormalize(double* norm_before, bool wait);
+  int upload_psi(const double* h);
+  int download_c(int which, double* h);
+  int download_r(int which, double* h);
+  int check_flags();
+  int rescale_pending();
+
+  // precision conversion (the other engine's state -> this one)
+  template <class U> int import_state(const Engine<U>& o);
+
+ private:
+  int alloc(void** p, size_t n);
+  int cuda_ok(cudaError_t e, const char* what);
+  int refresh();
+  int lap_predict(double dt);
+  int lap_correct(double dt, bool want);
+  int rk_stage(int jr, double dt);
+  int reduce_finalize(int nblocks, int nq, int out0, int mode);
+  int read_sums(double* h, int n, int off);
+  int fft_y(CT** arrs, int n, int dir);
+  int zconv(const CT* const* in, CT* const (*out)[3], const T* const (*ker)[3], const int* nout, int nin);
+  int x_lines(int nreal) const;
+  size_t x_smem(int nl, int nreal) const;
+  int l_lines(int n, int nbuf) const;
+  size_t l_smem(int LT, int n, int nbuf) const;
+};

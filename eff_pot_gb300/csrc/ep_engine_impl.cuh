@@ -1,0 +1,808 @@
+// ep_engine_impl.cuh - Engine<T> method bodies (instantiated per precision).
+#pragma once
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+
+#include "ep_engine.h"
+#include "ep_kernels_impl.cuh"
+
+#define EP_ZC 16
+#define EP_RED_BLOCKS 1216
+#define EP_SMEM_CAP (110 * 1024)
+
+#define EP_LAUNCH(name, kern, grid, block, smem, ...)                 \
+  do {                                                                \
+    cudaEvent_t _a = nullptr;                                         \
+    int _c = -1;                                                      \
+    prof->begin(st, name, _a, _c);                                    \
+    kern<<<grid, block, smem, st>>>(__VA_ARGS__);                     \
+    prof->end(st, _c, _a);                                            \
+    cudaError_t _e = cudaGetLastError();                              \
+    if (_e != cudaSuccess) return cuda_ok(_e, name);                  \
+  } while (0)
+
+namespace {
+
+// Radix sequence for n = 2^a 3^b 5^c: as many 8s as possible, a 4 or 2 for
+// the rest of the power of two (two 4s instead of 8*2), then 3s and 5s.
+inline bool make_plan(int n, FftPlan& p) {
+  p.n = n;
+  p.nst = 0;
+  int m = n, e = 0;
+  while (m % 2 == 0) { m /= 2; ++e; }
+  int n8 = e / 3, rem = e % 3;
+  if (rem == 1 && n8 > 0) { --n8; rem = 4; }
+  for (int i = 0; i < n8; ++i) p.rad[p.nst++] = 8;
+  if (rem == 4) { p.rad[p.nst++] = 4; p.rad[p.nst++] = 4; }
+  else if (rem == 2) p.rad[p.nst++] = 4;
+  else if (rem == 1) p.rad[p.nst++] = 2;
+  while (m % 3 == 0) { m /= 3; p.rad[p.nst++] = 3; }
+  while (m % 5 == 0) { m /= 5; p.rad[p.nst++] = 5; }
+  return m == 1 && p.nst <= 12;
+}
+
+// Central-row weights of the (2R+1)-point stencils (closed forms of the
+// Bickley/Lagrange coefficients), at +k.
+inline void fd_weights(int R, long double* w1, long double* w2) {
+  long double lf[64];
+  lf[0] = 0.0L;
+  for (int i = 1; i < 64; ++i) lf[i] = lf[i - 1] + logl((long double)i);
+  long double c = 0.0L;
+  w1[0] = 0.0L;
+  for (int k = 1; k <= R; ++k) {
+    const long double mag = expl(2.0L * lf[R] - lf[R - k] - lf[R + k]);
+    const long double sg = (k & 1) ? 1.0L : -1.0L;
+    w1[k] = sg * mag / k;
+    w2[k] = 2.0L * sg * mag / ((long double)k * k);
+    c -= 2.0L / ((long double)k * k);
+  }
+  w2[0] = c;
+}
+
+template <class T, class CT>
+inline void twiddles(int n, std::vector<CT>& tw) {
+  tw.resize(n);
+  for (int k = 0; k < n; ++k) {
+    const long double a = -2.0L * 3.141592653589793238462643383279502884L * k / n;
+    tw[k].x = (T)(double)cosl(a);
+    tw[k].y = (T)(double)sinl(a);
+  }
+}
+
+}  // namespace
+
+template <class T>
+int Engine<T>::cuda_ok(cudaError_t e, const char* what) {
+  if (e == cudaSuccess) return EP_OK;
+  if (err) *err = std::string(what) + ": " + cudaGetErrorString(e);
+  return e == cudaErrorMemoryAllocation ? EP_ERR_OOM : EP_ERR_CUDA;
+}
+
+template <class T>
+int Engine<T>::alloc(void** p, size_t n) {
+  cudaError_t e = cudaMalloc(p, n);
+  if (e != cudaSuccess) {
+    *p = nullptr;
+    cudaGetLastError();
+    if (err) *err = "device allocation of " + std::to_string(n) + " bytes failed";
+    return EP_ERR_OOM;
+  }
+  bytes += (long long)n;
+  return EP_OK;
+}
+
+template <class T>
+size_t Engine<T>::x_smem(int nl, int nreal) const {
+  return 2 * (size_t)nl * (g.nx / 2 + 1) * sizeof(CT) + (size_t)g.nx * sizeof(CT) + (size_t)nreal * nl * g.nx * sizeof(T);
+}
+template <class T>
+int Engine<T>::x_lines(int nreal) const {
+  int nl = 16;
+  while (nl > 1 && x_smem(nl, nreal) > EP_SMEM_CAP) nl /= 2;
+  return nl;
+}
+template <class T>
+size_t Engine<T>::l_smem(int LT, int n, int nbuf) const {
+  return (size_t)nbuf * LT * (n + 1) * sizeof(CT) + (size_t)n * sizeof(CT) + (size_t)LT * sizeof(long long);
+}
+template <class T>
+int Engine<T>::l_lines(int n, int nbuf) const {
+  int LT = 16;
+  while (LT > 1 && l_smem(LT, n, nbuf) > EP_SMEM_CAP) LT /= 2;
+  return LT;
+}
+
+template <class T>
+int Engine<T>::init(const ep_config& c, cudaStream_t s, Prof* p, ImpState* im, std::string* e) {
+  cfg = c;
+  st = s;
+  prof = p;
+  imp = im;
+  err = e;
+  g.nx = c.nx; g.ny = c.ny; g.nz = c.nz; g.nxh = c.nx / 2 + 1;
+  g.N = (long long)c.nx * c.ny * c.nz;
+  g.Nh = (long long)g.nxh * c.ny * c.nz;
+  hx = 2.0 * std::fabs(c.xmax) / c.nx;
+  hy = 2.0 * std::fabs(c.ymax) / c.ny;
+  hz = 2.0 * std::fabs(c.zmax) / c.nz;
+  dxyz = hx * hy * hz;
+  if (!make_plan(c.nx / 2, p2) || !make_plan(c.ny, pY) || !make_plan(c.nz, pZ)) {
+    *err = "grid sizes must factor into 2, 3 and 5";
+    return EP_ERR_BAD_GRID;
+  }
+  // finite-difference weights scaled by 1/h^id (Deriv3D_p Sto = 1/h**id)
+  const int R = c.npd / 2;
+  long double w1[EP_MAX_R + 1], w2[EP_MAX_R + 1];
+  fd_weights(R, w1, w2);
+  FdW<T> fdl{};
+  const double hh[3] = {hx, hy, hz};
+  for (int a = 0; a < 3; ++a) {
+    const double s1 = 1.0 / hh[a], s2 = 1.0 / (hh[a] * hh[a]);
+    for (int k = 0; k <= R; ++k) {
+      fdl.w1[a][k] = (T)((double)w1[k] * s1);
+      fdl.w2[a][k] = (T)((double)w2[k] * s2);
+    }
+  }
+  fdl.R = R;
+  fdl.periodic = (c.icon == EP_ICON_PERIODIC) ? 1 : 0;
+  fd = fdl;
+  Phys phl{};
+  phl.cp4 = c.cp4; phl.cpp4 = c.cpp4; phl.a0 = c.cp4 / 2.0; phl.a1 = c.cpp4 / 3.0;
+  phl.den0s = c.den0s; phl.h2o2m4 = c.h2o2m4; phl.alphas = c.alphas;
+  phl.C = c.C; phl.beta = c.beta; phl.den_m = c.den_m;
+  phl.renor = 1.0 / ((double)c.nx * c.ny * c.nz);
+  phl.dxyz = dxyz;
+  phl.core = c.core;
+  phl.time_mode = c.time_mode;
+  phys = phl;
+
+  const size_t N = (size_t)g.N, Nh = (size_t)g.Nh;
+  int r;
+  CT** cbufs[] = {&psi, &spare, &po[0], &po[1], &po[2], &ph[0], &ph[1], &pc, &q};
+  for (CT** b : cbufs) if ((r = alloc((void**)b, N * sizeof(CT)))) return r;
+  T** rbufs[] = {&den, &pot4, &uimp, &dencg, &delj4, &dxd, &dyd, &dzd, &falfs, &intx, &inty, &intz,
+                 &ualphas, &gy, &gz, &dgx, &vpi, &delta};
+  for (T** b : rbufs) if ((r = alloc((void**)b, N * sizeof(T)))) return r;
+  for (int i = 0; i < 4; ++i) {
+    if ((r = alloc((void**)&S[i], Nh * sizeof(CT)))) return r;
+    if ((r = alloc((void**)&Tb[i], Nh * sizeof(CT)))) return r;
+  }
+  T** kbufs[] = {&fvlj4, &wcgk, &kalfs};
+  for (T** b : kbufs) if ((r = alloc((void**)b, Nh * sizeof(T)))) return r;
+  if ((r = alloc((void**)&twx, c.nx * sizeof(CT)))) return r;
+  if ((r = alloc((void**)&twy, c.ny * sizeof(CT)))) return r;
+  if ((r = alloc((void**)&twz, c.nz * sizeof(CT)))) return r;
+  const long long nbs = (long long)((c.nx + EP_TX - 1) / EP_TX) * ((c.ny + EP_TY - 1) / EP_TY) * ((c.nz + EP_ZC - 1) / EP_ZC);
+  npartials = std::max(nbs * 4, (long long)EP_RED_BLOCKS * 9);
+  if ((r = alloc((void**)&partials, npartials * sizeof(double)))) return r;
+  if ((r = alloc((void**)&sc, sizeof(DevScalars)))) return r;
+
+  for (CT** b : cbufs) if ((r = cuda_ok(cudaMemsetAsync(*b, 0, N * sizeof(CT), st), "memset"))) return r;
+  for (T** b : rbufs) if ((r = cuda_ok(cudaMemsetAsync(*b, 0, N * sizeof(T), st), "memset"))) return r;
+  if ((r = cuda_ok(cudaMemsetAsync(sc, 0, sizeof(DevScalars), st), "memset"))) return r;
+
+  std::vector<CT> tw;
+  twiddles<T>(c.nx, tw);
+  cudaMemcpyAsync(twx, tw.data(), c.nx * sizeof(CT), cudaMemcpyHostToDevice, st);
+  cudaStreamSynchronize(st);
+  twiddles<T>(c.ny, tw);
+  cudaMemcpyAsync(twy, tw.data(), c.ny * sizeof(CT), cudaMemcpyHostToDevice, st);
+  cudaStreamSynchronize(st);
+  twiddles<T>(c.nz, tw);
+  cudaMemcpyAsync(twz, tw.data(), c.nz * sizeof(CT), cudaMemcpyHostToDevice, st);
+  cudaStreamSynchronize(st);
+
+  // FFT-ordered momentum grid (DFT4He3d.f90:213-219,266-300).
+  {
+    const int nx = c.nx, ny = c.ny, nz = c.nz;
+    const double hpx = 1.0 / (nx * hx), hpy = 1.0 / (ny * hy), hpz = 1.0 / (nz * hz);
+    const double pmx = 1.0 / (2.0 * hx), pmy = 1.0 / (2.0 * hy), pmz = 1.0 / (2.0 * hz);
+    std::vector<double> pg(nx + ny + nz);
+    for (int i = 1; i <= nx / 2 + 1; ++i) pg[i - 1] = hpx * (i - 1);
+    for (int i = nx / 2 + 2; i <= nx; ++i) pg[i - 1] = -pmx + hpx * (i - (nx / 2 + 1));
+    for (int i = 1; i <= ny / 2 + 1; ++i) pg[nx + i - 1] = hpy * (i - 1);
+    for (int i = ny / 2 + 2; i <= ny; ++i) pg[nx + i - 1] = -pmy + hpy * (i - (ny / 2 + 1));
+    for (int i = 1; i <= nz / 2 + 1; ++i) pg[nx + ny + i - 1] = hpz * (i - 1);
+    for (int i = nz / 2 + 2; i <= nz; ++i) pg[nx + ny + i - 1] = -pmz + hpz * (i - (nz / 2 + 1));
+    double* dpg = nullptr;
+    if ((r = cuda_ok(cudaMalloc((void**)&dpg, pg.size() * sizeof(double)), "pgrid"))) return r;
+    cudaMemcpyAsync(dpg, pg.data(), pg.size() * sizeof(double), cudaMemcpyHostToDevice, st);
+    const double h4 = (c.core == EP_CORE_OP) ? c.h4op : c.h4ot;
+    // bforce (fforma.f90:256-280)
+    const double pi4 = 4.0 * 3.14159265358979323846, eps4 = 4.0 * c.eps4;
+    const double xx = std::pow(c.sigma4 / h4, 6), v0 = xx * (xx - 1.0) / std::pow(h4, 4);
+    const double s6 = std::pow(c.sigma4, 6), s12 = s6 * s6;
+    double bf = pi4 * eps4 * s12 / (9.0 * std::pow(h4, 9)) - pi4 * eps4 * s6 / (3.0 * std::pow(h4, 3));
+    if (c.core == EP_CORE_OP) bf += pi4 * eps4 * (v0 * std::pow(h4, 7)) / 7.0;
+    auto kf = k_formfactors<T>;
+    EP_LAUNCH("formfactors", kf, 4 * 152, 256, 0, g, dpg, dpg + nx, dpg + nx + ny, c.core, h4, c.eps4, c.sigma4,
+              bf, c.l, fvlj4, wcgk, kalfs);
+    cudaStreamSynchronize(st);
+    cudaFree(dpg);
+  }
+  const int big = 220 * 1024;
+  cudaFuncSetAttribute(k_x1<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, big);
+  cudaFuncSetAttribute(k_x2<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, big);
+  cudaFuncSetAttribute(k_x3<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, big);
+  cudaFuncSetAttribute(k_x4<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, big);
+  cudaFuncSetAttribute(k_c2c<T, -1>, cudaFuncAttributeMaxDynamicSharedMemorySize, big);
+  cudaFuncSetAttribute(k_c2c<T, +1>, cudaFuncAttributeMaxDynamicSharedMemorySize, big);
+  cudaFuncSetAttribute(k_zconv<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, big);
+  return cuda_ok(cudaStreamSynchronize(st), "init");
+}
+
+template <class T>
+void Engine<T>::release() {
+  void* bufs[] = {psi, spare, po[0], po[1], po[2], ph[0], ph[1], pc, q, den, pot4, uimp, dencg, delj4, dxd, dyd,
+                  dzd, falfs, intx, inty, intz, ualphas, gy, gz, dgx, vpi, delta, S[0], S[1], S[2], S[3], Tb[0],
+                  Tb[1], Tb[2], Tb[3], fvlj4, wcgk, kalfs, twx, twy, twz, partials, sc};
+  for (void* b : bufs)
+    if (b) cudaFree(b);
+  psi = nullptr;
+  bytes = 0;
+}
+
+// ---------------------------------------------------------------------------
+template <class T>
+int Engine<T>::fft_y(CT** arrs, int n, int dir) {
+  Arr8<T> a{};
+  for (int i = 0; i < n; ++i) a.a[i] = arrs[i];
+  LineSet ls{(long long)g.nxh, (long long)g.nxh * g.ny, (long long)g.nxh, (long long)g.nxh * g.nz};
+  const int LT = l_lines(g.ny, 2);
+  dim3 grid((unsigned)((ls.nlines + LT - 1) / LT), (unsigned)n);
+  const size_t sm = l_smem(LT, g.ny, 2);
+  if (dir < 0) {
+    auto k = k_c2c<T, -1>;
+    EP_LAUNCH("fft_y_fwd", k, grid, 256, sm, a, ls, pY, twy, LT);
+  } else {
+    auto k = k_c2c<T, +1>;
+    EP_LAUNCH("fft_y_inv", k, grid, 256, sm, a, ls, pY, twy, LT);
+  }
+  return EP_OK;
+}
+
+template <class T>
+int Engine<T>::zconv(const CT* const* in, CT* const (*out)[3], const T* const (*ker)[3], const int* nout, int nin) {
+  ConvSpec<T> cs{};
+  for (int i = 0; i < nin; ++i) {
+    cs.in[i] = in[i];
+    cs.nout[i] = nout[i];
+    for (int j = 0; j < nout[i]; ++j) { cs.out[i][j] = out[i][j]; cs.ker[i][j] = ker[i][j]; }
+  }
+  LineSet ls{(long long)g.nxh * g.ny, 0, (long long)g.nxh * g.ny, (long long)g.nxh * g.ny};
+  const int LT = l_lines(g.nz, 3);
+  dim3 grid((unsigned)((ls.nlines + LT - 1) / LT), (unsigned)nin);
+  auto k = k_zconv<T>;
+  EP_LAUNCH("fft_z_conv", k, grid, 256, l_smem(LT, g.nz, 3), cs, ls, pZ, twz, LT);
+  return EP_OK;
+}
+
+// poten() + derden() + term_alfa() (poten.f90:5-131, term_alfa.f90:5-109).
+template <class T>
+int Engine<T>::poten() {
+  const bool otc = cfg.core == EP_CORE_OTC;
+  const bool grad = otc || cfg.impurity != EP_IMPURITY_NONE;
+  const long long nlines = (long long)g.ny * g.nz;
+  int r;
+  {
+    const int nl = x_lines(1);
+    auto k = k_x1<T>;
+    EP_LAUNCH("x1_r2c_den", k, (unsigned)((nlines + nl - 1) / nl), 256, x_smem(nl, 1), g, den, S[0], dxd, dyd,
+              dzd, grad ? 1 : 0, p2, twx, fd, nl);
+  }
+  CT* a1[1] = {S[0]};
+  if ((r = fft_y(a1, 1, -1))) return r;
+  {
+    const CT* in[1] = {S[0]};
+    CT* const out[1][3] = {{Tb[0], Tb[1], Tb[2]}};
+    const T* const ker[1][3] = {{wcgk, fvlj4, kalfs}};
+    const int no[1] = {otc ? 3 : 2};
+    if ((r = zconv(in, out, ker, no, 1))) return r;
+  }
+  CT* b3[3] = {Tb[0], Tb[1], Tb[2]};
+  if ((r = fft_y(b3, otc ? 3 : 2, +1))) return r;
+  {
+    const int nl = x_lines(otc ? 3 : 2);
+    auto k = k_x2<T>;
+    EP_LAUNCH("x2_c2r_r2c", k, (unsigned)((nlines + nl - 1) / nl), 256, x_smem(nl, otc ? 3 : 2), g, phys, Tb[0],
+              Tb[1], Tb[2], den, dxd, dyd, dzd, dencg, delj4, pot4, falfs, S[0], S[1], S[2], S[3], p2, twx, nl);
+  }
+  CT* c4[4] = {S[0], S[1], S[2], S[3]};
+  if ((r = fft_y(c4, otc ? 4 : 1, -1))) return r;
+  {
+    const CT* in[4] = {S[0], S[1], S[2], S[3]};
+    CT* const out[4][3] = {{Tb[0]}, {Tb[1]}, {Tb[2]}, {Tb[3]}};
+    const T* const ker[4][3] = {{wcgk}, {kalfs}, {kalfs}, {kalfs}};
+    const int no[4] = {1, 1, 1, 1};
+    if ((r = zconv(in, out, ker, no, otc ? 4 : 1))) return r;
+  }
+  CT* d4[4] = {Tb[0], Tb[1], Tb[2], Tb[3]};
+  if ((r = fft_y(d4, otc ? 4 : 1, +1))) return r;
+  {
+    const int nl = x_lines(otc ? 4 : 1);
+    auto k = k_x3<T>;
+    EP_LAUNCH("x3_c2r_r2c", k, (unsigned)((nlines + nl - 1) / nl), 256, x_smem(nl, otc ? 4 : 1), g, phys, fd,
+              Tb[0], Tb[1], Tb[2], Tb[3], den, dxd, dyd, dzd, falfs, pot4, intx, inty, intz, gy, gz, dgx, S[0], p2,
+              twx, nl);
+  }
+  if (otc) {
+    if ((r = fft_y(a1, 1, -1))) return r;
+    const CT* in[1] = {S[0]};
+    CT* const out[1][3] = {{Tb[0]}};
+    const T* const ker[1][3] = {{kalfs}};
+    const int no[1] = {1};
+    if ((r = zconv(in, out, ker, no, 1))) return r;
+    CT* e1[1] = {Tb[0]};
+    if ((r = fft_y(e1, 1, +1))) return r;
+    const int nl = x_lines(1);
+    auto k = k_x4<T>;
+    EP_LAUNCH("x4_c2r_ualpha", k, (unsigned)((nlines + nl - 1) / nl), 256, x_smem(nl, 1), g, phys, fd, Tb[0], den,
+              dgx, gy, gz, pot4, ualphas, p2, twx, nl);
+  }
+  have_field = true;
+  return EP_OK;
+}
+
+template <class T>
+int Engine<T>::potenimp() {
+  if (cfg.impurity == EP_IMPURITY_NONE) return cuda_ok(cudaMemsetAsync(uimp, 0, g.N * sizeof(T), st), "uimp");
+  if (!imp->have_tables) {
+    *err = "impurity tables not set";
+    return EP_ERR_STATE;
+  }
+  const double rmax = (imp->npot - 1) * imp->delinter;
+  double2 iv[6];
+  for (int i = 0; i < 6; ++i) iv[i] = make_double2(imp->invar[i].real(), imp->invar[i].imag());
+  auto k = k_potenimp<T>;
+  EP_LAUNCH("potenimp", k, 4 * 152, 256, 0, g, cfg.xmax, cfg.ymax, cfg.zmax, hx, hy, hz, imp->rimp[0],
+            imp->rimp[1], imp->rimp[2], imp->d_potpi, imp->d_potdel, imp->npot, rmax, imp->umax_sigma, iv[0], iv[1],
+            iv[2], iv[3], iv[4], iv[5], vpi, delta, uimp);
+  return EP_OK;
+}
+
+template <class T>
+int Engine<T>::reduce_finalize(int nblocks, int nq, int out0, int mode) {
+  auto k = k_finalize;
+  const int renorm = (cfg.time_mode == EP_IMAGINARY_TIME && cfg.renormalize) ? 1 : 0;
+  EP_LAUNCH("finalize", k, 1, 256, 0, partials, nblocks, nq, sc, out0, mode, (double)g.N, dxyz, cfg.n4, renorm);
+  return EP_OK;
+}
+
+template <class T>
+int Engine<T>::read_sums(double* h, int n, int off) {
+  int r = cuda_ok(cudaMemcpyAsync(h, sc->sums + off, n * sizeof(double), cudaMemcpyDeviceToHost, st), "read sums");
+  if (r) return r;
+  return cuda_ok(cudaStreamSynchronize(st), "read sums");
+}
+
+template <class T>
+int Engine<T>::energy(ep_energies* e) {
+  if (!have_field) { *err = "poten() must run before energy()"; return EP_ERR_STATE; }
+  PotDev vp{imp->plus.kind, imp->plus.r_cutoff, imp->plus.umax, imp->plus.par[0], imp->plus.par[1], imp->plus.par[2]};
+  auto k = k_energy<T>;
+  EP_LAUNCH("energy", k, EP_RED_BLOCKS, 256, 0, g, fd, phys, psi, den, dencg, delj4, falfs, dxd, dyd, dzd, intx,
+            inty, intz, uimp, cfg.xmax, cfg.ymax, cfg.zmax, hx, hy, hz, imp->rimp[0], imp->rimp[1], imp->rimp[2],
+            cfg.z_exciplex_exclusion, vp, cfg.impurity != EP_IMPURITY_NONE ? 1 : 0, partials);
+  int r;
+  if ((r = reduce_finalize(EP_RED_BLOCKS, 8, 8, 0))) return r;
+  double s[8];
+  if ((r = read_sums(s, 8, 8))) return r;
+  const ep_config& c = cfg;
+  e->ekin4 = c.h2o2m4 * s[0] * dxyz;
+  e->elj4 = 0.5 * s[1] * dxyz;
+  e->ecor4 = s[2] * dxyz;
+  e->ealphas = (c.core == EP_CORE_OTC) ? -c.h2o2m4 * 0.5 * c.alphas * s[3] * dxyz : 0.0;
+  e->esolid = c.C * s[4] * dxyz;
+  e->etot4 = e->ekin4 + e->elj4 + e->ecor4;
+  if (c.core == EP_CORE_OTC) e->etot4 = e->etot4 + e->ealphas;
+  const double mAg_u = c.mimpur * 0.0207569277;
+  e->ekinx = 0.5 * mAg_u * (imp->vimp[0] * imp->vimp[0] + imp->vimp[1] * imp->vimp[1] + imp->vimp[2] * imp->vimp[2]);
+  e->eHeX = s[5] * dxyz;
+  e->uplus = s[6] * dxyz;
+  const std::complex<double>* iv = imp->invar;
+  std::complex<double> ivs[10];
+  for (int i = 0; i < 10; ++i) ivs[i] = std::conj(iv[i]);
+  e->eso = 0.5 * c.als_p * (2.0 * (ivs[0] * iv[5] - ivs[1] * iv[4]).real() +
+                            2.0 * (ivs[0] * iv[2] + ivs[3] * iv[1] + ivs[2] * iv[5] + ivs[3] * iv[4]).imag());
+  e->eimpu = e->ekinx + e->eHeX + e->eso;
+  e->etot = e->etot4 + e->eimpu;
+  e->n4 = s[7] * dxyz;
+  return check_flags();
+}
+
+template <class T>
+int Engine<T>::forceimp(double* F) {
+  auto k = k_impmoments<T>;
+  EP_LAUNCH("impmoments", k, EP_RED_BLOCKS, 256, 0, g, den, dxd, dyd, dzd, uimp, vpi, delta, cfg.xmax, cfg.ymax,
+            cfg.zmax, hx, hy, hz, imp->rimp[0], imp->rimp[1], imp->rimp[2], partials);
+  int r;
+  if ((r = reduce_finalize(EP_RED_BLOCKS, 9, 16, 0))) return r;
+  double s[9];
+  if ((r = read_sums(s, 9, 16))) return r;
+  for (int i = 0; i < 3; ++i) F[i] = -s[i] * dxyz;
+  return EP_OK;
+}
+
+// potinvar, P state (potenimp.f90:298-330, 487-492), from the moments left
+// by the last forceimp() call.
+template <class T>
+int Engine<T>::potinvar(std::complex<double>* Hiv) {
+  double s[9];
+  int r;
+  if ((r = read_sums(s, 9, 16))) return r;
+  const double uxx = s[3], uxy = s[4], uxz = s[5], uyy = s[6], uyz = s[7], uzz = s[8];
+  const std::complex<double>* iv = imp->invar;
+  const std::complex<double> uim(0.0, 1.0);
+  const double A = cfg.als_p / 2.0;
+  Hiv[0] = (uxx * iv[0] + uxy * iv[2] + uxz * iv[4]) * dxyz + A * (-uim * iv[2] + iv[5]);
+  Hiv[1] = (uxx * iv[1] + uxy * iv[3] + uxz * iv[5]) * dxyz + A * (uim * iv[3] - iv[4]);
+  Hiv[2] = (uxy * iv[0] + uyy * iv[2] + uyz * iv[4]) * dxyz + A * (uim * iv[0] - uim * iv[5]);
+  Hiv[3] = (uxy * iv[1] + uyy * iv[3] + uyz * iv[5]) * dxyz + A * (-uim * iv[1] - uim * iv[4]);
+  Hiv[4] = (uxz * iv[0] + uyz * iv[2] + uzz * iv[4]) * dxyz + A * (-iv[1] + uim * iv[3]);
+  Hiv[5] = (uxz * iv[1] + uyz * iv[3] + uzz * iv[5]) * dxyz + A * (iv[0] + uim * iv[2]);
+  for (int i = 6; i < 10; ++i) Hiv[i] = 0.0;
+  for (int i = 0; i < 10; ++i) Hiv[i] = -uim * (Hiv[i] - cfg.ev0 * iv[i]);
+  return EP_OK;
+}
+
+template <class T>
+int Engine<T>::refresh() {
+  const bool mov = cfg.impurity == EP_IMPURITY_MOVING;
+  int r;
+  if (mov && (r = potenimp())) return r;
+  if ((r = poten())) return r;
+  if (mov) {
+    double F[3];
+    if ((r = forceimp(F))) return r;
+    const double m = cfg.mimpur * 0.0207569277;
+    for (int i = 0; i < 3; ++i) imp->aimp[i] = F[i] / m;
+    if (!cfg.fix_lambda && (r = potinvar(imp->hinvar))) return r;
+  }
+  return EP_OK;
+}
+
+template <class T>
+int Engine<T>::lap_predict(double dt) {
+  const double c112 = 112.0 / 121.0, c4o3 = 4.0 / 3.0;
+  CT* po3 = po[ioldp[2]];
+  const CT* h1 = ph[ioldh[0]];
+  CT* h2 = ph[ioldh[1]];
+  dim3 grid((g.nx + EP_TX - 1) / EP_TX, (g.ny + EP_TY - 1) / EP_TY, (g.nz + EP_ZC - 1) / EP_ZC);
+  dim3 blk(EP_TX, EP_TY);
+  const T f = (T)(c4o3 * dt), c1 = (T)c112;
+#define EP_PRED(RR)                                                                                          \
+  case RR: {                                                                                                 \
+    auto k = k_predict<T, RR>;                                                                               \
+    EP_LAUNCH("predict", k, grid, blk, 0, g, fd, phys, EP_ZC, psi, pot4, uimp, po3, h1, h2, pc, den, f, c1); \
+  } break;
+  switch (fd.R) {
+    EP_PRED(1) EP_PRED(2) EP_PRED(3) EP_PRED(4) EP_PRED(5) EP_PRED(6)
+    default: *err = "npd > 13 not built"; return EP_ERR_UNSUPPORTED;
+  }
+#undef EP_PRED
+  std::swap(psi, po[ioldp[2]]);
+  std::swap(ioldh[0], ioldh[1]);
+  return EP_OK;
+}
+
+template <class T>
+int Engine<T>::lap_correct(double dt, bool want) {
+  (void)want;
+  const double c9 = 9.0 / 121.0;
+  const CT* po3 = po[ioldp[2]];
+  const CT* po2 = po[ioldp[1]];
+  const CT* h1 = ph[ioldh[0]];
+  const CT* h2 = ph[ioldh[1]];
+  dim3 grid((g.nx + EP_TX - 1) / EP_TX, (g.ny + EP_TY - 1) / EP_TY, (g.nz + EP_ZC - 1) / EP_ZC);
+  dim3 blk(EP_TX, EP_TY);
+  const T f3 = (T)(3.0 * dt), cc = (T)c9;
+#define EP_CORR(RR)                                                                                           \
+  case RR: {                                                                                                  \
+    auto k = k_correct<T, RR>;                                                                                \
+    EP_LAUNCH("correct", k, grid, blk, 0, g, fd, phys, EP_ZC, psi, pot4, uimp, po3, po2, h1, h2, pc, spare, den, \
+              f3, cc, partials);                                                                              \
+  } break;
+  switch (fd.R) {
+    EP_CORR(1) EP_CORR(2) EP_CORR(3) EP_CORR(4) EP_CORR(5) EP_CORR(6)
+    default: *err = "npd > 13 not built"; return EP_ERR_UNSUPPORTED;
+  }
+#undef EP_CORR
+  std::swap(psi, spare);
+  const int t = ioldp[2];
+  ioldp[2] = ioldp[1];
+  ioldp[1] = ioldp[0];
+  ioldp[0] = t;
+  return reduce_finalize((int)(grid.x * grid.y * grid.z), 4, 0, 1);
+}
+
+template <class T>
+int Engine<T>::rk_stage(int jr, double dt) {
+  const double s2 = std::sqrt(2.0);
+  const double arun[4] = {0.5, 1.0 - 1.0 / s2, 1.0 + 1.0 / s2, 1.0 / 6.0};
+  const double brun[4] = {2.0, 1.0, 1.0, 2.0};
+  const double crun[4] = {0.5, 1.0 - 1.0 / s2, 1.0 + 1.0 / s2, 0.5};
+  CT* out = (jr == 0) ? po[2] : spare;
+  CT* hout = (jr == 0) ? ph[1] : nullptr;
+  dim3 grid((g.nx + EP_TX - 1) / EP_TX, (g.ny + EP_TY - 1) / EP_TY, (g.nz + EP_ZC - 1) / EP_ZC);
+  dim3 blk(EP_TX, EP_TY);
+  const T a = (T)arun[jr], b = (T)brun[jr], cr = (T)crun[jr], d = (T)dt;
+#define EP_RK(RR)                                                                                              \
+  case RR: {                                                                                                   \
+    auto k = k_rkstage<T, RR>;                                                                                 \
+    EP_LAUNCH("rkstage", k, grid, blk, 0, g, fd, phys, EP_ZC, psi, pot4, uimp, q, out, hout, den, a, b, cr, d, sc); \
+  } break;
+  switch (fd.R) {
+    EP_RK(1) EP_RK(2) EP_RK(3) EP_RK(4) EP_RK(5) EP_RK(6)
+    default: *err = "npd > 13 not built"; return EP_ERR_UNSUPPORTED;
+  }
+#undef EP_RK
+  if (jr == 0) {
+    // hpsiold(2) = hpsiold(1); hpsiold(1) = H; psiold(3) = psiold(2);
+    // psiold(2) = psiold(1); psiold(1) = psi (steprk.f90:78-84)
+    CT* hn = ph[1];
+    ph[1] = ph[0];
+    ph[0] = hn;
+    CT* pn = po[2];
+    po[2] = po[1];
+    po[1] = po[0];
+    po[0] = psi;
+    psi = pn;
+  } else {
+    std::swap(psi, spare);
+  }
+  return EP_OK;
+}
+
+// steprk (steprk.f90:1-191).
+template <class T>
+int Engine<T>::steprk(double dt) {
+  if (!have_field) { *err = "poten() must run before steprk()"; return EP_ERR_STATE; }
+  const double s2 = std::sqrt(2.0);
+  const double arun[4] = {0.5, 1.0 - 1.0 / s2, 1.0 + 1.0 / s2, 1.0 / 6.0};
+  const double brun[4] = {2.0, 1.0, 1.0, 2.0};
+  const double crun[4] = {0.5, 1.0 - 1.0 / s2, 1.0 + 1.0 / s2, 0.5};
+  const bool mov = cfg.impurity == EP_IMPURITY_MOVING;
+  int r;
+  for (int jr = 0; jr < 4; ++jr) {
+    if ((r = rk_stage(jr, dt))) return r;
+    if (mov) {
+      ImpState& m = *imp;
+      const double a = arun[jr], b = brun[jr], cr = crun[jr];
+      for (int k = 0; k < 3; ++k) {
+        const double ax = a * (m.vimp[k] - b * m.qr[k]);
+        m.qr[k] = m.qr[k] + 3.0 * ax - cr * m.vimp[k];
+        if (jr == 0) { m.rimpold[k][2] = m.rimpold[k][1]; m.rimpold[k][1] = m.rimpold[k][0]; m.rimpold[k][0] = m.rimp[k]; }
+        m.rimp[k] = m.rimp[k] + dt * ax;
+      }
+      for (int k = 0; k < 3; ++k) {
+        const double ax = a * (m.aimp[k] - b * m.qv[k]);
+        m.qv[k] = m.qv[k] + 3.0 * ax - cr * m.aimp[k];
+        if (jr == 0) {
+          m.aimpold[k][1] = m.aimpold[k][0]; m.aimpold[k][0] = m.aimp[k];
+          m.vimpold[k][2] = m.vimpold[k][1]; m.vimpold[k][1] = m.vimpold[k][0]; m.vimpold[k][0] = m.vimp[k];
+        }
+        m.vimp[k] = m.vimp[k] + dt * ax;
+      }
+      if (!cfg.fix_lambda) {
+        for (int k = 0; k < 10; ++k) {
+          const std::complex<double> ax = a * (m.hinvar[k] - b * m.qiv[k]);
+          m.qiv[k] = m.qiv[k] + 3.0 * ax - cr * m.hinvar[k];
+          if (jr == 0) {
+            m.hinvarold[k][1] = m.hinvarold[k][0]; m.hinvarold[k][0] = m.hinvar[k];
+            m.invarold[k][2] = m.invarold[k][1]; m.invarold[k][1] = m.invarold[k][0]; m.invarold[k][0] = m.invar[k];
+          }
+          m.invar[k] = m.invar[k] + dt * ax;
+        }
+      }
+    }
+    if (jr <= 2 && (r = refresh())) return r;
+  }
+  for (int i = 0; i < 3; ++i) { ioldp[i] = i; imp->ioldr[i] = i; imp->ioldv[i] = i; imp->ioldiv[i] = i; }
+  for (int i = 0; i < 2; ++i) { ioldh[i] = i; imp->iolda[i] = i; imp->ioldhiv[i] = i; }
+  if ((r = cuda_ok(cudaStreamSynchronize(st), "steprk"))) return r;
+  return check_flags();
+}
+
+// steppc (steppc.f90:1-230).
+template <class T>
+int Engine<T>::steppc(double dt, ep_step_errors* e) {
+  if (!have_field) { *err = "poten() must run before steppc()"; return EP_ERR_STATE; }
+  const double c112 = 112.0 / 121.0, c9 = 9.0 / 121.0, c4o3 = 4.0 / 3.0;
+  const bool mov = cfg.impurity == EP_IMPURITY_MOVING;
+  int r;
+  if ((r = lap_predict(dt))) return r;
+  ImpState& m = *imp;
+  if (mov) {
+    double auxr[3];
+    const int r3 = m.ioldr[2], v1 = m.ioldv[0], v2 = m.ioldv[1], v3 = m.ioldv[2], a1 = m.iolda[0], a2 = m.iolda[1];
+    for (int k = 0; k < 3; ++k)
+      auxr[k] = m.rimpold[k][r3] + c4o3 * dt * (2.0 * m.vimp[k] - m.vimpold[k][v1] + 2.0 * m.vimpold[k][v2]);
+    for (int k = 0; k < 3; ++k) { m.rimpold[k][r3] = m.rimp[k]; m.rimp[k] = auxr[k] - c112 * m.pcr[k]; m.pcr[k] = auxr[k]; }
+    for (int k = 0; k < 3; ++k)
+      auxr[k] = m.vimpold[k][v3] + c4o3 * dt * (2.0 * m.aimp[k] - m.aimpold[k][a1] + 2.0 * m.aimpold[k][a2]);
+    for (int k = 0; k < 3; ++k) { m.vimpold[k][v3] = auxr[k] - c112 * m.pcv[k]; m.pcv[k] = auxr[k]; }
+    if (!cfg.fix_lambda) {
+      const int i3 = m.ioldiv[2], h1 = m.ioldhiv[0], h2 = m.ioldhiv[1];
+      std::complex<double> auxc[10];
+      for (int k = 0; k < 10; ++k)
+        auxc[k] = m.invarold[k][i3] + c4o3 * dt * (2.0 * m.hinvar[k] - m.hinvarold[k][h1] + 2.0 * m.hinvarold[k][h2]);
+      for (int k = 0; k < 10; ++k) { m.invarold[k][i3] = m.invar[k]; m.invar[k] = auxc[k] - c112 * m.pciv[k]; m.pciv[k] = auxc[k]; }
+    }
+    for (int k = 0; k < 3; ++k) m.aimpold[k][a2] = m.aimp[k];
+    for (int k = 0; k < 10; ++k) m.hinvarold[k][m.ioldhiv[1]] = m.hinvar[k];
+    std::swap(m.iolda[0], m.iolda[1]);
+    std::swap(m.ioldhiv[0], m.ioldhiv[1]);
+  }
+  if ((r = refresh())) return r;
+  if ((r = lap_correct(dt, e != nullptr))) return r;
+  double errimp = 0, errvimp = 0, erriv = 0;
+  if (mov) {
+    double auxr[3];
+    const int r2 = m.ioldr[1], r3 = m.ioldr[2], v1 = m.ioldv[0], v2 = m.ioldv[1], v3 = m.ioldv[2];
+    const int a1 = m.iolda[0], a2 = m.iolda[1];
+    for (int k = 0; k < 3; ++k)
+      auxr[k] = 0.125 * (9.0 * m.rimpold[k][r3] - m.rimpold[k][r2] + 3.0 * dt * (m.vimpold[k][v3] + 2.0 * m.vimp[k] - m.vimpold[k][v1]));
+    for (int k = 0; k < 3; ++k) { m.pcr[k] = m.pcr[k] - auxr[k]; m.rimp[k] = auxr[k] + c9 * m.pcr[k]; errimp += std::fabs(c9 * m.pcr[k]); }
+    errimp *= 0.3333333333;
+    { const int t = m.ioldr[2]; m.ioldr[2] = m.ioldr[1]; m.ioldr[1] = m.ioldr[0]; m.ioldr[0] = t; }
+    for (int k = 0; k < 3; ++k)
+      auxr[k] = 0.125 * (9.0 * m.vimp[k] - m.vimpold[k][v2] + 3.0 * dt * (m.aimp[k] + 2.0 * m.aimpold[k][a1] - m.aimpold[k][a2]));
+    for (int k = 0; k < 3; ++k) {
+      m.pcv[k] = m.pcv[k] - auxr[k];
+      m.vimpold[k][v3] = m.vimp[k];
+      m.vimp[k] = auxr[k] + c9 * m.pcv[k];
+      errvimp += std::fabs(c9 * m.pcv[k]);
+    }
+    errvimp *= 0.3333333333;
+    if (!cfg.fix_lambda) {
+      const int i3 = m.ioldiv[2], i2 = m.ioldiv[1], h1 = m.ioldhiv[0], h2 = m.ioldhiv[1];
+      std::complex<double> auxc[10];
+      for (int k = 0; k < 10; ++k)
+        auxc[k] = 0.125 * (9.0 * m.invarold[k][i3] - m.invarold[k][i2] + 3.0 * dt * (m.hinvar[k] + 2.0 * m.hinvarold[k][h1] - m.hinvarold[k][h2]));
+      for (int k = 0; k < 6; ++k) m.pciv[k] = m.pciv[k] - auxc[k];
+      for (int k = 0; k < 10; ++k) m.invar[k] = 0.0;
+      for (int k = 0; k < 6; ++k) m.invar[k] = auxc[k] + c9 * m.pciv[k];
+      for (int k = 0; k < 6; ++k) erriv += std::abs(c9 * m.pciv[k]);
+      erriv *= 0.1666666666666;
+    }
+    { const int t = m.ioldv[2]; m.ioldv[2] = m.ioldv[1]; m.ioldv[1] = m.ioldv[0]; m.ioldv[0] = t; }
+    { const int t = m.ioldiv[2]; m.ioldiv[2] = m.ioldiv[1]; m.ioldiv[1] = m.ioldiv[0]; m.ioldiv[0] = t; }
+  }
+  if (e) {
+    double s[4];
+    if ((r = read_sums(s, 4, 0))) return r;
+    e->errHe = c9 * s[0] / (double)g.N;
+    e->errimp = errimp;
+    e->errvimp = errvimp;
+    e->erriv = erriv;
+    last_norm = s[1] * dxyz;
+    last_mu = s[2] / s[3];
+    return check_flags();
+  }
+  return EP_OK;
+}
+
+template <class T>
+int Engine<T>::renormalize(double* norm_before, bool wait) {
+  // norm of psi -> scale -> rescale psi and den
+  auto kn = k_normsum<T>;
+  EP_LAUNCH("normsum", kn, EP_RED_BLOCKS, 256, 0, psi, g.N, partials);
+  int r;
+  if ((r = reduce_finalize(EP_RED_BLOCKS, 1, 25, 2))) return r;
+  auto ks = k_rescale<T>;
+  EP_LAUNCH("rescale", ks, 4 * 152, 256, 0, psi, den, g.N, sc);
+  if (wait || norm_before) {
+    double s;
+    if ((r = read_sums(&s, 1, 25))) return r;
+    last_norm = s * dxyz;
+    if (norm_before) *norm_before = last_norm;
+    return check_flags();
+  }
+  return EP_OK;
+}
+
+template <class T>
+int Engine<T>::check_flags() {
+  unsigned int f = 0;
+  int r = cuda_ok(cudaMemcpyAsync(&f, &sc->flags, sizeof(unsigned), cudaMemcpyDeviceToHost, st), "flags");
+  if (r) return r;
+  if ((r = cuda_ok(cudaStreamSynchronize(st), "flags"))) return r;
+  if (f) {
+    cudaMemsetAsync(&sc->flags, 0, sizeof(unsigned), st);
+    *err = (f & EP_FLAG_DEN_NONPOS) ? "density not positive (steprk trap)" : "non-finite value in a reduction";
+    return EP_ERR_NONFINITE;
+  }
+  return EP_OK;
+}
+
+template <class T>
+int Engine<T>::upload_psi(const double* h) {
+  int r;
+  if (sizeof(T) == sizeof(double)) {
+    if ((r = cuda_ok(cudaMemcpyAsync(psi, h, g.N * sizeof(CT), cudaMemcpyHostToDevice, st), "upload psi"))) return r;
+  } else {
+    double2* tmp = nullptr;
+    if ((r = cuda_ok(cudaMalloc((void**)&tmp, g.N * sizeof(double2)), "upload tmp"))) return r;
+    cudaMemcpyAsync(tmp, h, g.N * sizeof(double2), cudaMemcpyHostToDevice, st);
+    auto k = k_convert<double2, CT>;
+    EP_LAUNCH("convert", k, 4 * 152, 256, 0, tmp, psi, g.N);
+    cudaStreamSynchronize(st);
+    cudaFree(tmp);
+  }
+  auto k = k_psi_to_den<T>;
+  EP_LAUNCH("psi_to_den", k, 4 * 152, 256, 0, psi, den, g.N);
+  return cuda_ok(cudaStreamSynchronize(st), "upload psi");
+}
+
+template <class T>
+int Engine<T>::download_c(int which, double* h) {
+  const CT* src = nullptr;
+  switch (which) {
+    case EP_CFIELD_PSI: src = psi; break;
+    case EP_CFIELD_PSIOLD1: src = po[0]; break;
+    case EP_CFIELD_PSIOLD2: src = po[1]; break;
+    case EP_CFIELD_PSIOLD3: src = po[2]; break;
+    case EP_CFIELD_HPSIOLD1: src = ph[0]; break;
+    case EP_CFIELD_HPSIOLD2: src = ph[1]; break;
+    case EP_CFIELD_PC: src = pc; break;
+    case EP_CFIELD_Q: src = q; break;
+    default: *err = "unknown complex field"; return EP_ERR_INVALID_ARG;
+  }
+  int r;
+  if (sizeof(T) == sizeof(double)) {
+    if ((r = cuda_ok(cudaMemcpyAsync(h, src, g.N * sizeof(CT), cudaMemcpyDeviceToHost, st), "download"))) return r;
+  } else {
+    double2* tmp = nullptr;
+    if ((r = cuda_ok(cudaMalloc((void**)&tmp, g.N * sizeof(double2)), "download tmp"))) return r;
+    auto k = k_convert<CT, double2>;
+    EP_LAUNCH("convert", k, 4 * 152, 256, 0, src, tmp, g.N);
+    cudaMemcpyAsync(h, tmp, g.N * sizeof(double2), cudaMemcpyDeviceToHost, st);
+    cudaStreamSynchronize(st);
+    cudaFree(tmp);
+  }
+  return cuda_ok(cudaStreamSynchronize(st), "download");
+}
+
+template <class T>
+int Engine<T>::download_r(int which, double* h) {
+  const T* src = nullptr;
+  switch (which) {
+    case EP_FIELD_DEN: src = den; break;
+    case EP_FIELD_POT4: src = pot4; break;
+    case EP_FIELD_UIMP: src = uimp; break;
+    case EP_FIELD_DENCG: src = dencg; break;
+    case EP_FIELD_DELJ4: src = delj4; break;
+    case EP_FIELD_DXDEN: src = dxd; break;
+    case EP_FIELD_DYDEN: src = dyd; break;
+    case EP_FIELD_DZDEN: src = dzd; break;
+    case EP_FIELD_FALFS: src = falfs; break;
+    case EP_FIELD_INTXALF: src = intx; break;
+    case EP_FIELD_INTYALF: src = inty; break;
+    case EP_FIELD_INTZALF: src = intz; break;
+    case EP_FIELD_UALPHAS: src = ualphas; break;
+    case EP_FIELD_VPI: src = vpi; break;
+    case EP_FIELD_DELTA: src = delta; break;
+    default: *err = "unknown field"; return EP_ERR_INVALID_ARG;
+  }
+  int r;
+  if (sizeof(T) == sizeof(double)) {
+    if ((r = cuda_ok(cudaMemcpyAsync(h, src, g.N * sizeof(T), cudaMemcpyDeviceToHost, st), "download"))) return r;
+  } else {
+    double* tmp = nullptr;
+    if ((r = cuda_ok(cudaMalloc((void**)&tmp, g.N * sizeof(double)), "download tmp"))) return r;
+    auto k = k_convert<T, double>;
+    EP_LAUNCH("convert", k, 4 * 152, 256, 0, src, tmp, g.N);
+    cudaMemcpyAsync(h, tmp, g.N * sizeof(double), cudaMemcpyDeviceToHost, st);
+    cudaStreamSynchronize(st);
+    cudaFree(tmp);
+  }
+  return cuda_ok(cudaStreamSynchronize(st), "download");
+}
+
+template <class T>
+int Engine<T>::rescale_pending() {
+  auto ks = k_rescale<T>;
+  EP_LAUNCH("rescale", ks, 4 * 152, 256, 0, psi, den, g.N, sc);
+  return EP_OK;
+}

@@ -1,0 +1,193 @@
+// ep_fft.cuh - shared-memory FFT engine for batched 3-D real transforms.
+//
+// A 3-D r2c transform of an (nx,ny,nz) column-major array is three passes:
+//  X: each x-line (contiguous) is packed as nx/2 complex numbers, transformed
+//     with a half-length complex FFT and unpacked to nx/2+1 outputs;
+//  Y, Z: complex transforms of strided lines of the half spectrum.
+// A CTA stages a group of lines in shared memory (coalesced global access:
+// consecutive threads touch consecutive addresses), runs a self-sorting
+// (Stockham) mixed-radix FFT over them with butterflies of radix 8/4/2/3/5,
+// and writes them back.  The convolution kernels fuse the point-wise k-space
+// multiply between the forward and inverse Z transforms, and the X kernels
+// fuse the real-space arithmetic of poten/term_alfa around the transforms.
+//
+// Conventions match the reference's FFTW use (fft.f90:233-371): forward is
+// unnormalised with exp(-2 pi i k n / N); backward uses exp(+...) and the
+// caller applies 1/N.
+#pragma once
+#include "ep_common.cuh"
+
+namespace epfft {
+
+template <class T> struct K;
+template <> struct K<double> {
+  static constexpr double half = 0.5;
+  static constexpr double s3 = 0.86602540378443864676372317075294;   // sin(2pi/3)
+  static constexpr double c51 = 0.30901699437494742410229341718282;  // cos(2pi/5)
+  static constexpr double c52 = -0.80901699437494742410229341718282; // cos(4pi/5)
+  static constexpr double s51 = 0.95105651629515357211643933337938;  // sin(2pi/5)
+  static constexpr double s52 = 0.58778525229247312916870595463907;  // sin(4pi/5)
+  static constexpr double r2 = 0.70710678118654752440084436210485;   // 1/sqrt(2)
+};
+template <> struct K<float> {
+  static constexpr float half = 0.5f;
+  static constexpr float s3 = 0.86602540378443864676372317075294f;
+  static constexpr float c51 = 0.30901699437494742410229341718282f;
+  static constexpr float c52 = -0.80901699437494742410229341718282f;
+  static constexpr float s51 = 0.95105651629515357211643933337938f;
+  static constexpr float s52 = 0.58778525229247312916870595463907f;
+  static constexpr float r2 = 0.70710678118654752440084436210485f;
+};
+
+// w*z with w = DIR*i  (DIR = -1 forward, +1 backward)
+template <int DIR, class T2> EP_DEV T2 rot(T2 z) { return DIR < 0 ? mul_mi(z) : mul_i(z); }
+
+template <class T, int DIR> EP_DEV void dft2(C2<T>* v) {
+  C2<T> a = v[0], b = v[1];
+  v[0] = a + b; v[1] = a - b;
+}
+
+template <class T, int DIR> EP_DEV void dft3(C2<T>* v) {
+  C2<T> a = v[0], b = v[1], c = v[2];
+  C2<T> s = b + c, d = b - c;
+  C2<T> t = a - K<T>::half * s;
+  C2<T> u = rot<DIR>(K<T>::s3 * d);
+  v[0] = a + s; v[1] = t + u; v[2] = t - u;
+}
+
+template <class T, int DIR> EP_DEV void dft4(C2<T>* v) {
+  C2<T> a = v[0], b = v[1], c = v[2], d = v[3];
+  C2<T> s0 = a + c, d0 = a - c, s1 = b + d, d1 = rot<DIR>(b - d);
+  v[0] = s0 + s1; v[2] = s0 - s1; v[1] = d0 + d1; v[3] = d0 - d1;
+}
+
+template <class T, int DIR> EP_DEV void dft5(C2<T>* v) {
+  C2<T> a = v[0];
+  C2<T> s1 = v[1] + v[4], d1 = v[1] - v[4], s2 = v[2] + v[3], d2 = v[2] - v[3];
+  C2<T> t1 = a + K<T>::c51 * s1 + K<T>::c52 * s2;
+  C2<T> t2 = a + K<T>::c52 * s1 + K<T>::c51 * s2;
+  C2<T> u1 = rot<DIR>(K<T>::s51 * d1 + K<T>::s52 * d2);
+  C2<T> u2 = rot<DIR>(K<T>::s52 * d1 - K<T>::s51 * d2);
+  v[0] = a + s1 + s2;
+  v[1] = t1 + u1; v[4] = t1 - u1;
+  v[2] = t2 + u2; v[3] = t2 - u2;
+}
+
+template <class T, int DIR> EP_DEV void dft8(C2<T>* v) {
+  C2<T> e[4] = {v[0], v[2], v[4], v[6]};
+  C2<T> o[4] = {v[1], v[3], v[5], v[7]};
+  dft4<T, DIR>(e);
+  dft4<T, DIR>(o);
+  // o[k] *= w8^k, w8 = (1 + DIR i)/sqrt(2)
+  {
+    C2<T> z = o[1];
+    C2<T> r = cmk<T>(z.x - DIR * z.y, z.y + DIR * z.x);
+    o[1] = K<T>::r2 * r;
+  }
+  o[2] = rot<DIR>(o[2]);
+  {
+    C2<T> z = o[3];
+    C2<T> r = cmk<T>(-z.x - DIR * z.y, -z.y + DIR * z.x);
+    o[3] = K<T>::r2 * r;
+  }
+#pragma unroll
+  for (int k = 0; k < 4; ++k) { v[k] = e[k] + o[k]; v[k + 4] = e[k] - o[k]; }
+}
+
+template <class T, int R, int DIR> EP_DEV void dftR(C2<T>* v) {
+  if (R == 2) dft2<T, DIR>(v);
+  else if (R == 3) dft3<T, DIR>(v);
+  else if (R == 4) dft4<T, DIR>(v);
+  else if (R == 5) dft5<T, DIR>(v);
+  else dft8<T, DIR>(v);
+}
+
+// One Stockham stage of radix R over nl lines (line stride ld) of length n.
+// tw: roots exp(-2 pi i k / (n*tws)), accessed with stride tws.
+template <class T, int R, int DIR>
+EP_DEV void stage(const C2<T>* __restrict__ src, C2<T>* __restrict__ dst, int nl, int n, int ld,
+                  int Ns, const C2<T>* __restrict__ tw, int tws) {
+  const int m = n / R;
+  const int total = nl * m;
+  const int tstep = (n / (Ns * R)) * tws;
+  for (int b = threadIdx.x; b < total; b += blockDim.x) {
+    const int line = b / m;
+    const int j = b - line * m;
+    const int k = j % Ns;
+    const C2<T>* s = src + line * ld;
+    C2<T>* d = dst + line * ld;
+    C2<T> v[R];
+#pragma unroll
+    for (int t = 0; t < R; ++t) v[t] = s[j + t * m];
+    if (k != 0) {
+#pragma unroll
+      for (int t = 1; t < R; ++t) {
+        C2<T> w = tw[t * k * tstep];
+        v[t] = DIR < 0 ? cmul(v[t], w) : cmulc(v[t], w);
+      }
+    }
+    dftR<T, R, DIR>(v);
+    const int idxD = (j - k) * R + k;
+#pragma unroll
+    for (int u = 0; u < R; ++u) d[idxD + u * Ns] = v[u];
+  }
+}
+
+// Full FFT over nl lines held in a (ping) with b as scratch; returns the
+// buffer that holds the result.  Caller synchronises before the call; the
+// result is visible to all threads on return.
+template <class T, int DIR>
+EP_DEV C2<T>* lines(C2<T>* a, C2<T>* b, int nl, int ld, const FftPlan& p,
+                    const C2<T>* __restrict__ tw, int tws) {
+  int Ns = 1;
+  for (int s = 0; s < p.nst; ++s) {
+    const int R = p.rad[s];
+    switch (R) {
+      case 8: stage<T, 8, DIR>(a, b, nl, p.n, ld, Ns, tw, tws); break;
+      case 4: stage<T, 4, DIR>(a, b, nl, p.n, ld, Ns, tw, tws); break;
+      case 2: stage<T, 2, DIR>(a, b, nl, p.n, ld, Ns, tw, tws); break;
+      case 3: stage<T, 3, DIR>(a, b, nl, p.n, ld, Ns, tw, tws); break;
+      default: stage<T, 5, DIR>(a, b, nl, p.n, ld, Ns, tw, tws); break;
+    }
+    __syncthreads();
+    C2<T>* t = a; a = b; b = t;
+    Ns *= R;
+  }
+  return a;
+}
+
+// r2c unpack: Z (n2 = nx/2 complex per line, the FFT of the packed line)
+// -> X[k], k = 0..n2, written through the functor out(line, k, X).
+// twx: exp(-2 pi i k / nx), k = 0..nx-1.
+template <class T, class Out>
+EP_DEV void r2c_unpack(const C2<T>* Z, int nl, int ld, int n2, const C2<T>* __restrict__ twx, Out out) {
+  const int per = n2 + 1;
+  for (int b = threadIdx.x; b < nl * per; b += blockDim.x) {
+    const int line = b / per;
+    const int k = b - line * per;
+    const C2<T>* z = Z + line * ld;
+    const C2<T> zk = z[k == n2 ? 0 : k];
+    const C2<T> zc = conjg(z[k == 0 ? 0 : n2 - k]);
+    const C2<T> e = K<T>::half * (zk + zc);
+    const C2<T> o = K<T>::half * mul_mi(zk - zc);
+    out(line, k, e + cmul(twx[k], o));
+  }
+}
+
+// c2r pack: X[k] (k = 0..n2, line stride ldx) -> Z[k] = A + iB, k < n2,
+// A = X[k] + conj(X[n2-k]), B = (X[k] - conj(X[n2-k])) * exp(+2 pi i k/nx).
+template <class T>
+EP_DEV void c2r_pack(const C2<T>* X, int ldx, C2<T>* Z, int ldz, int nl, int n2,
+                     const C2<T>* __restrict__ twx) {
+  for (int b = threadIdx.x; b < nl * n2; b += blockDim.x) {
+    const int line = b / n2;
+    const int k = b - line * n2;
+    const C2<T> xk = X[line * ldx + k];
+    const C2<T> xc = conjg(X[line * ldx + n2 - k]);
+    const C2<T> A = xk + xc;
+    const C2<T> B = cmulc(xk - xc, twx[k]);
+    Z[line * ldz + k] = A + mul_i(B);
+  }
+}
+
+}  // namespace epfft

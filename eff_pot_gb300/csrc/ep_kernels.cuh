@@ -1,0 +1,678 @@
+// ep_kernels.cuh - device kernels of the eff_pot hot path, templated on the
+// field precision T (double or float).  Reductions always accumulate in FP64.
+#pragma once
+#include "ep_common.cuh"
+#include "ep_fft.cuh"
+
+// ---------------------------------------------------------------------------
+// Kernel parameter blocks.
+template <class T> struct FdW {
+  T w1[3][EP_MAX_R + 1];  // first derivative, weight at +k (at -k: -w1)
+  T w2[3][EP_MAX_R + 1];  // second derivative, weight at +-k; [0] = centre
+  int R;
+  int periodic;           // icon 8 (1) or icon 13 (0)
+};
+
+struct Phys {
+  double cp4, cpp4, a0, a1, den0s, h2o2m4, alphas, C, beta, den_m;
+  double renor, dxyz;
+  int core;               // EP_CORE_*
+  int time_mode;          // 0 imaginary, 1 real
+};
+
+// Lines of a strided pass: element k of line L lives at
+//   (L % Mi) + (L / Mi) * So + k * Sa.
+struct LineSet {
+  long long Mi, So, Sa, nlines;
+};
+
+template <class T> struct Arr8 { C2<T>* a[8]; };
+
+template <class T> struct ConvSpec {
+  const C2<T>* in[4];
+  C2<T>* out[4][3];
+  const T* ker[4][3];
+  int nout[4];
+};
+
+// ---------------------------------------------------------------------------
+// Small helpers.
+EP_DEV int wrapi(int i, int n) {
+  i %= n;
+  return i < 0 ? i + n : i;
+}
+
+// f at offset k along an axis of length n (index i, element stride st), with
+// the boundary mode of the finite differences.
+template <class T>
+EP_DEV T nbr(const T* __restrict__ f, long long p, int i, int k, int n, long long st, int periodic) {
+  int ii = i + k;
+  if (ii < 0 || ii >= n) {
+    if (!periodic) return T(0);
+    ii = wrapi(ii, n);
+  }
+  return f[p + (long long)(ii - i) * st];
+}
+
+// First derivative along an axis from global memory (pairs +k/-k).
+template <class T>
+EP_DEV T d1_global(const T* __restrict__ f, long long p, int i, int n, long long st, const T* w, int R, int periodic) {
+  T s = T(0);
+  for (int k = 1; k <= R; ++k) s += w[k] * (nbr(f, p, i, k, n, st, periodic) - nbr(f, p, i, -k, n, st, periodic));
+  return s;
+}
+
+// First derivative along a line held in shared memory (length n).
+template <class T>
+EP_DEV T d1_line(const T* __restrict__ line, int i, int n, const T* w, int R, int periodic) {
+  T s = T(0);
+  for (int k = 1; k <= R; ++k) {
+    int ip = i + k, im = i - k;
+    T fp, fm;
+    if (ip >= n) fp = periodic ? line[ip - n] : T(0); else fp = line[ip];
+    if (im < 0) fm = periodic ? line[im + n] : T(0); else fm = line[im];
+    s += w[k] * (fp - fm);
+  }
+  return s;
+}
+
+// Solid penalty C*(1 + t + beta*den*(1 - t^2)), t = tanh(beta*(den - den_m))
+// (poten.f90:80-81).  The FP32 form is written without the cancellation of
+// 1 + tanh(x) for x << 0: 1 + t = 2/(1 + e^{-2x}), 1 - t^2 = 4e^{2x}/(1+e^{2x})^2.
+EP_DEV double penalty_of(const Phys& ph, double den) {
+  const double t = tanh(ph.beta * (den - ph.den_m));
+  return ph.C * (1.0 + t + ph.beta * den * (1.0 - t * t));
+}
+EP_DEV float penalty_of(const Phys& ph, float den) {
+  const float x = (float)ph.beta * (den - (float)ph.den_m);
+  const float e = __expf(2.0f * x);
+  const float onept = 2.0f * e / (1.0f + e);
+  const float omt2 = 4.0f * e / ((1.0f + e) * (1.0f + e));
+  return (float)ph.C * (onept + (float)ph.beta * den * omt2);
+}
+
+// H-apply of steppc.f90:53 / steprk.f90:74-75:
+//   imaginary time: (lap*h2o2m4 - pot4*psi) - uimp*psi
+//   real time:      i*(lap*h2o2m4 - pot4*psi) - i*uimp*psi
+template <class T>
+EP_DEV C2<T> happly(const Phys& ph, C2<T> lap, C2<T> psi, T pot4, T uimp) {
+  const T h = (T)ph.h2o2m4;
+  C2<T> L = cmk<T>(lap.x * h - pot4 * psi.x, lap.y * h - pot4 * psi.y);
+  if (ph.time_mode == 1) return cmk<T>(-L.y + uimp * psi.y, L.x - uimp * psi.x);
+  return cmk<T>(L.x - uimp * psi.x, L.y - uimp * psi.y);
+}
+
+// <psi|H|psi> integrand from the H-apply output (Hpsi = -H or i*H).
+template <class T>
+EP_DEV double hexp(const Phys& ph, C2<T> psi, C2<T> H) {
+  if (ph.time_mode == 1) return -(double)psi.x * H.y + (double)psi.y * H.x;
+  return -((double)psi.x * H.x + (double)psi.y * H.y);
+}
+
+// Block reduction of NQ doubles into partials[block * NQ + q].
+template <int NQ>
+EP_DEV void block_reduce_store(double (&v)[NQ], double* __restrict__ partials) {
+  __shared__ double red[NQ][32];
+  const int tid = threadIdx.x + blockDim.x * (threadIdx.y + blockDim.y * threadIdx.z);
+  const int nth = blockDim.x * blockDim.y * blockDim.z;
+  const int lane = tid & 31, warp = tid >> 5, nw = (nth + 31) >> 5;
+#pragma unroll
+  for (int q = 0; q < NQ; ++q) {
+    double s = v[q];
+    for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
+    if (lane == 0) red[q][warp] = s;
+  }
+  __syncthreads();
+  if (warp == 0) {
+#pragma unroll
+    for (int q = 0; q < NQ; ++q) {
+      double s = lane < nw ? red[q][lane] : 0.0;
+      for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
+      if (lane == 0) {
+        const long long b = blockIdx.x + (long long)gridDim.x * (blockIdx.y + (long long)gridDim.y * blockIdx.z);
+        partials[b * NQ + q] = s;
+      }
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------
+// X pass helpers (lines along x are contiguous; nl lines per CTA).
+template <class T>
+EP_DEV void x_inverse(const C2<T>* __restrict__ spec, long long line0, int nlv, int nl, int nx, int nxh,
+                      C2<T>* P, C2<T>* Q, int ld, const FftPlan& p2, const C2<T>* tw, T scale, T* Rout) {
+  const int n2 = nx / 2;
+  for (int e = threadIdx.x; e < nl * (n2 + 1); e += blockDim.x) {
+    const int l = e / (n2 + 1), k = e - l * (n2 + 1);
+    P[l * ld + k] = l < nlv ? spec[(line0 + l) * nxh + k] : cmk<T>(T(0), T(0));
+  }
+  __syncthreads();
+  epfft::c2r_pack<T>(P, ld, Q, ld, nl, n2, tw);
+  __syncthreads();
+  const C2<T>* z = epfft::lines<T, +1>(Q, P, nl, ld, p2, tw, 2);
+  for (int e = threadIdx.x; e < nl * n2; e += blockDim.x) {
+    const int l = e / n2, m = e - l * n2;
+    const C2<T> v = z[l * ld + m];
+    Rout[l * nx + 2 * m] = v.x * scale;
+    Rout[l * nx + 2 * m + 1] = v.y * scale;
+  }
+  __syncthreads();
+}
+
+template <class T, class F>
+EP_DEV void x_forward(F val, C2<T>* __restrict__ out, long long line0, int nlv, int nl, int nx, int nxh,
+                      C2<T>* P, C2<T>* Q, int ld, const FftPlan& p2, const C2<T>* tw) {
+  const int n2 = nx / 2;
+  for (int e = threadIdx.x; e < nl * n2; e += blockDim.x) {
+    const int l = e / n2, m = e - l * n2;
+    P[l * ld + m] = l < nlv ? cmk<T>(val(l, 2 * m), val(l, 2 * m + 1)) : cmk<T>(T(0), T(0));
+  }
+  __syncthreads();
+  const C2<T>* Z = epfft::lines<T, -1>(P, Q, nl, ld, p2, tw, 2);
+  epfft::r2c_unpack<T>(Z, nl, ld, n2, tw, [&](int l, int k, C2<T> v) {
+    if (l < nlv) out[(line0 + l) * nxh + k] = v;
+  });
+  __syncthreads();
+}
+
+// Shared-memory carve-up of the X kernels.
+template <class T>
+struct XSmem {
+  C2<T>* P;
+  C2<T>* Q;
+  C2<T>* tw;
+  T* R;  // nreal arrays of nl*nx
+  int ld;
+  EP_DEV XSmem(unsigned char* raw, int nl, int nx) {
+    ld = nx / 2 + 1;
+    P = reinterpret_cast<C2<T>*>(raw);
+    Q = P + nl * ld;
+    tw = Q + nl * ld;
+    R = reinterpret_cast<T*>(tw + nx);
+  }
+};
+
+// X1: den -> r2c along x (-> out); optionally grad den (derden,
+// energy.f90:207-227: three first derivatives).
+template <class T>
+__global__ void k_x1(Geo g, const T* __restrict__ den, C2<T>* __restrict__ out, T* __restrict__ dxo,
+                     T* __restrict__ dyo, T* __restrict__ dzo, int want_grad, FftPlan p2,
+                     const C2<T>* __restrict__ twx, FdW<T> fd, int nl) {
+  extern __shared__ __align__(16) unsigned char smraw[];
+  const int nx = g.nx;
+  XSmem<T> S(smraw, nl, nx);
+  const long long nlines = (long long)g.ny * g.nz;
+  const long long line0 = (long long)blockIdx.x * nl;
+  const int nlv = (int)min((long long)nl, nlines - line0);
+  for (int i = threadIdx.x; i < nx; i += blockDim.x) S.tw[i] = twx[i];
+  T* R0 = S.R;
+  for (int e = threadIdx.x; e < nlv * nx; e += blockDim.x) R0[e] = den[line0 * nx + e];
+  __syncthreads();
+  if (want_grad) {
+    for (int e = threadIdx.x; e < nlv * nx; e += blockDim.x) {
+      const int l = e / nx, i = e - l * nx;
+      const long long L = line0 + l, p = L * nx + i;
+      const int iy = (int)(L % g.ny), iz = (int)(L / g.ny);
+      dxo[p] = d1_line(R0 + l * nx, i, nx, fd.w1[0], fd.R, fd.periodic);
+      dyo[p] = d1_global(den, p, iy, g.ny, (long long)nx, fd.w1[1], fd.R, fd.periodic);
+      dzo[p] = d1_global(den, p, iz, g.nz, (long long)nx * g.ny, fd.w1[2], fd.R, fd.periodic);
+    }
+  }
+  x_forward<T>([&](int l, int i) { return R0[l * nx + i]; }, out, line0, nlv, nl, nx, g.nxh, S.P, S.Q, S.ld,
+               p2, S.tw);
+}
+
+// X2: c2r of the three products of fden -> dencg, delj4 (and denalf for
+// OTC); pot4 partial = delj4 + dencg^2 (a0 + a1 dencg) (poten.f90:34-92);
+// forward r2c of den*dencg*(cp4 + cpp4*dencg) (poten.f90:62-67) and, for
+// OTC, of f*grad(den), f = 1 - denalf/den0s (term_alfa.f90:157-170).
+template <class T>
+__global__ void k_x2(Geo g, Phys ph, const C2<T>* __restrict__ B0, const C2<T>* __restrict__ B1,
+                     const C2<T>* __restrict__ B2, const T* __restrict__ den, const T* __restrict__ dxd,
+                     const T* __restrict__ dyd, const T* __restrict__ dzd, T* __restrict__ dencg,
+                     T* __restrict__ delj4, T* __restrict__ pot4, T* __restrict__ falfs, C2<T>* C0, C2<T>* C1,
+                     C2<T>* C2o, C2<T>* C3, FftPlan p2, const C2<T>* __restrict__ twx, int nl) {
+  extern __shared__ __align__(16) unsigned char smraw[];
+  const int nx = g.nx, nxh = g.nxh;
+  XSmem<T> S(smraw, nl, nx);
+  const bool otc = (ph.core == 1);
+  const long long nlines = (long long)g.ny * g.nz;
+  const long long line0 = (long long)blockIdx.x * nl;
+  const int nlv = (int)min((long long)nl, nlines - line0);
+  for (int i = threadIdx.x; i < nx; i += blockDim.x) S.tw[i] = twx[i];
+  __syncthreads();
+  T* Rcg = S.R;
+  T* Rlj = S.R + nl * nx;
+  T* Ral = S.R + 2 * nl * nx;
+  const T rn = (T)ph.renor;
+  x_inverse<T>(B0, line0, nlv, nl, nx, nxh, S.P, S.Q, S.ld, p2, S.tw, rn, Rcg);
+  x_inverse<T>(B1, line0, nlv, nl, nx, nxh, S.P, S.Q, S.ld, p2, S.tw, rn, Rlj);
+  if (otc) x_inverse<T>(B2, line0, nlv, nl, nx, nxh, S.P, S.Q, S.ld, p2, S.tw, rn, Ral);
+  const T a0 = (T)ph.a0, a1 = (T)ph.a1, den0s = (T)ph.den0s, cp4 = (T)ph.cp4, cpp4 = (T)ph.cpp4;
+  for (int e = threadIdx.x; e < nlv * nx; e += blockDim.x) {
+    const long long p = line0 * nx + e;
+    const T cg = Rcg[e], lj = Rlj[e];
+    dencg[p] = cg;
+    delj4[p] = lj;
+    pot4[p] = lj + cg * cg * (a0 + a1 * cg);
+    if (otc) falfs[p] = T(1) - Ral[e] / den0s;
+  }
+  x_forward<T>(
+      [&](int l, int i) {
+        const T cg = Rcg[l * nx + i];
+        return den[(line0 + l) * nx + i] * cg * (cp4 + cpp4 * cg);
+      },
+      C0, line0, nlv, nl, nx, nxh, S.P, S.Q, S.ld, p2, S.tw);
+  if (otc) {
+    x_forward<T>([&](int l, int i) { return (T(1) - Ral[l * nx + i] / den0s) * dxd[(line0 + l) * nx + i]; },
+                 C1, line0, nlv, nl, nx, nxh, S.P, S.Q, S.ld, p2, S.tw);
+    x_forward<T>([&](int l, int i) { return (T(1) - Ral[l * nx + i] / den0s) * dyd[(line0 + l) * nx + i]; },
+                 C2o, line0, nlv, nl, nx, nxh, S.P, S.Q, S.ld, p2, S.tw);
+    x_forward<T>([&](int l, int i) { return (T(1) - Ral[l * nx + i] / den0s) * dzd[(line0 + l) * nx + i]; },
+                 C3, line0, nlv, nl, nx, nxh, S.P, S.Q, S.ld, p2, S.tw);
+  }
+}
+
+// X3: c2r of the correlation convolution -> pot4 (+ penalty for OT,
+// poten.f90:74,88-92,122-126).  OTC: c2r of the three alpha_s integrals
+// (term_alfa.f90:172-181), the x-derivative of f*I_x, f*I_y and f*I_z for
+// the divergence (:216-225), and forward r2c of grad(den).I (:194-201).
+template <class T>
+__global__ void k_x3(Geo g, Phys ph, FdW<T> fd, const C2<T>* __restrict__ D0, const C2<T>* __restrict__ D1,
+                     const C2<T>* __restrict__ D2, const C2<T>* __restrict__ D3, const T* __restrict__ den,
+                     const T* __restrict__ dxd, const T* __restrict__ dyd, const T* __restrict__ dzd,
+                     const T* __restrict__ falfs, T* __restrict__ pot4, T* __restrict__ intx, T* __restrict__ inty,
+                     T* __restrict__ intz, T* __restrict__ gy, T* __restrict__ gz, T* __restrict__ dgx,
+                     C2<T>* E0, FftPlan p2, const C2<T>* __restrict__ twx, int nl) {
+  extern __shared__ __align__(16) unsigned char smraw[];
+  const int nx = g.nx, nxh = g.nxh;
+  XSmem<T> S(smraw, nl, nx);
+  const bool otc = (ph.core == 1);
+  const long long nlines = (long long)g.ny * g.nz;
+  const long long line0 = (long long)blockIdx.x * nl;
+  const int nlv = (int)min((long long)nl, nlines - line0);
+  for (int i = threadIdx.x; i < nx; i += blockDim.x) S.tw[i] = twx[i];
+  __syncthreads();
+  const T rn = (T)ph.renor;
+  T* Rc = S.R;
+  x_inverse<T>(D0, line0, nlv, nl, nx, nxh, S.P, S.Q, S.ld, p2, S.tw, rn, Rc);
+  if (!otc) {
+    for (int e = threadIdx.x; e < nlv * nx; e += blockDim.x) {
+      const long long p = line0 * nx + e;
+      pot4[p] = (pot4[p] + Rc[e]) + penalty_of(ph, den[p]);
+    }
+    return;
+  }
+  T* Rx = S.R + nl * nx;
+  T* Ry = S.R + 2 * nl * nx;
+  T* Rz = S.R + 3 * nl * nx;
+  x_inverse<T>(D1, line0, nlv, nl, nx, nxh, S.P, S.Q, S.ld, p2, S.tw, rn, Rx);
+  x_inverse<T>(D2, line0, nlv, nl, nx, nxh, S.P, S.Q, S.ld, p2, S.tw, rn, Ry);
+  x_inverse<T>(D3, line0, nlv, nl, nx, nxh, S.P, S.Q, S.ld, p2, S.tw, rn, Rz);
+  for (int e = threadIdx.x; e < nlv * nx; e += blockDim.x) {
+    const long long p = line0 * nx + e;
+    pot4[p] = pot4[p] + Rc[e];
+    const T f = falfs[p];
+    intx[p] = Rx[e];
+    inty[p] = Ry[e];
+    intz[p] = Rz[e];
+    gy[p] = f * Ry[e];
+    gz[p] = f * Rz[e];
+    Rc[e] = f * Rx[e];
+  }
+  __syncthreads();
+  for (int e = threadIdx.x; e < nlv * nx; e += blockDim.x) {
+    const int l = e / nx, i = e - l * nx;
+    dgx[line0 * nx + e] = d1_line(Rc + l * nx, i, nx, fd.w1[0], fd.R, fd.periodic);
+  }
+  x_forward<T>(
+      [&](int l, int i) {
+        const int e = l * nx + i;
+        const long long p = line0 * nx + e;
+        return (dxd[p] * Rx[e]) + (dyd[p] * Ry[e]) + (dzd[p] * Rz[e]);
+      },
+      E0, line0, nlv, nl, nx, nxh, S.P, S.Q, S.ld, p2, S.tw);
+}
+
+// X4 (OTC): c2r of kalfs*FFT(grad(den).I) -> U_alpha = (u/den0s + div(f I))
+// * h2o2m4 * alphas (term_alfa.f90:203-236); pot4 += U_alpha + penalty.
+template <class T>
+__global__ void k_x4(Geo g, Phys ph, FdW<T> fd, const C2<T>* __restrict__ F0, const T* __restrict__ den,
+                     const T* __restrict__ dgx, const T* __restrict__ gy, const T* __restrict__ gz,
+                     T* __restrict__ pot4, T* __restrict__ ualphas, FftPlan p2, const C2<T>* __restrict__ twx,
+                     int nl) {
+  extern __shared__ __align__(16) unsigned char smraw[];
+  const int nx = g.nx, nxh = g.nxh;
+  XSmem<T> S(smraw, nl, nx);
+  const long long nlines = (long long)g.ny * g.nz;
+  const long long line0 = (long long)blockIdx.x * nl;
+  const int nlv = (int)min((long long)nl, nlines - line0);
+  for (int i = threadIdx.x; i < nx; i += blockDim.x) S.tw[i] = twx[i];
+  __syncthreads();
+  T* Ru = S.R;
+  x_inverse<T>(F0, line0, nlv, nl, nx, nxh, S.P, S.Q, S.ld, p2, S.tw, (T)ph.renor, Ru);
+  const T den0s = (T)ph.den0s, h2 = (T)ph.h2o2m4, al = (T)ph.alphas;
+  for (int e = threadIdx.x; e < nlv * nx; e += blockDim.x) {
+    const long long L = line0 + e / nx;
+    const long long p = line0 * nx + e;
+    const int iy = (int)(L % g.ny), iz = (int)(L / g.ny);
+    const T dyy = d1_global(gy, p, iy, g.ny, (long long)nx, fd.w1[1], fd.R, fd.periodic);
+    const T dzz = d1_global(gz, p, iz, g.nz, (long long)nx * g.ny, fd.w1[2], fd.R, fd.periodic);
+    const T ua = (((Ru[e] / den0s + dgx[p]) + dyy) + dzz) * h2 * al;
+    ualphas[p] = ua;
+    pot4[p] = (pot4[p] + ua) + penalty_of(ph, den[p]);
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Strided complex passes (Y and Z).
+template <class T>
+struct LSmem {
+  C2<T>* A;
+  C2<T>* B;
+  C2<T>* S;
+  C2<T>* tw;
+  long long* base;
+  int ld;
+};
+
+template <class T>
+EP_DEV LSmem<T> lsmem(unsigned char* raw, int LT, int n, int nbuf) {
+  LSmem<T> s;
+  s.ld = n + 1;
+  s.A = reinterpret_cast<C2<T>*>(raw);
+  s.B = s.A + LT * s.ld;
+  s.S = nbuf > 2 ? s.B + LT * s.ld : nullptr;
+  s.tw = s.B + (nbuf - 1) * LT * s.ld;
+  s.base = reinterpret_cast<long long*>(s.tw + n);
+  return s;
+}
+
+template <class T, int DIR>
+__global__ void k_c2c(Arr8<T> arr, LineSet ls, FftPlan p, const C2<T>* __restrict__ twg, int LT) {
+  extern __shared__ __align__(16) unsigned char smraw[];
+  const int n = p.n;
+  LSmem<T> s = lsmem<T>(smraw, LT, n, 2);
+  C2<T>* a = arr.a[blockIdx.y];
+  const long long L0 = (long long)blockIdx.x * LT;
+  for (int i = threadIdx.x; i < n; i += blockDim.x) s.tw[i] = twg[i];
+  for (int t = threadIdx.x; t < LT; t += blockDim.x) {
+    const long long L = L0 + t;
+    s.base[t] = L < ls.nlines ? (L % ls.Mi) + (L / ls.Mi) * ls.So : -1;
+  }
+  __syncthreads();
+  for (int e = threadIdx.x; e < LT * n; e += blockDim.x) {
+    const int k = e / LT, t = e - k * LT;
+    const long long b = s.base[t];
+    s.A[t * s.ld + k] = b >= 0 ? a[b + k * ls.Sa] : cmk<T>(T(0), T(0));
+  }
+  __syncthreads();
+  const C2<T>* r = epfft::lines<T, DIR>(s.A, s.B, LT, s.ld, p, s.tw, 1);
+  for (int e = threadIdx.x; e < LT * n; e += blockDim.x) {
+    const int k = e / LT, t = e - k * LT;
+    const long long b = s.base[t];
+    if (b >= 0) a[b + k * ls.Sa] = r[t * s.ld + k];
+  }
+}
+
+// Forward transform along the pass axis, then for each kernel table: multiply
+// (the k-space product of poten.f90:34-36,46-48,69-71,95-97 and
+// term_alfa.f90:172-176,203-205) and inverse transform.
+template <class T>
+__global__ void k_zconv(ConvSpec<T> cs, LineSet ls, FftPlan p, const C2<T>* __restrict__ twg, int LT) {
+  extern __shared__ __align__(16) unsigned char smraw[];
+  const int n = p.n;
+  LSmem<T> s = lsmem<T>(smraw, LT, n, 3);
+  const int which = blockIdx.y;
+  const C2<T>* in = cs.in[which];
+  const long long L0 = (long long)blockIdx.x * LT;
+  for (int i = threadIdx.x; i < n; i += blockDim.x) s.tw[i] = twg[i];
+  for (int t = threadIdx.x; t < LT; t += blockDim.x) {
+    const long long L = L0 + t;
+    s.base[t] = L < ls.nlines ? (L % ls.Mi) + (L / ls.Mi) * ls.So : -1;
+  }
+  __syncthreads();
+  for (int e = threadIdx.x; e < LT * n; e += blockDim.x) {
+    const int k = e / LT, t = e - k * LT;
+    const long long b = s.base[t];
+    s.A[t * s.ld + k] = b >= 0 ? in[b + k * ls.Sa] : cmk<T>(T(0), T(0));
+  }
+  __syncthreads();
+  C2<T>* r = epfft::lines<T, -1>(s.A, s.B, LT, s.ld, p, s.tw, 1);
+  C2<T>* o1 = (r == s.A) ? s.B : s.A;
+  C2<T>* o2 = s.S;
+  for (int j = 0; j < cs.nout[which]; ++j) {
+    const T* ker = cs.ker[which][j];
+    for (int e = threadIdx.x; e < LT * n; e += blockDim.x) {
+      const int k = e / LT, t = e - k * LT;
+      const long long b = s.base[t];
+      const T kv = b >= 0 ? ker[b + k * ls.Sa] : T(0);
+      const C2<T> v = r[t * s.ld + k];
+      o1[t * s.ld + k] = cmk<T>(v.x * kv, v.y * kv);
+    }
+    __syncthreads();
+    const C2<T>* q = epfft::lines<T, +1>(o1, o2, LT, s.ld, p, s.tw, 1);
+    C2<T>* out = cs.out[which][j];
+    for (int e = threadIdx.x; e < LT * n; e += blockDim.x) {
+      const int k = e / LT, t = e - k * LT;
+      const long long b = s.base[t];
+      if (b >= 0) out[b + k * ls.Sa] = q[t * s.ld + k];
+    }
+    __syncthreads();
+  }
+}
+
+// ---------------------------------------------------------------------------
+// 2.5-D stencil march: a (TX x TY) tile of (x,y) columns walks z; the x/y
+// neighbours of each plane come from a shared-memory tile with halo R, the
+// z neighbours from a per-thread register queue.  f(p, psi, lap) is called
+// for every grid point with lap = d2x + d2y + d2z (Deriv3D_pc,
+// init_deriv_parallel.f90:923-1197, summed as steppc.f90:53).
+#define EP_TX 32
+#define EP_TY 8
+
+template <class T, int R, class F>
+EP_DEV void lap_march(const Geo& g, const C2<T>* __restrict__ psi, const FdW<T>& fd, int zc, C2<T>* sp, F&& f) {
+  const int tx = threadIdx.x, ty = threadIdx.y;
+  const int x = blockIdx.x * EP_TX + tx, y = blockIdx.y * EP_TY + ty;
+  const int z0 = blockIdx.z * zc, z1 = min(z0 + zc, g.nz);
+  const bool valid = (x < g.nx) && (y < g.ny);
+  const int per = fd.periodic;
+  const long long sxy = (long long)g.nx * g.ny;
+  auto at = [&](int xx, int yy, int zz) -> C2<T> {
+    if (xx < 0 || xx >= g.nx || yy < 0 || yy >= g.ny || zz < 0 || zz >= g.nz) {
+      if (!per) return cmk<T>(T(0), T(0));
+      xx = wrapi(xx, g.nx); yy = wrapi(yy, g.ny); zz = wrapi(zz, g.nz);
+    }
+    return psi[xx + (long long)g.nx * yy + sxy * zz];
+  };
+  C2<T> q[2 * R + 1];
+#pragma unroll
+  for (int k = 0; k < 2 * R; ++k) q[k] = valid ? at(x, y, z0 - R + k) : cmk<T>(T(0), T(0));
+  const int W = EP_TX + 2 * R, H = EP_TY + 2 * R;
+  const int tid = ty * EP_TX + tx;
+  for (int z = z0; z < z1; ++z) {
+    q[2 * R] = valid ? at(x, y, z + R) : cmk<T>(T(0), T(0));
+    __syncthreads();
+    for (int e = tid; e < W * H; e += EP_TX * EP_TY) {
+      const int r = e / W, c = e - r * W;
+      sp[e] = at(blockIdx.x * EP_TX - R + c, blockIdx.y * EP_TY - R + r, z);
+    }
+    __syncthreads();
+    if (valid) {
+      const C2<T>* row = sp + (ty + R) * W + (tx + R);
+      const C2<T> c = q[R];
+      C2<T> lx = fd.w2[0][0] * c, ly = fd.w2[1][0] * c, lz = fd.w2[2][0] * c;
+#pragma unroll
+      for (int k = 1; k <= R; ++k) {
+        lx = lx + fd.w2[0][k] * (row[-k] + row[k]);
+        ly = ly + fd.w2[1][k] * (row[-k * W] + row[k * W]);
+        lz = lz + fd.w2[2][k] * (q[R - k] + q[R + k]);
+      }
+      f((long long)x + (long long)g.nx * y + sxy * z, c, (lx + ly) + lz);
+    }
+#pragma unroll
+    for (int k = 0; k < 2 * R; ++k) q[k] = q[k + 1];
+  }
+}
+
+// Predictor + modifier of steppc.f90:53-64.  The new psi is written over
+// psiold(ioldp(3)) (read here point-wise), so the host swaps buffers instead
+// of copying.
+template <class T, int R>
+__global__ void __launch_bounds__(EP_TX* EP_TY) k_predict(Geo g, FdW<T> fd, Phys ph, int zc,
+                                                         const C2<T>* __restrict__ psi, const T* __restrict__ pot4,
+                                                         const T* __restrict__ uimp, C2<T>* po3,
+                                                         const C2<T>* __restrict__ h1, C2<T>* h2, C2<T>* pc,
+                                                         T* __restrict__ den, T f, T c112) {
+  __shared__ C2<T> sp[(EP_TX + 2 * R) * (EP_TY + 2 * R)];
+  lap_march<T, R>(g, psi, fd, zc, sp, [&](long long p, C2<T> c, C2<T> lap) {
+    const C2<T> H = happly<T>(ph, lap, c, pot4[p], uimp[p]);
+    const C2<T> pp = po3[p] + f * ((T(2) * H - h1[p]) + T(2) * h2[p]);
+    const C2<T> pn = pp - c112 * pc[p];
+    po3[p] = pn;
+    pc[p] = pp;
+    h2[p] = H;
+    den[p] = pn.x * pn.x + pn.y * pn.y;
+  });
+}
+
+// Corrector + final value of steppc.f90:135-151 with fused reductions:
+// sum |pc|, sum |psi|^2 (new), <psi|H|psi> and sum |psi|^2 of the modified
+// psi (chemical potential).
+template <class T, int R>
+__global__ void __launch_bounds__(EP_TX* EP_TY) k_correct(Geo g, FdW<T> fd, Phys ph, int zc,
+                                                         const C2<T>* __restrict__ psi, const T* __restrict__ pot4,
+                                                         const T* __restrict__ uimp,
+                                                         const C2<T>* __restrict__ po3,
+                                                         const C2<T>* __restrict__ po2,
+                                                         const C2<T>* __restrict__ h1,
+                                                         const C2<T>* __restrict__ h2, C2<T>* pc,
+                                                         C2<T>* __restrict__ out, T* __restrict__ den, T f3, T c9,
+                                                         double* __restrict__ partials) {
+  __shared__ C2<T> sp[(EP_TX + 2 * R) * (EP_TY + 2 * R)];
+  double acc[4] = {0.0, 0.0, 0.0, 0.0};
+  lap_march<T, R>(g, psi, fd, zc, sp, [&](long long p, C2<T> c, C2<T> lap) {
+    const C2<T> H = happly<T>(ph, lap, c, pot4[p], uimp[p]);
+    const C2<T> p5 = T(0.125) * ((T(9) * po3[p] - po2[p]) + f3 * ((H + T(2) * h1[p]) - h2[p]));
+    const C2<T> pcn = pc[p] - p5;
+    pc[p] = pcn;
+    const C2<T> po = p5 + c9 * pcn;
+    out[p] = po;
+    const T dn = po.x * po.x + po.y * po.y;
+    den[p] = dn;
+    acc[0] += sqrt((double)pcn.x * pcn.x + (double)pcn.y * pcn.y);
+    acc[1] += (double)dn;
+    acc[2] += hexp<T>(ph, c, H);
+    acc[3] += (double)c.x * c.x + (double)c.y * c.y;
+  });
+  block_reduce_store<4>(acc, partials);
+}
+
+// One Runge-Kutta-Gill stage of steprk.f90:71-89 (jrun-independent part);
+// first stage also records H into hout (the history shift itself is done
+// by rotating buffers).  den <= 0 raises a flag (steprk.f90:94-110).
+template <class T, int R>
+__global__ void __launch_bounds__(EP_TX* EP_TY) k_rkstage(Geo g, FdW<T> fd, Phys ph, int zc,
+                                                         const C2<T>* __restrict__ psi, const T* __restrict__ pot4,
+                                                         const T* __restrict__ uimp, C2<T>* q,
+                                                         C2<T>* __restrict__ out, C2<T>* __restrict__ hout,
+                                                         T* __restrict__ den, T a, T b, T cr, T dt,
+                                                         DevScalars* sc) {
+  __shared__ C2<T> sp[(EP_TX + 2 * R) * (EP_TY + 2 * R)];
+  bool bad = false;
+  lap_march<T, R>(g, psi, fd, zc, sp, [&](long long p, C2<T> c, C2<T> lap) {
+    const C2<T> H = happly<T>(ph, lap, c, pot4[p], uimp[p]);
+    const C2<T> qq = q[p];
+    const C2<T> aux2 = a * (H - b * qq);
+    q[p] = (qq + T(3) * aux2) - cr * H;
+    if (hout) hout[p] = H;
+    const C2<T> pn = c + dt * aux2;
+    out[p] = pn;
+    const T dn = pn.x * pn.x + pn.y * pn.y;
+    den[p] = dn;
+    if (!(dn > T(0))) bad = true;
+  });
+  if (bad) atomicOr(&sc->flags, (unsigned)EP_FLAG_DEN_NONPOS);
+}
+
+// ---------------------------------------------------------------------------
+// Point-wise kernels.
+template <class T>
+__global__ void k_psi_to_den(const C2<T>* __restrict__ psi, T* __restrict__ den, long long N) {
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < N; i += (long long)gridDim.x * blockDim.x) {
+    const C2<T> v = psi[i];
+    den[i] = v.x * v.x + v.y * v.y;
+  }
+}
+
+// Imaginary-time renormalisation with the factor the finalize kernel left
+// in sc->scale.
+template <class T>
+__global__ void k_rescale(C2<T>* __restrict__ psi, T* __restrict__ den, long long N, const DevScalars* __restrict__ sc) {
+  const T s = (T)sc->scale;
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < N; i += (long long)gridDim.x * blockDim.x) {
+    C2<T> v = psi[i];
+    v.x *= s;
+    v.y *= s;
+    psi[i] = v;
+    den[i] = v.x * v.x + v.y * v.y;
+  }
+}
+
+// Sum of partials (fixed order, compensated) -> sc->sums[out0 + q].
+// mode 1: corrector epilogue (errHe, norm, mu, renormalisation factor).
+// mode 2: norm only (renormalisation factor).
+__global__ void k_finalize(const double* __restrict__ partials, int nblocks, int nq, DevScalars* sc, int out0,
+                           int mode, double N, double dxyz, double n4, int renorm);
+
+// Impurity field: updatepoten + potenimp P state (potenimp.f90:1-46,184-186,
+// 515-632).  Tables are FP64 (0..npot+1).
+template <class T>
+__global__ void k_potenimp(Geo g, double xmax, double ymax, double zmax, double hx, double hy, double hz,
+                           double r0, double r1, double r2, const double* __restrict__ potpi,
+                           const double* __restrict__ potdel, int npot, double rmax, double umax_sigma,
+                           double2 iv0, double2 iv1, double2 iv2, double2 iv3, double2 iv4, double2 iv5,
+                           T* __restrict__ vpi, T* __restrict__ delta, T* __restrict__ uimp);
+
+// Energy integrals of energy.f90:47-165 (8 sums, see the launcher).
+struct PotDev {
+  int kind;
+  double r_cutoff, umax, p0, p1, p2;
+};
+template <class T>
+__global__ void k_energy(Geo g, FdW<T> fd, Phys ph, const C2<T>* __restrict__ psi, const T* __restrict__ den,
+                         const T* __restrict__ dencg, const T* __restrict__ delj4, const T* __restrict__ falfs,
+                         const T* __restrict__ dxd, const T* __restrict__ dyd, const T* __restrict__ dzd,
+                         const T* __restrict__ ix, const T* __restrict__ iy, const T* __restrict__ iz,
+                         const T* __restrict__ uimp, double xmax, double ymax, double zmax, double hx, double hy,
+                         double hz, double r0, double r1, double r2, double zexc, PotDev vplus, int impurity,
+                         double* __restrict__ partials);
+
+// forceimp / potinvar moments (potenimp.f90:193-258, 298-317).
+template <class T>
+__global__ void k_impmoments(Geo g, const T* __restrict__ den, const T* __restrict__ dxd,
+                             const T* __restrict__ dyd, const T* __restrict__ dzd, const T* __restrict__ uimp,
+                             const T* __restrict__ vpi, const T* __restrict__ delta, double xmax, double ymax,
+                             double zmax, double hx, double hy, double hz, double r0, double r1, double r2,
+                             double* __restrict__ partials);
+
+// Form factors on the device (fforma.f90:11-60, initcg.f90:314-331,
+// DFT4He3d.f90:396-400), FP64 evaluation, stored in T.
+template <class T>
+__global__ void k_formfactors(Geo g, const double* __restrict__ px, const double* __restrict__ py,
+                              const double* __restrict__ pz, int core, double h4, double eps, double sigma,
+                              double bforce, double l, T* __restrict__ fvlj, T* __restrict__ wcgk,
+                              T* __restrict__ kalfs);
+
+// Precision conversion of a state array.
+template <class B, class A> EP_HD B conv(A a) { return (B)a; }
+template <> EP_HD float2 conv<float2, double2>(double2 a) { return make_float2((float)a.x, (float)a.y); }
+template <> EP_HD double2 conv<double2, float2>(float2 a) { return make_double2(a.x, a.y); }
+template <> EP_HD double2 conv<double2, double2>(double2 a) { return a; }
+template <> EP_HD float2 conv<float2, float2>(float2 a) { return a; }
+template <class A, class B>
+__global__ void k_convert(const A* __restrict__ in, B* __restrict__ out, long long n) {
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
+    out[i] = conv<B, A>(in[i]);
+}

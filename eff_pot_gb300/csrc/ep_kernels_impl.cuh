@@ -1,0 +1,290 @@
+// ep_kernels_impl.cuh - bodies of the point-wise and reduction kernels.
+#pragma once
+#include "ep_kernels.cuh"
+
+// Grid coordinate -xmax + h*i without contraction (x(i) of DFT4He3d.f90:248-256).
+EP_DEV double coord(double xmax, double h, int i) { return __dadd_rn(-xmax, __dmul_rn(h, (double)i)); }
+
+EP_DEV void idx3(const Geo& g, long long p, int& ix, int& iy, int& iz) {
+  ix = (int)(p % g.nx);
+  const long long r = p / g.nx;
+  iy = (int)(r % g.ny);
+  iz = (int)(r / g.ny);
+}
+
+// Parabolic interpolation in f(0:nint+1), the update() function of
+// potenimp.f90:588-632, restated.
+EP_DEV double interp_update(double r, int nint, double rmax, const double* __restrict__ f) {
+  const double h = rmax / (nint - 1);
+  const double c1oh = 1.0 / h;
+  const double c1o2h2 = c1oh * c1oh * 0.5;
+  int i0 = (int)(1.5 + r / h);
+  i0 = min(max(i0, 1), nint);
+  const double r0 = (i0 - 1) * h;
+  const double f0 = f[i0];
+  const bool lo = r < r0;
+  const double f1 = f[lo ? i0 - 1 : i0 + 1];
+  const double f2 = f[lo ? i0 + 1 : i0 - 1];
+  const double aa = (f2 - 2.0 * f0 + f1) * c1o2h2;
+  const double bb = ((lo ? f2 : f1) - f0) * c1oh - aa * (2.0 * r0 + h);
+  const double cc = f0 - r0 * (bb + r0 * aa);
+  return r * (aa * r + bb) + cc;
+}
+
+// Pair potential of the U+ integral (Select_Pot subset + Morse).
+EP_DEV double pot_eval(const PotDev& v, double r) {
+  if (v.kind == 0) return 0.0;
+  if (r < v.r_cutoff) return v.umax;
+  const double e = exp(-v.p2 * (r - v.p1));
+  return v.p0 * (e * e - 2.0 * e);
+}
+
+template <class T>
+__global__ void k_potenimp(Geo g, double xmax, double ymax, double zmax, double hx, double hy, double hz,
+                           double r0, double r1, double r2, const double* __restrict__ potpi,
+                           const double* __restrict__ potdel, int npot, double rmax, double umax_sigma,
+                           double2 iv0, double2 iv1, double2 iv2, double2 iv3, double2 iv4, double2 iv5,
+                           T* __restrict__ vpi, T* __restrict__ delta, T* __restrict__ uimp) {
+  for (long long p = blockIdx.x * (long long)blockDim.x + threadIdx.x; p < g.N; p += (long long)gridDim.x * blockDim.x) {
+    int ix, iy, iz;
+    idx3(g, p, ix, iy, iz);
+    const double xx = coord(xmax, hx, ix) - r0;
+    const double yy = coord(ymax, hy, iy) - r1;
+    const double zz = coord(zmax, hz, iz) - r2;
+    const double zt = zz * zz;
+    const double yt = yy * yy + zt;
+    const double rr2 = xx * xx + yt;
+    const double r = sqrt(rr2);
+    const double vp = interp_update(r, npot, rmax, potpi);
+    const double dl = r > 1e-3 ? interp_update(r, npot, rmax, potdel) / rr2 : umax_sigma;
+    const double ox = iv0.x * xx + iv2.x * yy + iv4.x * zz, oy = iv0.y * xx + iv2.y * yy + iv4.y * zz;
+    const double ex = iv1.x * xx + iv3.x * yy + iv5.x * zz, ey = iv1.y * xx + iv3.y * yy + iv5.y * zz;
+    const double u = vp + dl * ((ox * ox + oy * oy) + (ex * ex + ey * ey));
+    vpi[p] = (T)vp;
+    delta[p] = (T)dl;
+    uimp[p] = (T)fmin(u, 1000.0);
+  }
+}
+
+// Sum of |psi|^2 (block partials).
+template <class T>
+__global__ void k_normsum(const C2<T>* __restrict__ psi, long long N, double* __restrict__ partials) {
+  double acc[1] = {0.0};
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < N; i += (long long)gridDim.x * blockDim.x) {
+    const C2<T> v = psi[i];
+    acc[0] += (double)v.x * v.x + (double)v.y * v.y;
+  }
+  block_reduce_store<1>(acc, partials);
+}
+
+// Complex first derivative from global memory.
+template <class T>
+EP_DEV C2<T> d1c_global(const C2<T>* __restrict__ f, long long p, int i, int n, long long st, const T* w, int R,
+                        int periodic) {
+  C2<T> s = cmk<T>(T(0), T(0));
+  for (int k = 1; k <= R; ++k) {
+    int ip = i + k, im = i - k;
+    C2<T> fp, fm;
+    if (ip >= n) fp = periodic ? f[p + (long long)(ip - n - i) * st] : cmk<T>(T(0), T(0));
+    else fp = f[p + (long long)k * st];
+    if (im < 0) fm = periodic ? f[p + (long long)(im + n - i) * st] : cmk<T>(T(0), T(0));
+    else fm = f[p - (long long)k * st];
+    s = s + w[k] * (fp - fm);
+  }
+  return s;
+}
+
+template <class T>
+__global__ void k_energy(Geo g, FdW<T> fd, Phys ph, const C2<T>* __restrict__ psi, const T* __restrict__ den,
+                         const T* __restrict__ dencg, const T* __restrict__ delj4, const T* __restrict__ falfs,
+                         const T* __restrict__ dxd, const T* __restrict__ dyd, const T* __restrict__ dzd,
+                         const T* __restrict__ ix_, const T* __restrict__ iy_, const T* __restrict__ iz_,
+                         const T* __restrict__ uimp, double xmax, double ymax, double zmax, double hx, double hy,
+                         double hz, double r0, double r1, double r2, double zexc, PotDev vplus, int impurity,
+                         double* __restrict__ partials) {
+  double acc[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+  const bool otc = ph.core == 1;
+  const double aux1 = 0.5 * ph.cp4, aux2 = (1.0 / 3.0) * ph.cpp4;
+  for (long long p = blockIdx.x * (long long)blockDim.x + threadIdx.x; p < g.N; p += (long long)gridDim.x * blockDim.x) {
+    int ix, iy, iz;
+    idx3(g, p, ix, iy, iz);
+    const C2<T> dx = d1c_global(psi, p, ix, g.nx, 1, fd.w1[0], fd.R, fd.periodic);
+    const C2<T> dy = d1c_global(psi, p, iy, g.ny, (long long)g.nx, fd.w1[1], fd.R, fd.periodic);
+    const C2<T> dz = d1c_global(psi, p, iz, g.nz, (long long)g.nx * g.ny, fd.w1[2], fd.R, fd.periodic);
+    const double dn = den[p], cg = dencg[p];
+    acc[0] += ((double)dx.x * dx.x + (double)dx.y * dx.y) + ((double)dy.x * dy.x + (double)dy.y * dy.y) +
+              ((double)dz.x * dz.x + (double)dz.y * dz.y);
+    acc[1] += (double)delj4[p] * dn;
+    acc[2] += dn * (cg * cg) * (aux1 + aux2 * cg);
+    if (otc)
+      acc[3] += (double)falfs[p] * ((double)dxd[p] * ix_[p] + (double)dyd[p] * iy_[p] + (double)dzd[p] * iz_[p]);
+    acc[4] += dn * (1.0 + tanh(ph.beta * (dn - ph.den_m)));
+    if (impurity) {
+      const double a = r0 - coord(xmax, hx, ix), b = r1 - coord(ymax, hy, iy), c = r2 - coord(zmax, hz, iz);
+      const double r = sqrt(a * a + b * b + c * c);
+      if (r >= zexc) {
+        acc[5] += dn * (double)uimp[p];
+        acc[6] += dn * pot_eval(vplus, r);
+      }
+    }
+    acc[7] += dn;
+  }
+  block_reduce_store<8>(acc, partials);
+}
+
+template <class T>
+__global__ void k_impmoments(Geo g, const T* __restrict__ den, const T* __restrict__ dxd,
+                             const T* __restrict__ dyd, const T* __restrict__ dzd, const T* __restrict__ uimp,
+                             const T* __restrict__ vpi, const T* __restrict__ delta, double xmax, double ymax,
+                             double zmax, double hx, double hy, double hz, double r0, double r1, double r2,
+                             double* __restrict__ partials) {
+  double acc[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
+  for (long long p = blockIdx.x * (long long)blockDim.x + threadIdx.x; p < g.N; p += (long long)gridDim.x * blockDim.x) {
+    int ix, iy, iz;
+    idx3(g, p, ix, iy, iz);
+    const double u = uimp[p];
+    acc[0] += (double)dxd[p] * u;
+    acc[1] += (double)dyd[p] * u;
+    acc[2] += (double)dzd[p] * u;
+    const double xx = coord(xmax, hx, ix) - r0, yy = coord(ymax, hy, iy) - r1, zz = coord(zmax, hz, iz) - r2;
+    const double a1 = den[p], a2 = delta[p], a3 = vpi[p];
+    acc[3] += a1 * (a2 * xx * xx + a3);
+    acc[4] += a1 * a2 * xx * yy;
+    acc[5] += a1 * a2 * xx * zz;
+    acc[6] += a1 * (a2 * yy * yy + a3);
+    acc[7] += a1 * a2 * yy * zz;
+    acc[8] += a1 * (a2 * zz * zz + a3);
+  }
+  block_reduce_store<9>(acc, partials);
+}
+
+// ---------------------------------------------------------------------------
+// Sine integral Si(x): power series for |x| <= 4, else the continued fraction
+// of E1(ix) by the modified Lentz method (Numerical Recipes 6.9).
+EP_DEV double si_dev(double x) {
+  const double ax = fabs(x);
+  double r;
+  if (ax <= 4.0) {
+    double term = ax, sum = ax;
+    const double x2 = ax * ax;
+    for (int k = 1; k < 60; ++k) {
+      term *= -x2 / ((2.0 * k) * (2.0 * k + 1.0));
+      const double t = term / (2.0 * k + 1.0);
+      sum += t;
+      if (fabs(t) < 1e-18 * fabs(sum)) break;
+    }
+    r = sum;
+  } else {
+    double br = 1.0, bi = ax, cr = 1e300, ci = 0.0;
+    double den = br * br + bi * bi;
+    double dr = br / den, di = -bi / den;
+    double hr = dr, hi = di;
+    for (int i = 2; i < 1000; ++i) {
+      const double a = -(double)(i - 1) * (double)(i - 1);
+      br += 2.0;
+      // d = 1/(a*d + b)
+      const double tr = a * dr + br, ti = a * di + bi;
+      den = tr * tr + ti * ti;
+      dr = tr / den;
+      di = -ti / den;
+      // c = b + a/c
+      const double cd = cr * cr + ci * ci;
+      const double ncr = br + a * cr / cd, nci = bi - a * ci / cd;
+      cr = ncr;
+      ci = nci;
+      const double er = cr * dr - ci * di, ei = cr * di + ci * dr;
+      const double nhr = hr * er - hi * ei, nhi = hr * ei + hi * er;
+      hr = nhr;
+      hi = nhi;
+      if (fabs(er - 1.0) + fabs(ei) < 3e-16) break;
+    }
+    double s, c;
+    sincos(ax, &s, &c);
+    // h *= (cos x - i sin x)
+    const double fi = hi * c - hr * s;
+    r = 1.5707963267948966192313216916397514 + fi;
+  }
+  return x < 0 ? -r : r;
+}
+
+EP_DEV double ipow(double x, int n) {
+  double r = 1.0;
+  for (int i = 0; i < n; ++i) r *= x;
+  return r;
+}
+
+// Integral of sin(a t)/t^11 and sin(a t)/t^5 from x to infinity, closed forms
+// of fforma.f90:73-137 (integration by parts down to Si).
+EP_DEV double sinint_tail(double a, double x) {
+  const double res = si_dev(a * x);
+  return a > 0.0 ? 1.5707963267948966192313216916397514 - res : 1.5707963267948966192313216916397514 + res;
+}
+EP_DEV double sinx11_dev(double a, double x) {
+  const double y = a * x, y2 = y * y;
+  const double bd = 40320.0 - 720.0 * y2 + 24.0 * (y2 * y2) - 2.0 * (y2 * y2 * y2) + (y2 * y2 * y2 * y2);
+  const double cd = 362880.0 - 5040.0 * y2 + 120.0 * (y2 * y2) - 6.0 * (y2 * y2 * y2) + (y2 * y2 * y2 * y2);
+  double s, c;
+  sincos(y, &s, &c);
+  const double res1 = (a * bd * c + cd * s / x) / (3628800.0 * ipow(x, 9));
+  const double res2 = -(ipow(a, 10) * sinint_tail(a, x)) / 3628800.0;
+  return res1 + res2;
+}
+EP_DEV double sinx5_dev(double a, double x) {
+  const double y = a * x, y2 = y * y;
+  double s, c;
+  sincos(y, &s, &c);
+  const double res1 = -(a * (-2.0 + y2) * c + (-6.0 + y2) * s / x) / (24.0 * x * x * x);
+  const double res2 = (ipow(a, 4) * sinint_tail(a, x)) / 24.0;
+  return res1 + res2;
+}
+EP_DEV double intcore_dev(double a, double x) {
+  const double y = a * x, y2 = y * y;
+  const double d0 = x / ipow(a, 5), e0 = 1.0 / ipow(a, 6);
+  const double bd = -120.0 * d0 + 20.0 * (d0 * y2) - (d0 * y2 * y2);
+  const double ce = 120.0 * e0 - 60.0 * (e0 * y2) + 5.0 * (e0 * y2 * y2);
+  double s, c;
+  sincos(y, &s, &c);
+  return bd * c + ce * s;
+}
+
+template <class T>
+__global__ void k_formfactors(Geo g, const double* __restrict__ px, const double* __restrict__ py,
+                              const double* __restrict__ pz, int core, double h4, double eps, double sigma,
+                              double bforce, double l, T* __restrict__ fvlj, T* __restrict__ wcgk,
+                              T* __restrict__ kalfs) {
+  const double pi = 3.14159265358979323846264338327950288;
+  const double twopi = 2.0 * pi;
+  const double sigma6 = ipow(sigma, 6), aux1 = 8.0 * eps, aux3 = sigma6 / ipow(h4, 6);
+  for (long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x; q < g.Nh; q += (long long)gridDim.x * blockDim.x) {
+    const int ipx = (int)(q % g.nxh);
+    const long long r = q / g.nxh;
+    const int ipy = (int)(r % g.ny), ipz = (int)(r / g.ny);
+    const double a = px[ipx], b = py[ipy], c = pz[ipz];
+    const double p = sqrt(__dadd_rn(__dadd_rn(__dmul_rn(a, a), __dmul_rn(b, b)), __dmul_rn(c, c)));
+    double fv;
+    if (fabs(p) < 1e-10) {
+      fv = bforce;
+    } else {
+      const double a2 = twopi * p;
+      const double t1 = sinx11_dev(a2, h4), t2 = sinx5_dev(a2, h4);
+      if (core == 2) {
+        const double v0 = aux1 * aux3 * (aux3 - 1.0) / ipow(h4, 4);
+        fv = (aux1 * sigma6 * (sigma6 * t1 - t2) + v0 * intcore_dev(a2, h4)) / p;
+      } else {
+        fv = (aux1 * sigma6 * (sigma6 * t1 - t2)) / p;
+      }
+    }
+    double wc = 1.0;
+    if (p > 0.0) {
+      const double arg = twopi * p * h4;
+      double s, cc;
+      sincos(arg, &s, &cc);
+      const double aux = s - arg * cc;
+      wc = fabs(aux) < 1e-10 ? 1.0 : 3.0 * aux / (arg * arg * arg);
+    }
+    const double t = pi * l * p;
+    fvlj[q] = (T)fv;
+    wcgk[q] = (T)wc;
+    kalfs[q] = (T)exp(-(t * t));
+  }
+}

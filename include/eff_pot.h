@@ -1,0 +1,203 @@
+/*
+ * eff_pot.h - C ABI of the GB300-native Orsay-Trento helium order-parameter
+ * time-evolution hot path (libeffpot.so).
+ *
+ * The reference program keeps all state in Fortran modules and calls
+ * argument-light external subroutines.  This ABI replaces those subroutines
+ * one for one behind an opaque solver context; every array lives in HBM and
+ * is owned by the context.  Host pointers passed in are borrowed for the
+ * duration of the call only.  Arrays are column-major (x fastest), exactly
+ * the Fortran layout (nx,ny,nz); complex arrays are interleaved (re,im)
+ * doubles, i.e. Fortran complex(kind=8) / C double _Complex.
+ *
+ * Every entry point returns an ep_status; none aborts or traps.  The text of
+ * the last failure is available from ep_last_error().
+ */
+#ifndef EFF_POT_H
+#define EFF_POT_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes (the reference STOPs instead) ------------------------ */
+typedef enum ep_status {
+  EP_OK = 0,
+  EP_ERR_INVALID_ARG = 1,   /* bad pointer / value                         */
+  EP_ERR_BAD_GRID = 2,      /* grid size not a product of 2,3,5 or odd     */
+  EP_ERR_CUDA = 3,          /* CUDA runtime error                          */
+  EP_ERR_OOM = 4,           /* device allocation failed                    */
+  EP_ERR_NONFINITE = 5,     /* NaN / Inf / non-positive density detected   */
+  EP_ERR_STATE = 6,         /* call made in the wrong order                */
+  EP_ERR_NO_DEVICE = 7,     /* no CUDA device visible                      */
+  EP_ERR_UNSUPPORTED = 8,   /* option not built                            */
+  EP_ERR_TIMEOUT = 9        /* a bounded device wait ran out               */
+} ep_status;
+
+/* ---- functional cores (DFT4He3d.f90:346-363) --------------------------- */
+enum { EP_CORE_OT = 0, EP_CORE_OTC = 1, EP_CORE_OP = 2 };
+/* ---- evolution kind: timec = 1 (imaginary) or i (real) ----------------- */
+enum { EP_IMAGINARY_TIME = 0, EP_REAL_TIME = 1 };
+/* ---- impurity treatment ------------------------------------------------- */
+enum { EP_IMPURITY_NONE = 0, EP_IMPURITY_FIXED = 1, EP_IMPURITY_MOVING = 2 };
+/* ---- arithmetic of the bulk field updates ------------------------------ */
+enum { EP_FP64 = 0, EP_FP32 = 1 };
+/* ---- boundary modes of the finite differences (newder.f ICON) ---------- */
+enum { EP_ICON_PERIODIC = 8, EP_ICON_ZERO_OUTSIDE = 13 };
+
+/*
+ * Solver configuration.  ep_config_init() fills every field with the
+ * defaults of the reference modules (modules.f90:15-19,116-135,187-199;
+ * V_impur.f90:1-16; DFT4He3d.f90 namelist defaults).
+ */
+typedef struct ep_config {
+  int nx, ny, nz;            /* grid points (even, factors 2,3,5)           */
+  double xmax, ymax, zmax;   /* box half-widths, x(i) = -xmax + hx*(i-1)    */
+  int npd;                   /* FD stencil points, odd 3..25 (default 13)   */
+  int icon;                  /* EP_ICON_PERIODIC or EP_ICON_ZERO_OUTSIDE    */
+  int core;                  /* EP_CORE_*                                   */
+  /* Orsay-Trento functional (module he4 / lenard4)                         */
+  double cp4, cpp4, den4c, alphas, l, den0s, h2o2m4;
+  double C, beta, den_m;     /* solid penalty                               */
+  double h4ot, h4op, eps4, sigma4, b4;
+  /* evolution                                                              */
+  int time_mode;             /* EP_IMAGINARY_TIME / EP_REAL_TIME            */
+  int renormalize;           /* imaginary time: rescale psi to n4 per step  */
+  double n4;                 /* number of helium atoms                      */
+  /* classical impurity (module classicimp)                                 */
+  int impurity;              /* EP_IMPURITY_*                               */
+  double mimpur;             /* impurity mass in u (mAg_u = mimpur*mp_u)    */
+  int fix_lambda;            /* Lfix_lambda: freeze the internal variables  */
+  double als_p;              /* spin-orbit splitting, P state               */
+  double ev0;                /* phase reference of potinvar                 */
+  double z_exciplex_exclusion;
+  int precision;             /* EP_FP64 / EP_FP32                           */
+  int device;                /* CUDA device ordinal                         */
+} ep_config;
+
+/* Pair potentials (a subset of the Select_Pot registry, V_impur.f90:87-932,
+ * plus the Morse selector this project adds).  r < r_cutoff -> umax.       */
+enum { EP_POT_NULL = 0, EP_POT_MORSE = 1 };
+typedef struct ep_potential {
+  int kind;                  /* EP_POT_*                                    */
+  double r_cutoff, umax;
+  double par[4];             /* Morse: De (K), re (A), alpha (1/A)          */
+} ep_potential;
+
+/* Energies printed by DFT4He3d.f90:460-463 (module energies). */
+typedef struct ep_energies {
+  double etot, etot4, ekin4, elj4, ecor4, ealphas, esolid;
+  double eimpu, ekinx, eHeX, uplus, eso;
+  double n4;                 /* integral of the density                    */
+} ep_energies;
+
+/* Per-call diagnostics of one predictor-corrector step (steppc.f90:1). */
+typedef struct ep_step_errors {
+  double errHe, errimp, errvimp, erriv;
+} ep_step_errors;
+
+/* Statistics of ep_run (the time loop this project adds). */
+typedef struct ep_run_stats {
+  double errHe;              /* last step                                   */
+  double mu;                 /* <psi|H|psi>/N of the last corrector         */
+  double norm;               /* integral |psi|^2 before renormalisation     */
+  int steps_done;
+} ep_run_stats;
+
+/* Field identifiers for ep_download_field. */
+enum {
+  EP_FIELD_DEN = 0, EP_FIELD_POT4 = 1, EP_FIELD_UIMP = 2, EP_FIELD_DENCG = 3,
+  EP_FIELD_DELJ4 = 4, EP_FIELD_DXDEN = 5, EP_FIELD_DYDEN = 6, EP_FIELD_DZDEN = 7,
+  EP_FIELD_FALFS = 8, EP_FIELD_INTXALF = 9, EP_FIELD_INTYALF = 10,
+  EP_FIELD_INTZALF = 11, EP_FIELD_UALPHAS = 12, EP_FIELD_VPI = 13,
+  EP_FIELD_DELTA = 14, EP_FIELD_COUNT = 15
+};
+/* Complex-field identifiers for ep_download_cfield. */
+enum {
+  EP_CFIELD_PSI = 0, EP_CFIELD_PSIOLD1 = 1, EP_CFIELD_PSIOLD2 = 2,
+  EP_CFIELD_PSIOLD3 = 3, EP_CFIELD_HPSIOLD1 = 4, EP_CFIELD_HPSIOLD2 = 5,
+  EP_CFIELD_PC = 6, EP_CFIELD_Q = 7
+};
+
+typedef struct ep_ctx ep_ctx;
+
+/* Defaults of the reference modules. */
+int ep_config_init(ep_config* cfg);
+
+/* Replaces dimen() + fftini() + fforma() + initcg() + kalfs + Init_deriv_p
+ * (dimen.f90:8, fft.f90:233, fforma.f90:11, initcg.f90:5,
+ * DFT4He3d.f90:170,396-400).  Grid validity replaces tstgrid (widened to any
+ * even size whose prime factors are 2, 3 and 5). */
+int ep_create(const ep_config* cfg, ep_ctx** out);
+int ep_destroy(ep_ctx* ctx);
+const char* ep_last_error(const ep_ctx* ctx);
+/* Text of the last ep_create failure (no context exists yet). */
+const char* ep_create_error(void);
+
+/* Impurity pair potentials; builds the 1-D tables of potenimpini
+ * (potenimpini.f90:1-72).  plus = selec_plus used for U+ in energy(). */
+int ep_set_impurity_potentials(ep_ctx* ctx, const ep_potential* pi,
+                               const ep_potential* sigma,
+                               const ep_potential* plus);
+/* Raw tables potpi(0:npot+1), potdel(0:npot+1) with spacing delinter, for
+ * callers that tabulate Select_Pot themselves (interpol module). */
+int ep_set_impurity_tables(ep_ctx* ctx, const double* potpi,
+                           const double* potdel, int npot, double delinter,
+                           double umax_sigma);
+/* rimp(3), vimp(3) (A, A*K), invar(10) complex as 20 doubles. */
+int ep_set_impurity_state(ep_ctx* ctx, const double* rimp, const double* vimp,
+                          const double* invar);
+int ep_get_impurity_state(ep_ctx* ctx, double* rimp, double* vimp,
+                          double* aimp, double* invar);
+
+/* psi in, den = |psi|^2 (readenc.f90:104-105, DFT4He3d.f90:436). */
+int ep_upload_psi(ep_ctx* ctx, const double* psi);
+int ep_download_psi(ep_ctx* ctx, double* psi);
+int ep_download_cfield(ep_ctx* ctx, int which, double* out);
+int ep_download_field(ep_ctx* ctx, int which, double* out);
+
+/* potenimp(rimp,invar) incl. updatepoten (potenimp.f90:1-189,515-632). */
+int ep_potenimp(ep_ctx* ctx);
+/* poten() incl. derden() and term_alfa() (poten.f90:5, term_alfa.f90:5). */
+int ep_poten(ep_ctx* ctx);
+/* energy() (energy.f90:12-202), eHeX/uplus accumulators zeroed. */
+int ep_energy(ep_ctx* ctx, ep_energies* e);
+/* forceimp(rimp,F) (potenimp.f90:193-258). */
+int ep_forceimp(ep_ctx* ctx, double* F);
+/* potinvar(rimp,invar,Hinvar), P state (potenimp.f90:261-492). */
+int ep_potinvar(ep_ctx* ctx, double* hinvar);
+
+/* steprk(deltat) (steprk.f90:1-191). */
+int ep_steprk(ep_ctx* ctx, double deltat);
+/* steppc(deltat,errHe,errimp,errvimp,erriv) (steppc.f90:1-230).  err may be
+ * NULL, in which case the call does not wait for the device. */
+int ep_steppc(ep_ctx* ctx, double deltat, ep_step_errors* err);
+/* Time loop: nsteps steppc calls with imaginary-time renormalisation as
+ * configured; stats may be NULL (no device wait). */
+int ep_run(ep_ctx* ctx, int nsteps, double deltat, ep_run_stats* stats);
+/* Renormalise psi to n4 now (imaginary time). */
+int ep_renormalize(ep_ctx* ctx, double* norm_before);
+
+/* Device synchronisation, timing and counters. */
+int ep_synchronize(ep_ctx* ctx);
+/* The CUDA stream all work of this context is launched on (cudaStream_t). */
+void* ep_stream(ep_ctx* ctx);
+/* Events on the context stream for device-side timing: record into one of
+ * 16 slots; elapsed ms between two recorded slots (waits for the second). */
+int ep_event_record(ep_ctx* ctx, int slot);
+int ep_event_elapsed(ep_ctx* ctx, int slot_a, int slot_b, double* ms);
+/* Kernel launches made by this context since creation. */
+long long ep_kernel_launches(const ep_ctx* ctx);
+/* Per-kernel-class event timing of every launch made while enabled. */
+int ep_profile_enable(ep_ctx* ctx, int on);
+/* Fills names (NUL-separated, cap bytes), per-class total ms and launch
+ * counts; returns the number of classes in *n. */
+int ep_profile_read(ep_ctx* ctx, char* names, int cap, double* ms,
+                    long long* launches, int maxn, int* n);
+/* Bytes of device memory held by the context. */
+long long ep_device_bytes(const ep_ctx* ctx);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* EFF_POT_H */

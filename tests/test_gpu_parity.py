@@ -1,0 +1,168 @@
+"""CUDA path against the CPU FP64 oracle on the same seeded inputs.
+
+Tolerances: the FP64 path computes in the same arithmetic as the oracle but
+with a different FFT, stencil summation order and FMA contraction, so fields
+agree to ~1e-13 relative and energies to ~1e-12; the gates below are
+1e-11 (fields), 1e-10 (energies and chemical potential, the drop-in bar)
+and 1e-9 A^-3 max-abs in the density.  The FP32 path is gated at 1e-5
+relative on energies of one field refresh.
+"""
+import numpy as np
+import pytest
+
+import eff_pot_gb300 as ep
+from eff_pot_gb300 import _abi
+from eff_pot_gb300.build import build
+
+pytestmark = pytest.mark.gpu
+
+FIELDS_ALL = ["den", "pot4", "dencg", "delj4", "dxden", "dyden", "dzden", "falfs",
+              "intxalf", "intyalf", "intzalf", "ualphas", "uimp"]
+
+
+@pytest.fixture(scope="module", autouse=True)
+def _lib():
+    build()
+    ep.load_library()
+
+
+def rel(a, b):
+    d = np.max(np.abs(np.asarray(a) - np.asarray(b)))
+    s = np.max(np.abs(np.asarray(b)))
+    return d / s if s > 0 else d
+
+
+def droplet_case(n=32, xmax=16.0, n4=200.0, seed=3, **kw):
+    base = dict(nx=n, ny=n, nz=n, xmax=xmax, ymax=xmax, zmax=xmax, icon=_abi.EP_ICON_PERIODIC,
+                core="OTC", n4=n4, impurity=_abi.EP_IMPURITY_FIXED)
+    base.update(kw)
+    cfg = ep.make_config(**base)
+    psi = ep.woods_saxon_psi(cfg.nx, cfg.ny, cfg.nz, cfg.xmax, cfg.ymax, cfg.zmax, n4, seed=seed)
+    return cfg, psi
+
+
+def pair(cfg, psi, rimp=(0.3, -0.2, 0.7), vimp=(0.0, 0.0, 0.0), oracle=None):
+    g = ep.Solver(cfg)
+    o = oracle.OracleSolver(cfg)
+    pot = ep.morse(10.0, 4.5, 1.2, r_cutoff=0.0, umax=1000.0)
+    plus = ep.morse(12.0, 4.0, 1.1)
+    inv = np.zeros(10, dtype=np.complex128)
+    inv[0] = 1.0
+    for s in (g, o):
+        s.set_impurity_potentials(pot, pot, plus)
+        s.set_impurity(rimp=rimp, vimp=vimp, invar=inv)
+        s.start(psi)
+    return g, o
+
+
+@pytest.mark.parametrize("core,icon", [("OTC", 8), ("OT ", 8), ("OTC", 13), ("OP ", 13)])
+def test_poten_fields_match_oracle(oracle, core, icon):
+    cfg, psi = droplet_case(core=core, icon=icon)
+    g, o = pair(cfg, psi, oracle=oracle)
+    with g, o:
+        names = FIELDS_ALL if core == "OTC" else ["den", "pot4", "dencg", "delj4", "uimp"]
+        for f in names:
+            r = rel(g.field(f), o.field(f))
+            assert r < 1e-11, (f, r)
+
+
+def test_energy_matches_oracle(oracle):
+    cfg, psi = droplet_case()
+    g, o = pair(cfg, psi, oracle=oracle)
+    with g, o:
+        eg, eo = g.energy(), o.energy()
+        for k in eo:
+            tol = 1e-10 * max(1.0, abs(eo[k]))
+            assert abs(eg[k] - eo[k]) <= tol, (k, eg[k], eo[k])
+        assert eo["eHeX"] < 0 and eo["uplus"] != 0
+
+
+def test_potenimp_impurity_tables_and_moments(oracle):
+    cfg, psi = droplet_case(impurity=_abi.EP_IMPURITY_FIXED)
+    g, o = pair(cfg, psi, rimp=(1.13, -2.71, 0.05), oracle=oracle)
+    with g, o:
+        for f in ("uimp", "vpi", "delta"):
+            assert rel(g.field(f), o.field(f)) < 1e-13, f
+        assert rel(g.forceimp(), o.forceimp()) < 1e-10
+        assert rel(g.potinvar(), o.potinvar()) < 1e-10
+
+
+@pytest.mark.parametrize("icon", [8, 13])
+def test_rk_then_pc_imaginary_time_match_oracle(oracle, icon):
+    cfg, psi = droplet_case(icon=icon)
+    g, o = pair(cfg, psi, oracle=oracle)
+    dt = 2e-3
+    with g, o:
+        for _ in range(3):
+            g.steprk(dt)
+            o.steprk(dt)
+        assert rel(g.psi(), o.psi()) < 1e-11
+        for name in ("psiold1", "psiold2", "psiold3", "hpsiold1", "hpsiold2", "q"):
+            assert rel(g.cfield(name), o.cfield(name)) < 1e-11, name
+        sg = g.run(12, dt)
+        so = o.run(12, dt)
+        assert rel(g.psi(), o.psi()) < 1e-10
+        assert np.max(np.abs(g.field("den") - o.field("den"))) < 1e-9
+        assert abs(sg["mu"] - so["mu"]) < 1e-10 * abs(so["mu"])
+        assert abs(sg["errHe"] - so["errHe"]) < 1e-8 * abs(so["errHe"]) + 1e-20
+        g.poten()
+        o.poten()
+        eg, eo = g.energy(), o.energy()
+        assert abs(eg["etot"] - eo["etot"]) < 1e-10 * abs(eo["etot"])
+
+
+def test_real_time_moving_impurity_matches_oracle(oracle):
+    cfg, psi = droplet_case(time_mode=_abi.EP_REAL_TIME, impurity=_abi.EP_IMPURITY_MOVING,
+                            mimpur=85.4678, renormalize=0)
+    g, o = pair(cfg, psi, rimp=(0.4, 0.1, -0.3), vimp=(0.0, 0.0, 0.5 * ep.KTOPS), oracle=oracle)
+    dt = 6.546e-5 * 10
+    with g, o:
+        for _ in range(3):
+            g.steprk(dt)
+            o.steprk(dt)
+        for _ in range(6):
+            eg = g.steppc(dt)
+            eo = o.steppc(dt)
+        assert rel(g.psi(), o.psi()) < 1e-10
+        ig, io = g.impurity(), o.impurity()
+        for k in ("rimp", "vimp", "aimp"):
+            assert np.max(np.abs(ig[k] - io[k])) < 1e-9 * max(1.0, np.max(np.abs(io[k]))), k
+        assert np.max(np.abs(ig["invar"] - io["invar"])) < 1e-10
+        assert abs(eg["errimp"] - eo["errimp"]) < 1e-9 * max(1e-12, eo["errimp"])
+
+
+def test_fp32_path_tracks_oracle(oracle):
+    cfg, psi = droplet_case(precision=_abi.EP_FP32)
+    cfg64, _ = droplet_case()
+    g = ep.Solver(cfg)
+    o = oracle.OracleSolver(cfg64)
+    pot = ep.morse()
+    inv = np.zeros(10, dtype=np.complex128)
+    for s in (g, o):
+        s.set_impurity_potentials(pot, pot, pot)
+        s.set_impurity(rimp=(0.3, -0.2, 0.7), invar=inv)
+        s.start(psi)
+    with g, o:
+        eg, eo = g.energy(), o.energy()
+        for k in ("etot", "ekin4", "elj4", "ecor4", "ealphas", "eHeX", "n4"):
+            assert abs(eg[k] - eo[k]) < 2e-5 * max(1.0, abs(eo[k])), (k, eg[k], eo[k])
+        for _ in range(3):
+            g.steprk(2e-3)
+            o.steprk(2e-3)
+        g.run(10, 2e-3)
+        o.run(10, 2e-3)
+        assert rel(g.psi(), o.psi()) < 1e-4
+
+
+def test_nonfinite_input_is_reported_not_trapped(oracle):
+    cfg, psi = droplet_case()
+    psi = psi.copy()
+    psi[3, 4, 5] = np.nan
+    with ep.Solver(cfg) as g:
+        g.set_impurity_potentials(ep.morse(), ep.morse())
+        g.upload_psi(psi)
+        g.potenimp()
+        g.poten()
+        with pytest.raises(ep.EffPotError) as ei:
+            g.steprk(1e-3)
+        assert ei.value.status == 5
