@@ -108,6 +108,7 @@ _product_only = {
     "profile_enable": (_I, [_P, _I]),
     "profile_read": (_I, [_P, C.c_char_p, _I, _D, C.POINTER(C.c_longlong), _I, C.POINTER(_I)]),
     "device_bytes": (C.c_longlong, [_P]),
+    "convolve_noalloc": (_I, [_P, _P, _P, _I, _I, _I, _P]),
 }
 
 # Every symbol include/eff_pot.h declares.

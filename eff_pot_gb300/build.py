@@ -10,7 +10,7 @@ ROOT = os.path.dirname(HERE)
 CSRC = os.path.join(HERE, "csrc")
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(BUILD, "libeffpot.so")
-UNITS = ["ep_engine_fp64.cu", "ep_engine_fp32.cu", "ep_common.cu", "ep_api.cu"]
+UNITS = ["ep_engine_fp64.cu", "ep_engine_fp32.cu", "ep_common.cu", "ep_api.cu", "ep_noalloc.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-Xcompiler", "-O2",
          "-I" + os.path.join(ROOT, "include")]

@@ -197,6 +197,33 @@ int ep_profile_read(ep_ctx* ctx, char* names, int cap, double* ms,
 /* Bytes of device memory held by the context. */
 long long ep_device_bytes(const ep_ctx* ctx);
 
+/*
+ * Context-free density convolution that allocates nothing.  It has no
+ * counterpart in the reference: it exists for callers that can't call
+ * cudaMalloc (a host running inside a framework that owns the device memory
+ * pool, or code that runs while a CUDA graph is captured).
+ *
+ *   d_out = IFFT( FFT(d_in) * d_kernel ) / (nx*ny*nz)
+ *
+ * the k-space product poten() applies with wcgk, fvlj4 and kalfs
+ * (poten.f90:27-50).  d_in and d_out are real (nx,ny,nz) device arrays,
+ * d_kernel the real half-spectrum table (nx/2+1,ny,nz) on the device;
+ * stream is a cudaStream_t (NULL: the default stream).  The call is
+ * asynchronous on that stream.
+ *
+ * Scratch lives in one fixed device array of the library (4.3 MB, held on
+ * every GPU that loads the library until the process exits), so:
+ *  - sizes are limited to (nx/2+1)*ny*nz <= 33*64*64 (a 64^3 grid) and axes
+ *    of at most 320 points; larger grids return EP_ERR_UNSUPPORTED, odd nx
+ *    or axes with prime factors other than 2, 3, 5 EP_ERR_BAD_GRID;
+ *  - every call shares that array, so calls that overlap on the GPU (other
+ *    streams, other host threads) race; serialise them;
+ *  - the first call on a device looks the array up on that device (make it
+ *    before any stream capture); it calls no cudaMalloc or cudaFree.
+ */
+int ep_convolve_noalloc(const double* d_in, const double* d_kernel,
+                        double* d_out, int nx, int ny, int nz, void* stream);
+
 #ifdef __cplusplus
 }
 #endif
