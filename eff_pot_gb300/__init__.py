@@ -6,11 +6,11 @@ ctypes and mirrors the reference's subroutine interface (Solver).
 """
 from . import _abi
 from .config import make_config, config_dict, morse, null_potential, DEFAULTS, KTOPS, MP_U
-from .solver import Solver, EffPotError, load_library, library_config_defaults, LIBPATH
+from .solver import Solver, Batch, EffPotError, load_library, library_config_defaults, LIBPATH
 from .initial import woods_saxon_psi, grid_axes
 
 __all__ = [
-    "Solver", "EffPotError", "load_library", "library_config_defaults", "make_config",
+    "Solver", "Batch", "EffPotError", "load_library", "library_config_defaults", "make_config",
     "config_dict", "morse", "null_potential", "woods_saxon_psi", "grid_axes", "DEFAULTS",
     "KTOPS", "MP_U", "LIBPATH",
 ]

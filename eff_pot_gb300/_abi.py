@@ -109,6 +109,19 @@ _product_only = {
     "profile_read": (_I, [_P, C.c_char_p, _I, _D, C.POINTER(C.c_longlong), _I, C.POINTER(_I)]),
     "device_bytes": (C.c_longlong, [_P]),
     "convolve_noalloc": (_I, [_P, _P, _P, _I, _I, _I, _P]),
+    "set_precision": (_I, [_P, _I]),
+    "get_precision": (_I, [_P]),
+    "batch_create": (_I, [C.POINTER(EpConfig), _I, C.POINTER(_P)]),
+    "batch_destroy": (_I, [_P]),
+    "batch_size": (_I, [_P]),
+    "batch_ctx": (_P, [_P, _I]),
+    "batch_run": (_I, [_P, _I, C.c_double, C.POINTER(EpRunStats)]),
+    "batch_steprk": (_I, [_P, C.c_double]),
+    "batch_set_precision": (_I, [_P, _I]),
+    "batch_synchronize": (_I, [_P]),
+    "batch_event_record": (_I, [_P, _I]),
+    "batch_event_elapsed": (_I, [_P, _I, _I, _D]),
+    "batch_kernel_launches": (C.c_longlong, [_P]),
 }
 
 # Every symbol include/eff_pot.h declares.

@@ -22,7 +22,17 @@ struct ep_ctx {
   std::string err;
   Engine<double>* e64 = nullptr;
   Engine<float>* e32 = nullptr;
+  int active = EP_FP64;
   cudaEvent_t ev[16] = {};
+};
+
+struct ep_batch {
+  std::vector<ep_ctx*> ctx;
+  cudaStream_t st = nullptr;
+  cudaEvent_t fork = nullptr;
+  std::vector<cudaEvent_t> join;
+  cudaEvent_t ev[16] = {};
+  int device = 0;
 };
 
 namespace {
@@ -56,8 +66,8 @@ double select_pot(const ep_potential& p, double r) {
 template <class F>
 int dispatch(ep_ctx* c, F f) {
   if (!c) return EP_ERR_INVALID_ARG;
-  if (c->e64) return f(*c->e64);
-  if (c->e32) return f(*c->e32);
+  if (c->active == EP_FP64 && c->e64) return f(*c->e64);
+  if (c->active == EP_FP32 && c->e32) return f(*c->e32);
   return fail(c, EP_ERR_STATE, "context has no engine");
 }
 
@@ -142,6 +152,7 @@ int ep_create(const ep_config* cfg, ep_ctx** out) {
     return EP_ERR_CUDA;
   }
   int r;
+  x->active = c.precision;
   if (c.precision == EP_FP64) {
     x->e64 = new Engine<double>();
     r = x->e64->init(c, x->st, &x->prof, &x->imp, &x->err);
@@ -321,6 +332,180 @@ int ep_run(ep_ctx* c, int nsteps, double dt, ep_run_stats* stats) {
 
 int ep_renormalize(ep_ctx* c, double* norm_before) {
   return dispatch(c, [&](auto& e) -> int { return e.renormalize(norm_before, true); });
+}
+
+int ep_set_precision(ep_ctx* c, int precision) {
+  if (!c || (precision != EP_FP64 && precision != EP_FP32)) return EP_ERR_INVALID_ARG;
+  if (precision == c->active) return EP_OK;
+  cudaSetDevice(c->cfg.device);
+  ep_config cfg = c->cfg;
+  cfg.precision = precision;
+  int r;
+  if (precision == EP_FP64) {
+    if (!c->e64) {
+      c->e64 = new Engine<double>();
+      if ((r = c->e64->init(cfg, c->st, &c->prof, &c->imp, &c->err))) { c->e64->release(); delete c->e64; c->e64 = nullptr; return r; }
+    }
+    if ((r = c->e64->import_state(*c->e32))) return r;
+  } else {
+    if (!c->e32) {
+      c->e32 = new Engine<float>();
+      if ((r = c->e32->init(cfg, c->st, &c->prof, &c->imp, &c->err))) { c->e32->release(); delete c->e32; c->e32 = nullptr; return r; }
+    }
+    if ((r = c->e32->import_state(*c->e64))) return r;
+  }
+  c->active = precision;
+  c->cfg.precision = precision;
+  return EP_OK;
+}
+
+int ep_get_precision(const ep_ctx* c) { return c ? c->active : -1; }
+
+// ---------------------------------------------------------------------------
+// Batches.
+int ep_batch_create(const ep_config* cfgs, int n, ep_batch** out) {
+  if (!cfgs || n < 1 || !out) return EP_ERR_INVALID_ARG;
+  *out = nullptr;
+  ep_batch* b = new ep_batch();
+  b->device = cfgs[0].device;
+  for (int i = 0; i < n; ++i) {
+    if (cfgs[i].device != b->device) { g_create_error = "a batch lives on one device"; ep_batch_destroy(b); return EP_ERR_INVALID_ARG; }
+    ep_ctx* c = nullptr;
+    int r = ep_create(&cfgs[i], &c);
+    if (r) { ep_batch_destroy(b); return r; }
+    b->ctx.push_back(c);
+  }
+  cudaSetDevice(b->device);
+  if (cudaStreamCreateWithFlags(&b->st, cudaStreamNonBlocking) != cudaSuccess ||
+      cudaEventCreateWithFlags(&b->fork, cudaEventDisableTiming) != cudaSuccess) {
+    g_create_error = "batch stream creation failed";
+    ep_batch_destroy(b);
+    return EP_ERR_CUDA;
+  }
+  b->join.resize(n);
+  for (int i = 0; i < n; ++i) cudaEventCreateWithFlags(&b->join[i], cudaEventDisableTiming);
+  *out = b;
+  return EP_OK;
+}
+
+int ep_batch_destroy(ep_batch* b) {
+  if (!b) return EP_ERR_INVALID_ARG;
+  for (ep_ctx* c : b->ctx) ep_destroy(c);
+  cudaSetDevice(b->device);
+  for (cudaEvent_t e : b->join) if (e) cudaEventDestroy(e);
+  for (cudaEvent_t e : b->ev) if (e) cudaEventDestroy(e);
+  if (b->fork) cudaEventDestroy(b->fork);
+  if (b->st) cudaStreamDestroy(b->st);
+  delete b;
+  return EP_OK;
+}
+
+int ep_batch_size(const ep_batch* b) { return b ? (int)b->ctx.size() : 0; }
+
+ep_ctx* ep_batch_ctx(ep_batch* b, int i) {
+  if (!b || i < 0 || i >= (int)b->ctx.size()) return nullptr;
+  return b->ctx[i];
+}
+
+namespace {
+// Every instance stream waits for the batch stream, then the batch stream
+// waits for every instance: batch events bracket all instances' work.
+void batch_fork(ep_batch* b) {
+  cudaEventRecord(b->fork, b->st);
+  for (ep_ctx* c : b->ctx) cudaStreamWaitEvent(c->st, b->fork, 0);
+}
+void batch_join(ep_batch* b) {
+  for (size_t i = 0; i < b->ctx.size(); ++i) {
+    cudaEventRecord(b->join[i], b->ctx[i]->st);
+    cudaStreamWaitEvent(b->st, b->join[i], 0);
+  }
+}
+}  // namespace
+
+int ep_batch_run(ep_batch* b, int nsteps, double dt, ep_run_stats* stats) {
+  if (!b || nsteps < 0) return EP_ERR_INVALID_ARG;
+  cudaSetDevice(b->device);
+  batch_fork(b);
+  // step-major interleaving so the instances' kernels overlap
+  for (int s = 0; s < nsteps; ++s) {
+    const bool last = (s == nsteps - 1) && stats;
+    for (size_t i = 0; i < b->ctx.size(); ++i) {
+      ep_ctx* c = b->ctx[i];
+      const bool renorm = c->cfg.time_mode == EP_IMAGINARY_TIME && c->cfg.renormalize;
+      ep_step_errors se{};
+      int r = dispatch(c, [&](auto& e) -> int {
+        int q = e.steppc(dt, last ? &se : nullptr);
+        if (q) return q;
+        if (renorm && (q = e.rescale_pending())) return q;
+        if (last) {
+          stats[i].errHe = se.errHe;
+          stats[i].mu = e.last_mu;
+          stats[i].norm = e.last_norm;
+          stats[i].steps_done = nsteps;
+        }
+        return EP_OK;
+      });
+      if (r) return r;
+    }
+  }
+  batch_join(b);
+  if (stats) {
+    if (cudaStreamSynchronize(b->st) != cudaSuccess) return EP_ERR_CUDA;
+    for (ep_ctx* c : b->ctx) {
+      int r = dispatch(c, [&](auto& e) -> int { return e.check_flags(); });
+      if (r) return r;
+    }
+  }
+  return EP_OK;
+}
+
+int ep_batch_steprk(ep_batch* b, double dt) {
+  if (!b) return EP_ERR_INVALID_ARG;
+  for (ep_ctx* c : b->ctx) {
+    int r = ep_steprk(c, dt);
+    if (r) return r;
+  }
+  return EP_OK;
+}
+
+int ep_batch_set_precision(ep_batch* b, int precision) {
+  if (!b) return EP_ERR_INVALID_ARG;
+  for (ep_ctx* c : b->ctx) {
+    int r = ep_set_precision(c, precision);
+    if (r) return r;
+  }
+  return EP_OK;
+}
+
+int ep_batch_synchronize(ep_batch* b) {
+  if (!b) return EP_ERR_INVALID_ARG;
+  for (ep_ctx* c : b->ctx)
+    if (cudaStreamSynchronize(c->st) != cudaSuccess) return EP_ERR_CUDA;
+  return cudaStreamSynchronize(b->st) == cudaSuccess ? EP_OK : EP_ERR_CUDA;
+}
+
+int ep_batch_event_record(ep_batch* b, int slot) {
+  if (!b || slot < 0 || slot >= 16) return EP_ERR_INVALID_ARG;
+  cudaSetDevice(b->device);
+  if (!b->ev[slot] && cudaEventCreate(&b->ev[slot]) != cudaSuccess) return EP_ERR_CUDA;
+  batch_join(b);
+  return cudaEventRecord(b->ev[slot], b->st) == cudaSuccess ? EP_OK : EP_ERR_CUDA;
+}
+
+int ep_batch_event_elapsed(ep_batch* b, int a, int c, double* ms) {
+  if (!b || !ms || a < 0 || a >= 16 || c < 0 || c >= 16 || !b->ev[a] || !b->ev[c]) return EP_ERR_INVALID_ARG;
+  if (cudaEventSynchronize(b->ev[c]) != cudaSuccess) return EP_ERR_CUDA;
+  float t = 0.f;
+  if (cudaEventElapsedTime(&t, b->ev[a], b->ev[c]) != cudaSuccess) return EP_ERR_CUDA;
+  *ms = t;
+  return EP_OK;
+}
+
+long long ep_batch_kernel_launches(const ep_batch* b) {
+  long long n = 0;
+  if (b)
+    for (ep_ctx* c : b->ctx) n += c->prof.launches;
+  return n;
 }
 
 int ep_synchronize(ep_ctx* c) {

@@ -59,51 +59,7 @@ void Prof::release() {
   pool.clear();
 }
 
-// Two-sum accumulation (Neumaier) of the block partials, fixed order:
-// thread t takes partials t, t+256, ...; then a fixed pairwise tree.
-__device__ __forceinline__ void neu_add(double& s, double& c, double v) {
-  const double t = s + v;
-  if (fabs(s) >= fabs(v)) c += (s - t) + v; else c += (v - t) + s;
-  s = t;
-}
-
 __global__ void k_finalize(const double* __restrict__ partials, int nblocks, int nq, DevScalars* sc, int out0,
                            int mode, double N, double dxyz, double n4, int renorm) {
-  __shared__ double ss[256], cs[256];
-  const int tid = threadIdx.x;
-  for (int q = 0; q < nq; ++q) {
-    double s = 0.0, c = 0.0;
-    for (int b = tid; b < nblocks; b += blockDim.x) neu_add(s, c, partials[(long long)b * nq + q]);
-    ss[tid] = s;
-    cs[tid] = c;
-    __syncthreads();
-    for (int off = blockDim.x / 2; off > 0; off >>= 1) {
-      if (tid < off) {
-        double s1 = ss[tid], c1 = cs[tid] + cs[tid + off];
-        neu_add(s1, c1, ss[tid + off]);
-        ss[tid] = s1;
-        cs[tid] = c1;
-      }
-      __syncthreads();
-    }
-    if (tid == 0) sc->sums[out0 + q] = ss[0] + cs[0];
-    __syncthreads();
-  }
-  if (tid == 0) {
-    bool bad = false;
-    for (int q = 0; q < nq; ++q) bad |= !isfinite(sc->sums[out0 + q]);
-    if (mode == 1) {
-      const double norm = sc->sums[out0 + 1] * dxyz;
-      sc->norm = norm;
-      sc->mu = sc->sums[out0 + 2] / sc->sums[out0 + 3];
-      sc->errHe = sc->sums[out0] / N;
-      sc->scale = (renorm && norm > 0.0) ? sqrt(n4 / norm) : 1.0;
-    } else if (mode == 2) {
-      const double norm = sc->sums[out0] * dxyz;
-      sc->norm = norm;
-      sc->scale = norm > 0.0 ? sqrt(n4 / norm) : 1.0;
-      bad |= !(norm > 0.0);
-    }
-    if (bad) atomicOr(&sc->flags, (unsigned)EP_FLAG_NONFINITE);
-  }
+  finalize_block(partials, nblocks, nq, sc, out0, mode, N, dxyz, n4, renorm);
 }

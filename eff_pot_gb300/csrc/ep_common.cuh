@@ -42,6 +42,7 @@ struct DevScalars {
   double scale;         // pending imaginary-time renormalisation factor
   double errHe, norm, mu;
   unsigned int flags;   // bit 0: non-finite detected; bit 1: den <= 0
+  unsigned int counter; // blocks done (last-block finalisation), reset to 0
 };
 enum { EP_FLAG_NONFINITE = 1u, EP_FLAG_DEN_NONPOS = 2u };
 

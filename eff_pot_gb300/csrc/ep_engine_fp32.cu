@@ -2,3 +2,4 @@
 // FP64 reductions).
 #include "ep_engine_impl.cuh"
 template class Engine<float>;
+template int Engine<float>::import_state<double>(const Engine<double>&);

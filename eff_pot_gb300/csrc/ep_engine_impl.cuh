@@ -497,11 +497,12 @@ int Engine<T>::lap_correct(double dt, bool want) {
   dim3 grid((g.nx + EP_TX - 1) / EP_TX, (g.ny + EP_TY - 1) / EP_TY, (g.nz + EP_ZC - 1) / EP_ZC);
   dim3 blk(EP_TX, EP_TY);
   const T f3 = (T)(3.0 * dt), cc = (T)c9;
+  const int renorm = (cfg.time_mode == EP_IMAGINARY_TIME && cfg.renormalize) ? 1 : 0;
 #define EP_CORR(RR)                                                                                           \
   case RR: {                                                                                                  \
     auto k = k_correct<T, RR>;                                                                                \
     EP_LAUNCH("correct", k, grid, blk, 0, g, fd, phys, EP_ZC, psi, pot4, uimp, po3, po2, h1, h2, pc, spare, den, \
-              f3, cc, partials);                                                                              \
+              f3, cc, partials, sc, renorm, cfg.n4);                                                          \
   } break;
   switch (fd.R) {
     EP_CORR(1) EP_CORR(2) EP_CORR(3) EP_CORR(4) EP_CORR(5) EP_CORR(6)
@@ -513,7 +514,7 @@ int Engine<T>::lap_correct(double dt, bool want) {
   ioldp[2] = ioldp[1];
   ioldp[1] = ioldp[0];
   ioldp[0] = t;
-  return reduce_finalize((int)(grid.x * grid.y * grid.z), 4, 0, 1);
+  return EP_OK;
 }
 
 template <class T>
@@ -690,8 +691,9 @@ int Engine<T>::renormalize(double* norm_before, bool wait) {
   EP_LAUNCH("normsum", kn, EP_RED_BLOCKS, 256, 0, psi, g.N, partials);
   int r;
   if ((r = reduce_finalize(EP_RED_BLOCKS, 1, 25, 2))) return r;
+  HistPtrs<T> hp{{po[0], po[1], po[2], ph[0], ph[1], pc}};
   auto ks = k_rescale<T>;
-  EP_LAUNCH("rescale", ks, 4 * 152, 256, 0, psi, den, g.N, sc);
+  EP_LAUNCH("rescale", ks, 4 * 152, 256, 0, psi, den, hp, g.N, sc);
   if (wait || norm_before) {
     double s;
     if ((r = read_sums(&s, 1, 25))) return r;
@@ -802,7 +804,35 @@ int Engine<T>::download_r(int which, double* h) {
 
 template <class T>
 int Engine<T>::rescale_pending() {
+  HistPtrs<T> hp{{po[0], po[1], po[2], ph[0], ph[1], pc}};
   auto ks = k_rescale<T>;
-  EP_LAUNCH("rescale", ks, 4 * 152, 256, 0, psi, den, g.N, sc);
+  EP_LAUNCH("rescale", ks, 4 * 152, 256, 0, psi, den, hp, g.N, sc);
+  return EP_OK;
+}
+
+// Precision switch: convert the state of the other engine role by role
+// (psi, the multistep history, pc, q and every real field) into this one.
+template <class T>
+template <class U>
+int Engine<T>::import_state(const Engine<U>& o) {
+  typedef C2<U> OT;
+  const OT* cs[9] = {o.psi, o.spare, o.po[0], o.po[1], o.po[2], o.ph[0], o.ph[1], o.pc, o.q};
+  CT* cd[9] = {psi, spare, po[0], po[1], po[2], ph[0], ph[1], pc, q};
+  for (int i = 0; i < 9; ++i) {
+    auto k = k_convert<OT, CT>;
+    EP_LAUNCH("convert", k, 4 * 152, 256, 0, cs[i], cd[i], g.N);
+  }
+  const U* rs[15] = {o.den, o.pot4, o.uimp, o.dencg, o.delj4, o.dxd, o.dyd, o.dzd, o.falfs,
+                     o.intx, o.inty, o.intz, o.ualphas, o.vpi, o.delta};
+  T* rd[15] = {den, pot4, uimp, dencg, delj4, dxd, dyd, dzd, falfs, intx, inty, intz, ualphas, vpi, delta};
+  for (int i = 0; i < 15; ++i) {
+    auto k = k_convert<U, T>;
+    EP_LAUNCH("convert", k, 4 * 152, 256, 0, rs[i], rd[i], g.N);
+  }
+  for (int i = 0; i < 3; ++i) ioldp[i] = o.ioldp[i];
+  for (int i = 0; i < 2; ++i) ioldh[i] = o.ioldh[i];
+  have_field = o.have_field;
+  last_mu = o.last_mu;
+  last_norm = o.last_norm;
   return EP_OK;
 }

@@ -109,6 +109,81 @@ EP_DEV double hexp(const Phys& ph, C2<T> psi, C2<T> H) {
   return -((double)psi.x * H.x + (double)psi.y * H.y);
 }
 
+template <class T>
+EP_DEV T hexp_t(const Phys& ph, C2<T> psi, C2<T> H) {
+  if (ph.time_mode == 1) return -psi.x * H.y + psi.y * H.x;
+  return -(psi.x * H.x + psi.y * H.y);
+}
+
+// Per-thread accumulator: FP64 sums for FP64 fields; compensated (Kahan)
+// FP32 sums for FP32 fields, widened to FP64 once per thread.
+template <class T> struct Acc {
+  double s = 0.0;
+  EP_DEV void add(T v) { s += (double)v; }
+  EP_DEV double get() const { return s; }
+};
+template <> struct Acc<float> {
+  float s = 0.f, c = 0.f;
+  EP_DEV void add(float v) {
+    const float y = v - c;
+    const float t = s + y;
+    c = (t - s) - y;
+    s = t;
+  }
+  EP_DEV double get() const { return (double)s - (double)c; }
+};
+
+EP_DEV void neu_add_d(double& s, double& c, double v) {
+  const double t = s + v;
+  if (fabs(s) >= fabs(v)) c += (s - t) + v; else c += (v - t) + s;
+  s = t;
+}
+
+// Sum of block partials (fixed order, compensated) by one block of 256
+// threads -> sc->sums[out0 + q]; mode 1: corrector epilogue (norm, mu,
+// renormalisation factor), mode 2: norm only.
+EP_DEV void finalize_block(const double* partials, int nblocks, int nq, DevScalars* sc, int out0, int mode,
+                           double N, double dxyz, double n4, int renorm) {
+  __shared__ double ss[256], cs[256];
+  const int tid = threadIdx.x + blockDim.x * threadIdx.y;
+  const int nth = blockDim.x * blockDim.y;
+  for (int q = 0; q < nq; ++q) {
+    double s = 0.0, c = 0.0;
+    for (int b = tid; b < nblocks; b += nth) neu_add_d(s, c, __ldcg(partials + (long long)b * nq + q));
+    ss[tid] = s;
+    cs[tid] = c;
+    __syncthreads();
+    for (int off = nth / 2; off > 0; off >>= 1) {
+      if (tid < off) {
+        double s1 = ss[tid], c1 = cs[tid] + cs[tid + off];
+        neu_add_d(s1, c1, ss[tid + off]);
+        ss[tid] = s1;
+        cs[tid] = c1;
+      }
+      __syncthreads();
+    }
+    if (tid == 0) sc->sums[out0 + q] = ss[0] + cs[0];
+    __syncthreads();
+  }
+  if (tid == 0) {
+    bool bad = false;
+    for (int q = 0; q < nq; ++q) bad |= !isfinite(sc->sums[out0 + q]);
+    if (mode == 1) {
+      const double norm = sc->sums[out0 + 1] * dxyz;
+      sc->norm = norm;
+      sc->mu = sc->sums[out0 + 2] / sc->sums[out0 + 3];
+      sc->errHe = sc->sums[out0] / N;
+      sc->scale = (renorm && norm > 0.0) ? sqrt(n4 / norm) : 1.0;
+    } else if (mode == 2) {
+      const double norm = sc->sums[out0] * dxyz;
+      sc->norm = norm;
+      sc->scale = norm > 0.0 ? sqrt(n4 / norm) : 1.0;
+      bad |= !(norm > 0.0);
+    }
+    if (bad) atomicOr(&sc->flags, (unsigned)EP_FLAG_NONFINITE);
+  }
+}
+
 // Block reduction of NQ doubles into partials[block * NQ + q].
 template <int NQ>
 EP_DEV void block_reduce_store(double (&v)[NQ], double* __restrict__ partials) {
@@ -549,9 +624,10 @@ __global__ void __launch_bounds__(EP_TX* EP_TY) k_correct(Geo g, FdW<T> fd, Phys
                                                          const C2<T>* __restrict__ h1,
                                                          const C2<T>* __restrict__ h2, C2<T>* pc,
                                                          C2<T>* __restrict__ out, T* __restrict__ den, T f3, T c9,
-                                                         double* __restrict__ partials) {
+                                                         double* __restrict__ partials, DevScalars* sc, int renorm,
+                                                         double n4) {
   __shared__ C2<T> sp[(EP_TX + 2 * R) * (EP_TY + 2 * R)];
-  double acc[4] = {0.0, 0.0, 0.0, 0.0};
+  Acc<T> acc[4];
   lap_march<T, R>(g, psi, fd, zc, sp, [&](long long p, C2<T> c, C2<T> lap) {
     const C2<T> H = happly<T>(ph, lap, c, pot4[p], uimp[p]);
     const C2<T> p5 = T(0.125) * ((T(9) * po3[p] - po2[p]) + f3 * ((H + T(2) * h1[p]) - h2[p]));
@@ -561,12 +637,27 @@ __global__ void __launch_bounds__(EP_TX* EP_TY) k_correct(Geo g, FdW<T> fd, Phys
     out[p] = po;
     const T dn = po.x * po.x + po.y * po.y;
     den[p] = dn;
-    acc[0] += sqrt((double)pcn.x * pcn.x + (double)pcn.y * pcn.y);
-    acc[1] += (double)dn;
-    acc[2] += hexp<T>(ph, c, H);
-    acc[3] += (double)c.x * c.x + (double)c.y * c.y;
+    acc[0].add(sqrt(pcn.x * pcn.x + pcn.y * pcn.y));
+    acc[1].add(dn);
+    acc[2].add(hexp_t<T>(ph, c, H));
+    acc[3].add(c.x * c.x + c.y * c.y);
   });
-  block_reduce_store<4>(acc, partials);
+  double v[4] = {acc[0].get(), acc[1].get(), acc[2].get(), acc[3].get()};
+  block_reduce_store<4>(v, partials);
+  // The last block to finish sums all partials (no block waits for another).
+  __shared__ bool last;
+  const int tid = threadIdx.x + blockDim.x * threadIdx.y;
+  const unsigned nb = gridDim.x * gridDim.y * gridDim.z;
+  if (tid == 0) {
+    __threadfence();
+    last = atomicAdd(&sc->counter, 1u) == nb - 1;
+  }
+  __syncthreads();
+  if (last) {
+    __threadfence();
+    finalize_block(partials, (int)nb, 4, sc, 0, 1, (double)g.N, ph.dxyz, n4, renorm);
+    if (tid == 0) sc->counter = 0u;
+  }
 }
 
 // One Runge-Kutta-Gill stage of steprk.f90:71-89 (jrun-independent part);
@@ -607,9 +698,13 @@ __global__ void k_psi_to_den(const C2<T>* __restrict__ psi, T* __restrict__ den,
 }
 
 // Imaginary-time renormalisation with the factor the finalize kernel left
-// in sc->scale.
+// in sc->scale: psi and the whole multistep history (psiold x3, hpsiold x2,
+// pc) are scaled together so they keep describing one trajectory.
 template <class T>
-__global__ void k_rescale(C2<T>* __restrict__ psi, T* __restrict__ den, long long N, const DevScalars* __restrict__ sc) {
+struct HistPtrs { C2<T>* h[6]; };
+template <class T>
+__global__ void k_rescale(C2<T>* __restrict__ psi, T* __restrict__ den, HistPtrs<T> hist, long long N,
+                          const DevScalars* __restrict__ sc) {
   const T s = (T)sc->scale;
   for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < N; i += (long long)gridDim.x * blockDim.x) {
     C2<T> v = psi[i];
@@ -617,6 +712,13 @@ __global__ void k_rescale(C2<T>* __restrict__ psi, T* __restrict__ den, long lon
     v.y *= s;
     psi[i] = v;
     den[i] = v.x * v.x + v.y * v.y;
+#pragma unroll
+    for (int k = 0; k < 6; ++k) {
+      C2<T> w = hist.h[k][i];
+      w.x *= s;
+      w.y *= s;
+      hist.h[k][i] = w;
+    }
   }
 }
 

@@ -47,7 +47,8 @@ def step_bytes(nx, ny, nz, otc=True, grad=True, s=8, renorm=True):
     else:
         b["x3_c2r_r2c"] = c * Nh + 2 * s * N + s * N
     if renorm:
-        b["rescale"] = (2 * c + s) * N
+        # psi and the history (psiold x3, hpsiold x2, pc) read + written, den written
+        b["rescale"] = (14 * c + s) * N
     return b
 
 

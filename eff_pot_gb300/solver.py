@@ -66,6 +66,21 @@ class Solver:
         if st != _abi.EP_OK:
             raise EffPotError(st, self._create_error())
         self._h = h
+        self._owned = True
+        self._init_geometry()
+
+    @classmethod
+    def _view(cls, cfg, handle):
+        """A Solver over a context owned by someone else (a batch)."""
+        self = cls.__new__(cls)
+        self._f = self._bind()
+        self.cfg = cfg
+        self._h = C.c_void_p(handle)
+        self._owned = False
+        self._init_geometry()
+        return self
+
+    def _init_geometry(self):
         c = self.cfg
         self.shape = (c.nx, c.ny, c.nz)
         self.N = c.nx * c.ny * c.nz
@@ -88,7 +103,8 @@ class Solver:
 
     def close(self):
         if getattr(self, "_h", None):
-            self._f["destroy"](self._h)
+            if getattr(self, "_owned", True):
+                self._f["destroy"](self._h)
             self._h = None
 
     def __del__(self):
@@ -217,6 +233,14 @@ class Solver:
         self._check(self._f["renormalize"](self._h, C.byref(n)), "renormalize")
         return n.value
 
+    def set_precision(self, precision):
+        """'fp32'/'fp64' (or EP_FP32/EP_FP64): convert the state and go on."""
+        p = {"fp32": _abi.EP_FP32, "fp64": _abi.EP_FP64}.get(precision, precision)
+        self._check(self._f["set_precision"](self._h, p), "set_precision")
+
+    def precision(self):
+        return "fp32" if self._f["get_precision"](self._h) == _abi.EP_FP32 else "fp64"
+
     # -- product-only services ----------------------------------------------
     def synchronize(self):
         self._check(self._f["synchronize"](self._h), "synchronize")
@@ -255,3 +279,77 @@ class Solver:
 def mass_units(mimpur):
     """mAg_u of DFT4He3d.f90:203."""
     return mimpur * MP_U
+
+
+class Batch:
+    """Many independent instances advanced together (ep_batch_*)."""
+
+    def __init__(self, cfgs):
+        _, self._f = load_library()
+        self.cfgs = list(cfgs)
+        n = len(self.cfgs)
+        arr = (_abi.EpConfig * n)(*self.cfgs)
+        h = C.c_void_p()
+        st = self._f["batch_create"](arr, n, C.byref(h))
+        if st != _abi.EP_OK:
+            raise EffPotError(st, self._f["create_error"]().decode())
+        self._h = h
+        self.solvers = [Solver._view(self.cfgs[i], self._f["batch_ctx"](h, i)) for i in range(n)]
+
+    def __len__(self):
+        return len(self.solvers)
+
+    def __getitem__(self, i):
+        return self.solvers[i]
+
+    def _check(self, st, what):
+        if st != _abi.EP_OK:
+            raise EffPotError(st, what)
+
+    def steprk(self, deltat):
+        self._check(self._f["batch_steprk"](self._h, deltat), "batch_steprk")
+
+    def run(self, nsteps, deltat, wait=True):
+        if not wait:
+            self._check(self._f["batch_run"](self._h, nsteps, deltat, None), "batch_run")
+            return None
+        stats = (_abi.EpRunStats * len(self))()
+        self._check(self._f["batch_run"](self._h, nsteps, deltat, stats), "batch_run")
+        return [dict(errHe=s.errHe, mu=s.mu, norm=s.norm, steps_done=s.steps_done) for s in stats]
+
+    def set_precision(self, precision):
+        p = {"fp32": _abi.EP_FP32, "fp64": _abi.EP_FP64}.get(precision, precision)
+        self._check(self._f["batch_set_precision"](self._h, p), "batch_set_precision")
+
+    def synchronize(self):
+        self._check(self._f["batch_synchronize"](self._h), "batch_synchronize")
+
+    def event_record(self, slot):
+        self._check(self._f["batch_event_record"](self._h, slot), "batch_event_record")
+
+    def event_elapsed(self, a, b):
+        ms = C.c_double()
+        self._check(self._f["batch_event_elapsed"](self._h, a, b, C.byref(ms)), "batch_event_elapsed")
+        return ms.value
+
+    def kernel_launches(self):
+        return int(self._f["batch_kernel_launches"](self._h))
+
+    def close(self):
+        if getattr(self, "_h", None):
+            for s in self.solvers:
+                s._h = None
+            self._f["batch_destroy"](self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()

@@ -178,6 +178,37 @@ int ep_run(ep_ctx* ctx, int nsteps, double deltat, ep_run_stats* stats);
 /* Renormalise psi to n4 now (imaginary time). */
 int ep_renormalize(ep_ctx* ctx, double* norm_before);
 
+/* Switch the arithmetic of the bulk fields between EP_FP32 and EP_FP64,
+ * keeping the state: psi, the multistep history (psiold, hpsiold, pc, q)
+ * and every field are converted and the next steps run in the new
+ * precision.  FP32 -> FP64 starts the FP64 refinement sweeps of a FP32 run;
+ * the first switch allocates the FP64 buffers. */
+int ep_set_precision(ep_ctx* ctx, int precision);
+int ep_get_precision(const ep_ctx* ctx);
+
+/* ---- batches: many independent instances (droplets / impurity positions,
+ * grids of any size) advanced together, each on its own stream so their
+ * kernels overlap on the GPU.  This replaces the one-process-per-density
+ * scan of loop.sh / get_impurity_energy.sh. ------------------------------ */
+typedef struct ep_batch ep_batch;
+int ep_batch_create(const ep_config* cfgs, int n, ep_batch** out);
+int ep_batch_destroy(ep_batch* b);
+int ep_batch_size(const ep_batch* b);
+/* The context of instance i (to upload psi, set the impurity, read
+ * energies with the single-instance calls). */
+ep_ctx* ep_batch_ctx(ep_batch* b, int i);
+/* nsteps steppc steps of every instance (imaginary-time renormalisation as
+ * configured); stats (n entries) may be NULL: then the call does not wait. */
+int ep_batch_run(ep_batch* b, int nsteps, double deltat, ep_run_stats* stats);
+int ep_batch_steprk(ep_batch* b, double deltat);
+int ep_batch_set_precision(ep_batch* b, int precision);
+int ep_batch_synchronize(ep_batch* b);
+/* Events on the batch stream, which every ep_batch_run forks from and joins
+ * back into: elapsed time of whole-batch work. */
+int ep_batch_event_record(ep_batch* b, int slot);
+int ep_batch_event_elapsed(ep_batch* b, int slot_a, int slot_b, double* ms);
+long long ep_batch_kernel_launches(const ep_batch* b);
+
 /* Device synchronisation, timing and counters. */
 int ep_synchronize(ep_ctx* ctx);
 /* The CUDA stream all work of this context is launched on (cudaStream_t). */

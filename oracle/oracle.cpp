@@ -1243,8 +1243,9 @@ int oc_steppc(oc_ctx* c, double deltat, ep_step_errors* err) {
   return EP_OK;
 }
 
-// Imaginary-time renormalisation: psi <- sqrt(n4 / int|psi|^2) psi,
-// den <- |psi|^2.
+// Imaginary-time renormalisation: psi <- s psi, den <- |psi|^2 with
+// s = sqrt(n4 / int|psi|^2); the multistep history (psiold, hpsiold, pc) is
+// scaled by the same s so that it keeps describing one trajectory.
 int oc_renormalize(oc_ctx* c, double* norm_before) {
   if (!c) return EP_ERR_INVALID_ARG;
   const double nrm = par_sum(c->N, [&](size_t i) { return std::norm(c->psi[i]); }) * c->dxyz;
@@ -1254,6 +1255,9 @@ int oc_renormalize(oc_ctx* c, double* norm_before) {
   for (long long i = 0; i < (long long)c->N; ++i) {
     c->psi[i] *= s;
     c->den[i] = std::norm(c->psi[i]);
+    for (int k = 0; k < 3; ++k) c->psiold[k][i] *= s;
+    for (int k = 0; k < 2; ++k) c->hpsiold[k][i] *= s;
+    c->pc[i] *= s;
   }
   c->last_norm = nrm;
   if (norm_before) *norm_before = nrm;
