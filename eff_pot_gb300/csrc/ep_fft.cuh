@@ -102,6 +102,16 @@ template <class T, int R, int DIR> EP_DEV void dftR(C2<T>* v) {
   else dft8<T, DIR>(v);
 }
 
+// q = a / d, r = a - q d for 0 <= a < 2^22 through a float reciprocal
+// (one correction step makes it exact); far cheaper than integer division.
+EP_DEV int fdivmod(int a, int d, float inv_d, int& r) {
+  int q = __float2int_rz(__fmul_rz((float)a, inv_d));
+  r = a - q * d;
+  if (r >= d) { ++q; r -= d; }
+  if (r < 0) { --q; r += d; }
+  return q;
+}
+
 // One Stockham stage of radix R over nl lines (line stride ld) of length n.
 // tw: roots exp(-2 pi i k / (n*tws)), accessed with stride tws.
 template <class T, int R, int DIR>
@@ -110,10 +120,11 @@ EP_DEV void stage(const C2<T>* __restrict__ src, C2<T>* __restrict__ dst, int nl
   const int m = n / R;
   const int total = nl * m;
   const int tstep = (n / (Ns * R)) * tws;
+  const float inv_m = 1.0f / (float)m, inv_ns = 1.0f / (float)Ns;
   for (int b = threadIdx.x; b < total; b += blockDim.x) {
-    const int line = b / m;
-    const int j = b - line * m;
-    const int k = j % Ns;
+    int j, k;
+    const int line = fdivmod(b, m, inv_m, j);
+    fdivmod(j, Ns, inv_ns, k);
     const C2<T>* s = src + line * ld;
     C2<T>* d = dst + line * ld;
     C2<T> v[R];
@@ -162,9 +173,10 @@ EP_DEV C2<T>* lines(C2<T>* a, C2<T>* b, int nl, int ld, const FftPlan& p,
 template <class T, class Out>
 EP_DEV void r2c_unpack(const C2<T>* Z, int nl, int ld, int n2, const C2<T>* __restrict__ twx, Out out) {
   const int per = n2 + 1;
+  const float inv = 1.0f / (float)per;
   for (int b = threadIdx.x; b < nl * per; b += blockDim.x) {
-    const int line = b / per;
-    const int k = b - line * per;
+    int k;
+    const int line = fdivmod(b, per, inv, k);
     const C2<T>* z = Z + line * ld;
     const C2<T> zk = z[k == n2 ? 0 : k];
     const C2<T> zc = conjg(z[k == 0 ? 0 : n2 - k]);
@@ -179,9 +191,10 @@ EP_DEV void r2c_unpack(const C2<T>* Z, int nl, int ld, int n2, const C2<T>* __re
 template <class T>
 EP_DEV void c2r_pack(const C2<T>* X, int ldx, C2<T>* Z, int ldz, int nl, int n2,
                      const C2<T>* __restrict__ twx) {
+  const float inv = 1.0f / (float)n2;
   for (int b = threadIdx.x; b < nl * n2; b += blockDim.x) {
-    const int line = b / n2;
-    const int k = b - line * n2;
+    int k;
+    const int line = fdivmod(b, n2, inv, k);
     const C2<T> xk = X[line * ldx + k];
     const C2<T> xc = conjg(X[line * ldx + n2 - k]);
     const C2<T> A = xk + xc;

@@ -54,10 +54,16 @@ EP_DEV T nbr(const T* __restrict__ f, long long p, int i, int k, int n, long lon
   return f[p + (long long)(ii - i) * st];
 }
 
-// First derivative along an axis from global memory (pairs +k/-k).
+// First derivative along an axis from global memory (pairs +k/-k); points
+// at least R away from both ends skip the boundary logic.
 template <class T>
 EP_DEV T d1_global(const T* __restrict__ f, long long p, int i, int n, long long st, const T* w, int R, int periodic) {
   T s = T(0);
+  if (i >= R && i < n - R) {
+    const T* c = f + p;
+    for (int k = 1; k <= R; ++k) s += w[k] * (__ldg(c + k * st) - __ldg(c - k * st));
+    return s;
+  }
   for (int k = 1; k <= R; ++k) s += w[k] * (nbr(f, p, i, k, n, st, periodic) - nbr(f, p, i, -k, n, st, periodic));
   return s;
 }
@@ -147,22 +153,19 @@ EP_DEV void finalize_block(const double* partials, int nblocks, int nq, DevScala
   __shared__ double ss[256], cs[256];
   const int tid = threadIdx.x + blockDim.x * threadIdx.y;
   const int nth = blockDim.x * blockDim.y;
+  // partials are already FP64 block sums: a fixed-order pairwise tree keeps
+  // the relative error near log2(nblocks) ulp with few FP64 operations
+  (void)cs;
   for (int q = 0; q < nq; ++q) {
-    double s = 0.0, c = 0.0;
-    for (int b = tid; b < nblocks; b += nth) neu_add_d(s, c, __ldcg(partials + (long long)b * nq + q));
+    double s = 0.0;
+    for (int b = tid; b < nblocks; b += nth) s += __ldcg(partials + (long long)b * nq + q);
     ss[tid] = s;
-    cs[tid] = c;
     __syncthreads();
     for (int off = nth / 2; off > 0; off >>= 1) {
-      if (tid < off) {
-        double s1 = ss[tid], c1 = cs[tid] + cs[tid + off];
-        neu_add_d(s1, c1, ss[tid + off]);
-        ss[tid] = s1;
-        cs[tid] = c1;
-      }
+      if (tid < off) ss[tid] += ss[tid + off];
       __syncthreads();
     }
-    if (tid == 0) sc->sums[out0 + q] = ss[0] + cs[0];
+    if (tid == 0) sc->sums[out0 + q] = ss[0];
     __syncthreads();
   }
   if (tid == 0) {
@@ -217,8 +220,10 @@ template <class T>
 EP_DEV void x_inverse(const C2<T>* __restrict__ spec, long long line0, int nlv, int nl, int nx, int nxh,
                       C2<T>* P, C2<T>* Q, int ld, const FftPlan& p2, const C2<T>* tw, T scale, T* Rout) {
   const int n2 = nx / 2;
+  const float inv1 = 1.0f / (float)(n2 + 1), inv2 = 1.0f / (float)n2;
   for (int e = threadIdx.x; e < nl * (n2 + 1); e += blockDim.x) {
-    const int l = e / (n2 + 1), k = e - l * (n2 + 1);
+    int k;
+    const int l = epfft::fdivmod(e, n2 + 1, inv1, k);
     P[l * ld + k] = l < nlv ? spec[(line0 + l) * nxh + k] : cmk<T>(T(0), T(0));
   }
   __syncthreads();
@@ -226,7 +231,8 @@ EP_DEV void x_inverse(const C2<T>* __restrict__ spec, long long line0, int nlv, 
   __syncthreads();
   const C2<T>* z = epfft::lines<T, +1>(Q, P, nl, ld, p2, tw, 2);
   for (int e = threadIdx.x; e < nl * n2; e += blockDim.x) {
-    const int l = e / n2, m = e - l * n2;
+    int m;
+    const int l = epfft::fdivmod(e, n2, inv2, m);
     const C2<T> v = z[l * ld + m];
     Rout[l * nx + 2 * m] = v.x * scale;
     Rout[l * nx + 2 * m + 1] = v.y * scale;
@@ -238,8 +244,10 @@ template <class T, class F>
 EP_DEV void x_forward(F val, C2<T>* __restrict__ out, long long line0, int nlv, int nl, int nx, int nxh,
                       C2<T>* P, C2<T>* Q, int ld, const FftPlan& p2, const C2<T>* tw) {
   const int n2 = nx / 2;
+  const float inv2 = 1.0f / (float)n2;
   for (int e = threadIdx.x; e < nl * n2; e += blockDim.x) {
-    const int l = e / n2, m = e - l * n2;
+    int m;
+    const int l = epfft::fdivmod(e, n2, inv2, m);
     P[l * ld + m] = l < nlv ? cmk<T>(val(l, 2 * m), val(l, 2 * m + 1)) : cmk<T>(T(0), T(0));
   }
   __syncthreads();
@@ -285,7 +293,8 @@ __global__ void k_x1(Geo g, const T* __restrict__ den, C2<T>* __restrict__ out, 
   __syncthreads();
   if (want_grad) {
     for (int e = threadIdx.x; e < nlv * nx; e += blockDim.x) {
-      const int l = e / nx, i = e - l * nx;
+      int i;
+      const int l = epfft::fdivmod(e, nx, 1.0f / (float)nx, i);
       const long long L = line0 + l, p = L * nx + i;
       const int iy = (int)(L % g.ny), iz = (int)(L / g.ny);
       dxo[p] = d1_line(R0 + l * nx, i, nx, fd.w1[0], fd.R, fd.periodic);
@@ -397,7 +406,8 @@ __global__ void k_x3(Geo g, Phys ph, FdW<T> fd, const C2<T>* __restrict__ D0, co
   }
   __syncthreads();
   for (int e = threadIdx.x; e < nlv * nx; e += blockDim.x) {
-    const int l = e / nx, i = e - l * nx;
+    int i;
+      const int l = epfft::fdivmod(e, nx, 1.0f / (float)nx, i);
     dgx[line0 * nx + e] = d1_line(Rc + l * nx, i, nx, fd.w1[0], fd.R, fd.periodic);
   }
   x_forward<T>(
@@ -463,6 +473,48 @@ EP_DEV LSmem<T> lsmem(unsigned char* raw, int LT, int n, int nbuf) {
   return s;
 }
 
+// Line loads/stores of the strided passes: LT is a power of two; up to 8
+// loads per thread are issued before their shared-memory stores (ILP).
+template <class T>
+EP_DEV void load_lines(const C2<T>* __restrict__ a, const LSmem<T>& s, int LT, int n, long long Sa,
+                       C2<T>* __restrict__ dst) {
+  const int total = LT * n;
+  const int lg = __ffs(LT) - 1;
+  for (int e0 = threadIdx.x; e0 < total; e0 += 8 * blockDim.x) {
+    C2<T> v[8];
+#pragma unroll
+    for (int i = 0; i < 8; ++i) {
+      const int e = e0 + i * blockDim.x;
+      v[i] = cmk<T>(T(0), T(0));
+      if (e < total) {
+        const int k = e >> lg, t = e & (LT - 1);
+        const long long b = s.base[t];
+        if (b >= 0) v[i] = a[b + k * Sa];
+      }
+    }
+#pragma unroll
+    for (int i = 0; i < 8; ++i) {
+      const int e = e0 + i * blockDim.x;
+      if (e < total) {
+        const int k = e >> lg, t = e & (LT - 1);
+        dst[t * s.ld + k] = v[i];
+      }
+    }
+  }
+}
+
+template <class T>
+EP_DEV void store_lines(C2<T>* __restrict__ a, const LSmem<T>& s, int LT, int n, long long Sa,
+                        const C2<T>* __restrict__ src) {
+  const int total = LT * n;
+  const int lg = __ffs(LT) - 1;
+  for (int e = threadIdx.x; e < total; e += blockDim.x) {
+    const int k = e >> lg, t = e & (LT - 1);
+    const long long b = s.base[t];
+    if (b >= 0) a[b + k * Sa] = src[t * s.ld + k];
+  }
+}
+
 template <class T, int DIR>
 __global__ void k_c2c(Arr8<T> arr, LineSet ls, FftPlan p, const C2<T>* __restrict__ twg, int LT) {
   extern __shared__ __align__(16) unsigned char smraw[];
@@ -476,18 +528,10 @@ __global__ void k_c2c(Arr8<T> arr, LineSet ls, FftPlan p, const C2<T>* __restric
     s.base[t] = L < ls.nlines ? (L % ls.Mi) + (L / ls.Mi) * ls.So : -1;
   }
   __syncthreads();
-  for (int e = threadIdx.x; e < LT * n; e += blockDim.x) {
-    const int k = e / LT, t = e - k * LT;
-    const long long b = s.base[t];
-    s.A[t * s.ld + k] = b >= 0 ? a[b + k * ls.Sa] : cmk<T>(T(0), T(0));
-  }
+  load_lines<T>(a, s, LT, n, ls.Sa, s.A);
   __syncthreads();
   const C2<T>* r = epfft::lines<T, DIR>(s.A, s.B, LT, s.ld, p, s.tw, 1);
-  for (int e = threadIdx.x; e < LT * n; e += blockDim.x) {
-    const int k = e / LT, t = e - k * LT;
-    const long long b = s.base[t];
-    if (b >= 0) a[b + k * ls.Sa] = r[t * s.ld + k];
-  }
+  store_lines<T>(a, s, LT, n, ls.Sa, r);
 }
 
 // Forward transform along the pass axis, then for each kernel table: multiply
@@ -507,32 +551,38 @@ __global__ void k_zconv(ConvSpec<T> cs, LineSet ls, FftPlan p, const C2<T>* __re
     s.base[t] = L < ls.nlines ? (L % ls.Mi) + (L / ls.Mi) * ls.So : -1;
   }
   __syncthreads();
-  for (int e = threadIdx.x; e < LT * n; e += blockDim.x) {
-    const int k = e / LT, t = e - k * LT;
-    const long long b = s.base[t];
-    s.A[t * s.ld + k] = b >= 0 ? in[b + k * ls.Sa] : cmk<T>(T(0), T(0));
-  }
+  load_lines<T>(in, s, LT, n, ls.Sa, s.A);
   __syncthreads();
   C2<T>* r = epfft::lines<T, -1>(s.A, s.B, LT, s.ld, p, s.tw, 1);
   C2<T>* o1 = (r == s.A) ? s.B : s.A;
   C2<T>* o2 = s.S;
   for (int j = 0; j < cs.nout[which]; ++j) {
     const T* ker = cs.ker[which][j];
-    for (int e = threadIdx.x; e < LT * n; e += blockDim.x) {
-      const int k = e / LT, t = e - k * LT;
-      const long long b = s.base[t];
-      const T kv = b >= 0 ? ker[b + k * ls.Sa] : T(0);
-      const C2<T> v = r[t * s.ld + k];
-      o1[t * s.ld + k] = cmk<T>(v.x * kv, v.y * kv);
+    const int lg = __ffs(LT) - 1;
+    for (int e0 = threadIdx.x; e0 < LT * n; e0 += 8 * blockDim.x) {
+      T kv[8];
+#pragma unroll
+      for (int i = 0; i < 8; ++i) {
+        const int e = e0 + i * blockDim.x;
+        kv[i] = T(0);
+        if (e < LT * n) {
+          const long long b = s.base[e & (LT - 1)];
+          if (b >= 0) kv[i] = ker[b + (e >> lg) * ls.Sa];
+        }
+      }
+#pragma unroll
+      for (int i = 0; i < 8; ++i) {
+        const int e = e0 + i * blockDim.x;
+        if (e < LT * n) {
+          const int k = e >> lg, t = e & (LT - 1);
+          const C2<T> v = r[t * s.ld + k];
+          o1[t * s.ld + k] = cmk<T>(v.x * kv[i], v.y * kv[i]);
+        }
+      }
     }
     __syncthreads();
     const C2<T>* q = epfft::lines<T, +1>(o1, o2, LT, s.ld, p, s.tw, 1);
-    C2<T>* out = cs.out[which][j];
-    for (int e = threadIdx.x; e < LT * n; e += blockDim.x) {
-      const int k = e / LT, t = e - k * LT;
-      const long long b = s.base[t];
-      if (b >= 0) out[b + k * ls.Sa] = q[t * s.ld + k];
-    }
+    store_lines<T>(cs.out[which][j], s, LT, n, ls.Sa, q);
     __syncthreads();
   }
 }
@@ -595,7 +645,7 @@ EP_DEV void lap_march(const Geo& g, const C2<T>* __restrict__ psi, const FdW<T>&
 // psiold(ioldp(3)) (read here point-wise), so the host swaps buffers instead
 // of copying.
 template <class T, int R>
-__global__ void __launch_bounds__(EP_TX* EP_TY) k_predict(Geo g, FdW<T> fd, Phys ph, int zc,
+__global__ void __launch_bounds__(EP_TX* EP_TY, sizeof(T) == 4 ? 4 : 2) k_predict(Geo g, FdW<T> fd, Phys ph, int zc,
                                                          const C2<T>* __restrict__ psi, const T* __restrict__ pot4,
                                                          const T* __restrict__ uimp, C2<T>* po3,
                                                          const C2<T>* __restrict__ h1, C2<T>* h2, C2<T>* pc,
@@ -616,7 +666,7 @@ __global__ void __launch_bounds__(EP_TX* EP_TY) k_predict(Geo g, FdW<T> fd, Phys
 // sum |pc|, sum |psi|^2 (new), <psi|H|psi> and sum |psi|^2 of the modified
 // psi (chemical potential).
 template <class T, int R>
-__global__ void __launch_bounds__(EP_TX* EP_TY) k_correct(Geo g, FdW<T> fd, Phys ph, int zc,
+__global__ void __launch_bounds__(EP_TX* EP_TY, sizeof(T) == 4 ? 4 : 2) k_correct(Geo g, FdW<T> fd, Phys ph, int zc,
                                                          const C2<T>* __restrict__ psi, const T* __restrict__ pot4,
                                                          const T* __restrict__ uimp,
                                                          const C2<T>* __restrict__ po3,
@@ -664,7 +714,7 @@ __global__ void __launch_bounds__(EP_TX* EP_TY) k_correct(Geo g, FdW<T> fd, Phys
 // first stage also records H into hout (the history shift itself is done
 // by rotating buffers).  den <= 0 raises a flag (steprk.f90:94-110).
 template <class T, int R>
-__global__ void __launch_bounds__(EP_TX* EP_TY) k_rkstage(Geo g, FdW<T> fd, Phys ph, int zc,
+__global__ void __launch_bounds__(EP_TX* EP_TY, sizeof(T) == 4 ? 4 : 2) k_rkstage(Geo g, FdW<T> fd, Phys ph, int zc,
                                                          const C2<T>* __restrict__ psi, const T* __restrict__ pot4,
                                                          const T* __restrict__ uimp, C2<T>* q,
                                                          C2<T>* __restrict__ out, C2<T>* __restrict__ hout,
