@@ -271,13 +271,17 @@ int ep_download_field(ep_ctx* c, int which, double* out) {
 
 int ep_potenimp(ep_ctx* c) {
   return dispatch(c, [&](auto& e) -> int {
-    int r = e.potenimp();
+    int r = e.ensure_materialized();
+    if (r) return r;
+    r = e.potenimp();
     return r ? r : e.check_flags();
   });
 }
 int ep_poten(ep_ctx* c) {
   return dispatch(c, [&](auto& e) -> int {
-    int r = e.poten();
+    int r = e.ensure_materialized();
+    if (r) return r;
+    r = e.poten();
     return r ? r : e.check_flags();
   });
 }
@@ -287,13 +291,18 @@ int ep_energy(ep_ctx* c, ep_energies* out) {
 }
 int ep_forceimp(ep_ctx* c, double* F) {
   if (!F) return EP_ERR_INVALID_ARG;
-  return dispatch(c, [&](auto& e) -> int { return e.forceimp(F); });
+  return dispatch(c, [&](auto& e) -> int {
+    int r = e.ensure_materialized();
+    return r ? r : e.forceimp(F);
+  });
 }
 int ep_potinvar(ep_ctx* c, double* hinvar) {
   if (!hinvar) return EP_ERR_INVALID_ARG;
   return dispatch(c, [&](auto& e) -> int {
     double F[3];
-    int r = e.forceimp(F);
+    int r = e.ensure_materialized();
+    if (r) return r;
+    r = e.forceimp(F);
     if (r) return r;
     std::complex<double> H[10];
     r = e.potinvar(H);
@@ -317,8 +326,8 @@ int ep_run(ep_ctx* c, int nsteps, double dt, ep_run_stats* stats) {
       const bool last = (s == nsteps - 1) && stats;
       int r = e.steppc(dt, last ? &se : nullptr);
       if (r) return r;
-      if (renorm && (r = e.rescale_pending())) return r;
     }
+    (void)renorm;
     if (stats) {
       stats->errHe = se.errHe;
       stats->mu = e.last_mu;
@@ -346,12 +355,14 @@ int ep_set_precision(ep_ctx* c, int precision) {
       c->e64 = new Engine<double>();
       if ((r = c->e64->init(cfg, c->st, &c->prof, &c->imp, &c->err))) { c->e64->release(); delete c->e64; c->e64 = nullptr; return r; }
     }
+    if ((r = c->e32->ensure_materialized())) return r;
     if ((r = c->e64->import_state(*c->e32))) return r;
   } else {
     if (!c->e32) {
       c->e32 = new Engine<float>();
       if ((r = c->e32->init(cfg, c->st, &c->prof, &c->imp, &c->err))) { c->e32->release(); delete c->e32; c->e32 = nullptr; return r; }
     }
+    if ((r = c->e64->ensure_materialized())) return r;
     if ((r = c->e32->import_state(*c->e64))) return r;
   }
   c->active = precision;
@@ -436,7 +447,7 @@ int ep_batch_run(ep_batch* b, int nsteps, double dt, ep_run_stats* stats) {
       int r = dispatch(c, [&](auto& e) -> int {
         int q = e.steppc(dt, last ? &se : nullptr);
         if (q) return q;
-        if (renorm && (q = e.rescale_pending())) return q;
+        (void)renorm;
         if (last) {
           stats[i].errHe = se.errHe;
           stats[i].mu = e.last_mu;

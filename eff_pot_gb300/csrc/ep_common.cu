@@ -63,3 +63,8 @@ __global__ void k_finalize(const double* __restrict__ partials, int nblocks, int
                            int mode, double N, double dxyz, double n4, int renorm) {
   finalize_block(partials, nblocks, nq, sc, out0, mode, N, dxyz, n4, renorm);
 }
+
+__global__ void k_reset_scales(DevScalars* sc) {
+  if (threadIdx.x < EP_NSLOTS) sc->bscale[threadIdx.x] = 1.0;
+  if (threadIdx.x == 0) sc->den_scale = 1.0;
+}

@@ -43,7 +43,13 @@ struct DevScalars {
   double errHe, norm, mu;
   unsigned int flags;   // bit 0: non-finite detected; bit 1: den <= 0
   unsigned int counter; // blocks done (last-block finalisation), reset to 0
+  unsigned int counter2;
+  // Lazy renormalisation: the logical value of rotating state buffer k is
+  // stored * bscale[k]; den's logical value is stored * den_scale.
+  double bscale[8];
+  double den_scale;
 };
+#define EP_NSLOTS 8
 enum { EP_FLAG_NONFINITE = 1u, EP_FLAG_DEN_NONPOS = 2u };
 
 // ---------------------------------------------------------------------------

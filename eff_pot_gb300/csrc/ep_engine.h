@@ -106,6 +106,10 @@ class Engine {
   int download_r(int which, double* h);
   int check_flags();
   int rescale_pending();
+  // Apply the lazy renormalisation scales before host-visible operations.
+  int ensure_materialized();
+  bool lazy = false;
+  CT* slot_base[EP_NSLOTS] = {};
 
   // precision conversion (the other engine's state -> this one)
   template <class U> int import_state(const Engine<U>& o);
@@ -121,6 +125,7 @@ class Engine {
   int read_sums(double* h, int n, int off);
   int fft_y(CT** arrs, int n, int dir);
   int zconv(const CT* const* in, CT* const (*out)[3], const T* const (*ker)[3], const int* nout, int nin);
+  int slot_of(const CT* p) const;
   int x_lines(int nreal) const;
   size_t x_smem(int nl, int nreal) const;
   int l_lines(int n, int nbuf) const;

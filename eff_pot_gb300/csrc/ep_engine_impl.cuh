@@ -178,9 +178,17 @@ int Engine<T>::init(const ep_config& c, cudaStream_t s, Prof* p, ImpState* im, s
   if ((r = alloc((void**)&partials, npartials * sizeof(double)))) return r;
   if ((r = alloc((void**)&sc, sizeof(DevScalars)))) return r;
 
+  {
+    CT* sb[EP_NSLOTS] = {psi, spare, po[0], po[1], po[2], ph[0], ph[1], pc};
+    for (int k = 0; k < EP_NSLOTS; ++k) slot_base[k] = sb[k];
+  }
   for (CT** b : cbufs) if ((r = cuda_ok(cudaMemsetAsync(*b, 0, N * sizeof(CT), st), "memset"))) return r;
   for (T** b : rbufs) if ((r = cuda_ok(cudaMemsetAsync(*b, 0, N * sizeof(T), st), "memset"))) return r;
   if ((r = cuda_ok(cudaMemsetAsync(sc, 0, sizeof(DevScalars), st), "memset"))) return r;
+  {
+    auto kr = k_reset_scales;
+    EP_LAUNCH("reset_scales", kr, 1, 32, 0, sc);
+  }
 
   std::vector<CT> tw;
   twiddles<T>(c.nx, tw);
@@ -379,6 +387,8 @@ int Engine<T>::read_sums(double* h, int n, int off) {
 template <class T>
 int Engine<T>::energy(ep_energies* e) {
   if (!have_field) { *err = "poten() must run before energy()"; return EP_ERR_STATE; }
+  int r0 = ensure_materialized();
+  if (r0) return r0;
   PotDev vp{imp->plus.kind, imp->plus.r_cutoff, imp->plus.umax, imp->plus.par[0], imp->plus.par[1], imp->plus.par[2]};
   auto k = k_energy<T>;
   EP_LAUNCH("energy", k, EP_RED_BLOCKS, 256, 0, g, fd, phys, psi, den, dencg, delj4, falfs, dxd, dyd, dzd, intx,
@@ -471,10 +481,12 @@ int Engine<T>::lap_predict(double dt) {
   dim3 grid((g.nx + EP_TX - 1) / EP_TX, (g.ny + EP_TY - 1) / EP_TY, (g.nz + EP_ZC - 1) / EP_ZC);
   dim3 blk(EP_TX, EP_TY);
   const T f = (T)(c4o3 * dt), c1 = (T)c112;
+  const Slots sl{slot_of(psi), slot_of(po3), -1, slot_of(h1), slot_of(h2), slot_of(pc), -1};
 #define EP_PRED(RR)                                                                                          \
   case RR: {                                                                                                 \
     auto k = k_predict<T, RR>;                                                                               \
-    EP_LAUNCH("predict", k, grid, blk, 0, g, fd, phys, EP_ZC, psi, pot4, uimp, po3, h1, h2, pc, den, f, c1); \
+    EP_LAUNCH("predict", k, grid, blk, 0, g, fd, phys, EP_ZC, psi, pot4, uimp, po3, h1, h2, pc, den, f, c1,  \
+              sc, sl);                                                                                       \
   } break;
   switch (fd.R) {
     EP_PRED(1) EP_PRED(2) EP_PRED(3) EP_PRED(4) EP_PRED(5) EP_PRED(6)
@@ -498,11 +510,12 @@ int Engine<T>::lap_correct(double dt, bool want) {
   dim3 blk(EP_TX, EP_TY);
   const T f3 = (T)(3.0 * dt), cc = (T)c9;
   const int renorm = (cfg.time_mode == EP_IMAGINARY_TIME && cfg.renormalize) ? 1 : 0;
+  const Slots sl{slot_of(psi), slot_of(po3), slot_of(po2), slot_of(h1), slot_of(h2), slot_of(pc), slot_of(spare)};
 #define EP_CORR(RR)                                                                                           \
   case RR: {                                                                                                  \
     auto k = k_correct<T, RR>;                                                                                \
     EP_LAUNCH("correct", k, grid, blk, 0, g, fd, phys, EP_ZC, psi, pot4, uimp, po3, po2, h1, h2, pc, spare, den, \
-              f3, cc, partials, sc, renorm, cfg.n4);                                                          \
+              f3, cc, partials, sc, renorm, cfg.n4, sl);                                                      \
   } break;
   switch (fd.R) {
     EP_CORR(1) EP_CORR(2) EP_CORR(3) EP_CORR(4) EP_CORR(5) EP_CORR(6)
@@ -514,6 +527,7 @@ int Engine<T>::lap_correct(double dt, bool want) {
   ioldp[2] = ioldp[1];
   ioldp[1] = ioldp[0];
   ioldp[0] = t;
+  if (renorm) lazy = true;
   return EP_OK;
 }
 
@@ -559,6 +573,10 @@ int Engine<T>::rk_stage(int jr, double dt) {
 template <class T>
 int Engine<T>::steprk(double dt) {
   if (!have_field) { *err = "poten() must run before steprk()"; return EP_ERR_STATE; }
+  {
+    int r0 = ensure_materialized();
+    if (r0) return r0;
+  }
   const double s2 = std::sqrt(2.0);
   const double arun[4] = {0.5, 1.0 - 1.0 / s2, 1.0 + 1.0 / s2, 1.0 / 6.0};
   const double brun[4] = {2.0, 1.0, 1.0, 2.0};
@@ -686,7 +704,9 @@ int Engine<T>::steppc(double dt, ep_step_errors* e) {
 
 template <class T>
 int Engine<T>::renormalize(double* norm_before, bool wait) {
-  // norm of psi -> scale -> rescale psi and den
+  // norm of psi -> scale -> rescale psi, the history and den
+  int r0 = ensure_materialized();
+  if (r0) return r0;
   auto kn = k_normsum<T>;
   EP_LAUNCH("normsum", kn, EP_RED_BLOCKS, 256, 0, psi, g.N, partials);
   int r;
@@ -721,6 +741,7 @@ int Engine<T>::check_flags() {
 template <class T>
 int Engine<T>::upload_psi(const double* h) {
   int r;
+  if ((r = ensure_materialized())) return r;
   if (sizeof(T) == sizeof(double)) {
     if ((r = cuda_ok(cudaMemcpyAsync(psi, h, g.N * sizeof(CT), cudaMemcpyHostToDevice, st), "upload psi"))) return r;
   } else {
@@ -739,6 +760,8 @@ int Engine<T>::upload_psi(const double* h) {
 
 template <class T>
 int Engine<T>::download_c(int which, double* h) {
+  int r0 = ensure_materialized();
+  if (r0) return r0;
   const CT* src = nullptr;
   switch (which) {
     case EP_CFIELD_PSI: src = psi; break;
@@ -768,6 +791,8 @@ int Engine<T>::download_c(int which, double* h) {
 
 template <class T>
 int Engine<T>::download_r(int which, double* h) {
+  int r0 = ensure_materialized();
+  if (r0) return r0;
   const T* src = nullptr;
   switch (which) {
     case EP_FIELD_DEN: src = den; break;
@@ -800,6 +825,26 @@ int Engine<T>::download_r(int which, double* h) {
     cudaFree(tmp);
   }
   return cuda_ok(cudaStreamSynchronize(st), "download");
+}
+
+template <class T>
+int Engine<T>::slot_of(const CT* p) const {
+  for (int k = 0; k < EP_NSLOTS; ++k)
+    if (slot_base[k] == p) return k;
+  return 0;
+}
+
+template <class T>
+int Engine<T>::ensure_materialized() {
+  if (!lazy) return EP_OK;
+  SlotPtrs<T> sp{};
+  for (int k = 0; k < EP_NSLOTS; ++k) sp.b[k] = slot_base[k];
+  auto km = k_materialize<T>;
+  EP_LAUNCH("materialize", km, 4 * 152, 256, 0, sp, den, g.N, sc);
+  auto kr = k_reset_scales;
+  EP_LAUNCH("reset_scales", kr, 1, 32, 0, sc);
+  lazy = false;
+  return EP_OK;
 }
 
 template <class T>

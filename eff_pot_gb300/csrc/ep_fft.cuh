@@ -120,10 +120,12 @@ EP_DEV void stage(const C2<T>* __restrict__ src, C2<T>* __restrict__ dst, int nl
   const int m = n / R;
   const int total = nl * m;
   const int tstep = (n / (Ns * R)) * tws;
-  const float inv_m = 1.0f / (float)m, inv_ns = 1.0f / (float)Ns;
+  const float inv_nl = 1.0f / (float)nl, inv_ns = 1.0f / (float)Ns;
+  // consecutive threads take the same butterfly of consecutive lines: the
+  // line stride ld is odd, so every access of a warp hits distinct banks
   for (int b = threadIdx.x; b < total; b += blockDim.x) {
-    int j, k;
-    const int line = fdivmod(b, m, inv_m, j);
+    int line, k;
+    const int j = fdivmod(b, nl, inv_nl, line);
     fdivmod(j, Ns, inv_ns, k);
     const C2<T>* s = src + line * ld;
     C2<T>* d = dst + line * ld;

@@ -597,7 +597,8 @@ __global__ void k_zconv(ConvSpec<T> cs, LineSet ls, FftPlan p, const C2<T>* __re
 #define EP_TY 8
 
 template <class T, int R, class F>
-EP_DEV void lap_march(const Geo& g, const C2<T>* __restrict__ psi, const FdW<T>& fd, int zc, C2<T>* sp, F&& f) {
+EP_DEV void lap_march(const Geo& g, const C2<T>* __restrict__ psi, const FdW<T>& fd, int zc, C2<T>* sp, F&& f,
+                      T scale = T(1)) {
   const int tx = threadIdx.x, ty = threadIdx.y;
   const int x = blockIdx.x * EP_TX + tx, y = blockIdx.y * EP_TY + ty;
   const int z0 = blockIdx.z * zc, z1 = min(z0 + zc, g.nz);
@@ -609,7 +610,8 @@ EP_DEV void lap_march(const Geo& g, const C2<T>* __restrict__ psi, const FdW<T>&
       if (!per) return cmk<T>(T(0), T(0));
       xx = wrapi(xx, g.nx); yy = wrapi(yy, g.ny); zz = wrapi(zz, g.nz);
     }
-    return psi[xx + (long long)g.nx * yy + sxy * zz];
+    const C2<T> v = psi[xx + (long long)g.nx * yy + sxy * zz];
+    return cmk<T>(v.x * scale, v.y * scale);
   };
   C2<T> q[2 * R + 1];
 #pragma unroll
@@ -641,6 +643,26 @@ EP_DEV void lap_march(const Geo& g, const C2<T>* __restrict__ psi, const FdW<T>&
   }
 }
 
+// Scale slots of the buffers a stencil kernel touches (see DevScalars).
+struct Slots {
+  int psi, a, b, h1, h2, pc, out;
+};
+
+// Last block of a kernel (every other block has finished and counted):
+// returns true in all threads of that block.
+EP_DEV bool last_block(unsigned int* counter) {
+  __shared__ bool last;
+  const int tid = threadIdx.x + blockDim.x * threadIdx.y;
+  const unsigned nb = gridDim.x * gridDim.y * gridDim.z;
+  __syncthreads();
+  if (tid == 0) {
+    __threadfence();
+    last = atomicAdd(counter, 1u) == nb - 1;
+  }
+  __syncthreads();
+  return last;
+}
+
 // Predictor + modifier of steppc.f90:53-64.  The new psi is written over
 // psiold(ioldp(3)) (read here point-wise), so the host swaps buffers instead
 // of copying.
@@ -649,17 +671,32 @@ __global__ void __launch_bounds__(EP_TX* EP_TY, sizeof(T) == 4 ? 4 : 2) k_predic
                                                          const C2<T>* __restrict__ psi, const T* __restrict__ pot4,
                                                          const T* __restrict__ uimp, C2<T>* po3,
                                                          const C2<T>* __restrict__ h1, C2<T>* h2, C2<T>* pc,
-                                                         T* __restrict__ den, T f, T c112) {
+                                                         T* __restrict__ den, T f, T c112, DevScalars* sc,
+                                                         Slots sl) {
   __shared__ C2<T> sp[(EP_TX + 2 * R) * (EP_TY + 2 * R)];
-  lap_march<T, R>(g, psi, fd, zc, sp, [&](long long p, C2<T> c, C2<T> lap) {
-    const C2<T> H = happly<T>(ph, lap, c, pot4[p], uimp[p]);
-    const C2<T> pp = po3[p] + f * ((T(2) * H - h1[p]) + T(2) * h2[p]);
-    const C2<T> pn = pp - c112 * pc[p];
-    po3[p] = pn;
-    pc[p] = pp;
-    h2[p] = H;
-    den[p] = pn.x * pn.x + pn.y * pn.y;
-  });
+  const T s3 = (T)sc->bscale[sl.a], s1 = (T)sc->bscale[sl.h1], s2 = (T)sc->bscale[sl.h2],
+          sp_ = (T)sc->bscale[sl.pc];
+  lap_march<T, R>(
+      g, psi, fd, zc, sp,
+      [&](long long p, C2<T> c, C2<T> lap) {
+        const C2<T> H = happly<T>(ph, lap, c, pot4[p], uimp[p]);
+        const C2<T> pp = s3 * po3[p] + f * ((T(2) * H - s1 * h1[p]) + T(2) * (s2 * h2[p]));
+        const C2<T> pn = pp - c112 * (sp_ * pc[p]);
+        po3[p] = pn;
+        pc[p] = pp;
+        h2[p] = H;
+        den[p] = pn.x * pn.x + pn.y * pn.y;
+      },
+      (T)sc->bscale[sl.psi]);
+  if (last_block(&sc->counter2)) {
+    if (threadIdx.x == 0 && threadIdx.y == 0) {
+      sc->bscale[sl.a] = 1.0;
+      sc->bscale[sl.h2] = 1.0;
+      sc->bscale[sl.pc] = 1.0;
+      sc->den_scale = 1.0;
+      sc->counter2 = 0u;
+    }
+  }
 }
 
 // Corrector + final value of steppc.f90:135-151 with fused reductions:
@@ -675,13 +712,15 @@ __global__ void __launch_bounds__(EP_TX* EP_TY, sizeof(T) == 4 ? 4 : 2) k_correc
                                                          const C2<T>* __restrict__ h2, C2<T>* pc,
                                                          C2<T>* __restrict__ out, T* __restrict__ den, T f3, T c9,
                                                          double* __restrict__ partials, DevScalars* sc, int renorm,
-                                                         double n4) {
+                                                         double n4, Slots sl) {
   __shared__ C2<T> sp[(EP_TX + 2 * R) * (EP_TY + 2 * R)];
   Acc<T> acc[4];
+  const T s3 = (T)sc->bscale[sl.a], s2o = (T)sc->bscale[sl.b], s1 = (T)sc->bscale[sl.h1],
+          s2 = (T)sc->bscale[sl.h2], sp_ = (T)sc->bscale[sl.pc];
   lap_march<T, R>(g, psi, fd, zc, sp, [&](long long p, C2<T> c, C2<T> lap) {
     const C2<T> H = happly<T>(ph, lap, c, pot4[p], uimp[p]);
-    const C2<T> p5 = T(0.125) * ((T(9) * po3[p] - po2[p]) + f3 * ((H + T(2) * h1[p]) - h2[p]));
-    const C2<T> pcn = pc[p] - p5;
+    const C2<T> p5 = T(0.125) * ((T(9) * (s3 * po3[p]) - s2o * po2[p]) + f3 * ((H + T(2) * (s1 * h1[p])) - s2 * h2[p]));
+    const C2<T> pcn = sp_ * pc[p] - p5;
     pc[p] = pcn;
     const C2<T> po = p5 + c9 * pcn;
     out[p] = po;
@@ -691,7 +730,7 @@ __global__ void __launch_bounds__(EP_TX* EP_TY, sizeof(T) == 4 ? 4 : 2) k_correc
     acc[1].add(dn);
     acc[2].add(hexp_t<T>(ph, c, H));
     acc[3].add(c.x * c.x + c.y * c.y);
-  });
+  }, (T)sc->bscale[sl.psi]);
   double v[4] = {acc[0].get(), acc[1].get(), acc[2].get(), acc[3].get()};
   block_reduce_store<4>(v, partials);
   // The last block to finish sums all partials (no block waits for another).
@@ -706,7 +745,16 @@ __global__ void __launch_bounds__(EP_TX* EP_TY, sizeof(T) == 4 ? 4 : 2) k_correc
   if (last) {
     __threadfence();
     finalize_block(partials, (int)nb, 4, sc, 0, 1, (double)g.N, ph.dxyz, n4, renorm);
-    if (tid == 0) sc->counter = 0u;
+    if (tid == 0) {
+      // renormalise lazily: every logical state value is multiplied by s;
+      // the buffers written here restart their scale at s
+      const double s = sc->scale;
+      for (int k = 0; k < EP_NSLOTS; ++k) sc->bscale[k] *= s;
+      sc->bscale[sl.pc] = s;
+      sc->bscale[sl.out] = s;
+      sc->den_scale = s * s;
+      sc->counter = 0u;
+    }
   }
 }
 
@@ -771,6 +819,31 @@ __global__ void k_rescale(C2<T>* __restrict__ psi, T* __restrict__ den, HistPtrs
     }
   }
 }
+
+// Apply the pending scales to the state buffers and den (then the scales
+// are reset by k_reset_scales, launched after this kernel).
+template <class T>
+struct SlotPtrs { C2<T>* b[EP_NSLOTS]; };
+template <class T>
+__global__ void k_materialize(SlotPtrs<T> bufs, T* __restrict__ den, long long N, const DevScalars* __restrict__ sc) {
+  T f[EP_NSLOTS];
+#pragma unroll
+  for (int k = 0; k < EP_NSLOTS; ++k) f[k] = (T)sc->bscale[k];
+  const T fd = (T)sc->den_scale;
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < N; i += (long long)gridDim.x * blockDim.x) {
+#pragma unroll
+    for (int k = 0; k < EP_NSLOTS; ++k) {
+      if (f[k] != T(1)) {
+        C2<T> v = bufs.b[k][i];
+        v.x *= f[k];
+        v.y *= f[k];
+        bufs.b[k][i] = v;
+      }
+    }
+    if (fd != T(1)) den[i] *= fd;
+  }
+}
+__global__ void k_reset_scales(DevScalars* sc);
 
 // Sum of partials (fixed order, compensated) -> sc->sums[out0 + q].
 // mode 1: corrector epilogue (errHe, norm, mu, renormalisation factor).
