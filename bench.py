@@ -142,6 +142,7 @@ def time_single(precision, psi, steps, warmup, device, profile=False):
     import eff_pot_gb300 as ep
     s = ep.Solver(make_cfg(precision, device=device))
     prepare(s, psi, 0.0)
+    tuned = s.autotune()
     for _ in range(3):
         s.steprk(DT)
     s.run(warmup, DT)
@@ -157,7 +158,7 @@ def time_single(precision, psi, steps, warmup, device, profile=False):
     launches = s.kernel_launches() - l0
     prof = s.profile_read() if profile else {}
     s.close()
-    return ms.value, launches, prof
+    return ms.value, launches, prof, tuned
 
 
 def run_reference(args):
@@ -236,8 +237,8 @@ def run_ours(args):
     k32 = K - k64
 
     # --- single instance: plain FP64 path, FP32 path with per-kernel events
-    ms64, _, _ = time_single("fp64", psi, K, args.warmup, local)
-    ms32, l32, prof = time_single("fp32", psi, K, args.warmup, local, profile=True)
+    ms64, _, _, tuned64 = time_single("fp64", psi, K, args.warmup, local)
+    ms32, l32, prof, tuned32 = time_single("fp32", psi, K, args.warmup, local, profile=True)
 
     # --- the batched scan, FP32 then FP64 refinement
     zs = [1.25 * k for k in range(args.batch)]
@@ -245,12 +246,15 @@ def run_ours(args):
     b = ep.Batch(cfgs)
     for s, z in zip(b, zs):
         prepare(s, psi, z)
+    b.autotune()
     b.steprk(DT)
     b.steprk(DT)
     b.steprk(DT)
-    # warm-up, including one precision round trip (allocates the FP64 buffers)
+    # warm-up, including one precision round trip (allocates the FP64 buffers,
+    # whose launch shapes are tuned too)
     b.run(args.warmup, DT)
     b.set_precision("fp64")
+    b.autotune()
     b.run(1, DT)
     b.set_precision("fp32")
     b.run(1, DT)
@@ -357,6 +361,7 @@ def run_ours(args):
                      "measured_on": "single FP32 instance, kernels timed alone (burst peak)",
                      "peak_source": "MEASURED_PEAKS.json hbm_gbs (of measured)" if "hbm_gbs" in peaks else "fallback"},
         "kernels_ms_per_step_fp32_single": {k: round(v, 4) for k, v in sorted(per_step.items(), key=lambda t: -t[1])},
+        "autotune": {"fp32": tuned32, "fp64": tuned64},
         "gpu_launches": launches,
         "clocks": clk.summary(),
         "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": args.batch * 16 * n3 / K,

@@ -122,6 +122,10 @@ _product_only = {
     "batch_event_record": (_I, [_P, _I]),
     "batch_event_elapsed": (_I, [_P, _I, _I, _D]),
     "batch_kernel_launches": (C.c_longlong, [_P]),
+    "autotune": (_I, [_P, C.c_char_p, _I]),
+    "get_launch_shapes": (_I, [_P, C.POINTER(_I)]),
+    "set_launch_shapes": (_I, [_P, C.POINTER(_I)]),
+    "batch_autotune": (_I, [_P]),
 }
 
 # Every symbol include/eff_pot.h declares.

@@ -519,6 +519,73 @@ long long ep_batch_kernel_launches(const ep_batch* b) {
   return n;
 }
 
+}  // extern "C"
+
+namespace {
+template <class E>
+void shapes_out(const E& e, int* s) {
+  s[0] = e.shp.xnl; s[1] = e.shp.xthr; s[2] = e.shp.ylt; s[3] = e.shp.ythr; s[4] = e.shp.zlt; s[5] = e.shp.zthr;
+}
+bool shapes_ok(const int* s) {
+  auto pow2 = [](int v) { return v >= 1 && v <= 64 && (v & (v - 1)) == 0; };
+  auto thr = [](int v) { return v >= 32 && v <= 1024 && v % 32 == 0; };
+  return s[0] >= 1 && s[0] <= 64 && thr(s[1]) && pow2(s[2]) && thr(s[3]) && pow2(s[4]) && thr(s[5]);
+}
+}  // namespace
+
+extern "C" {
+
+int ep_autotune(ep_ctx* c, char* report, int cap) {
+  return dispatch(c, [&](auto& e) -> int {
+    std::string rep;
+    int r = e.autotune(&rep);
+    if (report && cap > 0) {
+      std::strncpy(report, rep.c_str(), (size_t)cap - 1);
+      report[cap - 1] = 0;
+    }
+    return r;
+  });
+}
+
+int ep_get_launch_shapes(const ep_ctx* c, int* s) {
+  if (!c || !s) return EP_ERR_INVALID_ARG;
+  if (c->active == EP_FP64 && c->e64) shapes_out(*c->e64, s);
+  else if (c->e32) shapes_out(*c->e32, s);
+  else return EP_ERR_STATE;
+  return EP_OK;
+}
+
+int ep_set_launch_shapes(ep_ctx* c, const int* s) {
+  if (!c || !s || !shapes_ok(s)) return EP_ERR_INVALID_ARG;
+  Shapes sh;
+  sh.xnl = s[0]; sh.xthr = s[1]; sh.ylt = s[2]; sh.ythr = s[3]; sh.zlt = s[4]; sh.zthr = s[5];
+  if (c->active == EP_FP64 && c->e64) c->e64->shp = sh;
+  else if (c->e32) c->e32->shp = sh;
+  else return EP_ERR_STATE;
+  return EP_OK;
+}
+
+int ep_batch_autotune(ep_batch* b) {
+  if (!b) return EP_ERR_INVALID_ARG;
+  std::vector<int> done(b->ctx.size(), 0);
+  for (size_t i = 0; i < b->ctx.size(); ++i) {
+    if (done[i]) continue;
+    int r = ep_autotune(b->ctx[i], nullptr, 0);
+    if (r) return r;
+    int sh[6];
+    ep_get_launch_shapes(b->ctx[i], sh);
+    const ep_config& ci = b->ctx[i]->cfg;
+    for (size_t j = i; j < b->ctx.size(); ++j) {
+      const ep_config& cj = b->ctx[j]->cfg;
+      if (cj.nx == ci.nx && cj.ny == ci.ny && cj.nz == ci.nz && b->ctx[j]->active == b->ctx[i]->active) {
+        ep_set_launch_shapes(b->ctx[j], sh);
+        done[j] = 1;
+      }
+    }
+  }
+  return EP_OK;
+}
+
 int ep_synchronize(ep_ctx* c) {
   if (!c) return EP_ERR_INVALID_ARG;
   if (cudaStreamSynchronize(c->st) != cudaSuccess) return fail(c, EP_ERR_CUDA, cudaGetErrorString(cudaGetLastError()));

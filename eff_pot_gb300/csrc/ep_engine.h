@@ -47,9 +47,18 @@ struct ImpState {
   bool have_tables = false;
 };
 
+// Launch shapes of the FFT passes (lines per CTA and threads per CTA),
+// chosen by Engine::autotune.
+struct Shapes {
+  int xnl = 16, xthr = 256;  // X passes: x-lines per CTA, threads
+  int ylt = 16, ythr = 256;  // Y passes
+  int zlt = 16, zthr = 256;  // Z convolution passes
+};
+
 template <class T>
 class Engine {
  public:
+  Shapes shp;
   typedef C2<T> CT;
   ep_config cfg{};
   Geo g{};
@@ -105,6 +114,7 @@ class Engine {
   int download_c(int which, double* h);
   int download_r(int which, double* h);
   int check_flags();
+  int autotune(std::string* report);
   int rescale_pending();
   // Apply the lazy renormalisation scales before host-visible operations.
   int ensure_materialized();

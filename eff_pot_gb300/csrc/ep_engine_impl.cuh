@@ -98,7 +98,7 @@ size_t Engine<T>::x_smem(int nl, int nreal) const {
 }
 template <class T>
 int Engine<T>::x_lines(int nreal) const {
-  int nl = 16;
+  int nl = shp.xnl;
   while (nl > 1 && x_smem(nl, nreal) > EP_SMEM_CAP) nl /= 2;
   return nl;
 }
@@ -108,7 +108,7 @@ size_t Engine<T>::l_smem(int LT, int n, int nbuf) const {
 }
 template <class T>
 int Engine<T>::l_lines(int n, int nbuf) const {
-  int LT = 16;
+  int LT = nbuf == 3 ? shp.zlt : shp.ylt;
   while (LT > 1 && l_smem(LT, n, nbuf) > EP_SMEM_CAP) LT /= 2;
   return LT;
 }
@@ -237,6 +237,17 @@ int Engine<T>::init(const ep_config& c, cudaStream_t s, Prof* p, ImpState* im, s
   cudaFuncSetAttribute(k_c2c<T, -1>, cudaFuncAttributeMaxDynamicSharedMemorySize, big);
   cudaFuncSetAttribute(k_c2c<T, +1>, cudaFuncAttributeMaxDynamicSharedMemorySize, big);
   cudaFuncSetAttribute(k_zconv<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, big);
+  {
+    int dev = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&dev_sm, cudaDevAttrMultiProcessorCount, dev);
+    if (dev_sm <= 0) dev_sm = 152;
+  }
+#define EP_ATTR(RR)                                                                                      \
+  cudaFuncSetAttribute(k_predict<T, RR>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)march_smem<T, RR, 4, 2>()); \
+  cudaFuncSetAttribute(k_correct<T, RR>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)march_smem<T, RR, 5, 2>());
+  EP_ATTR(1) EP_ATTR(2) EP_ATTR(3) EP_ATTR(4) EP_ATTR(5) EP_ATTR(6)
+#undef EP_ATTR
   return cuda_ok(cudaStreamSynchronize(st), "init");
 }
 
@@ -262,10 +273,10 @@ int Engine<T>::fft_y(CT** arrs, int n, int dir) {
   const size_t sm = l_smem(LT, g.ny, 2);
   if (dir < 0) {
     auto k = k_c2c<T, -1>;
-    EP_LAUNCH("fft_y_fwd", k, grid, 256, sm, a, ls, pY, twy, LT);
+    EP_LAUNCH("fft_y_fwd", k, grid, shp.ythr, sm, a, ls, pY, twy, LT);
   } else {
     auto k = k_c2c<T, +1>;
-    EP_LAUNCH("fft_y_inv", k, grid, 256, sm, a, ls, pY, twy, LT);
+    EP_LAUNCH("fft_y_inv", k, grid, shp.ythr, sm, a, ls, pY, twy, LT);
   }
   return EP_OK;
 }
@@ -282,7 +293,7 @@ int Engine<T>::zconv(const CT* const* in, CT* const (*out)[3], const T* const (*
   const int LT = l_lines(g.nz, 3);
   dim3 grid((unsigned)((ls.nlines + LT - 1) / LT), (unsigned)nin);
   auto k = k_zconv<T>;
-  EP_LAUNCH("fft_z_conv", k, grid, 256, l_smem(LT, g.nz, 3), cs, ls, pZ, twz, LT);
+  EP_LAUNCH("fft_z_conv", k, grid, shp.zthr, l_smem(LT, g.nz, 3), cs, ls, pZ, twz, LT);
   return EP_OK;
 }
 
@@ -296,7 +307,7 @@ int Engine<T>::poten() {
   {
     const int nl = x_lines(1);
     auto k = k_x1<T>;
-    EP_LAUNCH("x1_r2c_den", k, (unsigned)((nlines + nl - 1) / nl), 256, x_smem(nl, 1), g, den, S[0], dxd, dyd,
+    EP_LAUNCH("x1_r2c_den", k, (unsigned)((nlines + nl - 1) / nl), shp.xthr, x_smem(nl, 1), g, den, S[0], dxd, dyd,
               dzd, grad ? 1 : 0, p2, twx, fd, nl);
   }
   CT* a1[1] = {S[0]};
@@ -313,7 +324,7 @@ int Engine<T>::poten() {
   {
     const int nl = x_lines(otc ? 3 : 2);
     auto k = k_x2<T>;
-    EP_LAUNCH("x2_c2r_r2c", k, (unsigned)((nlines + nl - 1) / nl), 256, x_smem(nl, otc ? 3 : 2), g, phys, Tb[0],
+    EP_LAUNCH("x2_c2r_r2c", k, (unsigned)((nlines + nl - 1) / nl), shp.xthr, x_smem(nl, otc ? 3 : 2), g, phys, Tb[0],
               Tb[1], Tb[2], den, dxd, dyd, dzd, dencg, delj4, pot4, falfs, S[0], S[1], S[2], S[3], p2, twx, nl);
   }
   CT* c4[4] = {S[0], S[1], S[2], S[3]};
@@ -330,7 +341,7 @@ int Engine<T>::poten() {
   {
     const int nl = x_lines(otc ? 4 : 1);
     auto k = k_x3<T>;
-    EP_LAUNCH("x3_c2r_r2c", k, (unsigned)((nlines + nl - 1) / nl), 256, x_smem(nl, otc ? 4 : 1), g, phys, fd,
+    EP_LAUNCH("x3_c2r_r2c", k, (unsigned)((nlines + nl - 1) / nl), shp.xthr, x_smem(nl, otc ? 4 : 1), g, phys, fd,
               Tb[0], Tb[1], Tb[2], Tb[3], den, dxd, dyd, dzd, falfs, pot4, intx, inty, intz, gy, gz, dgx, S[0], p2,
               twx, nl);
   }
@@ -345,7 +356,7 @@ int Engine<T>::poten() {
     if ((r = fft_y(e1, 1, +1))) return r;
     const int nl = x_lines(1);
     auto k = k_x4<T>;
-    EP_LAUNCH("x4_c2r_ualpha", k, (unsigned)((nlines + nl - 1) / nl), 256, x_smem(nl, 1), g, phys, fd, Tb[0], den,
+    EP_LAUNCH("x4_c2r_ualpha", k, (unsigned)((nlines + nl - 1) / nl), shp.xthr, x_smem(nl, 1), g, phys, fd, Tb[0], den,
               dgx, gy, gz, pot4, ualphas, p2, twx, nl);
   }
   have_field = true;
@@ -485,7 +496,7 @@ int Engine<T>::lap_predict(double dt) {
 #define EP_PRED(RR)                                                                                          \
   case RR: {                                                                                                 \
     auto k = k_predict<T, RR>;                                                                               \
-    EP_LAUNCH("predict", k, grid, blk, 0, g, fd, phys, EP_ZC, psi, pot4, uimp, po3, h1, h2, pc, den, f, c1,  \
+    EP_LAUNCH("predict", k, grid, blk, (march_smem<T, RR, 4, 2>()), g, fd, phys, EP_ZC, psi, pot4, uimp, po3, h1, h2, pc, den, f, c1,  \
               sc, sl);                                                                                       \
   } break;
   switch (fd.R) {
@@ -514,7 +525,7 @@ int Engine<T>::lap_correct(double dt, bool want) {
 #define EP_CORR(RR)                                                                                           \
   case RR: {                                                                                                  \
     auto k = k_correct<T, RR>;                                                                                \
-    EP_LAUNCH("correct", k, grid, blk, 0, g, fd, phys, EP_ZC, psi, pot4, uimp, po3, po2, h1, h2, pc, spare, den, \
+    EP_LAUNCH("correct", k, grid, blk, (march_smem<T, RR, 5, 2>()), g, fd, phys, EP_ZC, psi, pot4, uimp, po3, po2, h1, h2, pc, spare, den, \
               f3, cc, partials, sc, renorm, cfg.n4, sl);                                                      \
   } break;
   switch (fd.R) {
@@ -880,4 +891,69 @@ int Engine<T>::import_state(const Engine<U>& o) {
   last_mu = o.last_mu;
   last_norm = o.last_norm;
   return EP_OK;
+}
+
+// Autotuner of the FFT-pass launch shapes: times the idempotent poten()
+// pipeline on the current density for candidate (lines, threads) per pass
+// class, coordinate by coordinate, and keeps the fastest.
+template <class T>
+int Engine<T>::autotune(std::string* report) {
+  int r;
+  if ((r = ensure_materialized())) return r;
+  cudaEvent_t a = nullptr, b = nullptr;
+  cudaEventCreate(&a);
+  cudaEventCreate(&b);
+  auto timed = [&](float& best) -> int {
+    best = 1e30f;
+    for (int rep = 0; rep < 3; ++rep) {
+      cudaEventRecord(a, st);
+      int q = poten();
+      if (q) return q;
+      cudaEventRecord(b, st);
+      cudaEventSynchronize(b);
+      float ms = 0.f;
+      cudaEventElapsedTime(&ms, a, b);
+      if (rep > 0) best = std::min(best, ms);
+    }
+    return EP_OK;
+  };
+  const int lts[] = {4, 8, 16, 32};
+  const int nls[] = {2, 4, 8, 16, 32};
+  const int thrs[] = {64, 128, 256};
+  float base = 0.f;
+  if ((r = timed(base))) goto done;
+  for (int round = 0; round < 2; ++round) {
+    for (int cls = 0; cls < 3; ++cls) {
+      Shapes keep = shp;
+      float best = 1e30f;
+      Shapes bestS = shp;
+      for (int li = 0; li < (cls == 0 ? 5 : 4); ++li) {
+        for (int th : thrs) {
+          Shapes c = keep;
+          if (cls == 0) { c.xnl = nls[li]; c.xthr = th; if (x_smem(c.xnl, 4) > EP_SMEM_CAP) continue; }
+          else if (cls == 1) { c.ylt = lts[li]; c.ythr = th; if (l_smem(c.ylt, g.ny, 2) > EP_SMEM_CAP) continue; }
+          else { c.zlt = lts[li]; c.zthr = th; if (l_smem(c.zlt, g.nz, 3) > EP_SMEM_CAP) continue; }
+          shp = c;
+          float t = 0.f;
+          if ((r = timed(t))) goto done;
+          if (t < best) { best = t; bestS = c; }
+        }
+      }
+      shp = bestS;
+    }
+  }
+  {
+    float fin = 0.f;
+    if ((r = timed(fin))) goto done;
+    if (report) {
+      char buf[256];
+      snprintf(buf, sizeof buf, "poten %.3f -> %.3f ms; X %d lines x %d thr, Y %d x %d, Z %d x %d", base, fin,
+               shp.xnl, shp.xthr, shp.ylt, shp.ythr, shp.zlt, shp.zthr);
+      *report = buf;
+    }
+  }
+done:
+  cudaEventDestroy(a);
+  cudaEventDestroy(b);
+  return r;
 }

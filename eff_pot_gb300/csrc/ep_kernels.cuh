@@ -332,15 +332,20 @@ __global__ void k_x2(Geo g, Phys ph, const C2<T>* __restrict__ B0, const C2<T>* 
   x_inverse<T>(B0, line0, nlv, nl, nx, nxh, S.P, S.Q, S.ld, p2, S.tw, rn, Rcg);
   x_inverse<T>(B1, line0, nlv, nl, nx, nxh, S.P, S.Q, S.ld, p2, S.tw, rn, Rlj);
   if (otc) x_inverse<T>(B2, line0, nlv, nl, nx, nxh, S.P, S.Q, S.ld, p2, S.tw, rn, Ral);
-  const T a0 = (T)ph.a0, a1 = (T)ph.a1, den0s = (T)ph.den0s, cp4 = (T)ph.cp4, cpp4 = (T)ph.cpp4;
+  const T a0 = (T)ph.a0, a1 = (T)ph.a1, rden0s = (T)(1.0 / ph.den0s), cp4 = (T)ph.cp4, cpp4 = (T)ph.cpp4;
   for (int e = threadIdx.x; e < nlv * nx; e += blockDim.x) {
     const long long p = line0 * nx + e;
     const T cg = Rcg[e], lj = Rlj[e];
     dencg[p] = cg;
     delj4[p] = lj;
     pot4[p] = lj + cg * cg * (a0 + a1 * cg);
-    if (otc) falfs[p] = T(1) - Ral[e] / den0s;
+    if (otc) {
+      const T f = T(1) - Ral[e] * rden0s;
+      falfs[p] = f;
+      Ral[e] = f;  // the f * grad(den) transforms below reuse it
+    }
   }
+  __syncthreads();
   x_forward<T>(
       [&](int l, int i) {
         const T cg = Rcg[l * nx + i];
@@ -348,11 +353,11 @@ __global__ void k_x2(Geo g, Phys ph, const C2<T>* __restrict__ B0, const C2<T>* 
       },
       C0, line0, nlv, nl, nx, nxh, S.P, S.Q, S.ld, p2, S.tw);
   if (otc) {
-    x_forward<T>([&](int l, int i) { return (T(1) - Ral[l * nx + i] / den0s) * dxd[(line0 + l) * nx + i]; },
+    x_forward<T>([&](int l, int i) { return Ral[l * nx + i] * dxd[(line0 + l) * nx + i]; },
                  C1, line0, nlv, nl, nx, nxh, S.P, S.Q, S.ld, p2, S.tw);
-    x_forward<T>([&](int l, int i) { return (T(1) - Ral[l * nx + i] / den0s) * dyd[(line0 + l) * nx + i]; },
+    x_forward<T>([&](int l, int i) { return Ral[l * nx + i] * dyd[(line0 + l) * nx + i]; },
                  C2o, line0, nlv, nl, nx, nxh, S.P, S.Q, S.ld, p2, S.tw);
-    x_forward<T>([&](int l, int i) { return (T(1) - Ral[l * nx + i] / den0s) * dzd[(line0 + l) * nx + i]; },
+    x_forward<T>([&](int l, int i) { return Ral[l * nx + i] * dzd[(line0 + l) * nx + i]; },
                  C3, line0, nlv, nl, nx, nxh, S.P, S.Q, S.ld, p2, S.tw);
   }
 }
@@ -436,14 +441,14 @@ __global__ void k_x4(Geo g, Phys ph, FdW<T> fd, const C2<T>* __restrict__ F0, co
   __syncthreads();
   T* Ru = S.R;
   x_inverse<T>(F0, line0, nlv, nl, nx, nxh, S.P, S.Q, S.ld, p2, S.tw, (T)ph.renor, Ru);
-  const T den0s = (T)ph.den0s, h2 = (T)ph.h2o2m4, al = (T)ph.alphas;
+  const T rden0s = (T)(1.0 / ph.den0s), h2 = (T)ph.h2o2m4, al = (T)ph.alphas;
   for (int e = threadIdx.x; e < nlv * nx; e += blockDim.x) {
     const long long L = line0 + e / nx;
     const long long p = line0 * nx + e;
     const int iy = (int)(L % g.ny), iz = (int)(L / g.ny);
     const T dyy = d1_global(gy, p, iy, g.ny, (long long)nx, fd.w1[1], fd.R, fd.periodic);
     const T dzz = d1_global(gz, p, iz, g.nz, (long long)nx * g.ny, fd.w1[2], fd.R, fd.periodic);
-    const T ua = (((Ru[e] / den0s + dgx[p]) + dyy) + dzz) * h2 * al;
+    const T ua = (((Ru[e] * rden0s + dgx[p]) + dyy) + dzz) * h2 * al;
     ualphas[p] = ua;
     pot4[p] = (pot4[p] + ua) + penalty_of(ph, den[p]);
   }
@@ -643,6 +648,101 @@ EP_DEV void lap_march(const Geo& g, const C2<T>* __restrict__ psi, const FdW<T>&
   }
 }
 
+
+// Shared memory of the pipelined march: two planes with halo, two z-queue
+// slots, two copies of NC complex and NR real per-point inputs.
+template <class T, int R, int NC, int NR>
+constexpr size_t march_smem() {
+  return (size_t)2 * (EP_TX + 2 * R) * (EP_TY + 2 * R) * sizeof(C2<T>) + (size_t)2 * EP_TX * EP_TY * sizeof(C2<T>) +
+         (size_t)2 * NC * EP_TX * EP_TY * sizeof(C2<T>) + (size_t)2 * NR * EP_TX * EP_TY * sizeof(T);
+}
+
+// The 2.5-D march of lap_march, software-pipelined: while plane z is
+// computed, cp.async brings plane z+1 (with halo), the z-queue element
+// (x, y, z+1+R) and the NC complex / NR real per-point inputs of plane z+1
+// into the other half of a double buffer.  f(p, psi, lap, ic, ir) gets the
+// point's inputs as ic[i * NT] / ir[i * NT] in shared memory.  psi values
+// are stored raw and multiplied by scale once (the Laplacian is linear).
+template <class T, int R, int NC, int NR, class F>
+EP_DEV void lap_march_async(const Geo& g, const C2<T>* __restrict__ psi, const FdW<T>& fd, int zc,
+                            unsigned char* smem, const C2<T>* const* cin, const T* const* rin, T scale, F&& f) {
+  typedef C2<T> CT;
+  constexpr int W = EP_TX + 2 * R, H = EP_TY + 2 * R, PL = W * H, NT = EP_TX * EP_TY;
+  CT* sp = reinterpret_cast<CT*>(smem);
+  CT* sq = sp + 2 * PL;
+  CT* sc_ = sq + 2 * NT;
+  T* sr = reinterpret_cast<T*>(sc_ + 2 * NC * NT);
+  const int tx = threadIdx.x, ty = threadIdx.y, tid = ty * EP_TX + tx;
+  const int x = blockIdx.x * EP_TX + tx, y = blockIdx.y * EP_TY + ty;
+  const int z0 = blockIdx.z * zc, z1 = min(z0 + zc, g.nz);
+  const bool valid = (x < g.nx) && (y < g.ny);
+  const int per = fd.periodic;
+  const long long sxy = (long long)g.nx * g.ny;
+  auto addr = [&](int xx, int yy, int zz) -> long long {
+    if (xx < 0 || xx >= g.nx || yy < 0 || yy >= g.ny || zz < 0 || zz >= g.nz) {
+      if (!per) return -1;
+      xx = wrapi(xx, g.nx);
+      yy = wrapi(yy, g.ny);
+      zz = wrapi(zz, g.nz);
+    }
+    return xx + (long long)g.nx * yy + sxy * zz;
+  };
+  auto prefetch = [&](int z, int buf) {
+    CT* P = sp + buf * PL;
+    for (int e = tid; e < PL; e += NT) {
+      const int r = e / W, c = e - r * W;
+      const long long a = addr(blockIdx.x * EP_TX - R + c, blockIdx.y * EP_TY - R + r, z);
+      if (a >= 0) cp_async<sizeof(CT)>(P + e, psi + a);
+      else P[e] = cmk<T>(T(0), T(0));
+    }
+    if (valid) {
+      const long long aq = addr(x, y, z + R);
+      if (aq >= 0) cp_async<sizeof(CT)>(sq + buf * NT + tid, psi + aq);
+      else sq[buf * NT + tid] = cmk<T>(T(0), T(0));
+      const long long p = x + (long long)g.nx * y + sxy * z;
+#pragma unroll
+      for (int i = 0; i < NC; ++i) cp_async<sizeof(CT)>(sc_ + (buf * NC + i) * NT + tid, cin[i] + p);
+#pragma unroll
+      for (int i = 0; i < NR; ++i) cp_async<sizeof(T)>(sr + (buf * NR + i) * NT + tid, rin[i] + p);
+    }
+    cp_commit();
+  };
+  CT q[2 * R + 1];
+#pragma unroll
+  for (int k = 0; k < 2 * R; ++k) {
+    const long long a = valid ? addr(x, y, z0 - R + k) : -1;
+    q[k] = a >= 0 ? psi[a] : cmk<T>(T(0), T(0));
+  }
+  prefetch(z0, 0);
+  for (int z = z0; z < z1; ++z) {
+    const int buf = (z - z0) & 1;
+    if (z + 1 < z1) {
+      prefetch(z + 1, buf ^ 1);
+      cp_wait<1>();
+    } else {
+      cp_wait<0>();
+    }
+    __syncthreads();
+    if (valid) {
+      q[2 * R] = sq[buf * NT + tid];
+      const CT* row = sp + buf * PL + (ty + R) * W + (tx + R);
+      const CT c = q[R];
+      CT lx = fd.w2[0][0] * c, ly = fd.w2[1][0] * c, lz = fd.w2[2][0] * c;
+#pragma unroll
+      for (int k = 1; k <= R; ++k) {
+        lx = lx + fd.w2[0][k] * (row[-k] + row[k]);
+        ly = ly + fd.w2[1][k] * (row[-k * W] + row[k * W]);
+        lz = lz + fd.w2[2][k] * (q[R - k] + q[R + k]);
+      }
+      f((long long)x + (long long)g.nx * y + sxy * z, scale * c, scale * ((lx + ly) + lz),
+        sc_ + buf * NC * NT + tid, sr + buf * NR * NT + tid);
+    }
+#pragma unroll
+    for (int k = 0; k < 2 * R; ++k) q[k] = q[k + 1];
+    __syncthreads();
+  }
+}
+
 // Scale slots of the buffers a stencil kernel touches (see DevScalars).
 struct Slots {
   int psi, a, b, h1, h2, pc, out;
@@ -673,21 +773,23 @@ __global__ void __launch_bounds__(EP_TX* EP_TY, sizeof(T) == 4 ? 4 : 2) k_predic
                                                          const C2<T>* __restrict__ h1, C2<T>* h2, C2<T>* pc,
                                                          T* __restrict__ den, T f, T c112, DevScalars* sc,
                                                          Slots sl) {
-  __shared__ C2<T> sp[(EP_TX + 2 * R) * (EP_TY + 2 * R)];
+  extern __shared__ __align__(16) unsigned char smraw[];
+  constexpr int NT = EP_TX * EP_TY;
   const T s3 = (T)sc->bscale[sl.a], s1 = (T)sc->bscale[sl.h1], s2 = (T)sc->bscale[sl.h2],
           sp_ = (T)sc->bscale[sl.pc];
-  lap_march<T, R>(
-      g, psi, fd, zc, sp,
-      [&](long long p, C2<T> c, C2<T> lap) {
-        const C2<T> H = happly<T>(ph, lap, c, pot4[p], uimp[p]);
-        const C2<T> pp = s3 * po3[p] + f * ((T(2) * H - s1 * h1[p]) + T(2) * (s2 * h2[p]));
-        const C2<T> pn = pp - c112 * (sp_ * pc[p]);
+  const C2<T>* cin[4] = {po3, h1, h2, pc};
+  const T* rin[2] = {pot4, uimp};
+  lap_march_async<T, R, 4, 2>(
+      g, psi, fd, zc, smraw, cin, rin, (T)sc->bscale[sl.psi],
+      [&](long long p, C2<T> c, C2<T> lap, const C2<T>* ic, const T* ir) {
+        const C2<T> H = happly<T>(ph, lap, c, ir[0], ir[NT]);
+        const C2<T> pp = s3 * ic[0] + f * ((T(2) * H - s1 * ic[NT]) + T(2) * (s2 * ic[2 * NT]));
+        const C2<T> pn = pp - c112 * (sp_ * ic[3 * NT]);
         po3[p] = pn;
         pc[p] = pp;
         h2[p] = H;
         den[p] = pn.x * pn.x + pn.y * pn.y;
-      },
-      (T)sc->bscale[sl.psi]);
+      });
   if (last_block(&sc->counter2)) {
     if (threadIdx.x == 0 && threadIdx.y == 0) {
       sc->bscale[sl.a] = 1.0;
@@ -713,14 +815,18 @@ __global__ void __launch_bounds__(EP_TX* EP_TY, sizeof(T) == 4 ? 4 : 2) k_correc
                                                          C2<T>* __restrict__ out, T* __restrict__ den, T f3, T c9,
                                                          double* __restrict__ partials, DevScalars* sc, int renorm,
                                                          double n4, Slots sl) {
-  __shared__ C2<T> sp[(EP_TX + 2 * R) * (EP_TY + 2 * R)];
+  extern __shared__ __align__(16) unsigned char smraw[];
+  constexpr int NT = EP_TX * EP_TY;
   Acc<T> acc[4];
   const T s3 = (T)sc->bscale[sl.a], s2o = (T)sc->bscale[sl.b], s1 = (T)sc->bscale[sl.h1],
           s2 = (T)sc->bscale[sl.h2], sp_ = (T)sc->bscale[sl.pc];
-  lap_march<T, R>(g, psi, fd, zc, sp, [&](long long p, C2<T> c, C2<T> lap) {
-    const C2<T> H = happly<T>(ph, lap, c, pot4[p], uimp[p]);
-    const C2<T> p5 = T(0.125) * ((T(9) * (s3 * po3[p]) - s2o * po2[p]) + f3 * ((H + T(2) * (s1 * h1[p])) - s2 * h2[p]));
-    const C2<T> pcn = sp_ * pc[p] - p5;
+  const C2<T>* cin[5] = {po3, po2, h1, h2, pc};
+  const T* rin[2] = {pot4, uimp};
+  lap_march_async<T, R, 5, 2>(g, psi, fd, zc, smraw, cin, rin, (T)sc->bscale[sl.psi],
+                              [&](long long p, C2<T> c, C2<T> lap, const C2<T>* ic, const T* ir) {
+    const C2<T> H = happly<T>(ph, lap, c, ir[0], ir[NT]);
+    const C2<T> p5 = T(0.125) * ((T(9) * (s3 * ic[0]) - s2o * ic[NT]) + f3 * ((H + T(2) * (s1 * ic[2 * NT])) - s2 * ic[3 * NT]));
+    const C2<T> pcn = sp_ * ic[4 * NT] - p5;
     pc[p] = pcn;
     const C2<T> po = p5 + c9 * pcn;
     out[p] = po;
@@ -730,7 +836,7 @@ __global__ void __launch_bounds__(EP_TX* EP_TY, sizeof(T) == 4 ? 4 : 2) k_correc
     acc[1].add(dn);
     acc[2].add(hexp_t<T>(ph, c, H));
     acc[3].add(c.x * c.x + c.y * c.y);
-  }, (T)sc->bscale[sl.psi]);
+  });
   double v[4] = {acc[0].get(), acc[1].get(), acc[2].get(), acc[3].get()};
   block_reduce_store<4>(v, partials);
   // The last block to finish sums all partials (no block waits for another).

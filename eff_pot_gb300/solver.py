@@ -241,6 +241,21 @@ class Solver:
     def precision(self):
         return "fp32" if self._f["get_precision"](self._h) == _abi.EP_FP32 else "fp64"
 
+    def autotune(self):
+        """Pick the FFT-pass launch shapes for this grid (needs a density)."""
+        buf = C.create_string_buffer(256)
+        self._check(self._f["autotune"](self._h, buf, 256), "autotune")
+        return buf.value.decode()
+
+    def launch_shapes(self):
+        a = (C.c_int * 6)()
+        self._check(self._f["get_launch_shapes"](self._h, a), "get_launch_shapes")
+        return list(a)
+
+    def set_launch_shapes(self, shapes):
+        a = (C.c_int * 6)(*shapes)
+        self._check(self._f["set_launch_shapes"](self._h, a), "set_launch_shapes")
+
     # -- product-only services ----------------------------------------------
     def synchronize(self):
         self._check(self._f["synchronize"](self._h), "synchronize")
@@ -320,6 +335,9 @@ class Batch:
     def set_precision(self, precision):
         p = {"fp32": _abi.EP_FP32, "fp64": _abi.EP_FP64}.get(precision, precision)
         self._check(self._f["batch_set_precision"](self._h, p), "batch_set_precision")
+
+    def autotune(self):
+        self._check(self._f["batch_autotune"](self._h), "batch_autotune")
 
     def synchronize(self):
         self._check(self._f["batch_synchronize"](self._h), "batch_synchronize")

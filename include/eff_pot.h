@@ -209,6 +209,18 @@ int ep_batch_event_record(ep_batch* b, int slot);
 int ep_batch_event_elapsed(ep_batch* b, int slot_a, int slot_b, double* ms);
 long long ep_batch_kernel_launches(const ep_batch* b);
 
+/* Autotuner: times the poten() pipeline on the current density for
+ * candidate launch shapes of the FFT passes (lines and threads per CTA of
+ * the X, Y and Z passes) and keeps the fastest.  Needs a density (after
+ * ep_upload_psi).  report (cap bytes, may be NULL) receives a summary.
+ * shapes[6] = {x lines, x threads, y lines, y threads, z lines, z threads}. */
+int ep_autotune(ep_ctx* ctx, char* report, int cap);
+int ep_get_launch_shapes(const ep_ctx* ctx, int* shapes);
+int ep_set_launch_shapes(ep_ctx* ctx, const int* shapes);
+/* Tunes each distinct grid of the batch once and gives the shapes to every
+ * instance with that grid. */
+int ep_batch_autotune(ep_batch* b);
+
 /* Device synchronisation, timing and counters. */
 int ep_synchronize(ep_ctx* ctx);
 /* The CUDA stream all work of this context is launched on (cudaStream_t). */

@@ -114,3 +114,25 @@ def test_fp32_then_fp64_refinement_reaches_the_fp64_ground_state():
     # of the slow modes that the FP64 sweeps leave: gate it at 1e-6 relative.
     assert abs(e64["ustar"]) > 1.0
     assert abs(e32["ustar"] - e64["ustar"]) < 1e-6 * abs(e64["ustar"]), (e32["ustar"], e64["ustar"])
+
+
+@pytest.mark.parametrize("prec", [_abi.EP_FP64, _abi.EP_FP32])
+def test_autotune_keeps_results_bit_identical(prec):
+    """Launch shapes only change the thread-to-work mapping, never the
+    arithmetic: poten fields agree bit for bit before and after tuning."""
+    cfg = cfg_of(n=48, xmax=24.0, precision=prec)
+    psi = ep.woods_saxon_psi(48, 48, 48, 24.0, 24.0, 24.0, 200.0, seed=7)
+    with ep.Solver(cfg) as s:
+        prepare(s, psi, (0.3, 0.0, -0.2))
+        before = {f: s.field(f) for f in ("pot4", "dencg", "delj4", "ualphas", "intxalf")}
+        rep = s.autotune()
+        assert "poten" in rep
+        sh = s.launch_shapes()
+        s.set_launch_shapes([2, 64, 4, 64, 4, 64])
+        s.poten()
+        odd = {f: s.field(f) for f in before}
+        s.set_launch_shapes(sh)
+        s.poten()
+        for f in before:
+            assert np.array_equal(before[f], s.field(f)), f
+            assert np.array_equal(before[f], odd[f]), f
