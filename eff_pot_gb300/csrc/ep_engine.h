@@ -134,6 +134,8 @@ class Engine {
   int reduce_finalize(int nblocks, int nq, int out0, int mode);
   int read_sums(double* h, int n, int off);
   int fft_y(CT** arrs, int n, int dir);
+  template <int N> int rfft_y(const Arr8<T>& a, int n, const LineSet& ls, int dir);
+  template <int N> int rfft_z(const ConvSpec<T>& cs, int nin, const LineSet& ls);
   int zconv(const CT* const* in, CT* const (*out)[3], const T* const (*ker)[3], const int* nout, int nin);
   int slot_of(const CT* p) const;
   int x_lines(int nreal) const;

@@ -6,6 +6,7 @@
 
 #include "ep_engine.h"
 #include "ep_kernels_impl.cuh"
+#include "ep_rfft.cuh"
 
 #define EP_ZC 16
 #define EP_RED_BLOCKS 1216
@@ -237,6 +238,12 @@ int Engine<T>::init(const ep_config& c, cudaStream_t s, Prof* p, ImpState* im, s
   cudaFuncSetAttribute(k_c2c<T, -1>, cudaFuncAttributeMaxDynamicSharedMemorySize, big);
   cudaFuncSetAttribute(k_c2c<T, +1>, cudaFuncAttributeMaxDynamicSharedMemorySize, big);
   cudaFuncSetAttribute(k_zconv<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, big);
+#define EP_RFFT_ATTR(NN)                                                                                  \
+  cudaFuncSetAttribute(k_c2c_r<T, NN, -1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)rfft::smem_bytes<T, NN>()); \
+  cudaFuncSetAttribute(k_c2c_r<T, NN, +1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)rfft::smem_bytes<T, NN>()); \
+  cudaFuncSetAttribute(k_zconv_r<T, NN>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)rfft::smem_bytes<T, NN>());
+  EP_RFFT_ATTR(32) EP_RFFT_ATTR(64) EP_RFFT_ATTR(128) EP_RFFT_ATTR(256)
+#undef EP_RFFT_ATTR
   {
     int dev = 0;
     cudaGetDevice(&dev);
@@ -263,11 +270,43 @@ void Engine<T>::release() {
 }
 
 // ---------------------------------------------------------------------------
+// Register-resident transforms (ep_rfft.cuh) of lines of length N.
+template <class T>
+template <int N>
+int Engine<T>::rfft_y(const Arr8<T>& a, int n, const LineSet& ls, int dir) {
+  dim3 grid((unsigned)((ls.nlines + 31) / 32), (unsigned)n), blk(32, rfft::Shape<N>::P);
+  const size_t sm = rfft::smem_bytes<T, N>();
+  if (dir < 0) {
+    auto k = k_c2c_r<T, N, -1>;
+    EP_LAUNCH("fft_y_fwd", k, grid, blk, sm, a, ls, twy);
+  } else {
+    auto k = k_c2c_r<T, N, +1>;
+    EP_LAUNCH("fft_y_inv", k, grid, blk, sm, a, ls, twy);
+  }
+  return EP_OK;
+}
+
+template <class T>
+template <int N>
+int Engine<T>::rfft_z(const ConvSpec<T>& cs, int nin, const LineSet& ls) {
+  dim3 grid((unsigned)((ls.nlines + 31) / 32), (unsigned)nin), blk(32, rfft::Shape<N>::P);
+  auto k = k_zconv_r<T, N>;
+  EP_LAUNCH("fft_z_conv", k, grid, blk, (rfft::smem_bytes<T, N>()), cs, ls, twz);
+  return EP_OK;
+}
+
 template <class T>
 int Engine<T>::fft_y(CT** arrs, int n, int dir) {
   Arr8<T> a{};
   for (int i = 0; i < n; ++i) a.a[i] = arrs[i];
   LineSet ls{(long long)g.nxh, (long long)g.nxh * g.ny, (long long)g.nxh, (long long)g.nxh * g.nz};
+  switch (g.ny) {
+    case 32: return rfft_y<32>(a, n, ls, dir);
+    case 64: return rfft_y<64>(a, n, ls, dir);
+    case 128: return rfft_y<128>(a, n, ls, dir);
+    case 256: return rfft_y<256>(a, n, ls, dir);
+    default: break;
+  }
   const int LT = l_lines(g.ny, 2);
   dim3 grid((unsigned)((ls.nlines + LT - 1) / LT), (unsigned)n);
   const size_t sm = l_smem(LT, g.ny, 2);
@@ -290,6 +329,13 @@ int Engine<T>::zconv(const CT* const* in, CT* const (*out)[3], const T* const (*
     for (int j = 0; j < nout[i]; ++j) { cs.out[i][j] = out[i][j]; cs.ker[i][j] = ker[i][j]; }
   }
   LineSet ls{(long long)g.nxh * g.ny, 0, (long long)g.nxh * g.ny, (long long)g.nxh * g.ny};
+  switch (g.nz) {
+    case 32: return rfft_z<32>(cs, nin, ls);
+    case 64: return rfft_z<64>(cs, nin, ls);
+    case 128: return rfft_z<128>(cs, nin, ls);
+    case 256: return rfft_z<256>(cs, nin, ls);
+    default: break;
+  }
   const int LT = l_lines(g.nz, 3);
   dim3 grid((unsigned)((ls.nlines + LT - 1) / LT), (unsigned)nin);
   auto k = k_zconv<T>;
@@ -924,6 +970,8 @@ int Engine<T>::autotune(std::string* report) {
   if ((r = timed(base))) goto done;
   for (int round = 0; round < 2; ++round) {
     for (int cls = 0; cls < 3; ++cls) {
+      // register-resident Y / Z transforms have a fixed shape
+      if ((cls == 1 && rfft::supported(g.ny)) || (cls == 2 && rfft::supported(g.nz))) continue;
       Shapes keep = shp;
       float best = 1e30f;
       Shapes bestS = shp;

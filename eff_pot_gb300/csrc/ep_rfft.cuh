@@ -1,0 +1,207 @@
+// ep_rfft.cuh - register-resident FFTs of strided lines (the Y and Z passes)
+// for line lengths N in {32, 64, 128, 256}.
+//
+// A CTA owns 32 lines whose first elements are (nearly) contiguous in memory
+// (the x index runs fastest) and P threads per line: lane = line, warp = t.
+// With N = E * P every thread holds E elements, and the transform is the
+// two-factor decomposition
+//
+//   n = t + P a   (t < P, a < E),     k = ka + E kt   (ka < E, kt < P)
+//   X[ka + E kt] = sum_t w_P^(t kt) w_N^(t ka) sum_a x[t + P a] w_E^(a ka)
+//
+// step 1: thread t loads x[t + P a] straight from global memory (each warp
+//         load touches 32 consecutive lines: coalesced), runs the E-point
+//         DFT over a in registers and applies w_N^(t ka);
+// exchange: one pass through shared memory (row stride N+1: conflict-free);
+// step 2: thread w runs the P-point DFTs of ka = w + P j (j < E/P) and then
+//         holds X[w + P m] with m = j + (E/P) kt -- the same stride-P
+//         subsequence step 1 reads, so a product in k-space followed by the
+//         inverse transform needs no further exchange, and stores are again
+//         coalesced.
+// The general shared-memory Stockham engine (ep_fft.cuh) covers every other
+// length.  Conventions are those of ep_fft.cuh: forward exp(-2 pi i kn/N),
+// unnormalised both ways.
+#pragma once
+#include "ep_fft.cuh"
+#include "ep_kernels.cuh"
+
+namespace rfft {
+
+template <int N> struct Shape;
+template <> struct Shape<32> { static constexpr int P = 4, E = 8; };
+template <> struct Shape<64> { static constexpr int P = 8, E = 8; };
+template <> struct Shape<128> { static constexpr int P = 8, E = 16; };
+template <> struct Shape<256> { static constexpr int P = 16, E = 16; };
+
+inline constexpr bool supported(int n) { return n == 32 || n == 64 || n == 128 || n == 256; }
+
+template <class T> struct K16;
+template <> struct K16<double> {
+  static constexpr double c = 0.92387953251128675612818318939678829;  // cos(pi/8)
+  static constexpr double s = 0.38268343236508977172845998403039887;  // sin(pi/8)
+  static constexpr double r = 0.70710678118654752440084436210484904;  // 1/sqrt(2)
+};
+template <> struct K16<float> {
+  static constexpr float c = 0.92387953251128675612818318939678829f;
+  static constexpr float s = 0.38268343236508977172845998403039887f;
+  static constexpr float r = 0.70710678118654752440084436210484904f;
+};
+
+// z * (a + DIR b i)
+template <class T, int DIR> EP_DEV C2<T> rotc(C2<T> z, T a, T b) {
+  const T bb = DIR < 0 ? -b : b;
+  return cmk<T>(z.x * a - z.y * bb, z.x * bb + z.y * a);
+}
+
+// 16-point DFT as 4 x 4: n = 4 n1 + n2, k = k1 + 4 k2.
+template <class T, int DIR> EP_DEV void dft16(C2<T>* v) {
+  C2<T> y[16];
+#pragma unroll
+  for (int n2 = 0; n2 < 4; ++n2) {
+    C2<T> a[4] = {v[n2], v[4 + n2], v[8 + n2], v[12 + n2]};
+    epfft::dft4<T, DIR>(a);
+#pragma unroll
+    for (int k1 = 0; k1 < 4; ++k1) y[4 * n2 + k1] = a[k1];
+  }
+  // w16^(n2 k1) for n2, k1 in 1..3: exponents 1 2 3 / 2 4 6 / 3 6 9
+  const T c = K16<T>::c, s = K16<T>::s, r = K16<T>::r;
+  y[5] = rotc<T, DIR>(y[5], c, s);
+  y[6] = rotc<T, DIR>(y[6], r, r);
+  y[7] = rotc<T, DIR>(y[7], s, c);
+  y[9] = rotc<T, DIR>(y[9], r, r);
+  y[10] = epfft::rot<DIR>(y[10]);
+  y[11] = rotc<T, DIR>(y[11], -r, r);
+  y[13] = rotc<T, DIR>(y[13], s, c);
+  y[14] = rotc<T, DIR>(y[14], -r, r);
+  y[15] = rotc<T, DIR>(y[15], -c, -s);
+#pragma unroll
+  for (int k1 = 0; k1 < 4; ++k1) {
+    C2<T> b[4] = {y[k1], y[4 + k1], y[8 + k1], y[12 + k1]};
+    epfft::dft4<T, DIR>(b);
+#pragma unroll
+    for (int k2 = 0; k2 < 4; ++k2) v[k1 + 4 * k2] = b[k2];
+  }
+}
+
+template <class T, int R, int DIR> EP_DEV void dft(C2<T>* v) {
+  if (R == 16) dft16<T, DIR>(v);
+  else if (R == 8) epfft::dft8<T, DIR>(v);
+  else if (R == 4) epfft::dft4<T, DIR>(v);
+  else epfft::dft2<T, DIR>(v);
+}
+
+// Transform of the CTA's lines: on entry v[a] = x[t + P a], on return
+// v[m] = X[t + P m].  S: this line's exchange row (N + 1 entries); tw: the
+// table exp(-2 pi i k / N), k < N.  All threads of the CTA must call it.
+template <class T, int N, int DIR>
+EP_DEV void lines(C2<T>* v, C2<T>* S, const C2<T>* __restrict__ tw, int t) {
+  constexpr int P = Shape<N>::P, E = Shape<N>::E;
+  dft<T, E, DIR>(v);
+  if (t != 0) {
+#pragma unroll
+    for (int ka = 1; ka < E; ++ka) {
+      const C2<T> w = tw[t * ka];
+      v[ka] = DIR < 0 ? cmul(v[ka], w) : cmulc(v[ka], w);
+    }
+  }
+  __syncthreads();  // the previous transform has read its exchange rows
+#pragma unroll
+  for (int ka = 0; ka < E; ++ka) S[ka * P + t] = v[ka];
+  __syncthreads();
+#pragma unroll
+  for (int j = 0; j < E / P; ++j) {
+    C2<T> u[P];
+#pragma unroll
+    for (int tt = 0; tt < P; ++tt) u[tt] = S[(t + P * j) * P + tt];
+    dft<T, P, DIR>(u);
+#pragma unroll
+    for (int kt = 0; kt < P; ++kt) v[j + (E / P) * kt] = u[kt];
+  }
+}
+
+template <class T, int N>
+constexpr size_t smem_bytes() {
+  return (size_t)(32 * (N + 1) + N) * sizeof(C2<T>);
+}
+
+// Line base address of line L of a LineSet-like description.
+EP_DEV long long line_base(long long L, long long Mi, long long So) { return (L % Mi) + (L / Mi) * So; }
+
+}  // namespace rfft
+
+// Blocks per SM the launch bounds ask for (FP32 / FP64).
+template <class T, int N> struct Occ {
+  static constexpr int c2c = sizeof(T) == 4 ? (N <= 64 ? 4 : (N == 128 ? 3 : 2)) : (N <= 64 ? 2 : 1);
+  static constexpr int conv = sizeof(T) == 4 ? (N <= 64 ? 3 : (N == 128 ? 2 : 1)) : 1;
+};
+
+// In-place transforms along a strided axis of up to 8 arrays (blockIdx.y).
+// Element m of a thread sits at offset m * (P Sa) from its first one (32-bit
+// offsets: N Sa < 2^31 for every supported grid).
+template <class T, int N, int DIR>
+__global__ void __launch_bounds__(32 * rfft::Shape<N>::P, (Occ<T, N>::c2c))
+    k_c2c_r(const __grid_constant__ Arr8<T> arr, LineSet ls, const C2<T>* __restrict__ twg) {
+  constexpr int P = rfft::Shape<N>::P, E = rfft::Shape<N>::E;
+  extern __shared__ __align__(16) unsigned char smraw[];
+  C2<T>* S = reinterpret_cast<C2<T>*>(smraw);
+  C2<T>* tw = S + 32 * (N + 1);
+  const int lane = threadIdx.x, t = threadIdx.y;
+  for (int i = t * 32 + lane; i < N; i += 32 * P) tw[i] = twg[i];
+  const long long L = (long long)blockIdx.x * 32 + lane;
+  const bool valid = L < ls.nlines;
+  const int stp = P * (int)ls.Sa;
+  C2<T>* a = arr.a[blockIdx.y] + (valid ? rfft::line_base(L, ls.Mi, ls.So) : 0) + (long long)t * ls.Sa;
+  C2<T> v[E];
+#pragma unroll
+  for (int m = 0; m < E; ++m) v[m] = valid ? a[m * stp] : cmk<T>(T(0), T(0));
+  __syncthreads();  // tw complete
+  rfft::lines<T, N, DIR>(v, S + lane * (N + 1), tw, t);
+  if (valid) {
+#pragma unroll
+    for (int m = 0; m < E; ++m) a[m * stp] = v[m];
+  }
+}
+
+// Forward transform along the pass axis, then per kernel table the k-space
+// product and the inverse transform (poten.f90:34-36,46-48,69-71,95-97 and
+// term_alfa.f90:172-176,203-205), all in registers between the exchanges.
+template <class T, int N>
+__global__ void __launch_bounds__(32 * rfft::Shape<N>::P, (Occ<T, N>::conv))
+    k_zconv_r(const __grid_constant__ ConvSpec<T> cs, LineSet ls, const C2<T>* __restrict__ twg) {
+  constexpr int P = rfft::Shape<N>::P, E = rfft::Shape<N>::E;
+  extern __shared__ __align__(16) unsigned char smraw[];
+  C2<T>* S = reinterpret_cast<C2<T>*>(smraw);
+  C2<T>* tw = S + 32 * (N + 1);
+  const int lane = threadIdx.x, t = threadIdx.y;
+  for (int i = t * 32 + lane; i < N; i += 32 * P) tw[i] = twg[i];
+  const int which = blockIdx.y;
+  const long long L = (long long)blockIdx.x * 32 + lane;
+  const bool valid = L < ls.nlines;
+  const long long b = (valid ? rfft::line_base(L, ls.Mi, ls.So) : 0) + (long long)t * ls.Sa;
+  const int stp = P * (int)ls.Sa;
+  C2<T>* Srow = S + lane * (N + 1);
+  C2<T> v[E];
+  {
+    const C2<T>* in = cs.in[which] + b;
+#pragma unroll
+    for (int m = 0; m < E; ++m) v[m] = valid ? in[m * stp] : cmk<T>(T(0), T(0));
+  }
+  __syncthreads();  // tw complete
+  rfft::lines<T, N, -1>(v, Srow, tw, t);
+  const int nout = cs.nout[which];
+  for (int j = 0; j < nout; ++j) {
+    const T* ker = cs.ker[which][j] + b;
+    C2<T> u[E];
+#pragma unroll
+    for (int m = 0; m < E; ++m) {
+      const T kv = valid ? ker[m * stp] : T(0);
+      u[m] = cmk<T>(v[m].x * kv, v[m].y * kv);
+    }
+    rfft::lines<T, N, +1>(u, Srow, tw, t);
+    if (valid) {
+      C2<T>* o = cs.out[which][j] + b;
+#pragma unroll
+      for (int m = 0; m < E; ++m) o[m * stp] = u[m];
+    }
+  }
+}
