@@ -68,6 +68,8 @@ class Engine {
   ImpState* imp = nullptr;
   std::string* err = nullptr;
   int dev_sm = 0;
+  int zc_pc = 16, zc_rk = 16;  // z planes per CTA of the stencil marches
+  int march_zchunk(int blocks_per_sm) const;
   long long bytes = 0;
   Phys phys{};
   FdW<T> fd{};

@@ -8,7 +8,6 @@
 #include "ep_kernels_impl.cuh"
 #include "ep_rfft.cuh"
 
-#define EP_ZC 16
 #define EP_RED_BLOCKS 1216
 #define EP_SMEM_CAP (110 * 1024)
 
@@ -24,6 +23,23 @@
   } while (0)
 
 namespace {
+
+// Planes per CTA of a stencil march over a (gx, gy) grid of column tiles:
+// minimise waves x (planes + prologue) over the chunk counts, so that the
+// last wave is as full as the SM count allows.
+inline int march_chunk(long long nxy, int nz, long long slots, int R) {
+  int best = nz;
+  long long cost = -1;
+  for (int nch = 1; nch <= nz; ++nch) {
+    const int zc = (nz + nch - 1) / nch;
+    if (zc < 4 && nch > 1) break;
+    const long long nblk = nxy * ((nz + zc - 1) / zc);
+    const long long waves = (nblk + slots - 1) / slots;
+    const long long c = waves * (zc + R);
+    if (cost < 0 || c < cost) { cost = c; best = zc; }
+  }
+  return best;
+}
 
 // Radix sequence for n = 2^a 3^b 5^c: as many 8s as possible, a 4 or 2 for
 // the rest of the power of two (two 4s instead of 8*2), then 3s and 5s.
@@ -174,9 +190,6 @@ int Engine<T>::init(const ep_config& c, cudaStream_t s, Prof* p, ImpState* im, s
   if ((r = alloc((void**)&twx, c.nx * sizeof(CT)))) return r;
   if ((r = alloc((void**)&twy, c.ny * sizeof(CT)))) return r;
   if ((r = alloc((void**)&twz, c.nz * sizeof(CT)))) return r;
-  const long long nbs = (long long)((c.nx + EP_TX - 1) / EP_TX) * ((c.ny + EP_TY - 1) / EP_TY) * ((c.nz + EP_ZC - 1) / EP_ZC);
-  npartials = std::max(nbs * 4, (long long)EP_RED_BLOCKS * 9);
-  if ((r = alloc((void**)&partials, npartials * sizeof(double)))) return r;
   if ((r = alloc((void**)&sc, sizeof(DevScalars)))) return r;
 
   {
@@ -255,7 +268,35 @@ int Engine<T>::init(const ep_config& c, cudaStream_t s, Prof* p, ImpState* im, s
   cudaFuncSetAttribute(k_correct<T, RR>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)march_smem<T, RR, 5, 2>());
   EP_ATTR(1) EP_ATTR(2) EP_ATTR(3) EP_ATTR(4) EP_ATTR(5) EP_ATTR(6)
 #undef EP_ATTR
+  {
+    // z-chunk lengths of the stencil marches from their resident blocks per SM
+    int occ_pc = 0, occ_rk = 0;
+    const int nt = EP_TX * EP_TY;
+#define EP_OCC(RR)                                                                                         \
+  case RR:                                                                                                 \
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_pc, k_correct<T, RR>, nt, march_smem<T, RR, 5, 2>()); \
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_rk, k_rkstage<T, RR>, nt, 0);                       \
+    break;
+    switch (fd.R) { EP_OCC(1) EP_OCC(2) EP_OCC(3) EP_OCC(4) EP_OCC(5) EP_OCC(6) default: break; }
+#undef EP_OCC
+    zc_pc = march_zchunk(occ_pc);
+    zc_rk = march_zchunk(occ_rk);
+  }
+  {
+    const long long nxy = (long long)((c.nx + EP_TX - 1) / EP_TX) * ((c.ny + EP_TY - 1) / EP_TY);
+    const int zmin = std::min(zc_pc, zc_rk);
+    const long long nbs = nxy * ((c.nz + zmin - 1) / zmin);
+    npartials = std::max(nbs * 4, (long long)EP_RED_BLOCKS * 9);
+    if ((r = alloc((void**)&partials, npartials * sizeof(double)))) return r;
+  }
   return cuda_ok(cudaStreamSynchronize(st), "init");
+}
+
+template <class T>
+int Engine<T>::march_zchunk(int blocks_per_sm) const {
+  const long long nxy = (long long)((g.nx + EP_TX - 1) / EP_TX) * ((g.ny + EP_TY - 1) / EP_TY);
+  const long long slots = (long long)dev_sm * std::max(1, blocks_per_sm);
+  return march_chunk(nxy, g.nz, slots, fd.R);
 }
 
 template <class T>
@@ -535,14 +576,14 @@ int Engine<T>::lap_predict(double dt) {
   CT* po3 = po[ioldp[2]];
   const CT* h1 = ph[ioldh[0]];
   CT* h2 = ph[ioldh[1]];
-  dim3 grid((g.nx + EP_TX - 1) / EP_TX, (g.ny + EP_TY - 1) / EP_TY, (g.nz + EP_ZC - 1) / EP_ZC);
+  dim3 grid((g.nx + EP_TX - 1) / EP_TX, (g.ny + EP_TY - 1) / EP_TY, (g.nz + zc_pc - 1) / zc_pc);
   dim3 blk(EP_TX, EP_TY);
   const T f = (T)(c4o3 * dt), c1 = (T)c112;
   const Slots sl{slot_of(psi), slot_of(po3), -1, slot_of(h1), slot_of(h2), slot_of(pc), -1};
 #define EP_PRED(RR)                                                                                          \
   case RR: {                                                                                                 \
     auto k = k_predict<T, RR>;                                                                               \
-    EP_LAUNCH("predict", k, grid, blk, (march_smem<T, RR, 4, 2>()), g, fd, phys, EP_ZC, psi, pot4, uimp, po3, h1, h2, pc, den, f, c1,  \
+    EP_LAUNCH("predict", k, grid, blk, (march_smem<T, RR, 4, 2>()), g, fd, phys, zc_pc, psi, pot4, uimp, po3, h1, h2, pc, den, f, c1,  \
               sc, sl);                                                                                       \
   } break;
   switch (fd.R) {
@@ -563,7 +604,7 @@ int Engine<T>::lap_correct(double dt, bool want) {
   const CT* po2 = po[ioldp[1]];
   const CT* h1 = ph[ioldh[0]];
   const CT* h2 = ph[ioldh[1]];
-  dim3 grid((g.nx + EP_TX - 1) / EP_TX, (g.ny + EP_TY - 1) / EP_TY, (g.nz + EP_ZC - 1) / EP_ZC);
+  dim3 grid((g.nx + EP_TX - 1) / EP_TX, (g.ny + EP_TY - 1) / EP_TY, (g.nz + zc_pc - 1) / zc_pc);
   dim3 blk(EP_TX, EP_TY);
   const T f3 = (T)(3.0 * dt), cc = (T)c9;
   const int renorm = (cfg.time_mode == EP_IMAGINARY_TIME && cfg.renormalize) ? 1 : 0;
@@ -571,7 +612,7 @@ int Engine<T>::lap_correct(double dt, bool want) {
 #define EP_CORR(RR)                                                                                           \
   case RR: {                                                                                                  \
     auto k = k_correct<T, RR>;                                                                                \
-    EP_LAUNCH("correct", k, grid, blk, (march_smem<T, RR, 5, 2>()), g, fd, phys, EP_ZC, psi, pot4, uimp, po3, po2, h1, h2, pc, spare, den, \
+    EP_LAUNCH("correct", k, grid, blk, (march_smem<T, RR, 5, 2>()), g, fd, phys, zc_pc, psi, pot4, uimp, po3, po2, h1, h2, pc, spare, den, \
               f3, cc, partials, sc, renorm, cfg.n4, sl);                                                      \
   } break;
   switch (fd.R) {
@@ -596,13 +637,13 @@ int Engine<T>::rk_stage(int jr, double dt) {
   const double crun[4] = {0.5, 1.0 - 1.0 / s2, 1.0 + 1.0 / s2, 0.5};
   CT* out = (jr == 0) ? po[2] : spare;
   CT* hout = (jr == 0) ? ph[1] : nullptr;
-  dim3 grid((g.nx + EP_TX - 1) / EP_TX, (g.ny + EP_TY - 1) / EP_TY, (g.nz + EP_ZC - 1) / EP_ZC);
+  dim3 grid((g.nx + EP_TX - 1) / EP_TX, (g.ny + EP_TY - 1) / EP_TY, (g.nz + zc_rk - 1) / zc_rk);
   dim3 blk(EP_TX, EP_TY);
   const T a = (T)arun[jr], b = (T)brun[jr], cr = (T)crun[jr], d = (T)dt;
 #define EP_RK(RR)                                                                                              \
   case RR: {                                                                                                   \
     auto k = k_rkstage<T, RR>;                                                                                 \
-    EP_LAUNCH("rkstage", k, grid, blk, 0, g, fd, phys, EP_ZC, psi, pot4, uimp, q, out, hout, den, a, b, cr, d, sc); \
+    EP_LAUNCH("rkstage", k, grid, blk, 0, g, fd, phys, zc_rk, psi, pot4, uimp, q, out, hout, den, a, b, cr, d, sc); \
   } break;
   switch (fd.R) {
     EP_RK(1) EP_RK(2) EP_RK(3) EP_RK(4) EP_RK(5) EP_RK(6)

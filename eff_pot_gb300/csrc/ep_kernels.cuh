@@ -654,7 +654,8 @@ EP_DEV void lap_march(const Geo& g, const C2<T>* __restrict__ psi, const FdW<T>&
 template <class T, int R, int NC, int NR>
 constexpr size_t march_smem() {
   return (size_t)2 * (EP_TX + 2 * R) * (EP_TY + 2 * R) * sizeof(C2<T>) + (size_t)2 * EP_TX * EP_TY * sizeof(C2<T>) +
-         (size_t)2 * NC * EP_TX * EP_TY * sizeof(C2<T>) + (size_t)2 * NR * EP_TX * EP_TY * sizeof(T);
+         (size_t)2 * NC * EP_TX * EP_TY * sizeof(C2<T>) + (size_t)2 * NR * EP_TX * EP_TY * sizeof(T) +
+         (size_t)(EP_TX + 2 * R) * (EP_TY + 2 * R) * sizeof(int);
 }
 
 // The 2.5-D march of lap_march, software-pipelined: while plane z is
@@ -663,6 +664,9 @@ constexpr size_t march_smem() {
 // into the other half of a double buffer.  f(p, psi, lap, ic, ir) gets the
 // point's inputs as ic[i * NT] / ir[i * NT] in shared memory.  psi values
 // are stored raw and multiplied by scale once (the Laplacian is linear).
+// The (x, y) offsets of the halo plane (wrapped, or -1 outside a
+// zero-boundary box) are tabulated once per CTA; each plane then costs one
+// shared-memory read per element.
 template <class T, int R, int NC, int NR, class F>
 EP_DEV void lap_march_async(const Geo& g, const C2<T>* __restrict__ psi, const FdW<T>& fd, int zc,
                             unsigned char* smem, const C2<T>* const* cin, const T* const* rin, T scale, F&& f) {
@@ -672,6 +676,7 @@ EP_DEV void lap_march_async(const Geo& g, const C2<T>* __restrict__ psi, const F
   CT* sq = sp + 2 * PL;
   CT* sc_ = sq + 2 * NT;
   T* sr = reinterpret_cast<T*>(sc_ + 2 * NC * NT);
+  int* soff = reinterpret_cast<int*>(sr + 2 * NR * NT);
   const int tx = threadIdx.x, ty = threadIdx.y, tid = ty * EP_TX + tx;
   const int x = blockIdx.x * EP_TX + tx, y = blockIdx.y * EP_TY + ty;
   const int z0 = blockIdx.z * zc, z1 = min(z0 + zc, g.nz);
@@ -687,12 +692,23 @@ EP_DEV void lap_march_async(const Geo& g, const C2<T>* __restrict__ psi, const F
     }
     return xx + (long long)g.nx * yy + sxy * zz;
   };
+  for (int e = tid; e < PL; e += NT) {
+    const int r = e / W, c = e - r * W;
+    int xx = blockIdx.x * EP_TX - R + c, yy = blockIdx.y * EP_TY - R + r;
+    int o = -1;
+    if (xx >= 0 && xx < g.nx && yy >= 0 && yy < g.ny) o = xx + g.nx * yy;
+    else if (per) o = wrapi(xx, g.nx) + g.nx * wrapi(yy, g.ny);
+    soff[e] = o;
+  }
+  __syncthreads();
   auto prefetch = [&](int z, int buf) {
     CT* P = sp + buf * PL;
+    int zz = z;
+    if (zz < 0 || zz >= g.nz) zz = per ? wrapi(zz, g.nz) : -1;
+    const CT* pz = psi + sxy * (zz < 0 ? 0 : zz);
     for (int e = tid; e < PL; e += NT) {
-      const int r = e / W, c = e - r * W;
-      const long long a = addr(blockIdx.x * EP_TX - R + c, blockIdx.y * EP_TY - R + r, z);
-      if (a >= 0) cp_async<sizeof(CT)>(P + e, psi + a);
+      const int o = zz < 0 ? -1 : soff[e];
+      if (o >= 0) cp_async<sizeof(CT)>(P + e, pz + o);
       else P[e] = cmk<T>(T(0), T(0));
     }
     if (valid) {
