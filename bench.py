@@ -317,7 +317,7 @@ def run_ours(args):
     if rank != 0:
         return 0
 
-    bytes32 = step_bytes(N_GRID, N_GRID, N_GRID, otc=True, grad=True, s=4, renorm=True)
+    bytes32 = step_bytes(N_GRID, N_GRID, N_GRID, otc=True, grad=True, s=4, renorm=False)
     per_step = {k: v[0] / K for k, v in prof.items()}
     dom = max((k for k in per_step if k in bytes32), key=lambda k: per_step[k])
     n_dom = prof[dom][1]
@@ -334,7 +334,7 @@ def run_ours(args):
     except Exception:
         pass
     b32 = sum(bytes32.values())
-    b64 = sum(step_bytes(N_GRID, N_GRID, N_GRID, otc=True, grad=True, s=8, renorm=True).values())
+    b64 = sum(step_bytes(N_GRID, N_GRID, N_GRID, otc=True, grad=True, s=8, renorm=False).values())
     batch_bytes = args.batch * (k32 * b32 + k64 * b64)
     cpu = None
     if not args.no_cpu:

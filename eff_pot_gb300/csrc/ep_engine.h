@@ -68,7 +68,9 @@ class Engine {
   ImpState* imp = nullptr;
   std::string* err = nullptr;
   int dev_sm = 0;
-  int zc_pc = 16, zc_rk = 16;  // z planes per CTA of the stencil marches
+  int zc_pc = 16, zc_rk = 16, zc_d1 = 16;  // z planes per CTA of the stencil marches
+  T* dyz = nullptr;                         // dy(gy) + dz(gz) of term_alfa
+  int d1march(int mode, const T* f, const T* f2, T* o0, T* o1, T* o2);
   int march_zchunk(int blocks_per_sm) const;
   long long bytes = 0;
   Phys phys{};

@@ -179,7 +179,7 @@ int Engine<T>::init(const ep_config& c, cudaStream_t s, Prof* p, ImpState* im, s
   CT** cbufs[] = {&psi, &spare, &po[0], &po[1], &po[2], &ph[0], &ph[1], &pc, &q};
   for (CT** b : cbufs) if ((r = alloc((void**)b, N * sizeof(CT)))) return r;
   T** rbufs[] = {&den, &pot4, &uimp, &dencg, &delj4, &dxd, &dyd, &dzd, &falfs, &intx, &inty, &intz,
-                 &ualphas, &gy, &gz, &dgx, &vpi, &delta};
+                 &ualphas, &gy, &gz, &dgx, &vpi, &delta, &dyz};
   for (T** b : rbufs) if ((r = alloc((void**)b, N * sizeof(T)))) return r;
   for (int i = 0; i < 4; ++i) {
     if ((r = alloc((void**)&S[i], Nh * sizeof(CT)))) return r;
@@ -270,17 +270,19 @@ int Engine<T>::init(const ep_config& c, cudaStream_t s, Prof* p, ImpState* im, s
 #undef EP_ATTR
   {
     // z-chunk lengths of the stencil marches from their resident blocks per SM
-    int occ_pc = 0, occ_rk = 0;
+    int occ_pc = 0, occ_rk = 0, occ_d1 = 0;
     const int nt = EP_TX * EP_TY;
 #define EP_OCC(RR)                                                                                         \
   case RR:                                                                                                 \
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_pc, k_correct<T, RR>, nt, march_smem<T, RR, 5, 2>()); \
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_rk, k_rkstage<T, RR>, nt, 0);                       \
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_d1, k_d1march<T, RR, 0>, nt, 0);                    \
     break;
     switch (fd.R) { EP_OCC(1) EP_OCC(2) EP_OCC(3) EP_OCC(4) EP_OCC(5) EP_OCC(6) default: break; }
 #undef EP_OCC
     zc_pc = march_zchunk(occ_pc);
     zc_rk = march_zchunk(occ_rk);
+    zc_d1 = march_zchunk(occ_d1);
   }
   {
     const long long nxy = (long long)((c.nx + EP_TX - 1) / EP_TX) * ((c.ny + EP_TY - 1) / EP_TY);
@@ -302,7 +304,7 @@ int Engine<T>::march_zchunk(int blocks_per_sm) const {
 template <class T>
 void Engine<T>::release() {
   void* bufs[] = {psi, spare, po[0], po[1], po[2], ph[0], ph[1], pc, q, den, pot4, uimp, dencg, delj4, dxd, dyd,
-                  dzd, falfs, intx, inty, intz, ualphas, gy, gz, dgx, vpi, delta, S[0], S[1], S[2], S[3], Tb[0],
+                  dzd, falfs, intx, inty, intz, ualphas, gy, gz, dgx, vpi, delta, dyz, S[0], S[1], S[2], S[3], Tb[0],
                   Tb[1], Tb[2], Tb[3], fvlj4, wcgk, kalfs, twx, twy, twz, partials, sc};
   for (void* b : bufs)
     if (b) cudaFree(b);
@@ -384,6 +386,29 @@ int Engine<T>::zconv(const CT* const* in, CT* const (*out)[3], const T* const (*
   return EP_OK;
 }
 
+// First-derivative marches (k_d1march): mode 0 = grad f, mode 1 = dy f + dz f2.
+template <class T>
+int Engine<T>::d1march(int mode, const T* f, const T* f2, T* o0, T* o1, T* o2) {
+  dim3 grid((g.nx + EP_TX - 1) / EP_TX, (g.ny + EP_TY - 1) / EP_TY, (g.nz + zc_d1 - 1) / zc_d1);
+  dim3 blk(EP_TX, EP_TY);
+#define EP_D1(RR)                                                                                  \
+  case RR:                                                                                         \
+    if (mode == 0) {                                                                               \
+      auto k = k_d1march<T, RR, 0>;                                                                \
+      EP_LAUNCH("grad_march", k, grid, blk, 0, g, fd, zc_d1, f, f2, o0, o1, o2);                  \
+    } else {                                                                                       \
+      auto k = k_d1march<T, RR, 1>;                                                                \
+      EP_LAUNCH("div_march", k, grid, blk, 0, g, fd, zc_d1, f, f2, o0, o1, o2);                   \
+    }                                                                                              \
+    break;
+  switch (fd.R) {
+    EP_D1(1) EP_D1(2) EP_D1(3) EP_D1(4) EP_D1(5) EP_D1(6)
+    default: *err = "npd > 13 not built"; return EP_ERR_UNSUPPORTED;
+  }
+#undef EP_D1
+  return EP_OK;
+}
+
 // poten() + derden() + term_alfa() (poten.f90:5-131, term_alfa.f90:5-109).
 template <class T>
 int Engine<T>::poten() {
@@ -394,9 +419,9 @@ int Engine<T>::poten() {
   {
     const int nl = x_lines(1);
     auto k = k_x1<T>;
-    EP_LAUNCH("x1_r2c_den", k, (unsigned)((nlines + nl - 1) / nl), shp.xthr, x_smem(nl, 1), g, den, S[0], dxd, dyd,
-              dzd, grad ? 1 : 0, p2, twx, fd, nl);
+    EP_LAUNCH("x1_r2c_den", k, (unsigned)((nlines + nl - 1) / nl), shp.xthr, x_smem(nl, 1), g, den, S[0], p2, twx, nl);
   }
+  if (grad && (r = d1march(0, den, nullptr, dxd, dyd, dzd))) return r;
   CT* a1[1] = {S[0]};
   if ((r = fft_y(a1, 1, -1))) return r;
   {
@@ -433,6 +458,7 @@ int Engine<T>::poten() {
               twx, nl);
   }
   if (otc) {
+    if ((r = d1march(1, gy, gz, dyz, nullptr, nullptr))) return r;
     if ((r = fft_y(a1, 1, -1))) return r;
     const CT* in[1] = {S[0]};
     CT* const out[1][3] = {{Tb[0]}};
@@ -443,8 +469,8 @@ int Engine<T>::poten() {
     if ((r = fft_y(e1, 1, +1))) return r;
     const int nl = x_lines(1);
     auto k = k_x4<T>;
-    EP_LAUNCH("x4_c2r_ualpha", k, (unsigned)((nlines + nl - 1) / nl), shp.xthr, x_smem(nl, 1), g, phys, fd, Tb[0], den,
-              dgx, gy, gz, pot4, ualphas, p2, twx, nl);
+    EP_LAUNCH("x4_c2r_ualpha", k, (unsigned)((nlines + nl - 1) / nl), shp.xthr, x_smem(nl, 1), g, phys, Tb[0], den,
+              dgx, dyz, pot4, ualphas, p2, twx, nl);
   }
   have_field = true;
   return EP_OK;

@@ -275,12 +275,10 @@ struct XSmem {
   }
 };
 
-// X1: den -> r2c along x (-> out); optionally grad den (derden,
-// energy.f90:207-227: three first derivatives).
+// X1: den -> r2c along x (-> out).  grad den is k_d1march<MODE 0>.
 template <class T>
-__global__ void k_x1(Geo g, const T* __restrict__ den, C2<T>* __restrict__ out, T* __restrict__ dxo,
-                     T* __restrict__ dyo, T* __restrict__ dzo, int want_grad, FftPlan p2,
-                     const C2<T>* __restrict__ twx, FdW<T> fd, int nl) {
+__global__ void k_x1(Geo g, const T* __restrict__ den, C2<T>* __restrict__ out, const __grid_constant__ FftPlan p2,
+                     const C2<T>* __restrict__ twx, int nl) {
   extern __shared__ __align__(16) unsigned char smraw[];
   const int nx = g.nx;
   XSmem<T> S(smraw, nl, nx);
@@ -291,17 +289,6 @@ __global__ void k_x1(Geo g, const T* __restrict__ den, C2<T>* __restrict__ out, 
   T* R0 = S.R;
   for (int e = threadIdx.x; e < nlv * nx; e += blockDim.x) R0[e] = den[line0 * nx + e];
   __syncthreads();
-  if (want_grad) {
-    for (int e = threadIdx.x; e < nlv * nx; e += blockDim.x) {
-      int i;
-      const int l = epfft::fdivmod(e, nx, 1.0f / (float)nx, i);
-      const long long L = line0 + l, p = L * nx + i;
-      const int iy = (int)(L % g.ny), iz = (int)(L / g.ny);
-      dxo[p] = d1_line(R0 + l * nx, i, nx, fd.w1[0], fd.R, fd.periodic);
-      dyo[p] = d1_global(den, p, iy, g.ny, (long long)nx, fd.w1[1], fd.R, fd.periodic);
-      dzo[p] = d1_global(den, p, iz, g.nz, (long long)nx * g.ny, fd.w1[2], fd.R, fd.periodic);
-    }
-  }
   x_forward<T>([&](int l, int i) { return R0[l * nx + i]; }, out, line0, nlv, nl, nx, g.nxh, S.P, S.Q, S.ld,
                p2, S.tw);
 }
@@ -315,7 +302,7 @@ __global__ void k_x2(Geo g, Phys ph, const C2<T>* __restrict__ B0, const C2<T>* 
                      const C2<T>* __restrict__ B2, const T* __restrict__ den, const T* __restrict__ dxd,
                      const T* __restrict__ dyd, const T* __restrict__ dzd, T* __restrict__ dencg,
                      T* __restrict__ delj4, T* __restrict__ pot4, T* __restrict__ falfs, C2<T>* C0, C2<T>* C1,
-                     C2<T>* C2o, C2<T>* C3, FftPlan p2, const C2<T>* __restrict__ twx, int nl) {
+                     C2<T>* C2o, C2<T>* C3, const __grid_constant__ FftPlan p2, const C2<T>* __restrict__ twx, int nl) {
   extern __shared__ __align__(16) unsigned char smraw[];
   const int nx = g.nx, nxh = g.nxh;
   XSmem<T> S(smraw, nl, nx);
@@ -367,12 +354,12 @@ __global__ void k_x2(Geo g, Phys ph, const C2<T>* __restrict__ B0, const C2<T>* 
 // (term_alfa.f90:172-181), the x-derivative of f*I_x, f*I_y and f*I_z for
 // the divergence (:216-225), and forward r2c of grad(den).I (:194-201).
 template <class T>
-__global__ void k_x3(Geo g, Phys ph, FdW<T> fd, const C2<T>* __restrict__ D0, const C2<T>* __restrict__ D1,
+__global__ void k_x3(Geo g, Phys ph, const __grid_constant__ FdW<T> fd, const C2<T>* __restrict__ D0, const C2<T>* __restrict__ D1,
                      const C2<T>* __restrict__ D2, const C2<T>* __restrict__ D3, const T* __restrict__ den,
                      const T* __restrict__ dxd, const T* __restrict__ dyd, const T* __restrict__ dzd,
                      const T* __restrict__ falfs, T* __restrict__ pot4, T* __restrict__ intx, T* __restrict__ inty,
                      T* __restrict__ intz, T* __restrict__ gy, T* __restrict__ gz, T* __restrict__ dgx,
-                     C2<T>* E0, FftPlan p2, const C2<T>* __restrict__ twx, int nl) {
+                     C2<T>* E0, const __grid_constant__ FftPlan p2, const C2<T>* __restrict__ twx, int nl) {
   extern __shared__ __align__(16) unsigned char smraw[];
   const int nx = g.nx, nxh = g.nxh;
   XSmem<T> S(smraw, nl, nx);
@@ -427,10 +414,9 @@ __global__ void k_x3(Geo g, Phys ph, FdW<T> fd, const C2<T>* __restrict__ D0, co
 // X4 (OTC): c2r of kalfs*FFT(grad(den).I) -> U_alpha = (u/den0s + div(f I))
 // * h2o2m4 * alphas (term_alfa.f90:203-236); pot4 += U_alpha + penalty.
 template <class T>
-__global__ void k_x4(Geo g, Phys ph, FdW<T> fd, const C2<T>* __restrict__ F0, const T* __restrict__ den,
-                     const T* __restrict__ dgx, const T* __restrict__ gy, const T* __restrict__ gz,
-                     T* __restrict__ pot4, T* __restrict__ ualphas, FftPlan p2, const C2<T>* __restrict__ twx,
-                     int nl) {
+__global__ void k_x4(Geo g, Phys ph, const C2<T>* __restrict__ F0, const T* __restrict__ den,
+                     const T* __restrict__ dgx, const T* __restrict__ dyz, T* __restrict__ pot4,
+                     T* __restrict__ ualphas, const __grid_constant__ FftPlan p2, const C2<T>* __restrict__ twx, int nl) {
   extern __shared__ __align__(16) unsigned char smraw[];
   const int nx = g.nx, nxh = g.nxh;
   XSmem<T> S(smraw, nl, nx);
@@ -443,12 +429,8 @@ __global__ void k_x4(Geo g, Phys ph, FdW<T> fd, const C2<T>* __restrict__ F0, co
   x_inverse<T>(F0, line0, nlv, nl, nx, nxh, S.P, S.Q, S.ld, p2, S.tw, (T)ph.renor, Ru);
   const T rden0s = (T)(1.0 / ph.den0s), h2 = (T)ph.h2o2m4, al = (T)ph.alphas;
   for (int e = threadIdx.x; e < nlv * nx; e += blockDim.x) {
-    const long long L = line0 + e / nx;
     const long long p = line0 * nx + e;
-    const int iy = (int)(L % g.ny), iz = (int)(L / g.ny);
-    const T dyy = d1_global(gy, p, iy, g.ny, (long long)nx, fd.w1[1], fd.R, fd.periodic);
-    const T dzz = d1_global(gz, p, iz, g.nz, (long long)nx * g.ny, fd.w1[2], fd.R, fd.periodic);
-    const T ua = (((Ru[e] * rden0s + dgx[p]) + dyy) + dzz) * h2 * al;
+    const T ua = ((Ru[e] * rden0s + dgx[p]) + dyz[p]) * h2 * al;
     ualphas[p] = ua;
     pot4[p] = (pot4[p] + ua) + penalty_of(ph, den[p]);
   }
@@ -521,7 +503,7 @@ EP_DEV void store_lines(C2<T>* __restrict__ a, const LSmem<T>& s, int LT, int n,
 }
 
 template <class T, int DIR>
-__global__ void k_c2c(Arr8<T> arr, LineSet ls, FftPlan p, const C2<T>* __restrict__ twg, int LT) {
+__global__ void k_c2c(const __grid_constant__ Arr8<T> arr, LineSet ls, const __grid_constant__ FftPlan p, const C2<T>* __restrict__ twg, int LT) {
   extern __shared__ __align__(16) unsigned char smraw[];
   const int n = p.n;
   LSmem<T> s = lsmem<T>(smraw, LT, n, 2);
@@ -543,7 +525,7 @@ __global__ void k_c2c(Arr8<T> arr, LineSet ls, FftPlan p, const C2<T>* __restric
 // (the k-space product of poten.f90:34-36,46-48,69-71,95-97 and
 // term_alfa.f90:172-176,203-205) and inverse transform.
 template <class T>
-__global__ void k_zconv(ConvSpec<T> cs, LineSet ls, FftPlan p, const C2<T>* __restrict__ twg, int LT) {
+__global__ void k_zconv(const __grid_constant__ ConvSpec<T> cs, LineSet ls, const __grid_constant__ FftPlan p, const C2<T>* __restrict__ twg, int LT) {
   extern __shared__ __align__(16) unsigned char smraw[];
   const int n = p.n;
   LSmem<T> s = lsmem<T>(smraw, LT, n, 3);
@@ -752,6 +734,99 @@ EP_DEV void lap_march_async(const Geo& g, const C2<T>* __restrict__ psi, const F
       }
       f((long long)x + (long long)g.nx * y + sxy * z, scale * c, scale * ((lx + ly) + lz),
         sc_ + buf * NC * NT + tid, sr + buf * NR * NT + tid);
+    }
+#pragma unroll
+    for (int k = 0; k < 2 * R; ++k) q[k] = q[k + 1];
+    __syncthreads();
+  }
+}
+
+// First derivatives of real fields by a 2.5-D march, software-pipelined like
+// lap_march_async (13-point derivnd stencils, init_deriv_parallel.f90, with
+// the boundary handling and summation order of d1_global):
+//   MODE 0: o0, o1, o2 = d/dx, d/dy, d/dz of f   (derden, energy.f90:207-227)
+//   MODE 1: o0 = d/dy f + d/dz f2                (term_alfa.f90:220-230)
+template <class T, int R, int MODE>
+__global__ void __launch_bounds__(EP_TX* EP_TY) k_d1march(Geo g, const __grid_constant__ FdW<T> fd, int zc,
+                                                         const T* __restrict__ f, const T* __restrict__ f2,
+                                                         T* __restrict__ o0, T* __restrict__ o1,
+                                                         T* __restrict__ o2) {
+  constexpr int HX = MODE == 0 ? R : 0;
+  constexpr int W = EP_TX + 2 * HX, H = EP_TY + 2 * R, PL = W * H, NT = EP_TX * EP_TY;
+  __shared__ __align__(16) T sp[2][PL];
+  __shared__ __align__(16) T sq[2][NT];
+  __shared__ int soff[PL];
+  const T* fq = MODE == 0 ? f : f2;
+  const int tx = threadIdx.x, ty = threadIdx.y, tid = ty * EP_TX + tx;
+  const int x = blockIdx.x * EP_TX + tx, y = blockIdx.y * EP_TY + ty;
+  const int z0 = blockIdx.z * zc, z1 = min(z0 + zc, g.nz);
+  const bool valid = (x < g.nx) && (y < g.ny);
+  const int per = fd.periodic;
+  const long long sxy = (long long)g.nx * g.ny;
+  for (int e = tid; e < PL; e += NT) {
+    const int r = e / W, c = e - r * W;
+    const int xx = blockIdx.x * EP_TX - HX + c, yy = blockIdx.y * EP_TY - R + r;
+    int o = -1;
+    if (xx >= 0 && xx < g.nx && yy >= 0 && yy < g.ny) o = xx + g.nx * yy;
+    else if (per) o = wrapi(xx, g.nx) + g.nx * wrapi(yy, g.ny);
+    soff[e] = o;
+  }
+  auto zwrap = [&](int zz) -> int {
+    if (zz < 0 || zz >= g.nz) return per ? wrapi(zz, g.nz) : -1;
+    return zz;
+  };
+  const long long pxy = (long long)x + (long long)g.nx * y;
+  T q[2 * R + 1];
+#pragma unroll
+  for (int k = 0; k < 2 * R; ++k) {
+    const int zz = zwrap(z0 - R + k);
+    q[k] = (valid && zz >= 0) ? fq[pxy + sxy * zz] : T(0);
+  }
+  __syncthreads();
+  auto prefetch = [&](int z, int buf) {
+    const int zz = zwrap(z);
+    const T* pz = f + sxy * (zz < 0 ? 0 : zz);
+    for (int e = tid; e < PL; e += NT) {
+      const int o = zz < 0 ? -1 : soff[e];
+      if (o >= 0) cp_async<sizeof(T)>(&sp[buf][e], pz + o);
+      else sp[buf][e] = T(0);
+    }
+    if (valid) {
+      const int zq = zwrap(z + R);
+      if (zq >= 0) cp_async<sizeof(T)>(&sq[buf][tid], fq + pxy + sxy * zq);
+      else sq[buf][tid] = T(0);
+    }
+    cp_commit();
+  };
+  prefetch(z0, 0);
+  for (int z = z0; z < z1; ++z) {
+    const int buf = (z - z0) & 1;
+    if (z + 1 < z1) {
+      prefetch(z + 1, buf ^ 1);
+      cp_wait<1>();
+    } else {
+      cp_wait<0>();
+    }
+    __syncthreads();
+    if (valid) {
+      q[2 * R] = sq[buf][tid];
+      const T* row = &sp[buf][(ty + R) * W + (tx + HX)];
+      const long long p = pxy + sxy * z;
+      T dy = T(0), dz = T(0);
+#pragma unroll
+      for (int k = 1; k <= R; ++k) dy += fd.w1[1][k] * (row[k * W] - row[-k * W]);
+#pragma unroll
+      for (int k = 1; k <= R; ++k) dz += fd.w1[2][k] * (q[R + k] - q[R - k]);
+      if (MODE == 0) {
+        T dx = T(0);
+#pragma unroll
+        for (int k = 1; k <= R; ++k) dx += fd.w1[0][k] * (row[k] - row[-k]);
+        o0[p] = dx;
+        o1[p] = dy;
+        o2[p] = dz;
+      } else {
+        o0[p] = dy + dz;
+      }
     }
 #pragma unroll
     for (int k = 0; k < 2 * R; ++k) q[k] = q[k + 1];

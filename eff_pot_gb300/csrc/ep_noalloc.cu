@@ -69,7 +69,7 @@ __global__ void k_noalloc_twiddles(double2* tw, int n) {
 }
 
 // Backward c2r along x of every line, scaled by 1/N, into a real array.
-__global__ void k_noalloc_xinv(Geo g, const double2* __restrict__ spec, double* __restrict__ out, FftPlan p2,
+__global__ void k_noalloc_xinv(Geo g, const double2* __restrict__ spec, double* __restrict__ out, const __grid_constant__ FftPlan p2,
                                const double2* __restrict__ twx, double scale, int nl) {
   extern __shared__ __align__(16) unsigned char smraw[];
   const int nx = g.nx;
@@ -150,9 +150,7 @@ extern "C" int ep_convolve_noalloc(const double* d_in, const double* d_kernel, d
   const long long nlines = (long long)ny * nz;
   int nl = 16;
   while (nl > 1 && x_smem_of(nl, nx) > 110 * 1024) nl /= 2;
-  FdW<double> fd{};
-  k_x1<double><<<(unsigned)((nlines + nl - 1) / nl), 256, x_smem_of(nl, nx), st>>>(
-      g, d_in, S, nullptr, nullptr, nullptr, 0, p2, twx, fd, nl);
+  k_x1<double><<<(unsigned)((nlines + nl - 1) / nl), 256, x_smem_of(nl, nx), st>>>(g, d_in, S, p2, twx, nl);
   Arr8<double> ay{};
   ay.a[0] = S;
   LineSet ly{(long long)g.nxh, (long long)g.nxh * ny, (long long)g.nxh, (long long)g.nxh * nz};

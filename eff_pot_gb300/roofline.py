@@ -19,8 +19,11 @@ def step_bytes(nx, ny, nz, otc=True, grad=True, s=8, renorm=True):
     # corrector: read psi, psiold3, psiold2, hpsi1, hpsi2, pc, pot4, uimp;
     # write pc, psi, den
     b["correct"] = (6 * c + 2 * s + 2 * c + s) * N
-    # X1: read den, write its x-transformed half spectrum (+ grad den)
-    b["x1_r2c_den"] = s * N + c * Nh + (3 * s * N if grad else 0)
+    # X1: read den, write its x-transformed half spectrum
+    b["x1_r2c_den"] = s * N + c * Nh
+    if grad:
+        # first-derivative march: read den, write its three derivatives
+        b["grad_march"] = 4 * s * N
     nconv1 = 3 if otc else 2
     nfwd2 = 4 if otc else 1
     # Y passes (in place): read + write each spectrum
@@ -42,12 +45,17 @@ def step_bytes(nx, ny, nz, otc=True, grad=True, s=8, renorm=True):
         # X3: read 4 spectra, grad den, falfs, pot4; write pot4, I_xyz, g_y,
         # g_z, d(f I_x)/dx and the forward spectrum of grad(den).I
         b["x3_c2r_r2c"] = 4 * c * Nh + 5 * s * N + 7 * s * N + c * Nh
-        # X4: read spectrum, den, dgx, g_y, g_z, pot4; write pot4, ualphas
-        b["x4_c2r_ualpha"] = c * Nh + 5 * s * N + 2 * s * N
+        # div march: read g_y, g_z; write dy g_y + dz g_z
+        b["div_march"] = 3 * s * N
+        # X4: read spectrum, den, dgx, dy g_y + dz g_z, pot4; write pot4, ualphas
+        b["x4_c2r_ualpha"] = c * Nh + 4 * s * N + 2 * s * N
     else:
         b["x3_c2r_r2c"] = c * Nh + 2 * s * N + s * N
     if renorm:
-        # psi and the history (psiold x3, hpsiold x2, pc) read + written, den written
+        # an explicit rescale pass: psi and the history (psiold x3, hpsiold x2,
+        # pc) read + written, den written.  The engines renormalise lazily
+        # (per-buffer scale factors applied by the next step's kernels), so
+        # their steps have no such pass.
         b["rescale"] = (14 * c + s) * N
     return b
 
