@@ -22,6 +22,19 @@
     if (_e != cudaSuccess) return cuda_ok(_e, name);                  \
   } while (0)
 
+// Launch an X kernel template KER<T, N2> with N2 = the register-transform
+// length of this grid (0: general engine).
+#define EP_XLAUNCH(name, KER, grid, block, smem, ...)                  \
+  do {                                                                 \
+    switch (x_reg_n2(g.nx / 2)) {                                      \
+      case 16: { auto k = KER<T, 16>; EP_LAUNCH(name, k, grid, block, smem, __VA_ARGS__); } break;   \
+      case 32: { auto k = KER<T, 32>; EP_LAUNCH(name, k, grid, block, smem, __VA_ARGS__); } break;   \
+      case 64: { auto k = KER<T, 64>; EP_LAUNCH(name, k, grid, block, smem, __VA_ARGS__); } break;   \
+      case 128: { auto k = KER<T, 128>; EP_LAUNCH(name, k, grid, block, smem, __VA_ARGS__); } break; \
+      default: { auto k = KER<T, 0>; EP_LAUNCH(name, k, grid, block, smem, __VA_ARGS__); } break;    \
+    }                                                                  \
+  } while (0)
+
 namespace {
 
 // Planes per CTA of a stencil march over a (gx, gy) grid of column tiles:
@@ -111,7 +124,7 @@ int Engine<T>::alloc(void** p, size_t n) {
 
 template <class T>
 size_t Engine<T>::x_smem(int nl, int nreal) const {
-  return 2 * (size_t)nl * (g.nx / 2 + 1) * sizeof(CT) + (size_t)g.nx * sizeof(CT) + (size_t)nreal * nl * g.nx * sizeof(T);
+  return x_smem_bytes<T>(nl, g.nx, nreal);
 }
 template <class T>
 int Engine<T>::x_lines(int nreal) const {
@@ -244,17 +257,21 @@ int Engine<T>::init(const ep_config& c, cudaStream_t s, Prof* p, ImpState* im, s
     cudaFree(dpg);
   }
   const int big = 220 * 1024;
-  cudaFuncSetAttribute(k_x1<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, big);
-  cudaFuncSetAttribute(k_x2<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, big);
-  cudaFuncSetAttribute(k_x3<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, big);
-  cudaFuncSetAttribute(k_x4<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, big);
+#define EP_XATTR(NN)                                                                \
+  cudaFuncSetAttribute(k_x1<T, NN>, cudaFuncAttributeMaxDynamicSharedMemorySize, big); \
+  cudaFuncSetAttribute(k_x2<T, NN>, cudaFuncAttributeMaxDynamicSharedMemorySize, big); \
+  cudaFuncSetAttribute(k_x3<T, NN>, cudaFuncAttributeMaxDynamicSharedMemorySize, big); \
+  cudaFuncSetAttribute(k_x4<T, NN>, cudaFuncAttributeMaxDynamicSharedMemorySize, big);
+  EP_XATTR(0) EP_XATTR(16) EP_XATTR(32) EP_XATTR(64) EP_XATTR(128)
+#undef EP_XATTR
   cudaFuncSetAttribute(k_c2c<T, -1>, cudaFuncAttributeMaxDynamicSharedMemorySize, big);
   cudaFuncSetAttribute(k_c2c<T, +1>, cudaFuncAttributeMaxDynamicSharedMemorySize, big);
   cudaFuncSetAttribute(k_zconv<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, big);
 #define EP_RFFT_ATTR(NN)                                                                                  \
   cudaFuncSetAttribute(k_c2c_r<T, NN, -1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)rfft::smem_bytes<T, NN>()); \
   cudaFuncSetAttribute(k_c2c_r<T, NN, +1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)rfft::smem_bytes<T, NN>()); \
-  cudaFuncSetAttribute(k_zconv_r<T, NN>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)rfft::smem_bytes<T, NN>());
+  cudaFuncSetAttribute(k_zconv_r<T, NN, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)rfft::smem_bytes<T, NN>()); \
+  cudaFuncSetAttribute(k_zconv_r<T, NN, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)rfft::smem_bytes<T, NN>());
   EP_RFFT_ATTR(32) EP_RFFT_ATTR(64) EP_RFFT_ATTR(128) EP_RFFT_ATTR(256)
 #undef EP_RFFT_ATTR
   {
@@ -333,8 +350,15 @@ template <class T>
 template <int N>
 int Engine<T>::rfft_z(const ConvSpec<T>& cs, int nin, const LineSet& ls) {
   dim3 grid((unsigned)((ls.nlines + 31) / 32), (unsigned)nin), blk(32, rfft::Shape<N>::P);
-  auto k = k_zconv_r<T, N>;
-  EP_LAUNCH("fft_z_conv", k, grid, blk, (rfft::smem_bytes<T, N>()), cs, ls, twz);
+  bool one = true;
+  for (int i = 0; i < nin; ++i) one = one && cs.nout[i] == 1;
+  if (one) {
+    auto k = k_zconv_r<T, N, true>;
+    EP_LAUNCH("fft_z_conv", k, grid, blk, (rfft::smem_bytes<T, N>()), cs, ls, twz);
+  } else {
+    auto k = k_zconv_r<T, N, false>;
+    EP_LAUNCH("fft_z_conv", k, grid, blk, (rfft::smem_bytes<T, N>()), cs, ls, twz);
+  }
   return EP_OK;
 }
 
@@ -418,8 +442,8 @@ int Engine<T>::poten() {
   int r;
   {
     const int nl = x_lines(1);
-    auto k = k_x1<T>;
-    EP_LAUNCH("x1_r2c_den", k, (unsigned)((nlines + nl - 1) / nl), shp.xthr, x_smem(nl, 1), g, den, S[0], p2, twx, nl);
+    EP_XLAUNCH("x1_r2c_den", k_x1, (unsigned)((nlines + nl - 1) / nl), shp.xthr, x_smem(nl, 1), g, den, S[0], p2, twx,
+               nl);
   }
   if (grad && (r = d1march(0, den, nullptr, dxd, dyd, dzd))) return r;
   CT* a1[1] = {S[0]};
@@ -435,8 +459,7 @@ int Engine<T>::poten() {
   if ((r = fft_y(b3, otc ? 3 : 2, +1))) return r;
   {
     const int nl = x_lines(otc ? 3 : 2);
-    auto k = k_x2<T>;
-    EP_LAUNCH("x2_c2r_r2c", k, (unsigned)((nlines + nl - 1) / nl), shp.xthr, x_smem(nl, otc ? 3 : 2), g, phys, Tb[0],
+    EP_XLAUNCH("x2_c2r_r2c", k_x2, (unsigned)((nlines + nl - 1) / nl), shp.xthr, x_smem(nl, otc ? 3 : 2), g, phys, Tb[0],
               Tb[1], Tb[2], den, dxd, dyd, dzd, dencg, delj4, pot4, falfs, S[0], S[1], S[2], S[3], p2, twx, nl);
   }
   CT* c4[4] = {S[0], S[1], S[2], S[3]};
@@ -452,8 +475,7 @@ int Engine<T>::poten() {
   if ((r = fft_y(d4, otc ? 4 : 1, +1))) return r;
   {
     const int nl = x_lines(otc ? 4 : 1);
-    auto k = k_x3<T>;
-    EP_LAUNCH("x3_c2r_r2c", k, (unsigned)((nlines + nl - 1) / nl), shp.xthr, x_smem(nl, otc ? 4 : 1), g, phys, fd,
+    EP_XLAUNCH("x3_c2r_r2c", k_x3, (unsigned)((nlines + nl - 1) / nl), shp.xthr, x_smem(nl, otc ? 4 : 1), g, phys, fd,
               Tb[0], Tb[1], Tb[2], Tb[3], den, dxd, dyd, dzd, falfs, pot4, intx, inty, intz, gy, gz, dgx, S[0], p2,
               twx, nl);
   }
@@ -468,8 +490,7 @@ int Engine<T>::poten() {
     CT* e1[1] = {Tb[0]};
     if ((r = fft_y(e1, 1, +1))) return r;
     const int nl = x_lines(1);
-    auto k = k_x4<T>;
-    EP_LAUNCH("x4_c2r_ualpha", k, (unsigned)((nlines + nl - 1) / nl), shp.xthr, x_smem(nl, 1), g, phys, Tb[0], den,
+    EP_XLAUNCH("x4_c2r_ualpha", k_x4, (unsigned)((nlines + nl - 1) / nl), shp.xthr, x_smem(nl, 1), g, phys, Tb[0], den,
               dgx, dyz, pot4, ualphas, p2, twx, nl);
   }
   have_field = true;

@@ -102,6 +102,61 @@ template <class T, int R, int DIR> EP_DEV void dftR(C2<T>* v) {
   else dft8<T, DIR>(v);
 }
 
+template <class T> struct K16;
+template <> struct K16<double> {
+  static constexpr double c = 0.92387953251128675612818318939678829;  // cos(pi/8)
+  static constexpr double s = 0.38268343236508977172845998403039887;  // sin(pi/8)
+  static constexpr double r = 0.70710678118654752440084436210484904;  // 1/sqrt(2)
+};
+template <> struct K16<float> {
+  static constexpr float c = 0.92387953251128675612818318939678829f;
+  static constexpr float s = 0.38268343236508977172845998403039887f;
+  static constexpr float r = 0.70710678118654752440084436210484904f;
+};
+
+// z * (a + DIR b i)
+template <class T, int DIR> EP_DEV C2<T> rotc(C2<T> z, T a, T b) {
+  const T bb = DIR < 0 ? -b : b;
+  return cmk<T>(z.x * a - z.y * bb, z.x * bb + z.y * a);
+}
+
+// 16-point DFT as 4 x 4: n = 4 n1 + n2, k = k1 + 4 k2.
+template <class T, int DIR> EP_DEV void dft16(C2<T>* v) {
+  C2<T> y[16];
+#pragma unroll
+  for (int n2 = 0; n2 < 4; ++n2) {
+    C2<T> a[4] = {v[n2], v[4 + n2], v[8 + n2], v[12 + n2]};
+    dft4<T, DIR>(a);
+#pragma unroll
+    for (int k1 = 0; k1 < 4; ++k1) y[4 * n2 + k1] = a[k1];
+  }
+  // w16^(n2 k1) for n2, k1 in 1..3: exponents 1 2 3 / 2 4 6 / 3 6 9
+  const T c = K16<T>::c, s = K16<T>::s, r = K16<T>::r;
+  y[5] = rotc<T, DIR>(y[5], c, s);
+  y[6] = rotc<T, DIR>(y[6], r, r);
+  y[7] = rotc<T, DIR>(y[7], s, c);
+  y[9] = rotc<T, DIR>(y[9], r, r);
+  y[10] = rot<DIR>(y[10]);
+  y[11] = rotc<T, DIR>(y[11], -r, r);
+  y[13] = rotc<T, DIR>(y[13], s, c);
+  y[14] = rotc<T, DIR>(y[14], -r, r);
+  y[15] = rotc<T, DIR>(y[15], -c, -s);
+#pragma unroll
+  for (int k1 = 0; k1 < 4; ++k1) {
+    C2<T> b[4] = {y[k1], y[4 + k1], y[8 + k1], y[12 + k1]};
+    dft4<T, DIR>(b);
+#pragma unroll
+    for (int k2 = 0; k2 < 4; ++k2) v[k1 + 4 * k2] = b[k2];
+  }
+}
+
+template <class T, int R, int DIR> EP_DEV void dft(C2<T>* v) {
+  if (R == 16) dft16<T, DIR>(v);
+  else if (R == 8) dft8<T, DIR>(v);
+  else if (R == 4) dft4<T, DIR>(v);
+  else dft2<T, DIR>(v);
+}
+
 // q = a / d, r = a - q d for 0 <= a < 2^22 through a float reciprocal
 // (one correction step makes it exact); far cheaper than integer division.
 EP_DEV int fdivmod(int a, int d, float inv_d, int& r) {

@@ -216,10 +216,129 @@ EP_DEV void block_reduce_store(double (&v)[NQ], double* __restrict__ partials) {
 
 // ---------------------------------------------------------------------------
 // X pass helpers (lines along x are contiguous; nl lines per CTA).
+//
+// Half-line transforms of N2 = nx/2 points.  N2 in {16, 32, 64, 128} use
+// xlines: P threads of one warp per line, E = N2/P points per thread, the
+// two-factor decomposition of ep_rfft.cuh with the exchange done in place in
+// the line's own shared-memory row (stride P+1 for the exchange), fenced by
+// __syncwarp only.  The row stride x_row() makes the step-1 reads, the
+// exchange and the step-2 reads conflict-free for 8- and 16-byte elements.
+// N2 = 0 selects the general shared-memory Stockham engine.
+template <int N2> struct XShape;
+template <> struct XShape<16> { static constexpr int P = 4, E = 4; };
+template <> struct XShape<32> { static constexpr int P = 4, E = 8; };
+template <> struct XShape<64> { static constexpr int P = 8, E = 8; };
+template <> struct XShape<128> { static constexpr int P = 8, E = 16; };
+
+__host__ __device__ constexpr int x_reg_n2(int n2) {
+  return (n2 == 16 || n2 == 32 || n2 == 64 || n2 == 128) ? n2 : 0;
+}
+// row stride (complex elements): >= n2 + 1 and >= E (P + 1), and congruent
+// to P modulo 16 so that the lines sharing a half-warp fall on distinct banks
+__host__ __device__ constexpr int x_row(int n2, int reg) {
+  return !reg ? n2 + 1 : (n2 == 16 ? 20 : n2 == 32 ? 52 : n2 == 64 ? 72 : 152);
+}
+// shared memory of an X kernel: two line buffers, the twiddles exp(-2 pi i
+// k/nx), the [ka][t] twiddle table of xlines, nreal real arrays
 template <class T>
+__host__ __device__ constexpr size_t x_smem_bytes(int nl, int nx, int nreal) {
+  return 2 * (size_t)nl * x_row(nx / 2, x_reg_n2(nx / 2)) * sizeof(C2<T>) + (size_t)nx * sizeof(C2<T>) +
+         (size_t)(x_reg_n2(nx / 2) ? nx / 2 : 0) * sizeof(C2<T>) + (size_t)nreal * nl * nx * sizeof(T);
+}
+
+template <class T, int N2, int DIR>
+EP_DEV void xlines(C2<T>* A, int nl, int ld, const C2<T>* __restrict__ twt) {
+  constexpr int P = XShape<N2>::P, E = XShape<N2>::E, LPW = 32 / P, Q = P + 1;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  const int t = lane % P, lsub = lane / P;
+  for (int base = warp * LPW; base < nl; base += nw * LPW) {
+    const int l = base + lsub;
+    const bool act = l < nl;
+    C2<T>* row = A + (act ? l : 0) * ld;
+    C2<T> v[E];
+#pragma unroll
+    for (int a = 0; a < E; ++a) v[a] = act ? row[t + P * a] : cmk<T>(T(0), T(0));
+    epfft::dft<T, E, DIR>(v);
+    if (t != 0) {
+#pragma unroll
+      for (int ka = 1; ka < E; ++ka) {
+        const C2<T> w = twt[ka * P + t];
+        v[ka] = DIR < 0 ? cmul(v[ka], w) : cmulc(v[ka], w);
+      }
+    }
+    __syncwarp();
+    if (act) {
+#pragma unroll
+      for (int ka = 0; ka < E; ++ka) row[ka * Q + t] = v[ka];
+    }
+    __syncwarp();
+#pragma unroll
+    for (int j = 0; j < E / P; ++j) {
+      C2<T> u[P];
+#pragma unroll
+      for (int tt = 0; tt < P; ++tt) u[tt] = row[(t + P * j) * Q + tt];
+      epfft::dft<T, P, DIR>(u);
+#pragma unroll
+      for (int kt = 0; kt < P; ++kt) v[j + (E / P) * kt] = u[kt];
+    }
+    __syncwarp();
+    if (act) {
+#pragma unroll
+      for (int m = 0; m < E; ++m) row[t + P * m] = v[m];
+    }
+  }
+  __syncthreads();
+}
+
+// Transform nl lines held in A (B: scratch); returns the buffer with the result.
+template <class T, int N2, int DIR>
+EP_DEV const C2<T>* x_lines(C2<T>* A, C2<T>* B, int nl, int ld, const FftPlan& p2, const C2<T>* tw,
+                            const C2<T>* twt) {
+  if constexpr (N2 != 0) {
+    xlines<T, N2, DIR>(A, nl, ld, twt);
+    return A;
+  } else {
+    return epfft::lines<T, DIR>(A, B, nl, ld, p2, tw, 2);
+  }
+}
+
+// Shared-memory carve-up of the X kernels.
+template <class T>
+struct XSmem {
+  C2<T>* P;
+  C2<T>* Q;
+  C2<T>* tw;
+  C2<T>* twt;  // [ka][t] twiddles of xlines
+  T* R;        // nreal arrays of nl*nx
+  int ld;
+  EP_DEV XSmem(unsigned char* raw, int nl, int nx, int n2reg) {
+    ld = x_row(nx / 2, n2reg);
+    P = reinterpret_cast<C2<T>*>(raw);
+    Q = P + nl * ld;
+    tw = Q + nl * ld;
+    twt = tw + nx;
+    R = reinterpret_cast<T*>(twt + (n2reg ? nx / 2 : 0));
+  }
+  // tw and (for the register transforms) twt from the global table twx;
+  // the caller synchronises before use
+  template <int N2> EP_DEV void load_twiddles(const C2<T>* __restrict__ twx, int nx) {
+    for (int i = threadIdx.x; i < nx; i += blockDim.x) tw[i] = twx[i];
+    if constexpr (N2 != 0) {
+      constexpr int P = XShape<N2>::P;
+      for (int i = threadIdx.x; i < N2; i += blockDim.x) {
+        const int ka = i / P, t = i - ka * P;
+        twt[i] = twx[2 * t * ka];
+      }
+    }
+  }
+};
+
+template <class T, int N2>
 EP_DEV void x_inverse(const C2<T>* __restrict__ spec, long long line0, int nlv, int nl, int nx, int nxh,
-                      C2<T>* P, C2<T>* Q, int ld, const FftPlan& p2, const C2<T>* tw, T scale, T* Rout) {
-  const int n2 = nx / 2;
+                      const XSmem<T>& S, const FftPlan& p2, T scale, T* Rout) {
+  const int n2 = nx / 2, ld = S.ld;
+  C2<T>* P = S.P;
+  C2<T>* Q = S.Q;
   const float inv1 = 1.0f / (float)(n2 + 1), inv2 = 1.0f / (float)n2;
   for (int e = threadIdx.x; e < nl * (n2 + 1); e += blockDim.x) {
     int k;
@@ -227,9 +346,9 @@ EP_DEV void x_inverse(const C2<T>* __restrict__ spec, long long line0, int nlv, 
     P[l * ld + k] = l < nlv ? spec[(line0 + l) * nxh + k] : cmk<T>(T(0), T(0));
   }
   __syncthreads();
-  epfft::c2r_pack<T>(P, ld, Q, ld, nl, n2, tw);
+  epfft::c2r_pack<T>(P, ld, Q, ld, nl, n2, S.tw);
   __syncthreads();
-  const C2<T>* z = epfft::lines<T, +1>(Q, P, nl, ld, p2, tw, 2);
+  const C2<T>* z = x_lines<T, N2, +1>(Q, P, nl, ld, p2, S.tw, S.twt);
   for (int e = threadIdx.x; e < nl * n2; e += blockDim.x) {
     int m;
     const int l = epfft::fdivmod(e, n2, inv2, m);
@@ -240,10 +359,11 @@ EP_DEV void x_inverse(const C2<T>* __restrict__ spec, long long line0, int nlv, 
   __syncthreads();
 }
 
-template <class T, class F>
+template <class T, int N2, class F>
 EP_DEV void x_forward(F val, C2<T>* __restrict__ out, long long line0, int nlv, int nl, int nx, int nxh,
-                      C2<T>* P, C2<T>* Q, int ld, const FftPlan& p2, const C2<T>* tw) {
-  const int n2 = nx / 2;
+                      const XSmem<T>& S, const FftPlan& p2) {
+  const int n2 = nx / 2, ld = S.ld;
+  C2<T>* P = S.P;
   const float inv2 = 1.0f / (float)n2;
   for (int e = threadIdx.x; e < nl * n2; e += blockDim.x) {
     int m;
@@ -251,53 +371,35 @@ EP_DEV void x_forward(F val, C2<T>* __restrict__ out, long long line0, int nlv, 
     P[l * ld + m] = l < nlv ? cmk<T>(val(l, 2 * m), val(l, 2 * m + 1)) : cmk<T>(T(0), T(0));
   }
   __syncthreads();
-  const C2<T>* Z = epfft::lines<T, -1>(P, Q, nl, ld, p2, tw, 2);
-  epfft::r2c_unpack<T>(Z, nl, ld, n2, tw, [&](int l, int k, C2<T> v) {
+  const C2<T>* Z = x_lines<T, N2, -1>(P, S.Q, nl, ld, p2, S.tw, S.twt);
+  epfft::r2c_unpack<T>(Z, nl, ld, n2, S.tw, [&](int l, int k, C2<T> v) {
     if (l < nlv) out[(line0 + l) * nxh + k] = v;
   });
   __syncthreads();
 }
 
-// Shared-memory carve-up of the X kernels.
-template <class T>
-struct XSmem {
-  C2<T>* P;
-  C2<T>* Q;
-  C2<T>* tw;
-  T* R;  // nreal arrays of nl*nx
-  int ld;
-  EP_DEV XSmem(unsigned char* raw, int nl, int nx) {
-    ld = nx / 2 + 1;
-    P = reinterpret_cast<C2<T>*>(raw);
-    Q = P + nl * ld;
-    tw = Q + nl * ld;
-    R = reinterpret_cast<T*>(tw + nx);
-  }
-};
-
 // X1: den -> r2c along x (-> out).  grad den is k_d1march<MODE 0>.
-template <class T>
+template <class T, int N2>
 __global__ void k_x1(Geo g, const T* __restrict__ den, C2<T>* __restrict__ out, const __grid_constant__ FftPlan p2,
                      const C2<T>* __restrict__ twx, int nl) {
   extern __shared__ __align__(16) unsigned char smraw[];
   const int nx = g.nx;
-  XSmem<T> S(smraw, nl, nx);
+  XSmem<T> S(smraw, nl, nx, N2);
   const long long nlines = (long long)g.ny * g.nz;
   const long long line0 = (long long)blockIdx.x * nl;
   const int nlv = (int)min((long long)nl, nlines - line0);
-  for (int i = threadIdx.x; i < nx; i += blockDim.x) S.tw[i] = twx[i];
+  S.template load_twiddles<N2>(twx, nx);
   T* R0 = S.R;
   for (int e = threadIdx.x; e < nlv * nx; e += blockDim.x) R0[e] = den[line0 * nx + e];
   __syncthreads();
-  x_forward<T>([&](int l, int i) { return R0[l * nx + i]; }, out, line0, nlv, nl, nx, g.nxh, S.P, S.Q, S.ld,
-               p2, S.tw);
+  x_forward<T, N2>([&](int l, int i) { return R0[l * nx + i]; }, out, line0, nlv, nl, nx, g.nxh, S, p2);
 }
 
 // X2: c2r of the three products of fden -> dencg, delj4 (and denalf for
 // OTC); pot4 partial = delj4 + dencg^2 (a0 + a1 dencg) (poten.f90:34-92);
 // forward r2c of den*dencg*(cp4 + cpp4*dencg) (poten.f90:62-67) and, for
 // OTC, of f*grad(den), f = 1 - denalf/den0s (term_alfa.f90:157-170).
-template <class T>
+template <class T, int N2>
 __global__ void k_x2(Geo g, Phys ph, const C2<T>* __restrict__ B0, const C2<T>* __restrict__ B1,
                      const C2<T>* __restrict__ B2, const T* __restrict__ den, const T* __restrict__ dxd,
                      const T* __restrict__ dyd, const T* __restrict__ dzd, T* __restrict__ dencg,
@@ -305,20 +407,20 @@ __global__ void k_x2(Geo g, Phys ph, const C2<T>* __restrict__ B0, const C2<T>* 
                      C2<T>* C2o, C2<T>* C3, const __grid_constant__ FftPlan p2, const C2<T>* __restrict__ twx, int nl) {
   extern __shared__ __align__(16) unsigned char smraw[];
   const int nx = g.nx, nxh = g.nxh;
-  XSmem<T> S(smraw, nl, nx);
+  XSmem<T> S(smraw, nl, nx, N2);
   const bool otc = (ph.core == 1);
   const long long nlines = (long long)g.ny * g.nz;
   const long long line0 = (long long)blockIdx.x * nl;
   const int nlv = (int)min((long long)nl, nlines - line0);
-  for (int i = threadIdx.x; i < nx; i += blockDim.x) S.tw[i] = twx[i];
+  S.template load_twiddles<N2>(twx, nx);
   __syncthreads();
   T* Rcg = S.R;
   T* Rlj = S.R + nl * nx;
   T* Ral = S.R + 2 * nl * nx;
   const T rn = (T)ph.renor;
-  x_inverse<T>(B0, line0, nlv, nl, nx, nxh, S.P, S.Q, S.ld, p2, S.tw, rn, Rcg);
-  x_inverse<T>(B1, line0, nlv, nl, nx, nxh, S.P, S.Q, S.ld, p2, S.tw, rn, Rlj);
-  if (otc) x_inverse<T>(B2, line0, nlv, nl, nx, nxh, S.P, S.Q, S.ld, p2, S.tw, rn, Ral);
+  x_inverse<T, N2>(B0, line0, nlv, nl, nx, nxh, S, p2, rn, Rcg);
+  x_inverse<T, N2>(B1, line0, nlv, nl, nx, nxh, S, p2, rn, Rlj);
+  if (otc) x_inverse<T, N2>(B2, line0, nlv, nl, nx, nxh, S, p2, rn, Ral);
   const T a0 = (T)ph.a0, a1 = (T)ph.a1, rden0s = (T)(1.0 / ph.den0s), cp4 = (T)ph.cp4, cpp4 = (T)ph.cpp4;
   for (int e = threadIdx.x; e < nlv * nx; e += blockDim.x) {
     const long long p = line0 * nx + e;
@@ -333,19 +435,19 @@ __global__ void k_x2(Geo g, Phys ph, const C2<T>* __restrict__ B0, const C2<T>* 
     }
   }
   __syncthreads();
-  x_forward<T>(
+  x_forward<T, N2>(
       [&](int l, int i) {
         const T cg = Rcg[l * nx + i];
         return den[(line0 + l) * nx + i] * cg * (cp4 + cpp4 * cg);
       },
-      C0, line0, nlv, nl, nx, nxh, S.P, S.Q, S.ld, p2, S.tw);
+      C0, line0, nlv, nl, nx, nxh, S, p2);
   if (otc) {
-    x_forward<T>([&](int l, int i) { return Ral[l * nx + i] * dxd[(line0 + l) * nx + i]; },
-                 C1, line0, nlv, nl, nx, nxh, S.P, S.Q, S.ld, p2, S.tw);
-    x_forward<T>([&](int l, int i) { return Ral[l * nx + i] * dyd[(line0 + l) * nx + i]; },
-                 C2o, line0, nlv, nl, nx, nxh, S.P, S.Q, S.ld, p2, S.tw);
-    x_forward<T>([&](int l, int i) { return Ral[l * nx + i] * dzd[(line0 + l) * nx + i]; },
-                 C3, line0, nlv, nl, nx, nxh, S.P, S.Q, S.ld, p2, S.tw);
+    x_forward<T, N2>([&](int l, int i) { return Ral[l * nx + i] * dxd[(line0 + l) * nx + i]; },
+                 C1, line0, nlv, nl, nx, nxh, S, p2);
+    x_forward<T, N2>([&](int l, int i) { return Ral[l * nx + i] * dyd[(line0 + l) * nx + i]; },
+                 C2o, line0, nlv, nl, nx, nxh, S, p2);
+    x_forward<T, N2>([&](int l, int i) { return Ral[l * nx + i] * dzd[(line0 + l) * nx + i]; },
+                 C3, line0, nlv, nl, nx, nxh, S, p2);
   }
 }
 
@@ -353,7 +455,7 @@ __global__ void k_x2(Geo g, Phys ph, const C2<T>* __restrict__ B0, const C2<T>* 
 // poten.f90:74,88-92,122-126).  OTC: c2r of the three alpha_s integrals
 // (term_alfa.f90:172-181), the x-derivative of f*I_x, f*I_y and f*I_z for
 // the divergence (:216-225), and forward r2c of grad(den).I (:194-201).
-template <class T>
+template <class T, int N2>
 __global__ void k_x3(Geo g, Phys ph, const __grid_constant__ FdW<T> fd, const C2<T>* __restrict__ D0, const C2<T>* __restrict__ D1,
                      const C2<T>* __restrict__ D2, const C2<T>* __restrict__ D3, const T* __restrict__ den,
                      const T* __restrict__ dxd, const T* __restrict__ dyd, const T* __restrict__ dzd,
@@ -362,16 +464,16 @@ __global__ void k_x3(Geo g, Phys ph, const __grid_constant__ FdW<T> fd, const C2
                      C2<T>* E0, const __grid_constant__ FftPlan p2, const C2<T>* __restrict__ twx, int nl) {
   extern __shared__ __align__(16) unsigned char smraw[];
   const int nx = g.nx, nxh = g.nxh;
-  XSmem<T> S(smraw, nl, nx);
+  XSmem<T> S(smraw, nl, nx, N2);
   const bool otc = (ph.core == 1);
   const long long nlines = (long long)g.ny * g.nz;
   const long long line0 = (long long)blockIdx.x * nl;
   const int nlv = (int)min((long long)nl, nlines - line0);
-  for (int i = threadIdx.x; i < nx; i += blockDim.x) S.tw[i] = twx[i];
+  S.template load_twiddles<N2>(twx, nx);
   __syncthreads();
   const T rn = (T)ph.renor;
   T* Rc = S.R;
-  x_inverse<T>(D0, line0, nlv, nl, nx, nxh, S.P, S.Q, S.ld, p2, S.tw, rn, Rc);
+  x_inverse<T, N2>(D0, line0, nlv, nl, nx, nxh, S, p2, rn, Rc);
   if (!otc) {
     for (int e = threadIdx.x; e < nlv * nx; e += blockDim.x) {
       const long long p = line0 * nx + e;
@@ -382,9 +484,9 @@ __global__ void k_x3(Geo g, Phys ph, const __grid_constant__ FdW<T> fd, const C2
   T* Rx = S.R + nl * nx;
   T* Ry = S.R + 2 * nl * nx;
   T* Rz = S.R + 3 * nl * nx;
-  x_inverse<T>(D1, line0, nlv, nl, nx, nxh, S.P, S.Q, S.ld, p2, S.tw, rn, Rx);
-  x_inverse<T>(D2, line0, nlv, nl, nx, nxh, S.P, S.Q, S.ld, p2, S.tw, rn, Ry);
-  x_inverse<T>(D3, line0, nlv, nl, nx, nxh, S.P, S.Q, S.ld, p2, S.tw, rn, Rz);
+  x_inverse<T, N2>(D1, line0, nlv, nl, nx, nxh, S, p2, rn, Rx);
+  x_inverse<T, N2>(D2, line0, nlv, nl, nx, nxh, S, p2, rn, Ry);
+  x_inverse<T, N2>(D3, line0, nlv, nl, nx, nxh, S, p2, rn, Rz);
   for (int e = threadIdx.x; e < nlv * nx; e += blockDim.x) {
     const long long p = line0 * nx + e;
     pot4[p] = pot4[p] + Rc[e];
@@ -402,31 +504,31 @@ __global__ void k_x3(Geo g, Phys ph, const __grid_constant__ FdW<T> fd, const C2
       const int l = epfft::fdivmod(e, nx, 1.0f / (float)nx, i);
     dgx[line0 * nx + e] = d1_line(Rc + l * nx, i, nx, fd.w1[0], fd.R, fd.periodic);
   }
-  x_forward<T>(
+  x_forward<T, N2>(
       [&](int l, int i) {
         const int e = l * nx + i;
         const long long p = line0 * nx + e;
         return (dxd[p] * Rx[e]) + (dyd[p] * Ry[e]) + (dzd[p] * Rz[e]);
       },
-      E0, line0, nlv, nl, nx, nxh, S.P, S.Q, S.ld, p2, S.tw);
+      E0, line0, nlv, nl, nx, nxh, S, p2);
 }
 
 // X4 (OTC): c2r of kalfs*FFT(grad(den).I) -> U_alpha = (u/den0s + div(f I))
 // * h2o2m4 * alphas (term_alfa.f90:203-236); pot4 += U_alpha + penalty.
-template <class T>
+template <class T, int N2>
 __global__ void k_x4(Geo g, Phys ph, const C2<T>* __restrict__ F0, const T* __restrict__ den,
                      const T* __restrict__ dgx, const T* __restrict__ dyz, T* __restrict__ pot4,
                      T* __restrict__ ualphas, const __grid_constant__ FftPlan p2, const C2<T>* __restrict__ twx, int nl) {
   extern __shared__ __align__(16) unsigned char smraw[];
   const int nx = g.nx, nxh = g.nxh;
-  XSmem<T> S(smraw, nl, nx);
+  XSmem<T> S(smraw, nl, nx, N2);
   const long long nlines = (long long)g.ny * g.nz;
   const long long line0 = (long long)blockIdx.x * nl;
   const int nlv = (int)min((long long)nl, nlines - line0);
-  for (int i = threadIdx.x; i < nx; i += blockDim.x) S.tw[i] = twx[i];
+  S.template load_twiddles<N2>(twx, nx);
   __syncthreads();
   T* Ru = S.R;
-  x_inverse<T>(F0, line0, nlv, nl, nx, nxh, S.P, S.Q, S.ld, p2, S.tw, (T)ph.renor, Ru);
+  x_inverse<T, N2>(F0, line0, nlv, nl, nx, nxh, S, p2, (T)ph.renor, Ru);
   const T rden0s = (T)(1.0 / ph.den0s), h2 = (T)ph.h2o2m4, al = (T)ph.alphas;
   for (int e = threadIdx.x; e < nlv * nx; e += blockDim.x) {
     const long long p = line0 * nx + e;

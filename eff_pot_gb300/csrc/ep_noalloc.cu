@@ -69,17 +69,17 @@ __global__ void k_noalloc_twiddles(double2* tw, int n) {
 }
 
 // Backward c2r along x of every line, scaled by 1/N, into a real array.
-__global__ void k_noalloc_xinv(Geo g, const double2* __restrict__ spec, double* __restrict__ out, const __grid_constant__ FftPlan p2,
-                               const double2* __restrict__ twx, double scale, int nl) {
+__global__ void k_noalloc_xinv(Geo g, const double2* __restrict__ spec, double* __restrict__ out,
+                               const __grid_constant__ FftPlan p2, const double2* __restrict__ twx, double scale, int nl) {
   extern __shared__ __align__(16) unsigned char smraw[];
   const int nx = g.nx;
-  XSmem<double> S(smraw, nl, nx);
+  XSmem<double> S(smraw, nl, nx, 0);
   const long long nlines = (long long)g.ny * g.nz;
   const long long line0 = (long long)blockIdx.x * nl;
   const int nlv = (int)min((long long)nl, nlines - line0);
   for (int i = threadIdx.x; i < nx; i += blockDim.x) S.tw[i] = twx[i];
   __syncthreads();
-  x_inverse<double>(spec, line0, nlv, nl, nx, g.nxh, S.P, S.Q, S.ld, p2, S.tw, scale, S.R);
+  x_inverse<double, 0>(spec, line0, nlv, nl, nx, g.nxh, S, p2, scale, S.R);
   for (int e = threadIdx.x; e < nlv * nx; e += blockDim.x) out[line0 * nx + e] = S.R[e];
 }
 
@@ -104,7 +104,7 @@ int device_setup(int dev, double2** out) {
     return EP_ERR_CUDA;
   }
   const int big = 220 * 1024;
-  if (cudaFuncSetAttribute(k_x1<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, big) != cudaSuccess ||
+  if (cudaFuncSetAttribute(k_x1<double, 0>, cudaFuncAttributeMaxDynamicSharedMemorySize, big) != cudaSuccess ||
       cudaFuncSetAttribute(k_c2c<double, -1>, cudaFuncAttributeMaxDynamicSharedMemorySize, big) != cudaSuccess ||
       cudaFuncSetAttribute(k_c2c<double, +1>, cudaFuncAttributeMaxDynamicSharedMemorySize, big) != cudaSuccess ||
       cudaFuncSetAttribute(k_zconv<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, big) != cudaSuccess ||
@@ -150,7 +150,7 @@ extern "C" int ep_convolve_noalloc(const double* d_in, const double* d_kernel, d
   const long long nlines = (long long)ny * nz;
   int nl = 16;
   while (nl > 1 && x_smem_of(nl, nx) > 110 * 1024) nl /= 2;
-  k_x1<double><<<(unsigned)((nlines + nl - 1) / nl), 256, x_smem_of(nl, nx), st>>>(g, d_in, S, p2, twx, nl);
+  k_x1<double, 0><<<(unsigned)((nlines + nl - 1) / nl), 256, x_smem_of(nl, nx), st>>>(g, d_in, S, p2, twx, nl);
   Arr8<double> ay{};
   ay.a[0] = S;
   LineSet ly{(long long)g.nxh, (long long)g.nxh * ny, (long long)g.nxh, (long long)g.nxh * nz};

@@ -35,68 +35,13 @@ template <> struct Shape<256> { static constexpr int P = 16, E = 16; };
 
 inline constexpr bool supported(int n) { return n == 32 || n == 64 || n == 128 || n == 256; }
 
-template <class T> struct K16;
-template <> struct K16<double> {
-  static constexpr double c = 0.92387953251128675612818318939678829;  // cos(pi/8)
-  static constexpr double s = 0.38268343236508977172845998403039887;  // sin(pi/8)
-  static constexpr double r = 0.70710678118654752440084436210484904;  // 1/sqrt(2)
-};
-template <> struct K16<float> {
-  static constexpr float c = 0.92387953251128675612818318939678829f;
-  static constexpr float s = 0.38268343236508977172845998403039887f;
-  static constexpr float r = 0.70710678118654752440084436210484904f;
-};
-
-// z * (a + DIR b i)
-template <class T, int DIR> EP_DEV C2<T> rotc(C2<T> z, T a, T b) {
-  const T bb = DIR < 0 ? -b : b;
-  return cmk<T>(z.x * a - z.y * bb, z.x * bb + z.y * a);
-}
-
-// 16-point DFT as 4 x 4: n = 4 n1 + n2, k = k1 + 4 k2.
-template <class T, int DIR> EP_DEV void dft16(C2<T>* v) {
-  C2<T> y[16];
-#pragma unroll
-  for (int n2 = 0; n2 < 4; ++n2) {
-    C2<T> a[4] = {v[n2], v[4 + n2], v[8 + n2], v[12 + n2]};
-    epfft::dft4<T, DIR>(a);
-#pragma unroll
-    for (int k1 = 0; k1 < 4; ++k1) y[4 * n2 + k1] = a[k1];
-  }
-  // w16^(n2 k1) for n2, k1 in 1..3: exponents 1 2 3 / 2 4 6 / 3 6 9
-  const T c = K16<T>::c, s = K16<T>::s, r = K16<T>::r;
-  y[5] = rotc<T, DIR>(y[5], c, s);
-  y[6] = rotc<T, DIR>(y[6], r, r);
-  y[7] = rotc<T, DIR>(y[7], s, c);
-  y[9] = rotc<T, DIR>(y[9], r, r);
-  y[10] = epfft::rot<DIR>(y[10]);
-  y[11] = rotc<T, DIR>(y[11], -r, r);
-  y[13] = rotc<T, DIR>(y[13], s, c);
-  y[14] = rotc<T, DIR>(y[14], -r, r);
-  y[15] = rotc<T, DIR>(y[15], -c, -s);
-#pragma unroll
-  for (int k1 = 0; k1 < 4; ++k1) {
-    C2<T> b[4] = {y[k1], y[4 + k1], y[8 + k1], y[12 + k1]};
-    epfft::dft4<T, DIR>(b);
-#pragma unroll
-    for (int k2 = 0; k2 < 4; ++k2) v[k1 + 4 * k2] = b[k2];
-  }
-}
-
-template <class T, int R, int DIR> EP_DEV void dft(C2<T>* v) {
-  if (R == 16) dft16<T, DIR>(v);
-  else if (R == 8) epfft::dft8<T, DIR>(v);
-  else if (R == 4) epfft::dft4<T, DIR>(v);
-  else epfft::dft2<T, DIR>(v);
-}
-
 // Transform of the CTA's lines: on entry v[a] = x[t + P a], on return
 // v[m] = X[t + P m].  S: this line's exchange row (N + 1 entries); tw: the
 // table exp(-2 pi i k / N), k < N.  All threads of the CTA must call it.
 template <class T, int N, int DIR>
 EP_DEV void lines(C2<T>* v, C2<T>* S, const C2<T>* __restrict__ tw, int t) {
   constexpr int P = Shape<N>::P, E = Shape<N>::E;
-  dft<T, E, DIR>(v);
+  epfft::dft<T, E, DIR>(v);
   if (t != 0) {
 #pragma unroll
     for (int ka = 1; ka < E; ++ka) {
@@ -113,7 +58,7 @@ EP_DEV void lines(C2<T>* v, C2<T>* S, const C2<T>* __restrict__ tw, int t) {
     C2<T> u[P];
 #pragma unroll
     for (int tt = 0; tt < P; ++tt) u[tt] = S[(t + P * j) * P + tt];
-    dft<T, P, DIR>(u);
+    epfft::dft<T, P, DIR>(u);
 #pragma unroll
     for (int kt = 0; kt < P; ++kt) v[j + (E / P) * kt] = u[kt];
   }
@@ -133,6 +78,7 @@ EP_DEV long long line_base(long long L, long long Mi, long long So) { return (L 
 template <class T, int N> struct Occ {
   static constexpr int c2c = sizeof(T) == 4 ? (N <= 64 ? 4 : (N == 128 ? 3 : 2)) : (N <= 64 ? 2 : 1);
   static constexpr int conv = sizeof(T) == 4 ? (N <= 64 ? 3 : (N == 128 ? 2 : 1)) : 1;
+  static constexpr int conv1 = c2c;  // one output per input: no spectrum kept
 };
 
 // In-place transforms along a strided axis of up to 8 arrays (blockIdx.y).
@@ -165,8 +111,8 @@ __global__ void __launch_bounds__(32 * rfft::Shape<N>::P, (Occ<T, N>::c2c))
 // Forward transform along the pass axis, then per kernel table the k-space
 // product and the inverse transform (poten.f90:34-36,46-48,69-71,95-97 and
 // term_alfa.f90:172-176,203-205), all in registers between the exchanges.
-template <class T, int N>
-__global__ void __launch_bounds__(32 * rfft::Shape<N>::P, (Occ<T, N>::conv))
+template <class T, int N, bool ONE>
+__global__ void __launch_bounds__(32 * rfft::Shape<N>::P, (ONE ? Occ<T, N>::conv1 : Occ<T, N>::conv))
     k_zconv_r(const __grid_constant__ ConvSpec<T> cs, LineSet ls, const C2<T>* __restrict__ twg) {
   constexpr int P = rfft::Shape<N>::P, E = rfft::Shape<N>::E;
   extern __shared__ __align__(16) unsigned char smraw[];
@@ -188,6 +134,22 @@ __global__ void __launch_bounds__(32 * rfft::Shape<N>::P, (Occ<T, N>::conv))
   }
   __syncthreads();  // tw complete
   rfft::lines<T, N, -1>(v, Srow, tw, t);
+  if (ONE) {
+    // a single kernel table: the product overwrites the spectrum
+    const T* ker = cs.ker[which][0] + b;
+#pragma unroll
+    for (int m = 0; m < E; ++m) {
+      const T kv = valid ? ker[m * stp] : T(0);
+      v[m] = cmk<T>(v[m].x * kv, v[m].y * kv);
+    }
+    rfft::lines<T, N, +1>(v, Srow, tw, t);
+    if (valid) {
+      C2<T>* o = cs.out[which][0] + b;
+#pragma unroll
+      for (int m = 0; m < E; ++m) o[m * stp] = v[m];
+    }
+    return;
+  }
   const int nout = cs.nout[which];
   for (int j = 0; j < nout; ++j) {
     const T* ker = cs.ker[which][j] + b;
