@@ -237,7 +237,7 @@ def run_ours(args):
     k32 = K - k64
 
     # --- single instance: plain FP64 path, FP32 path with per-kernel events
-    ms64, _, _, tuned64 = time_single("fp64", psi, K, args.warmup, local)
+    ms64, _, prof64, tuned64 = time_single("fp64", psi, K, args.warmup, local, profile=True)
     ms32, l32, prof, tuned32 = time_single("fp32", psi, K, args.warmup, local, profile=True)
 
     # --- the batched scan, FP32 then FP64 refinement
@@ -361,6 +361,8 @@ def run_ours(args):
                      "measured_on": "single FP32 instance, kernels timed alone (burst peak)",
                      "peak_source": "MEASURED_PEAKS.json hbm_gbs (of measured)" if "hbm_gbs" in peaks else "fallback"},
         "kernels_ms_per_step_fp32_single": {k: round(v, 4) for k, v in sorted(per_step.items(), key=lambda t: -t[1])},
+        "kernels_ms_per_step_fp64_single": {k: round(v[0] / K, 4)
+                                            for k, v in sorted(prof64.items(), key=lambda t: -t[1][0])},
         "autotune": {"fp32": tuned32, "fp64": tuned64},
         "gpu_launches": launches,
         "clocks": clk.summary(),

@@ -214,6 +214,49 @@ EP_DEV void block_reduce_store(double (&v)[NQ], double* __restrict__ partials) {
   }
 }
 
+// Block reduction of per-thread accumulators into partials[block * NQ + q].
+// FP32 accumulators (s, c) are summed across the warp as unevaluated pairs
+// with the error-free two-sum, so only one lane per warp widens to FP64
+// (the FP64 pipe is ~1/64 of the FP32 rate here).
+template <int NQ>
+EP_DEV void block_reduce_store_acc(Acc<double> (&acc)[NQ], double* __restrict__ partials) {
+  double v[NQ];
+#pragma unroll
+  for (int q = 0; q < NQ; ++q) v[q] = acc[q].get();
+  block_reduce_store<NQ>(v, partials);
+}
+template <int NQ>
+EP_DEV void block_reduce_store_acc(Acc<float> (&acc)[NQ], double* __restrict__ partials) {
+  __shared__ double red[NQ][32];
+  const int tid = threadIdx.x + blockDim.x * (threadIdx.y + blockDim.y * threadIdx.z);
+  const int nth = blockDim.x * blockDim.y * blockDim.z;
+  const int lane = tid & 31, warp = tid >> 5, nw = (nth + 31) >> 5;
+#pragma unroll
+  for (int q = 0; q < NQ; ++q) {
+    float hi = acc[q].s, lo = -acc[q].c;
+    for (int o = 16; o > 0; o >>= 1) {
+      const float h2 = __shfl_down_sync(0xffffffffu, hi, o), l2 = __shfl_down_sync(0xffffffffu, lo, o);
+      const float t = hi + h2, bb = t - hi;
+      const float e = (hi - (t - bb)) + (h2 - bb);
+      hi = t;
+      lo = (lo + l2) + e;
+    }
+    if (lane == 0) red[q][warp] = (double)hi + (double)lo;
+  }
+  __syncthreads();
+  if (warp == 0) {
+#pragma unroll
+    for (int q = 0; q < NQ; ++q) {
+      double s = lane < nw ? red[q][lane] : 0.0;
+      for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
+      if (lane == 0) {
+        const long long b = blockIdx.x + (long long)gridDim.x * (blockIdx.y + (long long)gridDim.y * blockIdx.z);
+        partials[b * NQ + q] = s;
+      }
+    }
+  }
+}
+
 // ---------------------------------------------------------------------------
 // X pass helpers (lines along x are contiguous; nl lines per CTA).
 //
@@ -998,7 +1041,7 @@ __global__ void __launch_bounds__(EP_TX* EP_TY, sizeof(T) == 4 ? 4 : 2) k_predic
 // sum |pc|, sum |psi|^2 (new), <psi|H|psi> and sum |psi|^2 of the modified
 // psi (chemical potential).
 template <class T, int R>
-__global__ void __launch_bounds__(EP_TX* EP_TY, sizeof(T) == 4 ? 4 : 2) k_correct(Geo g, FdW<T> fd, Phys ph, int zc,
+__global__ void __launch_bounds__(EP_TX* EP_TY, sizeof(T) == 4 ? 3 : 2) k_correct(Geo g, FdW<T> fd, Phys ph, int zc,
                                                          const C2<T>* __restrict__ psi, const T* __restrict__ pot4,
                                                          const T* __restrict__ uimp,
                                                          const C2<T>* __restrict__ po3,
@@ -1030,8 +1073,7 @@ __global__ void __launch_bounds__(EP_TX* EP_TY, sizeof(T) == 4 ? 4 : 2) k_correc
     acc[2].add(hexp_t<T>(ph, c, H));
     acc[3].add(c.x * c.x + c.y * c.y);
   });
-  double v[4] = {acc[0].get(), acc[1].get(), acc[2].get(), acc[3].get()};
-  block_reduce_store<4>(v, partials);
+  block_reduce_store_acc<4>(acc, partials);
   // The last block to finish sums all partials (no block waits for another).
   __shared__ bool last;
   const int tid = threadIdx.x + blockDim.x * threadIdx.y;
