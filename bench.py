@@ -339,7 +339,7 @@ def run_ours(args):
     cpu = None
     if not args.no_cpu:
         try:
-            cpu = cpu_sample(psi, steps=2)
+            cpu = cpu_sample(psi, steps=40)
         except Exception as exc:
             cpu = {"value": None, "unit": UNIT, "cores": os.cpu_count(), "kind": "port", "sample": f"failed: {exc}"}
     n3 = N_GRID ** 3

@@ -85,26 +85,38 @@ EP_DEV T d1_line(const T* __restrict__ line, int i, int n, const T* w, int R, in
 // Solid penalty C*(1 + t + beta*den*(1 - t^2)), t = tanh(beta*(den - den_m))
 // (poten.f90:80-81).  The FP32 form is written without the cancellation of
 // 1 + tanh(x) for x << 0: 1 + t = 2/(1 + e^{-2x}), 1 - t^2 = 4e^{2x}/(1+e^{2x})^2.
-EP_DEV double penalty_of(const Phys& ph, double den) {
-  const double t = tanh(ph.beta * (den - ph.den_m));
-  return ph.C * (1.0 + t + ph.beta * den * (1.0 - t * t));
+// Penalty constants in the field precision, converted once per thread (a
+// double -> float conversion per point would run on the FP64 pipe).
+template <class T> struct Pen {
+  T C, beta, den_m;
+  EP_DEV explicit Pen(const Phys& ph) : C((T)ph.C), beta((T)ph.beta), den_m((T)ph.den_m) {}
+};
+EP_DEV double penalty_of(const Pen<double>& pn, double den) {
+  const double t = tanh(pn.beta * (den - pn.den_m));
+  return pn.C * (1.0 + t + pn.beta * den * (1.0 - t * t));
 }
-EP_DEV float penalty_of(const Phys& ph, float den) {
-  const float x = (float)ph.beta * (den - (float)ph.den_m);
+EP_DEV float penalty_of(const Pen<float>& pn, float den) {
+  const float x = pn.beta * (den - pn.den_m);
   const float e = __expf(2.0f * x);
   const float onept = 2.0f * e / (1.0f + e);
   const float omt2 = 4.0f * e / ((1.0f + e) * (1.0f + e));
-  return (float)ph.C * (onept + (float)ph.beta * den * omt2);
+  return pn.C * (onept + pn.beta * den * omt2);
 }
 
 // H-apply of steppc.f90:53 / steprk.f90:74-75:
 //   imaginary time: (lap*h2o2m4 - pot4*psi) - uimp*psi
 //   real time:      i*(lap*h2o2m4 - pot4*psi) - i*uimp*psi
+// hbar^2/2m_4 in the field precision and the time mode, built once per thread.
+template <class T> struct HCoef {
+  T h;
+  int real_time;
+  EP_DEV explicit HCoef(const Phys& ph) : h((T)ph.h2o2m4), real_time(ph.time_mode == 1) {}
+};
 template <class T>
-EP_DEV C2<T> happly(const Phys& ph, C2<T> lap, C2<T> psi, T pot4, T uimp) {
-  const T h = (T)ph.h2o2m4;
+EP_DEV C2<T> happly(const HCoef<T>& hc, C2<T> lap, C2<T> psi, T pot4, T uimp) {
+  const T h = hc.h;
   C2<T> L = cmk<T>(lap.x * h - pot4 * psi.x, lap.y * h - pot4 * psi.y);
-  if (ph.time_mode == 1) return cmk<T>(-L.y + uimp * psi.y, L.x - uimp * psi.x);
+  if (hc.real_time) return cmk<T>(-L.y + uimp * psi.y, L.x - uimp * psi.x);
   return cmk<T>(L.x - uimp * psi.x, L.y - uimp * psi.y);
 }
 
@@ -518,9 +530,10 @@ __global__ void k_x3(Geo g, Phys ph, const __grid_constant__ FdW<T> fd, const C2
   T* Rc = S.R;
   x_inverse<T, N2>(D0, line0, nlv, nl, nx, nxh, S, p2, rn, Rc);
   if (!otc) {
+    const Pen<T> pn(ph);
     for (int e = threadIdx.x; e < nlv * nx; e += blockDim.x) {
       const long long p = line0 * nx + e;
-      pot4[p] = (pot4[p] + Rc[e]) + penalty_of(ph, den[p]);
+      pot4[p] = (pot4[p] + Rc[e]) + penalty_of(pn, den[p]);
     }
     return;
   }
@@ -573,11 +586,12 @@ __global__ void k_x4(Geo g, Phys ph, const C2<T>* __restrict__ F0, const T* __re
   T* Ru = S.R;
   x_inverse<T, N2>(F0, line0, nlv, nl, nx, nxh, S, p2, (T)ph.renor, Ru);
   const T rden0s = (T)(1.0 / ph.den0s), h2 = (T)ph.h2o2m4, al = (T)ph.alphas;
+  const Pen<T> pn(ph);
   for (int e = threadIdx.x; e < nlv * nx; e += blockDim.x) {
     const long long p = line0 * nx + e;
     const T ua = ((Ru[e] * rden0s + dgx[p]) + dyz[p]) * h2 * al;
     ualphas[p] = ua;
-    pot4[p] = (pot4[p] + ua) + penalty_of(ph, den[p]);
+    pot4[p] = (pot4[p] + ua) + penalty_of(pn, den[p]);
   }
 }
 
@@ -1011,6 +1025,7 @@ __global__ void __launch_bounds__(EP_TX* EP_TY, sizeof(T) == 4 ? 4 : 2) k_predic
                                                          Slots sl) {
   extern __shared__ __align__(16) unsigned char smraw[];
   constexpr int NT = EP_TX * EP_TY;
+  const HCoef<T> hc(ph);
   const T s3 = (T)sc->bscale[sl.a], s1 = (T)sc->bscale[sl.h1], s2 = (T)sc->bscale[sl.h2],
           sp_ = (T)sc->bscale[sl.pc];
   const C2<T>* cin[4] = {po3, h1, h2, pc};
@@ -1018,7 +1033,7 @@ __global__ void __launch_bounds__(EP_TX* EP_TY, sizeof(T) == 4 ? 4 : 2) k_predic
   lap_march_async<T, R, 4, 2>(
       g, psi, fd, zc, smraw, cin, rin, (T)sc->bscale[sl.psi],
       [&](long long p, C2<T> c, C2<T> lap, const C2<T>* ic, const T* ir) {
-        const C2<T> H = happly<T>(ph, lap, c, ir[0], ir[NT]);
+        const C2<T> H = happly<T>(hc, lap, c, ir[0], ir[NT]);
         const C2<T> pp = s3 * ic[0] + f * ((T(2) * H - s1 * ic[NT]) + T(2) * (s2 * ic[2 * NT]));
         const C2<T> pn = pp - c112 * (sp_ * ic[3 * NT]);
         po3[p] = pn;
@@ -1053,6 +1068,7 @@ __global__ void __launch_bounds__(EP_TX* EP_TY, sizeof(T) == 4 ? 3 : 2) k_correc
                                                          double n4, Slots sl) {
   extern __shared__ __align__(16) unsigned char smraw[];
   constexpr int NT = EP_TX * EP_TY;
+  const HCoef<T> hc(ph);
   Acc<T> acc[4];
   const T s3 = (T)sc->bscale[sl.a], s2o = (T)sc->bscale[sl.b], s1 = (T)sc->bscale[sl.h1],
           s2 = (T)sc->bscale[sl.h2], sp_ = (T)sc->bscale[sl.pc];
@@ -1060,7 +1076,7 @@ __global__ void __launch_bounds__(EP_TX* EP_TY, sizeof(T) == 4 ? 3 : 2) k_correc
   const T* rin[2] = {pot4, uimp};
   lap_march_async<T, R, 5, 2>(g, psi, fd, zc, smraw, cin, rin, (T)sc->bscale[sl.psi],
                               [&](long long p, C2<T> c, C2<T> lap, const C2<T>* ic, const T* ir) {
-    const C2<T> H = happly<T>(ph, lap, c, ir[0], ir[NT]);
+    const C2<T> H = happly<T>(hc, lap, c, ir[0], ir[NT]);
     const C2<T> p5 = T(0.125) * ((T(9) * (s3 * ic[0]) - s2o * ic[NT]) + f3 * ((H + T(2) * (s1 * ic[2 * NT])) - s2 * ic[3 * NT]));
     const C2<T> pcn = sp_ * ic[4 * NT] - p5;
     pc[p] = pcn;
@@ -1110,9 +1126,10 @@ __global__ void __launch_bounds__(EP_TX* EP_TY, sizeof(T) == 4 ? 4 : 2) k_rkstag
                                                          T* __restrict__ den, T a, T b, T cr, T dt,
                                                          DevScalars* sc) {
   __shared__ C2<T> sp[(EP_TX + 2 * R) * (EP_TY + 2 * R)];
+  const HCoef<T> hc(ph);
   bool bad = false;
   lap_march<T, R>(g, psi, fd, zc, sp, [&](long long p, C2<T> c, C2<T> lap) {
-    const C2<T> H = happly<T>(ph, lap, c, pot4[p], uimp[p]);
+    const C2<T> H = happly<T>(hc, lap, c, pot4[p], uimp[p]);
     const C2<T> qq = q[p];
     const C2<T> aux2 = a * (H - b * qq);
     q[p] = (qq + T(3) * aux2) - cr * H;
