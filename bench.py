@@ -138,7 +138,9 @@ def prepare(s, psi, z):
 
 
 def time_single(precision, psi, steps, warmup, device, profile=False):
-    """One instance: device-timed steppc steps (+ per-kernel event times)."""
+    """One instance: device-timed steppc steps (replayed from the step graph),
+    then, if asked, the same number of steps again with per-kernel events
+    (direct launches) for the per-kernel table."""
     import eff_pot_gb300 as ep
     s = ep.Solver(make_cfg(precision, device=device))
     prepare(s, psi, 0.0)
@@ -148,15 +150,17 @@ def time_single(precision, psi, steps, warmup, device, profile=False):
     s.run(warmup, DT)
     s.synchronize()
     l0 = s.kernel_launches()
-    if profile:
-        s.profile(True)
     s._f["event_record"](s._h, 0)
     s.run(steps, DT, wait=False)
     s._f["event_record"](s._h, 1)
     ms = C.c_double()
     s._f["event_elapsed"](s._h, 0, 1, C.byref(ms))
     launches = s.kernel_launches() - l0
-    prof = s.profile_read() if profile else {}
+    prof = {}
+    if profile:
+        s.profile(True)
+        s.run(steps, DT, wait=False)
+        prof = s.profile_read()
     s.close()
     return ms.value, launches, prof, tuned
 

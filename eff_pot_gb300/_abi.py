@@ -126,6 +126,8 @@ _product_only = {
     "get_launch_shapes": (_I, [_P, C.POINTER(_I)]),
     "set_launch_shapes": (_I, [_P, C.POINTER(_I)]),
     "batch_autotune": (_I, [_P]),
+    "set_step_graphs": (_I, [_P, _I]),
+    "batch_set_step_graphs": (_I, [_P, _I]),
 }
 
 # Every symbol include/eff_pot.h declares.

@@ -14,7 +14,31 @@
 #include "../../include/eff_pot.h"
 #include "ep_engine.h"
 
+// A captured steppc (one context, or one step of every context of a batch)
+// and, per context, its predictor / corrector nodes and the engine state the
+// capture depends on (which engine, its launch shapes).
+struct StepGraph {
+  cudaGraph_t graph = nullptr;  // kept alive: node updates name its nodes
+  cudaGraphExec_t exec = nullptr;
+  std::vector<std::pair<cudaGraphNode_t, cudaGraphNode_t>> nodes;
+  std::vector<const void*> engine;
+  std::vector<int> gen;
+  std::vector<long long> launches;  // kernels per replay, per context
+  void reset() {
+    if (exec) cudaGraphExecDestroy(exec);
+    if (graph) cudaGraphDestroy(graph);
+    exec = nullptr;
+    graph = nullptr;
+    nodes.clear();
+    engine.clear();
+    gen.clear();
+    launches.clear();
+  }
+};
+
 struct ep_ctx {
+  StepGraph graph;
+  bool use_graphs = true;
   ep_config cfg{};
   cudaStream_t st = nullptr;
   Prof prof;
@@ -27,6 +51,8 @@ struct ep_ctx {
 };
 
 struct ep_batch {
+  StepGraph graph;
+  bool use_graphs = true;
   std::vector<ep_ctx*> ctx;
   cudaStream_t st = nullptr;
   cudaEvent_t fork = nullptr;
@@ -69,6 +95,98 @@ int dispatch(ep_ctx* c, F f) {
   if (c->active == EP_FP64 && c->e64) return f(*c->e64);
   if (c->active == EP_FP32 && c->e32) return f(*c->e32);
   return fail(c, EP_ERR_STATE, "context has no engine");
+}
+
+// ---------------------------------------------------------------------------
+// Step graphs.  A steppc of a context with a fixed (or no) impurity launches
+// the same kernels every step; only the predictor and corrector see the
+// rotating history buffers.  One step (of one context, or of every context
+// of a batch on their forked streams) is captured once; later steps update
+// the two march nodes per context and launch the graph.
+const void* engine_of(ep_ctx* c) {
+  return c->active == EP_FP64 ? (const void*)c->e64 : (const void*)c->e32;
+}
+int gen_of(ep_ctx* c) {
+  return dispatch(c, [](auto& e) -> int { return e.shapes_gen; });
+}
+bool graph_eligible(ep_ctx* c) {
+  return c->use_graphs && dispatch(c, [](auto& e) -> int { return e.graph_ok() ? 1 : 0; }) == 1;
+}
+bool graph_valid(const StepGraph& G, const std::vector<ep_ctx*>& cs) {
+  if (!G.exec || G.engine.size() != cs.size()) return false;
+  for (size_t i = 0; i < cs.size(); ++i)
+    if (G.engine[i] != engine_of(cs[i]) || G.gen[i] != gen_of(cs[i])) return false;
+  return true;
+}
+
+// Every instance stream waits for the batch stream, then the batch stream
+// waits for every instance: batch events bracket all instances' work.
+void batch_fork(ep_batch* b) {
+  cudaEventRecord(b->fork, b->st);
+  for (ep_ctx* c : b->ctx) cudaStreamWaitEvent(c->st, b->fork, 0);
+}
+void batch_join(ep_batch* b) {
+  for (size_t i = 0; i < b->ctx.size(); ++i) {
+    cudaEventRecord(b->join[i], b->ctx[i]->st);
+    cudaStreamWaitEvent(b->st, b->join[i], 0);
+  }
+}
+
+// Capture one step of every context of cs into G on stream st (forked to the
+// contexts' streams when b is given) and run it.
+int capture_step(StepGraph& G, const std::vector<ep_ctx*>& cs, cudaStream_t st, ep_batch* b, double dt) {
+  G.reset();
+  const size_t n = cs.size();
+  G.nodes.assign(n, {nullptr, nullptr});
+  G.engine.assign(n, nullptr);
+  G.gen.assign(n, 0);
+  G.launches.assign(n, 0);
+  if (cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal) != cudaSuccess) return EP_ERR_CUDA;
+  if (b) batch_fork(b);
+  int r = EP_OK;
+  for (size_t i = 0; i < n && !r; ++i) {
+    ep_ctx* c = cs[i];
+    const long long l0 = c->prof.launches;
+    r = dispatch(c, [&](auto& e) -> int {
+      e.cap_nodes = &G.nodes[i];
+      const int q = e.steppc(dt, nullptr);
+      e.cap_nodes = nullptr;
+      return q;
+    });
+    G.launches[i] = c->prof.launches - l0;
+    G.engine[i] = engine_of(c);
+    G.gen[i] = gen_of(c);
+  }
+  if (b && !r) batch_join(b);
+  cudaGraph_t graph = nullptr;
+  const cudaError_t e = cudaStreamEndCapture(st, &graph);
+  if (r || e != cudaSuccess || !graph) {
+    if (graph) cudaGraphDestroy(graph);
+    G.reset();
+    cudaGetLastError();
+    return r ? r : EP_ERR_CUDA;
+  }
+  G.graph = graph;
+  const cudaError_t ei = cudaGraphInstantiate(&G.exec, graph, 0);
+  if (ei != cudaSuccess) {
+    G.exec = nullptr;
+    G.reset();
+    return EP_ERR_CUDA;
+  }
+  return cudaGraphLaunch(G.exec, st) == cudaSuccess ? EP_OK : EP_ERR_CUDA;
+}
+
+// One replayed step: the host half of every context's step, then the graph.
+int replay_step(StepGraph& G, const std::vector<ep_ctx*>& cs, cudaStream_t st, double dt) {
+  for (size_t i = 0; i < cs.size(); ++i) {
+    ep_ctx* c = cs[i];
+    const int r = dispatch(c, [&](auto& e) -> int {
+      return e.steppc_update(dt, G.exec, G.nodes[i].first, G.nodes[i].second);
+    });
+    if (r) return r;
+    c->prof.launches += G.launches[i];
+  }
+  return cudaGraphLaunch(G.exec, st) == cudaSuccess ? EP_OK : EP_ERR_CUDA;
 }
 
 }  // namespace
@@ -173,6 +291,7 @@ int ep_destroy(ep_ctx* c) {
   if (!c) return EP_ERR_INVALID_ARG;
   cudaSetDevice(c->cfg.device);
   if (c->st) cudaStreamSynchronize(c->st);
+  c->graph.reset();
   if (c->e64) { c->e64->release(); delete c->e64; }
   if (c->e32) { c->e32->release(); delete c->e32; }
   if (c->imp.d_potpi) cudaFree(c->imp.d_potpi);
@@ -320,9 +439,21 @@ int ep_steppc(ep_ctx* c, double dt, ep_step_errors* err) {
 int ep_run(ep_ctx* c, int nsteps, double dt, ep_run_stats* stats) {
   if (!c || nsteps < 0) return EP_ERR_INVALID_ARG;
   const bool renorm = c->cfg.time_mode == EP_IMAGINARY_TIME && c->cfg.renormalize;
+  int s0 = 0;
+  const int ng = nsteps - (stats ? 1 : 0);  // steps that need no host statistics
+  if (ng >= 2 && graph_eligible(c)) {
+    std::vector<ep_ctx*> one{c};
+    int r;
+    if (!graph_valid(c->graph, one)) {
+      if ((r = capture_step(c->graph, one, c->st, nullptr, dt))) return r;
+      s0 = 1;
+    }
+    for (; s0 < ng; ++s0)
+      if ((r = replay_step(c->graph, one, c->st, dt))) return r;
+  }
   return dispatch(c, [&](auto& e) -> int {
     ep_step_errors se{};
-    for (int s = 0; s < nsteps; ++s) {
+    for (int s = s0; s < nsteps; ++s) {
       const bool last = (s == nsteps - 1) && stats;
       int r = e.steppc(dt, last ? &se : nullptr);
       if (r) return r;
@@ -401,6 +532,8 @@ int ep_batch_create(const ep_config* cfgs, int n, ep_batch** out) {
 
 int ep_batch_destroy(ep_batch* b) {
   if (!b) return EP_ERR_INVALID_ARG;
+  if (b->st) cudaStreamSynchronize(b->st);
+  b->graph.reset();
   for (ep_ctx* c : b->ctx) ep_destroy(c);
   cudaSetDevice(b->device);
   for (cudaEvent_t e : b->join) if (e) cudaEventDestroy(e);
@@ -418,27 +551,25 @@ ep_ctx* ep_batch_ctx(ep_batch* b, int i) {
   return b->ctx[i];
 }
 
-namespace {
-// Every instance stream waits for the batch stream, then the batch stream
-// waits for every instance: batch events bracket all instances' work.
-void batch_fork(ep_batch* b) {
-  cudaEventRecord(b->fork, b->st);
-  for (ep_ctx* c : b->ctx) cudaStreamWaitEvent(c->st, b->fork, 0);
-}
-void batch_join(ep_batch* b) {
-  for (size_t i = 0; i < b->ctx.size(); ++i) {
-    cudaEventRecord(b->join[i], b->ctx[i]->st);
-    cudaStreamWaitEvent(b->st, b->join[i], 0);
-  }
-}
-}  // namespace
-
 int ep_batch_run(ep_batch* b, int nsteps, double dt, ep_run_stats* stats) {
   if (!b || nsteps < 0) return EP_ERR_INVALID_ARG;
   cudaSetDevice(b->device);
+  int s0 = 0;
+  const int ng = nsteps - (stats ? 1 : 0);
+  bool eligible = b->use_graphs && ng >= 2;
+  for (ep_ctx* c : b->ctx) eligible = eligible && graph_eligible(c);
+  if (eligible) {
+    int r;
+    if (!graph_valid(b->graph, b->ctx)) {
+      if ((r = capture_step(b->graph, b->ctx, b->st, b, dt))) return r;
+      s0 = 1;
+    }
+    for (; s0 < ng; ++s0)
+      if ((r = replay_step(b->graph, b->ctx, b->st, dt))) return r;
+  }
   batch_fork(b);
   // step-major interleaving so the instances' kernels overlap
-  for (int s = 0; s < nsteps; ++s) {
+  for (int s = s0; s < nsteps; ++s) {
     const bool last = (s == nsteps - 1) && stats;
     for (size_t i = 0; i < b->ctx.size(); ++i) {
       ep_ctx* c = b->ctx[i];
@@ -559,8 +690,8 @@ int ep_set_launch_shapes(ep_ctx* c, const int* s) {
   if (!c || !s || !shapes_ok(s)) return EP_ERR_INVALID_ARG;
   Shapes sh;
   sh.xnl = s[0]; sh.xthr = s[1]; sh.ylt = s[2]; sh.ythr = s[3]; sh.zlt = s[4]; sh.zthr = s[5];
-  if (c->active == EP_FP64 && c->e64) c->e64->shp = sh;
-  else if (c->e32) c->e32->shp = sh;
+  if (c->active == EP_FP64 && c->e64) { c->e64->shp = sh; ++c->e64->shapes_gen; }
+  else if (c->e32) { c->e32->shp = sh; ++c->e32->shapes_gen; }
   else return EP_ERR_STATE;
   return EP_OK;
 }
@@ -611,6 +742,19 @@ int ep_event_elapsed(ep_ctx* c, int a, int b, double* ms) {
 }
 
 long long ep_kernel_launches(const ep_ctx* c) { return c ? c->prof.launches : 0; }
+
+int ep_set_step_graphs(ep_ctx* c, int on) {
+  if (!c) return EP_ERR_INVALID_ARG;
+  c->use_graphs = on != 0;
+  return EP_OK;
+}
+
+int ep_batch_set_step_graphs(ep_batch* b, int on) {
+  if (!b) return EP_ERR_INVALID_ARG;
+  b->use_graphs = on != 0;
+  for (ep_ctx* c : b->ctx) c->use_graphs = on != 0;
+  return EP_OK;
+}
 
 int ep_profile_enable(ep_ctx* c, int on) {
   if (!c) return EP_ERR_INVALID_ARG;

@@ -4,6 +4,7 @@
 
 #include <complex>
 #include <string>
+#include <utility>
 #include <vector>
 
 #include "../../include/eff_pot.h"
@@ -71,6 +72,16 @@ class Engine {
   int zc_pc = 16, zc_rk = 16, zc_d1 = 16;  // z planes per CTA of the stencil marches
   T* dyz = nullptr;                         // dy(gy) + dz(gz) of term_alfa
   int d1march(int mode, const T* f, const T* f2, T* o0, T* o1, T* o2);
+  // Step graphs (CUDA-graph replay of steppc): while capturing, cap_nodes
+  // receives the predictor / corrector nodes; while replaying, upd_exec is the
+  // executable graph whose nodes lap_predict / lap_correct update.
+  std::pair<cudaGraphNode_t, cudaGraphNode_t>* cap_nodes = nullptr;
+  cudaGraphExec_t upd_exec = nullptr;
+  cudaGraphNode_t upd_pred = nullptr, upd_corr = nullptr;
+  int shapes_gen = 0;  // bumped whenever launch shapes change (invalidates graphs)
+  int launch_march(const void* fn, dim3 grid, dim3 blk, size_t smem, void** args, const char* name, int which);
+  int steppc_update(double dt, cudaGraphExec_t x, cudaGraphNode_t np, cudaGraphNode_t nc);
+  bool graph_ok() const { return cfg.impurity != EP_IMPURITY_MOVING && !prof->on; }
   int march_zchunk(int blocks_per_sm) const;
   long long bytes = 0;
   Phys phys{};

@@ -617,6 +617,44 @@ int Engine<T>::refresh() {
   return EP_OK;
 }
 
+// Launch of a stencil-march kernel, or -- while a step graph is replayed --
+// an update of its captured node (which = 0 predictor, 1 corrector).  While
+// a step is captured the node just recorded is remembered for the updates.
+template <class T>
+int Engine<T>::launch_march(const void* fn, dim3 grid, dim3 blk, size_t smem, void** args, const char* name,
+                            int which) {
+  if (upd_exec) {
+    cudaKernelNodeParams p{};
+    p.func = const_cast<void*>(fn);
+    p.gridDim = grid;
+    p.blockDim = blk;
+    p.sharedMemBytes = (unsigned)smem;
+    p.kernelParams = args;
+    p.extra = nullptr;
+    return cuda_ok(cudaGraphExecKernelNodeSetParams(upd_exec, which == 0 ? upd_pred : upd_corr, &p), name);
+  }
+  cudaEvent_t a = nullptr;
+  int c = -1;
+  prof->begin(st, name, a, c);
+  cudaError_t e = cudaLaunchKernel(fn, grid, blk, args, smem, st);
+  prof->end(st, c, a);
+  if (e == cudaSuccess) e = cudaGetLastError();
+  if (e != cudaSuccess) return cuda_ok(e, name);
+  if (cap_nodes) {
+    cudaStreamCaptureStatus cs;
+    const cudaGraphNode_t* deps = nullptr;
+    size_t nd = 0;
+    e = cudaStreamGetCaptureInfo(st, &cs, nullptr, nullptr, &deps, nullptr, &nd);
+    if (e != cudaSuccess) return cuda_ok(e, name);
+    if (cs != cudaStreamCaptureStatusActive || nd != 1) {
+      *err = "step capture: unexpected dependency set";
+      return EP_ERR_CUDA;
+    }
+    (which == 0 ? cap_nodes->first : cap_nodes->second) = deps[0];
+  }
+  return EP_OK;
+}
+
 template <class T>
 int Engine<T>::lap_predict(double dt) {
   const double c112 = 112.0 / 121.0, c4o3 = 4.0 / 3.0;
@@ -625,19 +663,23 @@ int Engine<T>::lap_predict(double dt) {
   CT* h2 = ph[ioldh[1]];
   dim3 grid((g.nx + EP_TX - 1) / EP_TX, (g.ny + EP_TY - 1) / EP_TY, (g.nz + zc_pc - 1) / zc_pc);
   dim3 blk(EP_TX, EP_TY);
-  const T f = (T)(c4o3 * dt), c1 = (T)c112;
-  const Slots sl{slot_of(psi), slot_of(po3), -1, slot_of(h1), slot_of(h2), slot_of(pc), -1};
-#define EP_PRED(RR)                                                                                          \
-  case RR: {                                                                                                 \
-    auto k = k_predict<T, RR>;                                                                               \
-    EP_LAUNCH("predict", k, grid, blk, (march_smem<T, RR, 4, 2>()), g, fd, phys, zc_pc, psi, pot4, uimp, po3, h1, h2, pc, den, f, c1,  \
-              sc, sl);                                                                                       \
-  } break;
+  T f = (T)(c4o3 * dt), c1 = (T)c112;
+  Slots sl{slot_of(psi), slot_of(po3), -1, slot_of(h1), slot_of(h2), slot_of(pc), -1};
+  const CT* psic = psi;
+  const T *pot4c = pot4, *uimpc = uimp;
+  int zc = zc_pc;
+  void* args[] = {&g, &fd, &phys, &zc, &psic, &pot4c, &uimpc, &po3, &h1, &h2, &pc, &den, &f, &c1, &sc, &sl};
+  const void* fn = nullptr;
+  size_t smem = 0;
+#define EP_PRED(RR) \
+  case RR: fn = (const void*)k_predict<T, RR>; smem = march_smem<T, RR, 4, 2>(); break;
   switch (fd.R) {
     EP_PRED(1) EP_PRED(2) EP_PRED(3) EP_PRED(4) EP_PRED(5) EP_PRED(6)
     default: *err = "npd > 13 not built"; return EP_ERR_UNSUPPORTED;
   }
 #undef EP_PRED
+  int r;
+  if ((r = launch_march(fn, grid, blk, smem, args, "predict", 0))) return r;
   std::swap(psi, po[ioldp[2]]);
   std::swap(ioldh[0], ioldh[1]);
   return EP_OK;
@@ -653,20 +695,26 @@ int Engine<T>::lap_correct(double dt, bool want) {
   const CT* h2 = ph[ioldh[1]];
   dim3 grid((g.nx + EP_TX - 1) / EP_TX, (g.ny + EP_TY - 1) / EP_TY, (g.nz + zc_pc - 1) / zc_pc);
   dim3 blk(EP_TX, EP_TY);
-  const T f3 = (T)(3.0 * dt), cc = (T)c9;
-  const int renorm = (cfg.time_mode == EP_IMAGINARY_TIME && cfg.renormalize) ? 1 : 0;
-  const Slots sl{slot_of(psi), slot_of(po3), slot_of(po2), slot_of(h1), slot_of(h2), slot_of(pc), slot_of(spare)};
-#define EP_CORR(RR)                                                                                           \
-  case RR: {                                                                                                  \
-    auto k = k_correct<T, RR>;                                                                                \
-    EP_LAUNCH("correct", k, grid, blk, (march_smem<T, RR, 5, 2>()), g, fd, phys, zc_pc, psi, pot4, uimp, po3, po2, h1, h2, pc, spare, den, \
-              f3, cc, partials, sc, renorm, cfg.n4, sl);                                                      \
-  } break;
+  T f3 = (T)(3.0 * dt), cc = (T)c9;
+  int renorm = (cfg.time_mode == EP_IMAGINARY_TIME && cfg.renormalize) ? 1 : 0;
+  Slots sl{slot_of(psi), slot_of(po3), slot_of(po2), slot_of(h1), slot_of(h2), slot_of(pc), slot_of(spare)};
+  const CT* psic = psi;
+  const T *pot4c = pot4, *uimpc = uimp;
+  int zc = zc_pc;
+  double n4 = cfg.n4;
+  void* args[] = {&g,  &fd,  &phys, &zc,  &psic, &pot4c, &uimpc,   &po3, &po2, &h1, &h2,
+                  &pc, &spare, &den, &f3, &cc,   &partials, &sc,   &renorm, &n4, &sl};
+  const void* fn = nullptr;
+  size_t smem = 0;
+#define EP_CORR(RR) \
+  case RR: fn = (const void*)k_correct<T, RR>; smem = march_smem<T, RR, 5, 2>(); break;
   switch (fd.R) {
     EP_CORR(1) EP_CORR(2) EP_CORR(3) EP_CORR(4) EP_CORR(5) EP_CORR(6)
     default: *err = "npd > 13 not built"; return EP_ERR_UNSUPPORTED;
   }
 #undef EP_CORR
+  int r;
+  if ((r = launch_march(fn, grid, blk, smem, args, "correct", 1))) return r;
   std::swap(psi, spare);
   const int t = ioldp[2];
   ioldp[2] = ioldp[1];
@@ -674,6 +722,21 @@ int Engine<T>::lap_correct(double dt, bool want) {
   ioldp[0] = t;
   if (renorm) lazy = true;
   return EP_OK;
+}
+
+// Host half of one steppc replayed from a step graph (fixed or no impurity):
+// the buffer rotation of lap_predict/lap_correct, with the predictor and
+// corrector nodes of graph x updated to this step's buffers.  poten() is in
+// the graph with fixed buffers.
+template <class T>
+int Engine<T>::steppc_update(double dt, cudaGraphExec_t x, cudaGraphNode_t np, cudaGraphNode_t nc) {
+  upd_exec = x;
+  upd_pred = np;
+  upd_corr = nc;
+  int r = lap_predict(dt);
+  if (!r) r = lap_correct(dt, false);
+  upd_exec = nullptr;
+  return r;
 }
 
 template <class T>
@@ -1089,6 +1152,7 @@ int Engine<T>::autotune(std::string* report) {
     }
   }
 done:
+  ++shapes_gen;  // captured step graphs used the old shapes
   cudaEventDestroy(a);
   cudaEventDestroy(b);
   return r;

@@ -162,12 +162,11 @@ EP_DEV void neu_add_d(double& s, double& c, double v) {
 // renormalisation factor), mode 2: norm only.
 EP_DEV void finalize_block(const double* partials, int nblocks, int nq, DevScalars* sc, int out0, int mode,
                            double N, double dxyz, double n4, int renorm) {
-  __shared__ double ss[256], cs[256];
+  __shared__ double ss[256];
   const int tid = threadIdx.x + blockDim.x * threadIdx.y;
   const int nth = blockDim.x * blockDim.y;
   // partials are already FP64 block sums: a fixed-order pairwise tree keeps
   // the relative error near log2(nblocks) ulp with few FP64 operations
-  (void)cs;
   for (int q = 0; q < nq; ++q) {
     double s = 0.0;
     for (int b = tid; b < nblocks; b += nth) s += __ldcg(partials + (long long)b * nq + q);

@@ -272,6 +272,11 @@ class Solver:
     def profile(self, on=True):
         self._check(self._f["profile_enable"](self._h, 1 if on else 0), "profile_enable")
 
+    def step_graphs(self, on=True):
+        """Replay run() steps from a captured CUDA graph (default) or launch
+        every kernel directly."""
+        self._check(self._f["set_step_graphs"](self._h, 1 if on else 0), "set_step_graphs")
+
     def profile_read(self):
         cap, maxn = 4096, 64
         names = C.create_string_buffer(cap)
@@ -352,6 +357,9 @@ class Batch:
 
     def kernel_launches(self):
         return int(self._f["batch_kernel_launches"](self._h))
+
+    def step_graphs(self, on=True):
+        self._check(self._f["batch_set_step_graphs"](self._h, 1 if on else 0), "batch_set_step_graphs")
 
     def close(self):
         if getattr(self, "_h", None):

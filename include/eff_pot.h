@@ -229,8 +229,17 @@ void* ep_stream(ep_ctx* ctx);
  * 16 slots; elapsed ms between two recorded slots (waits for the second). */
 int ep_event_record(ep_ctx* ctx, int slot);
 int ep_event_elapsed(ep_ctx* ctx, int slot_a, int slot_b, double* ms);
-/* Kernel launches made by this context since creation. */
+/* Kernel launches made by this context since creation (kernels replayed
+ * from step graphs included). */
 long long ep_kernel_launches(const ep_ctx* ctx);
+/* Step graphs (default on): ep_run / ep_batch_run capture one steppc of a
+ * context (or of every context of a batch) with a fixed or no impurity into
+ * a CUDA graph once and replay it, updating only the predictor / corrector
+ * nodes to the rotated history buffers.  Results are bit-identical to direct
+ * launches.  No reference counterpart (the reference loop calls steppc per
+ * step, DFT4He3d.f90). */
+int ep_set_step_graphs(ep_ctx* ctx, int on);
+int ep_batch_set_step_graphs(ep_batch* b, int on);
 /* Per-kernel-class event timing of every launch made while enabled. */
 int ep_profile_enable(ep_ctx* ctx, int on);
 /* Fills names (NUL-separated, cap bytes), per-class total ms and launch

@@ -136,3 +136,52 @@ def test_autotune_keeps_results_bit_identical(prec):
         for f in before:
             assert np.array_equal(before[f], s.field(f)), f
             assert np.array_equal(before[f], odd[f]), f
+
+
+@pytest.mark.parametrize("prec", [_abi.EP_FP64, _abi.EP_FP32])
+def test_step_graphs_match_direct_launches(prec):
+    """run() replays a captured step graph (only the predictor / corrector
+    nodes are updated to the rotated history buffers): same bits, same kernel
+    count as launching every kernel, also after the launch shapes change."""
+    cfg = cfg_of(n=32, xmax=16.0, precision=prec)
+    psi = ep.woods_saxon_psi(32, 32, 32, 16.0, 16.0, 16.0, 200.0, seed=3)
+    out = []
+    for graphs in (False, True):
+        with ep.Solver(cfg) as s:
+            s.step_graphs(graphs)
+            prepare(s, psi, (0.0, 0.0, 0.5))
+            for _ in range(3):
+                s.steprk(5e-4)
+            st1 = s.run(7, 5e-4)
+            s.set_launch_shapes([2, 64, 4, 64, 4, 64])
+            st2 = s.run(9, 5e-4)
+            s.run(4, 5e-4)
+            out.append((s.psi(), st1, st2, s.kernel_launches()))
+    assert np.array_equal(out[0][0], out[1][0])
+    assert out[0][1] == out[1][1] and out[0][2] == out[1][2]
+    assert out[0][3] == out[1][3]
+
+
+def test_batch_step_graphs_match_direct_launches():
+    grids = [32, 24, 32]
+    cfgs = [cfg_of(n=n, xmax=0.5 * n, precision=_abi.EP_FP32) for n in grids]
+    psis = [ep.woods_saxon_psi(c.nx, c.ny, c.nz, c.xmax, c.ymax, c.zmax, c.n4, seed=10 + i)
+            for i, c in enumerate(cfgs)]
+    res = []
+    for graphs in (False, True):
+        with ep.Batch(cfgs) as b:
+            b.step_graphs(graphs)
+            for s, psi, z in zip(b, psis, (0.0, 0.7, 1.4)):
+                prepare(s, psi, (0.0, 0.0, z))
+            for _ in range(3):
+                b.steprk(5e-4)
+            b.run(8, 5e-4)
+            b.set_precision("fp64")
+            b.run(5, 5e-4)
+            b.set_precision("fp32")
+            stats = b.run(6, 5e-4)
+            res.append(([s.psi() for s in b], stats, b.kernel_launches()))
+    for a, c in zip(res[0][0], res[1][0]):
+        assert np.array_equal(a, c)
+    assert res[0][1] == res[1][1]
+    assert res[0][2] == res[1][2]
