@@ -226,6 +226,20 @@ def cpu_sample(psi, steps=2):
                       f"C++ FP64 oracle, {threads} OpenMP threads"}
 
 
+def fp64_flop_roofline(steps_per_s):
+    """The FP64 path is bound by the FP64 pipe, not HBM: algorithmic FLOP/s of
+    the plain FP64 single instance against the measured FMA peak."""
+    from eff_pot_gb300.roofline import step_flops
+    achieved = step_flops(N_GRID, N_GRID, N_GRID, otc=True) * steps_per_s / 1e12
+    try:
+        peak = float(json.load(open(os.path.join(ROOT, "profiles", "fma_peaks.json")))["fp64_tflops"])
+        src = "profiles/fma_peaks.json (measured: python -m eff_pot_gb300.peaks)"
+    except Exception:
+        peak, src = 1.196, "earlier measurement on this pool"
+    return {"bound": "fp64 alu", "achieved": achieved, "peak": peak, "unit": "TFLOP/s", "frac": achieved / peak,
+            "peak_source": src}
+
+
 def run_ours(args):
     rank, world, local = dist_env()
     dist = dist_init(world)
@@ -360,6 +374,7 @@ def run_ours(args):
         "fp32_single_steps_per_s": K / (ms32 / 1e3),
         "speedup_vs_fp64_single": value / (world * K / (ms64 / 1e3)),
         "hbm_gbs_batch": batch_bytes / (ms_b / 1e3) / 1e9,
+        "fp64_flop_roofline": fp64_flop_roofline(K / (ms64 / 1e3)),
         "roofline": {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": achieved / peak, "traffic": traffic,
                      "measured_on": "single FP32 instance, kernels timed alone (burst peak)",

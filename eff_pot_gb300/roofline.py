@@ -62,3 +62,30 @@ def step_bytes(nx, ny, nz, otc=True, grad=True, s=8, renorm=True):
 
 def total_step_bytes(*a, **k):
     return sum(step_bytes(*a, **k).values())
+
+
+def step_flops(nx, ny, nz, otc=True):
+    """Algorithmic floating-point operations of one predictor-corrector step
+    (FMA = 2), the count behind the FP64 ALU roofline:
+
+    * real 3-D FFTs, 2.5 N log2 N each: 14 per OTC step (den forward; three
+      convolution inverses; four forward, four inverse for the second-stage
+      products; one forward, one inverse for div(f I)), 5 for OT;
+    * two complex 13-point Laplacians (predictor, corrector): 3 axes x 13
+      points of a real weight times a complex value, accumulated: 156 flop;
+    * first-derivative stencils: grad den (3), d/dy and d/dz of f I (2) and
+      the x-derivative of f I_x (1), 6 differences + 6 multiply-adds each =
+      18 flop;
+    * the k-space products (2 flop per half-spectrum point per table) and the
+      point-wise algebra of the step (about 100 flop per point).
+    """
+    import math
+    N = nx * ny * nz
+    Nh = (nx // 2 + 1) * ny * nz
+    nfft = 14 if otc else 5
+    f = nfft * 2.5 * N * math.log2(N)
+    f += 2 * 156 * N
+    f += (6 if otc else 3) * 18 * N
+    f += (8 if otc else 3) * 2 * Nh
+    f += 100 * N
+    return f
