@@ -10,6 +10,8 @@ ROOT = os.path.dirname(HERE)
 CSRC = os.path.join(HERE, "csrc")
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(BUILD, "libeffpot.so")
+DRIVER = os.path.join(BUILD, "ep_dft4he3d")
+DRIVER_SRC = ["ep_fortran_io.cpp", "ep_dft4he3d.cpp"]
 UNITS = ["ep_engine_fp64.cu", "ep_engine_fp32.cu", "ep_common.cu", "ep_api.cu", "ep_noalloc.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-Xcompiler", "-O2",
@@ -66,7 +68,25 @@ def build(verbose=False, force=False, extra=()):
         if r.returncode:
             sys.stderr.write(r.stdout + r.stderr)
             raise RuntimeError("link of libeffpot.so failed")
+    build_driver(force=force or bool(jobs))
     return LIB
+
+
+def build_driver(force=False):
+    """The DFT4He3d driver: host C++ over the C ABI, linked to libeffpot.so."""
+    ddir = os.path.join(CSRC, "driver")
+    srcs = [os.path.join(ddir, f) for f in DRIVER_SRC]
+    deps = srcs + [os.path.join(ddir, "ep_fortran_io.h"), os.path.join(ROOT, "include", "eff_pot.h"), LIB]
+    if not (force or _stale(deps, DRIVER)):
+        return DRIVER
+    cxx = shutil.which("g++") or "c++"
+    cmd = [cxx, "-O2", "-std=c++17", "-Wall", "-I" + os.path.join(ROOT, "include"), *srcs, "-o", DRIVER,
+           "-L" + BUILD, "-leffpot", "-Wl,-rpath,$ORIGIN", "-Wl,-rpath," + cuda_lib(nvcc())]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode:
+        sys.stderr.write(" ".join(cmd) + "\n" + r.stdout + r.stderr)
+        raise RuntimeError("build of the ep_dft4he3d driver failed")
+    return DRIVER
 
 
 if __name__ == "__main__":

@@ -410,10 +410,17 @@ int ep_energy(ep_ctx* c, ep_energies* out) {
 }
 int ep_forceimp(ep_ctx* c, double* F) {
   if (!F) return EP_ERR_INVALID_ARG;
-  return dispatch(c, [&](auto& e) -> int {
-    int r = e.ensure_materialized();
-    return r ? r : e.forceimp(F);
+  const int r = dispatch(c, [&](auto& e) -> int {
+    int q = e.ensure_materialized();
+    return q ? q : e.forceimp(F);
   });
+  // every reference call site follows forceimp with aimp = F / mAg_u
+  // (DFT4He3d.f90:454-455, steppc.f90:114-115, steprk.f90:169-170)
+  if (!r && c->cfg.impurity == EP_IMPURITY_MOVING) {
+    const double m = c->cfg.mimpur * 0.0207569277;
+    for (int i = 0; i < 3; ++i) c->imp.aimp[i] = F[i] / m;
+  }
+  return r;
 }
 int ep_potinvar(ep_ctx* c, double* hinvar) {
   if (!hinvar) return EP_ERR_INVALID_ARG;

@@ -162,7 +162,9 @@ int ep_potenimp(ep_ctx* ctx);
 int ep_poten(ep_ctx* ctx);
 /* energy() (energy.f90:12-202), eHeX/uplus accumulators zeroed. */
 int ep_energy(ep_ctx* ctx, ep_energies* e);
-/* forceimp(rimp,F) (potenimp.f90:193-258). */
+/* forceimp(rimp,F) (potenimp.f90:193-258); for a moving impurity also
+ * stores aimp = F / mAg_u, as every reference call site does next
+ * (DFT4He3d.f90:454-455). */
 int ep_forceimp(ep_ctx* ctx, double* F);
 /* potinvar(rimp,invar,Hinvar), P state (potenimp.f90:261-492). */
 int ep_potinvar(ep_ctx* ctx, double* hinvar);

@@ -949,6 +949,9 @@ int oc_forceimp(oc_ctx* c, double* F) {
   F[0] = -par_sum(N, [&](size_t i) { return c->dxden[i] * c->uimp[i]; }) * c->dxyz;
   F[1] = -par_sum(N, [&](size_t i) { return c->dyden[i] * c->uimp[i]; }) * c->dxyz;
   F[2] = -par_sum(N, [&](size_t i) { return c->dzden[i] * c->uimp[i]; }) * c->dxyz;
+  // the callers' aimp = F / mAg_u (DFT4He3d.f90:454-455, steppc.f90:114-115)
+  if (c->cfg.impurity == EP_IMPURITY_MOVING)
+    for (int i = 0; i < 3; ++i) c->aimp[i] = F[i] / (c->cfg.mimpur * 0.0207569277);
   return EP_OK;
 }
 

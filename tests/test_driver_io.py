@@ -1,0 +1,156 @@
+"""The Fortran I/O of the DFT4He3d driver (namelist, list-directed text,
+unformatted records) and its input checks that stop before any GPU call.
+
+The I/O module is compiled here with a small harness; the driver itself is
+built by build() and run on inputs that it must reject the way the reference
+does (DFT4He3d.f90:176-196, readenc.f90:170-245).
+"""
+import os
+import struct
+import subprocess
+import textwrap
+
+import pytest
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+DRV = os.path.join(ROOT, "eff_pot_gb300", "csrc", "driver")
+
+HARNESS = r"""
+#include <cstdio>
+#include <fstream>
+#include <iostream>
+#include <sstream>
+#include "ep_fortran_io.h"
+int main(int argc, char** argv) {
+  std::string what = argv[1];
+  if (what == "nml") {
+    fio::Namelist n; std::string err;
+    std::ifstream f(argv[2]);
+    if (!fio::parse_namelist(f, "input", n, err)) { std::printf("ERR %s\n", err.c_str()); return 0; }
+    for (auto& k : n.order) {
+      std::printf("%s", k.c_str());
+      for (auto& v : n.vars[k]) std::printf("|%s", v.c_str());
+      std::printf("\n");
+    }
+    std::printf("real=%.17g int=%ld log=%d\n", fio::to_real(n.vars["a"][0]), fio::to_int(n.vars["n"][0]),
+                (int)fio::to_logical(n.vars["flag"][0]));
+  } else if (what == "list") {
+    std::ifstream f(argv[2]);
+    fio::ListReader r(f);
+    r.skip_comments('#');
+    double h[3]; long n; bool l; double c[6];
+    r.reals(h, 3); r.integer(n); r.logical(l); r.end_statement();
+    r.complexes(c, 3); r.end_statement();
+    double tail[4]; r.reals(tail, 4);
+    std::printf("%.17g %.17g %.17g %ld %d\n", h[0], h[1], h[2], n, (int)l);
+    for (double v : c) std::printf("%.17g ", v);
+    std::printf("\n");
+    for (double v : tail) std::printf("%.17g ", v);
+    std::printf("\n");
+  } else if (what == "rec") {
+    std::ofstream o(argv[2], std::ios::binary);
+    double v[3] = {1.5, -2.25, 3.0}; int k = 7;
+    fio::write_record(o, v, sizeof v); fio::write_record(o, &k, sizeof k);
+    o.close();
+    std::ifstream i(argv[2], std::ios::binary);
+    std::vector<char> a, b;
+    const int ra = fio::read_record(i, a);
+    const int rb = fio::read_record(i, b);
+    std::printf("%d %d %zu %zu\n", ra, rb, a.size(), b.size());
+  }
+  return 0;
+}
+"""
+
+
+@pytest.fixture(scope="module")
+def harness(tmp_path_factory):
+    d = tmp_path_factory.mktemp("fio")
+    src = d / "h.cpp"
+    src.write_text(HARNESS)
+    exe = d / "h"
+    subprocess.check_call(["g++", "-O1", "-std=c++17", "-I" + DRV, str(src), os.path.join(DRV, "ep_fortran_io.cpp"),
+                           "-o", str(exe)])
+    return str(exe)
+
+
+def run(exe, *a):
+    return subprocess.run([exe, *map(str, a)], check=True, capture_output=True, text=True).stdout
+
+
+def test_namelist_forms(harness, tmp_path):
+    f = tmp_path / "in.nml"
+    f.write_text(textwrap.dedent("""\
+        ! comment before the group
+        &INPUT  title='He droplet, ''test''' , N=300
+           a = 1.5d-3   flag = .True.   core4 = 'OTC'   ! trailing comment
+           xs = 3*2.0, 1.0E2  , vals=2*'ab'
+           z = (1.0, -2.0)
+        /
+        """))
+    out = run(harness, "nml", f).splitlines()
+    assert out[0] == "title|He droplet, 'test'"
+    assert out[1] == "n|300"
+    assert "core4|OTC" in out
+    assert "xs|2.0|2.0|2.0|1.0E2" in out
+    assert "vals|ab|ab" in out
+    assert "z|(1.0,-2.0)" in out
+    assert out[-1] == "real=0.0015 int=300 log=1"
+
+
+def test_namelist_end_forms_and_errors(harness, tmp_path):
+    f = tmp_path / "a.nml"
+    f.write_text("$input n = 2, a = 1, flag = F $end\n")
+    assert run(harness, "nml", f).splitlines()[-1] == "real=1 int=2 log=0"
+    f.write_text("&other x=1 /\n")
+    assert run(harness, "nml", f).startswith("ERR namelist group &input not found")
+    f.write_text("&input n = 2\n")
+    assert "not terminated" in run(harness, "nml", f)
+
+
+def test_list_directed_reader(harness, tmp_path):
+    f = tmp_path / "d.txt"
+    f.write_text("# header line\n#  another\n 25.6D0, 25.6 ,0.4 64 T extra values ignored\n"
+                 " (1.0,2.0) 2*( 3.5 ,\n -4.0 )\n 3*0.25 7.0\n")
+    out = run(harness, "list", f).splitlines()
+    assert out[0] == "25.600000000000001 25.600000000000001 0.40000000000000002 64 1"
+    assert out[1].split() == ["1", "2", "3.5", "-4", "3.5", "-4"]
+    assert out[2].split() == ["0.25", "0.25", "0.25", "7"]
+
+
+def test_unformatted_records(harness, tmp_path):
+    f = tmp_path / "r.bin"
+    assert run(harness, "rec", f).split() == ["1", "1", "24", "4"]
+    raw = f.read_bytes()
+    assert struct.unpack("<i", raw[:4])[0] == 24 and struct.unpack("<i", raw[28:32])[0] == 24
+    assert struct.unpack("<3d", raw[4:28]) == (1.5, -2.25, 3.0)
+
+
+@pytest.fixture(scope="module")
+def driver():
+    from eff_pot_gb300.build import build, DRIVER
+    build()
+    return DRIVER
+
+
+def drive(driver, cwd, text):
+    return subprocess.run([driver], input=text, cwd=cwd, capture_output=True, text=True, timeout=120)
+
+
+def test_driver_time_step_checks(driver, tmp_path):
+    r = drive(driver, tmp_path, "&input nx=32, ny=32, nz=32 /\n")
+    assert r.returncode == 1
+    assert "You must specify either Deltat (in kelvin) or Deltatps (in picosecond)" in r.stdout
+    echo = (tmp_path / "DFT4He3d.namelist.read").read_text()
+    assert "nx = 32" in echo and echo.startswith("&INPUT")
+    r = drive(driver, tmp_path, "&input deltat=1.d-4, deltatps=1.0 /\n")
+    assert r.returncode == 1 and "Inconsistent deltat - deltatps" in r.stdout
+
+
+def test_driver_rejects_unknown_core_and_bad_namelist(driver, tmp_path):
+    r = drive(driver, tmp_path, "&input deltat=1.d-4, core4='XYZ' /\n")
+    assert r.returncode == 1 and "I do not know how to work with the core: XYZ" in r.stdout
+    r = drive(driver, tmp_path, "&input deltat=1.d-4, nx = 'abc' /\n")
+    assert r.returncode == 1 and "Error in input master file" in r.stdout
+    r = drive(driver, tmp_path, "no namelist here\n")
+    assert r.returncode == 1 and "Error in input master file" in r.stdout

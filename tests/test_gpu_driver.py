@@ -1,0 +1,150 @@
+"""The DFT4He3d driver on the GPU: namelist + readenc files in, the reference's
+first energy balance out, equal to the same calls made through the Python
+host mirror; evolution writes a printoutc file that reads back in mode 2."""
+import os
+import re
+import subprocess
+
+import numpy as np
+import pytest
+
+import eff_pot_gb300 as ep
+from eff_pot_gb300 import _abi
+from eff_pot_gb300.build import build, DRIVER
+
+pytestmark = pytest.mark.gpu
+
+N, XMAX, N4, DT = 32, 16.0, 200.0, 2.5e-4
+
+
+@pytest.fixture(scope="module", autouse=True)
+def _lib():
+    build()
+    ep.load_library()
+
+
+def fmt(v):
+    return f"{v:.17E}"
+
+
+def write_density(path, den, rimp):
+    """readenc mode 0: comment lines, header (limp, impurity position), den."""
+    h = 2 * XMAX / N
+    flat = np.asarray(den).ravel(order="F")
+    with open(path, "w") as f:
+        f.write("#  Density written for a test\n#  second comment line\n")
+        f.write(" ".join(fmt(v) for v in (XMAX, XMAX, XMAX, h, h, h)) + f" {N} {N} {N} T "
+                + " ".join(fmt(v) for v in rimp) + "\n")
+        # a repeat count and both separators, as list-directed writers produce
+        f.write(f" 2*{fmt(flat[0])}," if flat[0] == flat[1] else f" {fmt(flat[0])}, {fmt(flat[1])}")
+        for i in range(2, flat.size):
+            f.write((" " if i % 4 else "\n ") + fmt(flat[i]))
+        f.write("\n")
+
+
+def write_wavefunction(path, psi, rimp, vimp, invar):
+    """readenc mode 2 (the printoutc layout)."""
+    h = 2 * XMAX / N
+    with open(path, "w") as f:
+        f.write("#  Density after 0 iterations.\n#  Backup copy.\n")
+        f.write(" ".join(fmt(v) for v in (XMAX, XMAX, XMAX, h, h, h)) + f" {N} {N} {N}\n")
+        f.write(" ".join(fmt(v) for v in rimp) + "\n" + " ".join(fmt(v) for v in vimp) + "\n 10\n")
+        f.write(" ".join(f"({fmt(z.real)},{fmt(z.imag)})" for z in invar) + "\n")
+        for i, z in enumerate(np.asarray(psi).ravel(order="F")):
+            f.write(f" ({fmt(z.real)},{fmt(z.imag)})" + ("\n" if i % 2 else ""))
+        f.write("\n")
+
+
+def namelist(mode, extra=""):
+    return (f"&input\n title='driver test', n4={int(N4)}, mode={mode},\n"
+            f" nx={N}, ny={N}, nz={N}, xmax={XMAX}, ymax={XMAX}, zmax={XMAX},\n"
+            " core4='OTC', npd=13, icon=8, deltat=2.5d-4, mimpur=40.d0, Lfix_lambda=.true.,\n"
+            " selec_pi='Morse', selec_sigma='Morse', selec_plus='null', umax_pi=1000.d0, umax_sigma=1000.d0,\n"
+            " r_cutoff_pi=0.d0, r_cutoff_sigma=0.d0, morse_de=10.d0, morse_re=4.5d0, morse_alpha=1.2d0,\n"
+            f" filedenin='in.dat', filedenout='out.dat' {extra}\n/\n")
+
+
+def run_driver(cwd, text):
+    r = subprocess.run([DRIVER], input=text, cwd=cwd, capture_output=True, text=True, timeout=300)
+    assert r.returncode == 0, r.stdout + r.stderr
+    return r.stdout
+
+
+LABELS = {"etot4": "TOTAL   energy (He)", "ekin4": "Kinetic energy (He)", "elj4": "Lennard-Jones energy (He)",
+          "ealphas": "Alpha_s term  energy (He)", "esolid": "Solid energy (He)", "ecor4": "Correlation energy   (He)",
+          "eHeX": "Interaction energy (X*-He)", "etot": "TOTAL ENERGY (He+X)"}
+
+
+def balance(out):
+    vals = {}
+    for k, lab in LABELS.items():
+        m = re.search(re.escape(lab) + r" +\.*: +(-?\d+\.\d+) K", out)
+        assert m, (k, out)
+        vals[k] = m.group(1)
+    return vals
+
+
+def solver(rimp, invar, vimp=(0.0, 0.0, 0.0)):
+    cfg = ep.make_config(nx=N, ny=N, nz=N, xmax=XMAX, ymax=XMAX, zmax=XMAX, icon=_abi.EP_ICON_PERIODIC, core="OTC",
+                         n4=N4, impurity=_abi.EP_IMPURITY_MOVING, mimpur=40.0, fix_lambda=1)
+    s = ep.Solver(cfg)
+    m = ep.morse(10.0, 4.5, 1.2, r_cutoff=0.0, umax=1000.0)
+    s.set_impurity_potentials(m, m, ep.null_potential())
+    s.set_impurity(rimp=rimp, vimp=vimp, invar=invar)
+    return s
+
+
+def test_first_energy_balance_mode0(tmp_path):
+    psi = ep.woods_saxon_psi(N, N, N, XMAX, XMAX, XMAX, N4, seed=3)
+    den = np.abs(psi) ** 2
+    rimp = (0.5, -0.25, 1.0)
+    write_density(tmp_path / "in.dat", den, rimp)
+    (tmp_path / "invar.dat").write_text("\n".join(["(0.d0,0.d0)"] * 10) + "\n")
+    got = balance(run_driver(tmp_path, namelist(0, ", instate=5")))
+    with solver(rimp, np.zeros(10, dtype=np.complex128)) as s:
+        s.upload_psi(np.sqrt(den).astype(np.complex128))
+        s.potenimp()
+        s.poten()
+        e = s.energy()
+    for k, v in got.items():
+        assert v == f"{e[k]:.6f}", (k, v, e[k])
+    # the namelist echo
+    assert "core4 = OTC" in (tmp_path / "DFT4He3d.namelist.read").read_text()
+
+
+def test_mode2_evolution_writes_a_file_that_reads_back(tmp_path):
+    psi = ep.woods_saxon_psi(N, N, N, XMAX, XMAX, XMAX, N4, seed=4)
+    rimp = (0.0, 0.0, 0.75)
+    invar = np.zeros(10, dtype=np.complex128)
+    write_wavefunction(tmp_path / "in.dat", psi, rimp, (0.0, 0.0, 0.0), invar)
+    out = run_driver(tmp_path, namelist(2, ", niter=10, pener=4"))
+    rows = [ln.split() for ln in out.splitlines() if re.match(r"^\s+\d+ +-?\d+\.\d+ +-?\d+\.\d+ ", ln)]
+    assert [int(r[0]) for r in rows] == [7, 10]
+    with solver(rimp, invar) as s:
+        s.upload_psi(psi)
+        s.potenimp()
+        s.poten()
+        s.energy()
+        s.forceimp()  # as the driver does after the first balance
+        for _ in range(3):
+            s.steprk(DT)
+        s.run(4, DT)
+        s.poten()  # the driver prints the energy after every pener steps
+        s.energy()
+        st = s.run(3, DT)
+        s.poten()
+        e = s.energy()
+        final = s.psi()
+        imp = s.impurity()
+    assert rows[-1][1] == f"{st['mu']:.10f}" and rows[-1][2] == f"{e['etot']:.10f}"
+    # the printoutc file of the run is a valid mode-2 input holding the final state
+    text = (tmp_path / "out.dat").read_text()
+    assert re.match(r"#  Density after +10 iterations\.\n#  Actual delatatps", text)
+    os.replace(tmp_path / "out.dat", tmp_path / "in.dat")
+    got = balance(run_driver(tmp_path, namelist(2)))
+    with solver(tuple(imp["rimp"]), imp["invar"], tuple(imp["vimp"])) as s:
+        s.upload_psi(final)
+        s.potenimp()
+        s.poten()
+        e2 = s.energy()
+    assert got["etot"] == f"{e2['etot']:.6f}"
