@@ -81,7 +81,7 @@ def build_driver(force=False):
         return DRIVER
     cxx = shutil.which("g++") or "c++"
     cmd = [cxx, "-O2", "-std=c++17", "-Wall", "-I" + os.path.join(ROOT, "include"), *srcs, "-o", DRIVER,
-           "-L" + BUILD, "-leffpot", "-Wl,-rpath,$ORIGIN", "-Wl,-rpath," + cuda_lib(nvcc())]
+           "-pthread", "-L" + BUILD, "-leffpot", "-Wl,-rpath,$ORIGIN", "-Wl,-rpath," + cuda_lib(nvcc())]
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode:
         sys.stderr.write(" ".join(cmd) + "\n" + r.stdout + r.stderr)

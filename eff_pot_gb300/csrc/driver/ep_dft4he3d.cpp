@@ -16,6 +16,12 @@
 // morse_re, morse_alpha (selec_* = 'Morse'), precision ('fp64' | 'fp32'),
 // refine (final FP64 steps of an FP32 run), timemode, iprint.
 //
+// `ep_dft4he3d --scan file...` (namelist on standard input) is the U*/U+
+// post-processing scan of loop.sh / get_impurity_energy.sh as one job: the
+// first energy balance of every saved wave function, printed as the table
+// those scripts assemble (time, X-He centre-of-mass distance, Ekin(X), U*,
+// U+, E_SO per file).
+//
 // Not built here (listed as next): the P/D initial-state construction of
 // instates.f90 (instate 0..4 without Lexcite_state_fix) and the tabulated
 // Select_Pot potentials other than 'null' (V_impur.f90:87-932).
@@ -23,8 +29,11 @@
 #include <complex>
 #include <cstdio>
 #include <cstring>
+#include <algorithm>
 #include <fstream>
+#include <future>
 #include <iostream>
+#include <thread>
 #include <stdexcept>
 #include <string>
 #include <vector>
@@ -113,14 +122,29 @@ struct State {
   double rimp[3] = {0, 0, 0}, vimp[3] = {0, 0, 0};
   std::vector<double> invar = std::vector<double>(20, 0.0);
   bool have_invar = false;
+  double time_ps = 0.0;                       // from the file's comment lines
+  double auxn4 = 0, xc = 0, yc = 0, zc = 0;   // helium number and centre of mass
 };
 
 // readenc(mode) (readenc.f90:83-176); the grid of the file must match the
 // namelist's (the reference does not check and would misread).
-void readenc(const Input& in, const ep_config& cfg, int mode, State& s) {
-  const std::string fn = trim(in.get<std::string>("filedenin", "he4.input.density"));
+void readenc(const Input& in, const ep_config& cfg, int mode, const std::string& fn, State& s) {
   std::ifstream f(fn);
   if (!f) stop("readenc: cannot open '" + fn + "'");
+  {  // the evolution time printoutc records in the comment lines (read by loop.sh)
+    std::string l;
+    while (std::getline(f, l) && !l.empty() && l[0] == '#') {
+      const size_t k = l.find("Total evolution time");
+      if (k != std::string::npos && l.find(':', k) != std::string::npos) {
+        try {
+          s.time_ps = fio::to_real(trim(l.substr(l.find(':', k) + 1)));
+        } catch (const std::invalid_argument&) {
+        }
+      }
+    }
+    f.clear();
+    f.seekg(0);
+  }
   const size_t N = (size_t)cfg.nx * cfg.ny * cfg.nz;
   fio::ListReader r(f);
   r.skip_comments('#');
@@ -197,6 +221,86 @@ void prepare_invar(const Input& in, State& s) {
        "Lexcite_state_fix)");
 }
 
+// The state of one input file as DFT4He3d prepares it: impurity start values
+// from the namelist (DFT4He3d.f90:230-240, v in A/ps -> A K), readenc, the
+// initial-velocity phases (:314-330, :414-432), the helium number and centre
+// of mass.
+void load_state(const Input& in, const ep_config& cfg, const std::string& file, State& s) {
+  s.rimp[0] = in.get<double>("ximp", 0.0);
+  s.rimp[1] = in.get<double>("yimp", 0.0);
+  s.rimp[2] = in.get<double>("zimp", 0.0);
+
+  double vimp0[3] = {in.get<double>("vximp", 0.0) * kKtops, in.get<double>("vyimp", 0.0) * kKtops,
+                     in.get<double>("vzimp", 0.0) * kKtops};
+  const double n4 = cfg.n4, mimp = cfg.mimpur;
+  const double h2 = cfg.h2o2m4;
+  double xl0[3];
+  for (int k = 0; k < 3; ++k) {
+    s.vimp[k] = vimp0[k];
+    xl0[k] = -(vimp0[k] / kKtops) * mimp / (4.0 * n4);
+  }
+  const int mode = (int)in.get<long>("mode", 0L);
+  readenc(in, cfg, mode, file, s);
+  if (mode != 2) prepare_invar(in, s);
+  const size_t N = (size_t)cfg.nx * cfg.ny * cfg.nz;
+  const double hx = 2 * cfg.xmax / cfg.nx, hy = 2 * cfg.ymax / cfg.ny, hz = 2 * cfg.zmax / cfg.nz;
+  auto X = [&](int i) { return -cfg.xmax + hx * i; };
+  auto Y = [&](int i) { return -cfg.ymax + hy * i; };
+  auto Z = [&](int i) { return -cfg.zmax + hz * i; };
+  const bool vadd = in.get<bool>("l_v_aditional", false);
+  if (mode == 0) {
+    // psi = sqrt(den) exp(i k.r) with the initial-velocity phase (DFT4He3d.f90:414-432)
+    double xlx = in.get<double>("xlamdax", 0.0), xly = in.get<double>("xlamday", 0.0),
+           xlz = in.get<double>("xlamdaz", 0.0);
+    const double xlam = in.get<double>("xlamda", 0.0);
+    if (xlam != 0.0) xlz = xlam * kKtops / (2.0 * h2);
+    s.psi.resize(2 * N);
+    for (int iz = 0; iz < cfg.nz; ++iz)
+      for (int iy = 0; iy < cfg.ny; ++iy)
+        for (int ix = 0; ix < cfg.nx; ++ix) {
+          const size_t p = ix + (size_t)cfg.nx * (iy + (size_t)cfg.ny * iz);
+          const double a = X(ix) * xlx + Y(iy) * xly + Z(iz) * xlz, r = std::sqrt(s.den[p]);
+          s.psi[2 * p] = r * std::cos(a);
+          s.psi[2 * p + 1] = r * std::sin(a);
+        }
+  }
+  if (vadd) {  // DFT4He3d.f90:314-330 (for mode 0 the phase is overwritten there by sqrt(den))
+    for (int k = 0; k < 3; ++k) {
+      s.vimp[k] += vimp0[k];
+      xl0[k] = xl0[k] * kKtops / (2.0 * h2);
+    }
+    for (int iz = 0; iz < (mode == 0 ? 0 : cfg.nz); ++iz)
+      for (int iy = 0; iy < cfg.ny; ++iy)
+        for (int ix = 0; ix < cfg.nx; ++ix) {
+          const size_t p = ix + (size_t)cfg.nx * (iy + (size_t)cfg.ny * iz);
+          const std::complex<double> z(s.psi[2 * p], s.psi[2 * p + 1]);
+          const double a = X(ix) * xl0[0] + Y(iy) * xl0[1] + Z(iz) * xl0[2];
+          const std::complex<double> w = z * std::complex<double>(std::cos(a), std::sin(a));
+          s.psi[2 * p] = w.real();
+          s.psi[2 * p + 1] = w.imag();
+        }
+  }
+  // helium count and centre of mass of the density used
+  double auxn4 = 0, xc = 0, yc = 0, zc = 0;
+  for (int iz = 0; iz < cfg.nz; ++iz)
+    for (int iy = 0; iy < cfg.ny; ++iy)
+      for (int ix = 0; ix < cfg.nx; ++ix) {
+        const size_t p = ix + (size_t)cfg.nx * (iy + (size_t)cfg.ny * iz);
+        const double d = s.psi[2 * p] * s.psi[2 * p] + s.psi[2 * p + 1] * s.psi[2 * p + 1];
+        auxn4 += d;
+        xc += X(ix) * d;
+        yc += Y(iy) * d;
+        zc += Z(iz) * d;
+      }
+  xc /= auxn4;
+  yc /= auxn4;
+  zc /= auxn4;
+  auxn4 *= hx * hy * hz;
+  s.auxn4 = auxn4;
+  s.xc = xc;
+  s.yc = yc;
+  s.zc = zc;}
+
 void printoutc(const std::string& fn, int iprint, long iter, double time_ps, const ep_config& cfg,
                const State& s, double deltatps) {
   const size_t N = (size_t)cfg.nx * cfg.ny * cfg.nz;
@@ -269,10 +373,15 @@ void balance(const ep_energies& e, double auxn4) {
 
 int main(int argc, char** argv) {
   Input in;
+  std::vector<std::string> scan;  // --scan file...: the U*/U+ scan of loop.sh
+  if (argc > 1 && std::string(argv[1]) == "--scan") {
+    for (int i = 2; i < argc; ++i) scan.push_back(argv[i]);
+    if (scan.empty()) stop("--scan needs at least one wave-function file");
+  }
   {
     std::string err;
     bool ok;
-    if (argc > 1) {
+    if (argc > 1 && scan.empty()) {
       std::ifstream f(argv[1]);
       ok = f && fio::parse_namelist(f, "input", in.nml, err);
     } else {
@@ -337,77 +446,45 @@ int main(int argc, char** argv) {
     const ep_potential ppl = potential_of(in, "plus", "Ba_plus_2D2", 1.05, 6.260015e4);
     check(ep_set_impurity_potentials(ctx, &ppi, &psg, &ppl), ctx, "impurity potentials");
 
-    // impurity start values (DFT4He3d.f90:230-240): v in A/ps -> A K
-    State s;
-    s.rimp[0] = in.get<double>("ximp", 0.0);
-    s.rimp[1] = in.get<double>("yimp", 0.0);
-    s.rimp[2] = in.get<double>("zimp", 0.0);
-    double vimp0[3] = {in.get<double>("vximp", 0.0) * kKtops, in.get<double>("vyimp", 0.0) * kKtops,
-                       in.get<double>("vzimp", 0.0) * kKtops};
-    const double n4 = cfg.n4, mimp = cfg.mimpur;
-    const double h2 = cfg.h2o2m4;
-    double xl0[3];
-    for (int k = 0; k < 3; ++k) {
-      s.vimp[k] = vimp0[k];
-      xl0[k] = -(vimp0[k] / kKtops) * mimp / (4.0 * n4);
-    }
-    const int mode = (int)in.get<long>("mode", 0L);
-    readenc(in, cfg, mode, s);
-    if (mode != 2) prepare_invar(in, s);
-    const size_t N = (size_t)cfg.nx * cfg.ny * cfg.nz;
-    const double hx = 2 * cfg.xmax / cfg.nx, hy = 2 * cfg.ymax / cfg.ny, hz = 2 * cfg.zmax / cfg.nz;
-    auto X = [&](int i) { return -cfg.xmax + hx * i; };
-    auto Y = [&](int i) { return -cfg.ymax + hy * i; };
-    auto Z = [&](int i) { return -cfg.zmax + hz * i; };
-    const bool vadd = in.get<bool>("l_v_aditional", false);
-    if (mode == 0) {
-      // psi = sqrt(den) exp(i k.r) with the initial-velocity phase (DFT4He3d.f90:414-432)
-      double xlx = in.get<double>("xlamdax", 0.0), xly = in.get<double>("xlamday", 0.0),
-             xlz = in.get<double>("xlamdaz", 0.0);
-      const double xlam = in.get<double>("xlamda", 0.0);
-      if (xlam != 0.0) xlz = xlam * kKtops / (2.0 * h2);
-      s.psi.resize(2 * N);
-      for (int iz = 0; iz < cfg.nz; ++iz)
-        for (int iy = 0; iy < cfg.ny; ++iy)
-          for (int ix = 0; ix < cfg.nx; ++ix) {
-            const size_t p = ix + (size_t)cfg.nx * (iy + (size_t)cfg.ny * iz);
-            const double a = X(ix) * xlx + Y(iy) * xly + Z(iz) * xlz, r = std::sqrt(s.den[p]);
-            s.psi[2 * p] = r * std::cos(a);
-            s.psi[2 * p + 1] = r * std::sin(a);
-          }
-    }
-    if (vadd) {  // DFT4He3d.f90:314-330 (for mode 0 the phase is overwritten there by sqrt(den))
-      for (int k = 0; k < 3; ++k) {
-        s.vimp[k] += vimp0[k];
-        xl0[k] = xl0[k] * kKtops / (2.0 * h2);
+    if (!scan.empty()) {
+      // loop.sh + get_impurity_energy.sh in one job: every file's first energy
+      // balance, files parsed on host threads ahead of the GPU, one table line
+      // per file with the columns loop.sh extracts
+      std::printf("# time (ps)\tdX-HeCM (AA)\tEkin (K)\tU* (K)\t\tU+ (K)\t\tESO (K)\n");
+      const size_t nf = scan.size();
+      const size_t T = std::max<size_t>(1, std::min<size_t>(16, std::thread::hardware_concurrency()));
+      std::vector<std::future<State>> fut(nf);
+      size_t next = 0;
+      auto launch = [&] {
+        const size_t i = next++;
+        fut[i] = std::async(std::launch::async, [&in, &cfg, &scan, i] {
+          State st;
+          load_state(in, cfg, scan[i], st);
+          return st;
+        });
+      };
+      while (next < nf && next < T) launch();
+      for (size_t i = 0; i < nf; ++i) {
+        State st = fut[i].get();
+        if (next < nf) launch();
+        check(ep_upload_psi(ctx, st.psi.data()), ctx, "upload psi");
+        check(ep_set_impurity_state(ctx, st.rimp, st.vimp, st.invar.data()), ctx, "impurity state");
+        check(ep_potenimp(ctx), ctx, "potenimp");
+        check(ep_poten(ctx), ctx, "poten");
+        ep_energies e{};
+        check(ep_energy(ctx, &e), ctx, "energy");
+        const double rcm = std::sqrt((st.rimp[0] - st.xc) * (st.rimp[0] - st.xc) +
+                                     (st.rimp[1] - st.yc) * (st.rimp[1] - st.yc) +
+                                     (st.rimp[2] - st.zc) * (st.rimp[2] - st.zc));
+        std::printf("%.1f\t\t%f\t%f\t%f\t%f\t%f\n", st.time_ps, rcm, e.ekinx, e.eHeX, e.uplus, e.eso);
+        std::fflush(stdout);
       }
-      for (int iz = 0; iz < (mode == 0 ? 0 : cfg.nz); ++iz)
-        for (int iy = 0; iy < cfg.ny; ++iy)
-          for (int ix = 0; ix < cfg.nx; ++ix) {
-            const size_t p = ix + (size_t)cfg.nx * (iy + (size_t)cfg.ny * iz);
-            const std::complex<double> z(s.psi[2 * p], s.psi[2 * p + 1]);
-            const double a = X(ix) * xl0[0] + Y(iy) * xl0[1] + Z(iz) * xl0[2];
-            const std::complex<double> w = z * std::complex<double>(std::cos(a), std::sin(a));
-            s.psi[2 * p] = w.real();
-            s.psi[2 * p + 1] = w.imag();
-          }
+      ep_destroy(ctx);
+      return 0;
     }
-    // helium count and centre of mass of the density used
-    double auxn4 = 0, xc = 0, yc = 0, zc = 0;
-    for (int iz = 0; iz < cfg.nz; ++iz)
-      for (int iy = 0; iy < cfg.ny; ++iy)
-        for (int ix = 0; ix < cfg.nx; ++ix) {
-          const size_t p = ix + (size_t)cfg.nx * (iy + (size_t)cfg.ny * iz);
-          const double d = s.psi[2 * p] * s.psi[2 * p] + s.psi[2 * p + 1] * s.psi[2 * p + 1];
-          auxn4 += d;
-          xc += X(ix) * d;
-          yc += Y(iy) * d;
-          zc += Z(iz) * d;
-        }
-    xc /= auxn4;
-    yc /= auxn4;
-    zc /= auxn4;
-    auxn4 *= hx * hy * hz;
+    State s;
+    load_state(in, cfg, trim(in.get<std::string>("filedenin", "he4.input.density")), s);
+    const double auxn4 = s.auxn4, xc = s.xc, yc = s.yc, zc = s.zc;
     std::printf("\n\n     Title of the run: %s\n", in.get<std::string>("title", "Helium4 - 3dim.  ").c_str());
 
     check(ep_upload_psi(ctx, s.psi.data()), ctx, "upload psi");

@@ -148,3 +148,39 @@ def test_mode2_evolution_writes_a_file_that_reads_back(tmp_path):
         s.poten()
         e2 = s.energy()
     assert got["etot"] == f"{e2['etot']:.6f}"
+
+
+def per_file_line(cwd, path):
+    """get_impurity_energy.sh with this driver: run on one file, pick the awk
+    fields it picks, print them with its printf."""
+    out = run_driver(cwd, namelist(2).replace("filedenin='in.dat'", f"filedenin='{path}'"))
+    with open(path) as f:
+        head = [next(f) for _ in range(3)]
+    t = float([ln.split()[4] for ln in head if "Total evolution time" in ln][0].replace("D", "E"))
+
+    def field(pat, k):
+        return float([ln.split()[k - 1] for ln in out.splitlines() if re.search(pat, ln)][0])
+    vals = (field(r"X-HE CoM distance", 4), field(r"Kinetic energy \(X", 5), field(r"Interaction energy \(X\*", 5),
+            field(r"Interaction energy \(X\+", 5), field(r"Spin-Orbit energy", 5))
+    return "%.1f\t\t%f\t%f\t%f\t%f\t%f" % ((t,) + vals)
+
+
+def test_scan_matches_per_file_runs(tmp_path):
+    files = []
+    for k, z in enumerate((0.0, 1.5, 3.0)):
+        psi = ep.woods_saxon_psi(N, N, N, XMAX, XMAX, XMAX, N4, seed=20 + k)
+        p = tmp_path / f"density.{k}.out"
+        write_wavefunction(p, psi, (0.0, 0.0, z), (0.0, 0.0, 0.1 * k), np.zeros(10, dtype=np.complex128))
+        # the evolution time loop.sh reads from the third line
+        lines = p.read_text().splitlines(True)
+        lines.insert(2, f"#  Total evolution time(ps)...:  {2.5 * k:.12E}\n")
+        p.write_text("".join(lines))
+        files.append(str(p))
+    r = subprocess.run([DRIVER, "--scan", *files], input=namelist(2), cwd=tmp_path, capture_output=True, text=True,
+                       timeout=300)
+    assert r.returncode == 0, r.stdout + r.stderr
+    table = [ln for ln in r.stdout.splitlines() if ln and not ln.startswith("#") and "\t" in ln]
+    assert r.stdout.splitlines()[1].startswith("# time (ps)")
+    assert len(table) == 3
+    for line, f in zip(table, files):
+        assert line == per_file_line(tmp_path, f)
