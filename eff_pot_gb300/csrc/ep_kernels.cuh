@@ -832,8 +832,14 @@ EP_DEV void lap_march_async(const Geo& g, const C2<T>* __restrict__ psi, const F
     }
     return xx + (long long)g.nx * yy + sxy * zz;
   };
-  for (int e = tid; e < PL; e += NT) {
-    const int r = e / W, c = e - r * W;
+  // plane fetched in 16-byte chunks (two FP32 complex values) when the halo
+  // and nx are chunk-aligned, else element by element
+  constexpr int CH = 16 / (int)sizeof(CT);
+  constexpr bool CHUNKED = CH > 1 && (R % CH) == 0 && (EP_TX % CH) == 0;
+  const bool vec = CHUNKED && (g.nx % CH) == 0;
+  const int ulen = vec ? CH : 1, uperrow = W / ulen, nunits = uperrow * H;
+  for (int e = tid; e < nunits; e += NT) {
+    const int r = e / uperrow, c = (e - r * uperrow) * ulen;
     int xx = blockIdx.x * EP_TX - R + c, yy = blockIdx.y * EP_TY - R + r;
     int o = -1;
     if (xx >= 0 && xx < g.nx && yy >= 0 && yy < g.ny) o = xx + g.nx * yy;
@@ -846,10 +852,24 @@ EP_DEV void lap_march_async(const Geo& g, const C2<T>* __restrict__ psi, const F
     int zz = z;
     if (zz < 0 || zz >= g.nz) zz = per ? wrapi(zz, g.nz) : -1;
     const CT* pz = psi + sxy * (zz < 0 ? 0 : zz);
-    for (int e = tid; e < PL; e += NT) {
-      const int o = zz < 0 ? -1 : soff[e];
-      if (o >= 0) cp_async<sizeof(CT)>(P + e, pz + o);
-      else P[e] = cmk<T>(T(0), T(0));
+    if (CHUNKED && vec) {
+      for (int e = tid; e < nunits; e += NT) {
+        const int r = e / uperrow, c = (e - r * uperrow) * CH;
+        CT* dst = P + r * W + c;
+        const int o = zz < 0 ? -1 : soff[e];
+        if (o >= 0) {
+          cp_async<16>(dst, pz + o);
+        } else {
+#pragma unroll
+          for (int i = 0; i < CH; ++i) dst[i] = cmk<T>(T(0), T(0));
+        }
+      }
+    } else {
+      for (int e = tid; e < PL; e += NT) {
+        const int o = zz < 0 ? -1 : soff[e];
+        if (o >= 0) cp_async<sizeof(CT)>(P + e, pz + o);
+        else P[e] = cmk<T>(T(0), T(0));
+      }
     }
     if (valid) {
       const long long aq = addr(x, y, z + R);
@@ -909,8 +929,13 @@ __global__ void __launch_bounds__(EP_TX* EP_TY) k_d1march(Geo g, const __grid_co
                                                          const T* __restrict__ f, const T* __restrict__ f2,
                                                          T* __restrict__ o0, T* __restrict__ o1,
                                                          T* __restrict__ o2) {
-  constexpr int HX = MODE == 0 ? R : 0;
+  // The plane tile (x halo rounded up to whole 16-byte chunks) is fetched
+  // chunk by chunk when nx is a multiple of the chunk; element by element
+  // otherwise.  Offsets of chunks (or elements) are tabulated once per CTA.
+  constexpr int CH = 16 / (int)sizeof(T);
+  constexpr int HX = MODE == 0 ? ((R + CH - 1) / CH) * CH : 0;
   constexpr int W = EP_TX + 2 * HX, H = EP_TY + 2 * R, PL = W * H, NT = EP_TX * EP_TY;
+  constexpr int WC = W / CH, PC = WC * H;
   __shared__ __align__(16) T sp[2][PL];
   __shared__ __align__(16) T sq[2][NT];
   __shared__ int soff[PL];
@@ -920,9 +945,11 @@ __global__ void __launch_bounds__(EP_TX* EP_TY) k_d1march(Geo g, const __grid_co
   const int z0 = blockIdx.z * zc, z1 = min(z0 + zc, g.nz);
   const bool valid = (x < g.nx) && (y < g.ny);
   const int per = fd.periodic;
+  const bool vec = (g.nx % CH) == 0;
+  const int nunits = vec ? PC : PL, ulen = vec ? CH : 1, uperrow = vec ? WC : W;
   const long long sxy = (long long)g.nx * g.ny;
-  for (int e = tid; e < PL; e += NT) {
-    const int r = e / W, c = e - r * W;
+  for (int e = tid; e < nunits; e += NT) {
+    const int r = e / uperrow, c = (e - r * uperrow) * ulen;
     const int xx = blockIdx.x * EP_TX - HX + c, yy = blockIdx.y * EP_TY - R + r;
     int o = -1;
     if (xx >= 0 && xx < g.nx && yy >= 0 && yy < g.ny) o = xx + g.nx * yy;
@@ -944,10 +971,24 @@ __global__ void __launch_bounds__(EP_TX* EP_TY) k_d1march(Geo g, const __grid_co
   auto prefetch = [&](int z, int buf) {
     const int zz = zwrap(z);
     const T* pz = f + sxy * (zz < 0 ? 0 : zz);
-    for (int e = tid; e < PL; e += NT) {
-      const int o = zz < 0 ? -1 : soff[e];
-      if (o >= 0) cp_async<sizeof(T)>(&sp[buf][e], pz + o);
-      else sp[buf][e] = T(0);
+    if (vec) {
+      for (int e = tid; e < PC; e += NT) {
+        const int r = e / WC, c = (e - r * WC) * CH;
+        T* dst = &sp[buf][r * W + c];
+        const int o = zz < 0 ? -1 : soff[e];
+        if (o >= 0) {
+          cp_async<16>(dst, pz + o);
+        } else {
+#pragma unroll
+          for (int i = 0; i < CH; ++i) dst[i] = T(0);
+        }
+      }
+    } else {
+      for (int e = tid; e < PL; e += NT) {
+        const int o = zz < 0 ? -1 : soff[e];
+        if (o >= 0) cp_async<sizeof(T)>(&sp[buf][e], pz + o);
+        else sp[buf][e] = T(0);
+      }
     }
     if (valid) {
       const int zq = zwrap(z + R);
