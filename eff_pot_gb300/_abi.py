@@ -93,6 +93,7 @@ _prototypes = {
     "energy": (_I, [_P, C.POINTER(EpEnergies)]),
     "forceimp": (_I, [_P, _D]),
     "potinvar": (_I, [_P, _D]),
+    "impurity_moments": (_I, [_P, _D]),
     "steprk": (_I, [_P, C.c_double]),
     "steppc": (_I, [_P, C.c_double, C.POINTER(EpStepErrors)]),
     "run": (_I, [_P, _I, C.c_double, C.POINTER(EpRunStats)]),

@@ -76,7 +76,8 @@ def build_driver(force=False):
     """The DFT4He3d driver: host C++ over the C ABI, linked to libeffpot.so."""
     ddir = os.path.join(CSRC, "driver")
     srcs = [os.path.join(ddir, f) for f in DRIVER_SRC]
-    deps = srcs + [os.path.join(ddir, "ep_fortran_io.h"), os.path.join(ROOT, "include", "eff_pot.h"), LIB]
+    deps = srcs + [os.path.join(ddir, h) for h in ("ep_fortran_io.h", "ep_instates.h")]
+    deps += [os.path.join(ROOT, "include", "eff_pot.h"), LIB]
     if not (force or _stale(deps, DRIVER)):
         return DRIVER
     cxx = shutil.which("g++") or "c++"

@@ -22,9 +22,12 @@
 // those scripts assemble (time, X-He centre-of-mass distance, Ekin(X), U*,
 // U+, E_SO per file).
 //
-// Not built here (listed as next): the P/D initial-state construction of
-// instates.f90 (instate 0..4 without Lexcite_state_fix) and the tabulated
-// Select_Pot potentials other than 'null' (V_impur.f90:87-932).
+// P-state internal variables (instate 0..2) are built as instates.f90 does
+// in its default branch (ep_instates.h); Lexcite_state_fix gives its fixed
+// vectors, instate 5 reads invar.dat.  Not built here (listed as next): the
+// D states and the Ldiag_jz / Laverage_P_value / Lmixture / exciplex
+// variants of instates.f90, and the tabulated Select_Pot potentials other
+// than 'null' (V_impur.f90:87-932).
 #include <cmath>
 #include <complex>
 #include <cstdio>
@@ -40,6 +43,7 @@
 
 #include "../../../include/eff_pot.h"
 #include "ep_fortran_io.h"
+#include "ep_instates.h"
 
 namespace {
 
@@ -123,6 +127,7 @@ struct State {
   std::vector<double> invar = std::vector<double>(20, 0.0);
   bool have_invar = false;
   double time_ps = 0.0;                       // from the file's comment lines
+  int p_instate = -1;                         // P state to build from the field moments
   double auxn4 = 0, xc = 0, yc = 0, zc = 0;   // helium number and centre of mass
 };
 
@@ -210,15 +215,30 @@ void prepare_invar(const Input& in, State& s) {
     return;
   }
   if (instate > 5) stop("instate value invalid " + std::to_string(instate));
-  if (in.get<bool>("lexcite_state_fix", false) && instate <= 2) {  // fixed P states, instates.f90
+  const std::string lstate = trim(in.get<std::string>("lstate", "P"));
+  if (lstate != "P") stop("Lstate='" + lstate + "': the D-state internal variables are not built in this driver");
+  if (in.get<bool>("lexcite_state_fix", false) && instate <= 2) {  // fixed P states, instates.f90:300-320
     std::fill(s.invar.begin(), s.invar.end(), 0.0);
     const int n = (int)instate + 1;
     for (int k = 0; k < n; ++k) s.invar[2 * (2 * k)] = 1.0 / std::sqrt((double)n);
     return;
   }
-  stop("instate " + std::to_string(instate) +
-       ": the P/D initial states of instates.f90 are not built in this driver (use mode 2, instate 5 or "
-       "Lexcite_state_fix)");
+  for (const char* k : {"ldiag_jz", "laverage_p_value", "lmixture", "lexciplex_state_fix"})
+    if (in.get<bool>(k, false)) stop(std::string(k) + ": this instates.f90 variant is not built in this driver");
+  if (instate > 2) stop("instate " + std::to_string(instate) + " has no P state (0..2)");
+  s.p_instate = (int)instate;  // built from the field moments once the density is on the GPU
+}
+
+// instates.f90, P state: the moments of the impurity field on the current
+// density give the 6x6 V + (Als/2) SO; its pair of eigenvectors selected by
+// instate gives invar, then the impurity field is recomputed with it.
+void build_p_state(ep_ctx* ctx, const ep_config& cfg, State& s) {
+  if (s.p_instate < 0) return;
+  double m[6];
+  check(ep_impurity_moments(ctx, m), ctx, "impurity moments");
+  instates::p_state(m, cfg.als_p, s.p_instate, s.invar.data());
+  check(ep_set_impurity_state(ctx, s.rimp, s.vimp, s.invar.data()), ctx, "impurity state");
+  check(ep_potenimp(ctx), ctx, "potenimp");
 }
 
 // The state of one input file as DFT4He3d prepares it: impurity start values
@@ -470,6 +490,7 @@ int main(int argc, char** argv) {
         check(ep_upload_psi(ctx, st.psi.data()), ctx, "upload psi");
         check(ep_set_impurity_state(ctx, st.rimp, st.vimp, st.invar.data()), ctx, "impurity state");
         check(ep_potenimp(ctx), ctx, "potenimp");
+        build_p_state(ctx, cfg, st);
         check(ep_poten(ctx), ctx, "poten");
         ep_energies e{};
         check(ep_energy(ctx, &e), ctx, "energy");
@@ -490,6 +511,7 @@ int main(int argc, char** argv) {
     check(ep_upload_psi(ctx, s.psi.data()), ctx, "upload psi");
     check(ep_set_impurity_state(ctx, s.rimp, s.vimp, s.invar.data()), ctx, "impurity state");
     check(ep_potenimp(ctx), ctx, "potenimp");
+    build_p_state(ctx, cfg, s);
     check(ep_poten(ctx), ctx, "poten");
     ep_energies e{};
     check(ep_energy(ctx, &e), ctx, "energy");

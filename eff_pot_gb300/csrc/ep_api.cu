@@ -422,6 +422,17 @@ int ep_forceimp(ep_ctx* c, double* F) {
   }
   return r;
 }
+int ep_impurity_moments(ep_ctx* c, double* v6) {
+  if (!v6) return EP_ERR_INVALID_ARG;
+  return dispatch(c, [&](auto& e) -> int {
+    double F[3];
+    int r = e.ensure_materialized();
+    if (!r) r = e.forceimp(F);
+    if (!r) r = e.moments(v6);
+    return r;
+  });
+}
+
 int ep_potinvar(ep_ctx* c, double* hinvar) {
   if (!hinvar) return EP_ERR_INVALID_ARG;
   return dispatch(c, [&](auto& e) -> int {

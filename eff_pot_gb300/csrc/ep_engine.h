@@ -72,6 +72,7 @@ class Engine {
   int zc_pc = 16, zc_rk = 16, zc_d1 = 16;  // z planes per CTA of the stencil marches
   T* dyz = nullptr;                         // dy(gy) + dz(gz) of term_alfa
   int d1march(int mode, const T* f, const T* f2, T* o0, T* o1, T* o2);
+  int moments(double* v6);
   // Step graphs (CUDA-graph replay of steppc): while capturing, cap_nodes
   // receives the predictor / corrector nodes; while replaying, upd_exec is the
   // executable graph whose nodes lap_predict / lap_correct update.

@@ -579,6 +579,22 @@ int Engine<T>::forceimp(double* F) {
   return EP_OK;
 }
 
+// (Vx, Vy, Vz, Vxy, Vxz, Vyz) of instates.f90:123-147 from the moments left
+// by the last forceimp() call.
+template <class T>
+int Engine<T>::moments(double* v6) {
+  double s[9];
+  int r;
+  if ((r = read_sums(s, 9, 16))) return r;
+  v6[0] = s[3] * dxyz;
+  v6[1] = s[6] * dxyz;
+  v6[2] = s[8] * dxyz;
+  v6[3] = s[4] * dxyz;
+  v6[4] = s[5] * dxyz;
+  v6[5] = s[7] * dxyz;
+  return EP_OK;
+}
+
 // potinvar, P state (potenimp.f90:298-330, 487-492), from the moments left
 // by the last forceimp() call.
 template <class T>

@@ -204,6 +204,12 @@ class Solver:
         self._check(self._f["forceimp"](self._h, _abi.dptr(F)), "forceimp")
         return F
 
+    def impurity_moments(self):
+        """(Vx, Vy, Vz, Vxy, Vxz, Vyz): the P-state matrix of instates."""
+        v = np.zeros(6)
+        self._check(self._f["impurity_moments"](self._h, _abi.dptr(v)), "impurity_moments")
+        return v
+
     def potinvar(self):
         H = np.zeros(20)
         self._check(self._f["potinvar"](self._h, _abi.dptr(H)), "potinvar")

@@ -162,6 +162,11 @@ int ep_potenimp(ep_ctx* ctx);
 int ep_poten(ep_ctx* ctx);
 /* energy() (energy.f90:12-202), eHeX/uplus accumulators zeroed. */
 int ep_energy(ep_ctx* ctx, ep_energies* e);
+/* The six density-weighted moments of the impurity field,
+ * v6 = (Vx, Vy, Vz, Vxy, Vxz, Vyz), V_ij = sum den (V_Pi d_ij + Delta x_i x_j)
+ * dxyz with x = r - rimp, from the fields of the last ep_potenimp: the
+ * matrix of the P-state internal variables (instates.f90:123-147). */
+int ep_impurity_moments(ep_ctx* ctx, double* v6);
 /* forceimp(rimp,F) (potenimp.f90:193-258); for a moving impurity also
  * stores aimp = F / mAg_u, as every reference call site does next
  * (DFT4He3d.f90:454-455). */

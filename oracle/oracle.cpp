@@ -983,6 +983,25 @@ static void potinvar_(oc_ctx* c, cd* Hiv) {
   for (int i = 0; i < 10; ++i) Hiv[i] = -uim * (Hiv[i] - g.ev0 * iv[i]);
 }
 
+// (Vx, Vy, Vz, Vxy, Vxz, Vyz) of instates.f90:123-147.
+int oc_impurity_moments(oc_ctx* c, double* v6) {
+  if (!c || !v6) return EP_ERR_INVALID_ARG;
+  const int nx = c->nx, ny = c->ny;
+  const double* rr = c->rimp;
+  auto X = [&](size_t p) { return c->x[(int)(p % nx)] - rr[0]; };
+  auto Y = [&](size_t p) { return c->y[(int)((p / nx) % ny)] - rr[1]; };
+  auto Z = [&](size_t p) { return c->z[(int)(p / ((size_t)nx * ny))] - rr[2]; };
+  const size_t N = c->N;
+  v6[0] = par_sum(N, [&](size_t p) { double xx = X(p); return c->den[p] * (c->delta[p] * xx * xx + c->vpi[p]); });
+  v6[1] = par_sum(N, [&](size_t p) { double yy = Y(p); return c->den[p] * (c->delta[p] * yy * yy + c->vpi[p]); });
+  v6[2] = par_sum(N, [&](size_t p) { double zz = Z(p); return c->den[p] * (c->delta[p] * zz * zz + c->vpi[p]); });
+  v6[3] = par_sum(N, [&](size_t p) { return c->den[p] * c->delta[p] * X(p) * Y(p); });
+  v6[4] = par_sum(N, [&](size_t p) { return c->den[p] * c->delta[p] * X(p) * Z(p); });
+  v6[5] = par_sum(N, [&](size_t p) { return c->den[p] * c->delta[p] * Y(p) * Z(p); });
+  for (int k = 0; k < 6; ++k) v6[k] *= c->dxyz;
+  return EP_OK;
+}
+
 int oc_potinvar(oc_ctx* c, double* hinvar) {
   if (!c || !hinvar) return EP_ERR_INVALID_ARG;
   cd H[10];

@@ -47,6 +47,7 @@ int oc_poten(oc_ctx* c);
 int oc_energy(oc_ctx* c, ep_energies* e);
 int oc_forceimp(oc_ctx* c, double* F);
 int oc_potinvar(oc_ctx* c, double* hinvar);
+int oc_impurity_moments(oc_ctx* c, double* v6);
 int oc_steprk(oc_ctx* c, double deltat);
 int oc_steppc(oc_ctx* c, double deltat, ep_step_errors* err);
 int oc_run(oc_ctx* c, int nsteps, double deltat, ep_run_stats* stats);

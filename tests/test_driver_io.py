@@ -17,10 +17,12 @@ DRV = os.path.join(ROOT, "eff_pot_gb300", "csrc", "driver")
 
 HARNESS = r"""
 #include <cstdio>
+#include <cstdlib>
 #include <fstream>
 #include <iostream>
 #include <sstream>
 #include "ep_fortran_io.h"
+#include "ep_instates.h"
 int main(int argc, char** argv) {
   std::string what = argv[1];
   if (what == "nml") {
@@ -47,6 +49,25 @@ int main(int argc, char** argv) {
     std::printf("\n");
     for (double v : tail) std::printf("%.17g ", v);
     std::printf("\n");
+  } else if (what == "eig") {
+    // moments and Als from the command line; prints the P matrix, eigenvalues,
+    // eigenvectors (column-major re im) and the invar of instate 0, 1, 2
+    double m[6]; for (int i = 0; i < 6; ++i) m[i] = std::atof(argv[2 + i]);
+    const double als = std::atof(argv[8]);
+    auto M = instates::p_matrix(m, als);
+    for (auto z : M) std::printf("%.17g %.17g ", z.real(), z.imag());
+    std::printf("\n");
+    std::vector<double> w; std::vector<std::complex<double>> v;
+    instates::hermitian_eigen(6, M, w, v);
+    for (double x : w) std::printf("%.17g ", x);
+    std::printf("\n");
+    for (int k = 0; k < 6; ++k) for (int i = 0; i < 6; ++i) std::printf("%.17g %.17g ", v[i * 6 + k].real(), v[i * 6 + k].imag());
+    std::printf("\n");
+    for (int st = 0; st < 3; ++st) {
+      double iv[20]; instates::p_state(m, als, st, iv);
+      for (double x : iv) std::printf("%.17g ", x);
+      std::printf("\n");
+    }
   } else if (what == "rec") {
     std::ofstream o(argv[2], std::ios::binary);
     double v[3] = {1.5, -2.25, 3.0}; int k = 7;
@@ -154,3 +175,27 @@ def test_driver_rejects_unknown_core_and_bad_namelist(driver, tmp_path):
     assert r.returncode == 1 and "Error in input master file" in r.stdout
     r = drive(driver, tmp_path, "no namelist here\n")
     assert r.returncode == 1 and "Error in input master file" in r.stdout
+
+
+def test_p_state_eigenvectors(harness):
+    """The Jacobi eigen-solver of the P-state matrix V + (Als/2) SO
+    (instates.f90:150-193): eigenpairs of the Hermitian matrix, Kramers
+    pairs, and the j = 1/2 / 3/2 levels V0 - Als, V0 + Als/2 of an
+    isotropic field; invar = (v_2k + v_2k+1)/sqrt(2) lies in the pair."""
+    import numpy as np
+    for m, als in (([-3.0, -2.5, -2.0, 0.3, -0.2, 0.1], 4.0), ([-5.0, -5.0, -5.0, 0.0, 0.0, 0.0], 6.0)):
+        out = run(harness, "eig", *m, als).splitlines()
+        M = np.array([float(x) for x in out[0].split()]).view(np.complex128).reshape(6, 6)
+        assert np.allclose(M, M.conj().T)
+        w = np.array([float(x) for x in out[1].split()])
+        V = np.array([float(x) for x in out[2].split()]).view(np.complex128).reshape(6, 6).T
+        assert np.allclose(w, np.linalg.eigvalsh(M), atol=1e-13)
+        assert np.allclose(M @ V, V * w, atol=1e-12)
+        assert np.allclose(V.conj().T @ V, np.eye(6), atol=1e-13)
+        assert np.allclose(w[0::2], w[1::2], atol=1e-12)  # Kramers pairs
+        for st in range(3):
+            iv = np.array([float(x) for x in out[3 + st].split()]).view(np.complex128)
+            assert abs(np.vdot(iv, iv) - 1.0) < 1e-13 and np.all(iv[6:] == 0)
+            assert np.allclose(M @ iv[:6], w[2 * st] * iv[:6], atol=1e-12)
+        if m[3] == 0.0:
+            assert np.allclose(w, [m[0] - als] * 2 + [m[0] + als / 2] * 4, atol=1e-12)

@@ -184,3 +184,64 @@ def test_scan_matches_per_file_runs(tmp_path):
     assert len(table) == 3
     for line, f in zip(table, files):
         assert line == per_file_line(tmp_path, f)
+
+
+def test_impurity_moments_match_the_oracle():
+    from oracle import pyoracle
+    psi = ep.woods_saxon_psi(N, N, N, XMAX, XMAX, XMAX, N4, seed=6)
+    rimp = (0.7, -0.4, 1.1)
+    cfg = ep.make_config(nx=N, ny=N, nz=N, xmax=XMAX, ymax=XMAX, zmax=XMAX, icon=_abi.EP_ICON_PERIODIC, core="OTC",
+                         n4=N4, impurity=_abi.EP_IMPURITY_MOVING, mimpur=40.0, fix_lambda=1)
+    m1 = ep.morse(10.0, 4.5, 1.2, r_cutoff=0.0, umax=1000.0)
+    m2 = ep.morse(25.0, 4.0, 1.1, r_cutoff=0.0, umax=1000.0)  # sigma != pi: an anisotropic field
+    res = []
+    for S in (ep.Solver, pyoracle.OracleSolver):
+        with S(cfg) as s:
+            s.set_impurity_potentials(m1, m2, ep.null_potential())
+            s.set_impurity(rimp=rimp, invar=np.zeros(10, dtype=np.complex128))
+            s.upload_psi(psi)
+            s.potenimp()
+            res.append(s.impurity_moments())
+    assert np.allclose(res[0], res[1], rtol=1e-11, atol=1e-11 * np.abs(res[1]).max())
+    assert abs(res[1][3]) > 0  # off-diagonal moments are exercised
+
+
+def test_p_state_instate_matches_the_api(tmp_path):
+    psi = ep.woods_saxon_psi(N, N, N, XMAX, XMAX, XMAX, N4, seed=7)
+    den = np.abs(psi) ** 2
+    rimp = (0.3, 0.2, -0.6)
+    write_density(tmp_path / "in.dat", den, rimp)
+    for instate in (0, 1):
+        out = run_driver(tmp_path, namelist(0, f", instate={instate}, Als_P=5.d0"))
+        got = balance(out)
+        eso = float(re.search(r"Spin-Orbit energy \(X\) \.*: +(-?\d+\.\d+) K", out).group(1))
+        cfg = ep.make_config(nx=N, ny=N, nz=N, xmax=XMAX, ymax=XMAX, zmax=XMAX, icon=_abi.EP_ICON_PERIODIC,
+                             core="OTC", n4=N4, impurity=_abi.EP_IMPURITY_MOVING, mimpur=40.0, fix_lambda=1,
+                             als_p=5.0)
+        with ep.Solver(cfg) as s:
+            m = ep.morse(10.0, 4.5, 1.2, r_cutoff=0.0, umax=1000.0)
+            s.set_impurity_potentials(m, m, ep.null_potential())
+            s.set_impurity(rimp=rimp, invar=np.zeros(10, dtype=np.complex128))
+            s.upload_psi(np.sqrt(den).astype(np.complex128))
+            s.potenimp()
+            vx, vy, vz, vxy, vxz, vyz = s.impurity_moments()
+            M = np.zeros((6, 6), complex)
+            for (i, j), v in {(0, 0): vx, (1, 1): vx, (2, 2): vy, (3, 3): vy, (4, 4): vz, (5, 5): vz,
+                              (0, 2): vxy, (1, 3): vxy, (0, 4): vxz, (1, 5): vxz, (2, 4): vyz, (3, 5): vyz}.items():
+                M[i, j] = M[j, i] = v
+            so = {(0, 2): -1j, (1, 3): 1j, (1, 4): -1, (0, 5): 1, (3, 4): -1j, (2, 5): -1j}
+            for (i, j), v in so.items():
+                M[i, j] += 2.5 * v
+                M[j, i] += 2.5 * np.conj(v)
+            w, V = np.linalg.eigh(M)
+            iv = np.zeros(10, complex)
+            iv[:6] = (V[:, 2 * instate] + V[:, 2 * instate + 1]) / np.sqrt(2)
+            s.set_impurity(rimp=rimp, invar=iv)
+            s.potenimp()
+            s.poten()
+            e = s.energy()
+        # energies do not depend on the basis inside the Kramers pair
+        for k, v in got.items():
+            assert abs(float(v) - e[k]) < 2e-6, (instate, k, v, e[k])
+        assert abs(eso - e["eso"]) < 2e-6
+        assert abs(e["eso"] - 5.0 * (-1.0 if instate == 0 else 0.5)) < 0.3  # j = 1/2 vs 3/2 level
