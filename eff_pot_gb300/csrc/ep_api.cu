@@ -673,7 +673,7 @@ long long ep_batch_kernel_launches(const ep_batch* b) {
 namespace {
 template <class E>
 void shapes_out(const E& e, int* s) {
-  s[0] = e.shp.xnl; s[1] = e.shp.xthr; s[2] = e.shp.ylt; s[3] = e.shp.ythr; s[4] = e.shp.zlt; s[5] = e.shp.zthr;
+  s[0] = e.shp.xnl[0]; s[1] = e.shp.xthr[0]; s[2] = e.shp.ylt; s[3] = e.shp.ythr; s[4] = e.shp.zlt; s[5] = e.shp.zthr;
 }
 bool shapes_ok(const int* s) {
   auto pow2 = [](int v) { return v >= 1 && v <= 64 && (v & (v - 1)) == 0; };
@@ -707,7 +707,8 @@ int ep_get_launch_shapes(const ep_ctx* c, int* s) {
 int ep_set_launch_shapes(ep_ctx* c, const int* s) {
   if (!c || !s || !shapes_ok(s)) return EP_ERR_INVALID_ARG;
   Shapes sh;
-  sh.xnl = s[0]; sh.xthr = s[1]; sh.ylt = s[2]; sh.ythr = s[3]; sh.zlt = s[4]; sh.zthr = s[5];
+  for (int k = 0; k < 4; ++k) { sh.xnl[k] = s[0]; sh.xthr[k] = s[1]; }
+  sh.ylt = s[2]; sh.ythr = s[3]; sh.zlt = s[4]; sh.zthr = s[5];
   if (c->active == EP_FP64 && c->e64) { c->e64->shp = sh; ++c->e64->shapes_gen; }
   else if (c->e32) { c->e32->shp = sh; ++c->e32->shapes_gen; }
   else return EP_ERR_STATE;
@@ -721,13 +722,18 @@ int ep_batch_autotune(ep_batch* b) {
     if (done[i]) continue;
     int r = ep_autotune(b->ctx[i], nullptr, 0);
     if (r) return r;
-    int sh[6];
-    ep_get_launch_shapes(b->ctx[i], sh);
-    const ep_config& ci = b->ctx[i]->cfg;
+    // the tuned shapes (every X kernel's own) go to the instances of the same
+    // grid and precision
+    ep_ctx* ci_ = b->ctx[i];
+    const ep_config& ci = ci_->cfg;
     for (size_t j = i; j < b->ctx.size(); ++j) {
-      const ep_config& cj = b->ctx[j]->cfg;
-      if (cj.nx == ci.nx && cj.ny == ci.ny && cj.nz == ci.nz && b->ctx[j]->active == b->ctx[i]->active) {
-        ep_set_launch_shapes(b->ctx[j], sh);
+      ep_ctx* cj_ = b->ctx[j];
+      const ep_config& cj = cj_->cfg;
+      if (cj.nx == ci.nx && cj.ny == ci.ny && cj.nz == ci.nz && cj_->active == ci_->active) {
+        if (j != i) {
+          if (ci_->active == EP_FP64 && ci_->e64 && cj_->e64) { cj_->e64->shp = ci_->e64->shp; ++cj_->e64->shapes_gen; }
+          if (ci_->active == EP_FP32 && ci_->e32 && cj_->e32) { cj_->e32->shp = ci_->e32->shp; ++cj_->e32->shapes_gen; }
+        }
         done[j] = 1;
       }
     }

@@ -51,9 +51,9 @@ struct ImpState {
 // Launch shapes of the FFT passes (lines per CTA and threads per CTA),
 // chosen by Engine::autotune.
 struct Shapes {
-  int xnl = 16, xthr = 256;  // X passes: x-lines per CTA, threads
-  int ylt = 16, ythr = 256;  // Y passes
-  int zlt = 16, zthr = 256;  // Z convolution passes
+  int xnl[4] = {16, 16, 16, 16}, xthr[4] = {256, 256, 256, 256};  // X1..X4: x-lines per CTA, threads
+  int ylt = 16, ythr = 256;  // Y passes (shared-memory engine)
+  int zlt = 16, zthr = 256;  // Z convolution passes (shared-memory engine)
 };
 
 template <class T>
@@ -154,7 +154,7 @@ class Engine {
   template <int N> int rfft_z(const ConvSpec<T>& cs, int nin, const LineSet& ls);
   int zconv(const CT* const* in, CT* const (*out)[3], const T* const (*ker)[3], const int* nout, int nin);
   int slot_of(const CT* p) const;
-  int x_lines(int nreal) const;
+  int x_lines(int which, int nreal) const;
   size_t x_smem(int nl, int nreal) const;
   int l_lines(int n, int nbuf) const;
   size_t l_smem(int LT, int n, int nbuf) const;

@@ -387,9 +387,72 @@ struct XSmem {
   }
 };
 
+// Register-resident c2r of half-lines (N2 > 0): thread t of a line packs
+// Z[k] = A + iB (c2r_pack's algebra) for its own k = t + P a straight from
+// the spectrum in global memory, runs xlines' two steps and writes the real
+// line (x = 2m, 2m+1) to Rout.
+template <class T, int N2>
+EP_DEV void x_inverse_reg(const C2<T>* __restrict__ spec, long long line0, int nlv, int nl, int nx, int nxh,
+                          const XSmem<T>& S, T scale, T* Rout) {
+  constexpr int P = XShape<N2>::P, E = XShape<N2>::E, LPW = 32 / P, Q = P + 1;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  const int t = lane % P, lsub = lane / P;
+  const C2<T>* tw = S.tw;
+  for (int base = warp * LPW; base < nl; base += nw * LPW) {
+    const int l = base + lsub;
+    const bool act = l < nlv;
+    const C2<T>* X = spec + (line0 + (act ? l : 0)) * nxh;
+    C2<T> v[E];
+#pragma unroll
+    for (int a = 0; a < E; ++a) {
+      const int k = t + P * a;
+      const C2<T> xk = act ? X[k] : cmk<T>(T(0), T(0));
+      const C2<T> xc = act ? conjg(X[N2 - k]) : cmk<T>(T(0), T(0));
+      const C2<T> A = xk + xc;
+      const C2<T> B = cmulc(xk - xc, tw[k]);
+      v[a] = A + mul_i(B);
+    }
+    epfft::dft<T, E, +1>(v);
+    if (t != 0) {
+#pragma unroll
+      for (int ka = 1; ka < E; ++ka) v[ka] = cmulc(v[ka], S.twt[ka * P + t]);
+    }
+    C2<T>* row = S.P + (l < nl ? l : 0) * S.ld;
+    __syncwarp();
+    if (l < nl) {
+#pragma unroll
+      for (int ka = 0; ka < E; ++ka) row[ka * Q + t] = v[ka];
+    }
+    __syncwarp();
+#pragma unroll
+    for (int j = 0; j < E / P; ++j) {
+      C2<T> u[P];
+#pragma unroll
+      for (int tt = 0; tt < P; ++tt) u[tt] = row[(t + P * j) * Q + tt];
+      epfft::dft<T, P, +1>(u);
+#pragma unroll
+      for (int kt = 0; kt < P; ++kt) v[j + (E / P) * kt] = u[kt];
+    }
+    __syncwarp();
+    if (l < nl) {
+#pragma unroll
+      for (int m = 0; m < E; ++m) {
+        const int i = t + P * m;
+        Rout[l * nx + 2 * i] = v[m].x * scale;
+        Rout[l * nx + 2 * i + 1] = v[m].y * scale;
+      }
+    }
+  }
+  __syncthreads();
+}
+
 template <class T, int N2>
 EP_DEV void x_inverse(const C2<T>* __restrict__ spec, long long line0, int nlv, int nl, int nx, int nxh,
                       const XSmem<T>& S, const FftPlan& p2, T scale, T* Rout) {
+  if constexpr (N2 != 0) {
+    x_inverse_reg<T, N2>(spec, line0, nlv, nl, nx, nxh, S, scale, Rout);
+    return;
+  }
   const int n2 = nx / 2, ld = S.ld;
   C2<T>* P = S.P;
   C2<T>* Q = S.Q;
@@ -413,9 +476,91 @@ EP_DEV void x_inverse(const C2<T>* __restrict__ spec, long long line0, int nlv, 
   __syncthreads();
 }
 
+// Register-resident r2c of half-lines (N2 > 0): thread t packs its own
+// z[m] = val(2m) + i val(2m+1), m = t + P a, runs xlines' two steps, fetches
+// the partner Z[N2 - k] of each of its outputs with a warp shuffle (lane
+// P - t, register E - 1 - m; thread 0 holds its own partners) and writes
+// r2c_unpack's X[k] straight to global memory (thread 0 also X[N2]).
+template <class T, int N2, class F>
+EP_DEV void x_forward_reg(F val, C2<T>* __restrict__ out, long long line0, int nlv, int nl, int nxh,
+                          const XSmem<T>& S) {
+  constexpr int P = XShape<N2>::P, E = XShape<N2>::E, LPW = 32 / P, Q = P + 1;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  const int t = lane % P, lsub = lane / P;
+  const int plane = lane - t + (P - t) % P;
+  const C2<T>* tw = S.tw;
+  for (int base = warp * LPW; base < nl; base += nw * LPW) {
+    const int l = base + lsub;
+    const bool act = l < nlv;
+    C2<T> v[E];
+#pragma unroll
+    for (int a = 0; a < E; ++a) {
+      const int m = t + P * a;
+      v[a] = act ? cmk<T>(val(l, 2 * m), val(l, 2 * m + 1)) : cmk<T>(T(0), T(0));
+    }
+    epfft::dft<T, E, -1>(v);
+    if (t != 0) {
+#pragma unroll
+      for (int ka = 1; ka < E; ++ka) v[ka] = cmul(v[ka], S.twt[ka * P + t]);
+    }
+    C2<T>* row = S.P + (l < nl ? l : 0) * S.ld;
+    __syncwarp();
+    if (l < nl) {
+#pragma unroll
+      for (int ka = 0; ka < E; ++ka) row[ka * Q + t] = v[ka];
+    }
+    __syncwarp();
+#pragma unroll
+    for (int j = 0; j < E / P; ++j) {
+      C2<T> u[P];
+#pragma unroll
+      for (int tt = 0; tt < P; ++tt) u[tt] = row[(t + P * j) * Q + tt];
+      epfft::dft<T, P, -1>(u);
+#pragma unroll
+      for (int kt = 0; kt < P; ++kt) v[j + (E / P) * kt] = u[kt];
+    }
+    __syncwarp();
+    // v[m] = Z[t + P m]; w[m] = Z[(N2 - t - P m) mod N2]
+    C2<T> w[E];
+#pragma unroll
+    for (int j = 0; j < E; ++j) {
+      C2<T> u;
+      u.x = __shfl_sync(0xffffffffu, v[j].x, plane);
+      u.y = __shfl_sync(0xffffffffu, v[j].y, plane);
+      w[E - 1 - j] = u;
+    }
+    if (t == 0) {
+#pragma unroll
+      for (int m = 0; m < E; ++m) w[m] = v[(E - m) % E];
+    }
+    if (act) {
+      C2<T>* o = out + (line0 + l) * nxh;
+#pragma unroll
+      for (int m = 0; m < E; ++m) {
+        const int k = t + P * m;
+        const C2<T> zk = v[m], zc = conjg(w[m]);
+        const C2<T> e = epfft::K<T>::half * (zk + zc);
+        const C2<T> od = epfft::K<T>::half * mul_mi(zk - zc);
+        o[k] = e + cmul(tw[k], od);
+      }
+      if (t == 0) {
+        const C2<T> zk = v[0], zc = conjg(v[0]);
+        const C2<T> e = epfft::K<T>::half * (zk + zc);
+        const C2<T> od = epfft::K<T>::half * mul_mi(zk - zc);
+        o[N2] = e + cmul(tw[N2], od);
+      }
+    }
+  }
+  __syncthreads();
+}
+
 template <class T, int N2, class F>
 EP_DEV void x_forward(F val, C2<T>* __restrict__ out, long long line0, int nlv, int nl, int nx, int nxh,
                       const XSmem<T>& S, const FftPlan& p2) {
+  if constexpr (N2 != 0) {
+    x_forward_reg<T, N2>(val, out, line0, nlv, nl, nxh, S);
+    return;
+  }
   const int n2 = nx / 2, ld = S.ld;
   C2<T>* P = S.P;
   const float inv2 = 1.0f / (float)n2;
