@@ -282,7 +282,8 @@ int Engine<T>::init(const ep_config& c, cudaStream_t s, Prof* p, ImpState* im, s
   }
 #define EP_ATTR(RR)                                                                                      \
   cudaFuncSetAttribute(k_predict<T, RR>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)march_smem<T, RR, 4, 2>()); \
-  cudaFuncSetAttribute(k_correct<T, RR>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)march_smem<T, RR, 5, 2>());
+  cudaFuncSetAttribute(k_correct<T, RR, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)march_smem<T, RR, 5, 2>()); \
+  cudaFuncSetAttribute(k_correct<T, RR, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)march_smem<T, RR, 5, 2>());
   EP_ATTR(1) EP_ATTR(2) EP_ATTR(3) EP_ATTR(4) EP_ATTR(5) EP_ATTR(6)
 #undef EP_ATTR
   {
@@ -291,7 +292,7 @@ int Engine<T>::init(const ep_config& c, cudaStream_t s, Prof* p, ImpState* im, s
     const int nt = EP_TX * EP_TY;
 #define EP_OCC(RR)                                                                                         \
   case RR:                                                                                                 \
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_pc, k_correct<T, RR>, nt, march_smem<T, RR, 5, 2>()); \
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_pc, k_correct<T, RR, true>, nt, march_smem<T, RR, 5, 2>()); \
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_rk, k_rkstage<T, RR>, nt, 0);                       \
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_d1, k_d1march<T, RR, 0>, nt, 0);                    \
     break;
@@ -703,7 +704,6 @@ int Engine<T>::lap_predict(double dt) {
 
 template <class T>
 int Engine<T>::lap_correct(double dt, bool want) {
-  (void)want;
   const double c9 = 9.0 / 121.0;
   const CT* po3 = po[ioldp[2]];
   const CT* po2 = po[ioldp[1]];
@@ -722,8 +722,11 @@ int Engine<T>::lap_correct(double dt, bool want) {
                   &pc, &spare, &den, &f3, &cc,   &partials, &sc,   &renorm, &n4, &sl};
   const void* fn = nullptr;
   size_t smem = 0;
-#define EP_CORR(RR) \
-  case RR: fn = (const void*)k_correct<T, RR>; smem = march_smem<T, RR, 5, 2>(); break;
+#define EP_CORR(RR)                                                                                   \
+  case RR:                                                                                            \
+    fn = want ? (const void*)k_correct<T, RR, true> : (const void*)k_correct<T, RR, false>;           \
+    smem = march_smem<T, RR, 5, 2>();                                                                 \
+    break;
   switch (fd.R) {
     EP_CORR(1) EP_CORR(2) EP_CORR(3) EP_CORR(4) EP_CORR(5) EP_CORR(6)
     default: *err = "npd > 13 not built"; return EP_ERR_UNSUPPORTED;

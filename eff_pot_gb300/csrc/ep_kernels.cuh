@@ -161,7 +161,7 @@ EP_DEV void neu_add_d(double& s, double& c, double v) {
 // threads -> sc->sums[out0 + q]; mode 1: corrector epilogue (norm, mu,
 // renormalisation factor), mode 2: norm only.
 EP_DEV void finalize_block(const double* partials, int nblocks, int nq, DevScalars* sc, int out0, int mode,
-                           double N, double dxyz, double n4, int renorm) {
+                           double N, double dxyz, double n4, int renorm, int stats = 1) {
   __shared__ double ss[256];
   const int tid = threadIdx.x + blockDim.x * threadIdx.y;
   const int nth = blockDim.x * blockDim.y;
@@ -185,8 +185,10 @@ EP_DEV void finalize_block(const double* partials, int nblocks, int nq, DevScala
     if (mode == 1) {
       const double norm = sc->sums[out0 + 1] * dxyz;
       sc->norm = norm;
-      sc->mu = sc->sums[out0 + 2] / sc->sums[out0 + 3];
-      sc->errHe = sc->sums[out0] / N;
+      if (stats) {
+        sc->mu = sc->sums[out0 + 2] / sc->sums[out0 + 3];
+        sc->errHe = sc->sums[out0] / N;
+      }
       sc->scale = (renorm && norm > 0.0) ? sqrt(n4 / norm) : 1.0;
     } else if (mode == 2) {
       const double norm = sc->sums[out0] * dxyz;
@@ -1240,7 +1242,7 @@ __global__ void __launch_bounds__(EP_TX* EP_TY, sizeof(T) == 4 ? 4 : 2) k_predic
 // Corrector + final value of steppc.f90:135-151 with fused reductions:
 // sum |pc|, sum |psi|^2 (new), <psi|H|psi> and sum |psi|^2 of the modified
 // psi (chemical potential).
-template <class T, int R>
+template <class T, int R, bool STATS>
 __global__ void __launch_bounds__(EP_TX* EP_TY, sizeof(T) == 4 ? 3 : 2) k_correct(Geo g, FdW<T> fd, Phys ph, int zc,
                                                          const C2<T>* __restrict__ psi, const T* __restrict__ pot4,
                                                          const T* __restrict__ uimp,
@@ -1269,10 +1271,12 @@ __global__ void __launch_bounds__(EP_TX* EP_TY, sizeof(T) == 4 ? 3 : 2) k_correc
     out[p] = po;
     const T dn = po.x * po.x + po.y * po.y;
     den[p] = dn;
-    acc[0].add(sqrt(pcn.x * pcn.x + pcn.y * pcn.y));
     acc[1].add(dn);
-    acc[2].add(hexp_t<T>(ph, c, H));
-    acc[3].add(c.x * c.x + c.y * c.y);
+    if (STATS) {  // errHe and mu are read only when the caller asks for them
+      acc[0].add(sqrt(pcn.x * pcn.x + pcn.y * pcn.y));
+      acc[2].add(hexp_t<T>(ph, c, H));
+      acc[3].add(c.x * c.x + c.y * c.y);
+    }
   });
   block_reduce_store_acc<4>(acc, partials);
   // The last block to finish sums all partials (no block waits for another).
@@ -1286,7 +1290,7 @@ __global__ void __launch_bounds__(EP_TX* EP_TY, sizeof(T) == 4 ? 3 : 2) k_correc
   __syncthreads();
   if (last) {
     __threadfence();
-    finalize_block(partials, (int)nb, 4, sc, 0, 1, (double)g.N, ph.dxyz, n4, renorm);
+    finalize_block(partials, (int)nb, 4, sc, 0, 1, (double)g.N, ph.dxyz, n4, renorm, STATS ? 1 : 0);
     if (tid == 0) {
       // renormalise lazily: every logical state value is multiplied by s;
       // the buffers written here restart their scale at s
