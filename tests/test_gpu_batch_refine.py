@@ -185,3 +185,27 @@ def test_batch_step_graphs_match_direct_launches():
         assert np.array_equal(a, c)
     assert res[0][1] == res[1][1]
     assert res[0][2] == res[1][2]
+
+
+@pytest.mark.parametrize("n", [64, 128])
+def test_fp32_fields_track_fp64_at_production_sizes(n):
+    """At the grids of the benchmark configurations the FP32 path (register
+    FFTs in every direction) gives the mean-field potential and the energies
+    of the FP64 path to FP32 accuracy."""
+    xmax = 0.2 * n
+    psi = ep.woods_saxon_psi(n, n, n, xmax, xmax, xmax, 1000.0, seed=11)
+    fields = ("pot4", "dencg", "delj4", "ualphas", "intxalf")
+    res = {}
+    for prec in (_abi.EP_FP64, _abi.EP_FP32):
+        cfg = cfg_of(n=n, xmax=xmax, n4=1000.0, precision=prec)
+        with ep.Solver(cfg) as s:
+            prepare(s, psi, (0.0, 0.0, 1.0))
+            e = s.energy()
+            res[prec] = ({f: s.field(f) for f in fields}, e)
+    f64, e64 = res[_abi.EP_FP64]
+    f32, e32 = res[_abi.EP_FP32]
+    for f in fields:
+        scale = np.abs(f64[f]).max()
+        assert np.abs(f32[f] - f64[f]).max() < 2e-5 * scale, f
+    for k in ("etot", "ekin4", "elj4", "ecor4", "ealphas", "eHeX"):
+        assert abs(e32[k] - e64[k]) < 2e-5 * abs(e64["etot"]), k
