@@ -94,7 +94,7 @@ ep_potential potential_of(const Input& in, const char* which, const char* dflt_s
   ep_potential p{};
   p.r_cutoff = in.get<double>((std::string("r_cutoff_") + which).c_str(), dflt_rc);
   p.umax = in.get<double>((std::string("umax_") + which).c_str(), dflt_umax);
-  if (sel == "null") {
+  if (sel == "null" || sel == "table") {  // 'table': tabulated by pair_tables below
     p.kind = EP_POT_NULL;
   } else if (sel == "Morse" || sel == "morse") {
     p.kind = EP_POT_MORSE;
@@ -103,9 +103,73 @@ ep_potential potential_of(const Input& in, const char* which, const char* dflt_s
     p.par[2] = in.get<double>("morse_alpha", 1.2);
   } else {
     stop("selec_" + std::string(which) + "='" + sel +
-         "': this potential of Select_Pot is not tabulated by this driver (use 'null' or 'Morse')");
+         "': this potential of Select_Pot is not built into this driver (use 'null', 'Morse' or 'table' with "
+         "table_" + std::string(which) + " = a file of r (A), V (K) rows)");
   }
   return p;
+}
+
+// A pair potential given as a file of (r [A], V [K]) rows (comment lines
+// starting with '#'), evaluated as Select_Pot does: umax inside r_cutoff,
+// else the linear interpolant of the rows (the first / last value beyond
+// them).
+struct PairTable {
+  std::vector<double> r, v;
+  double r_cutoff = 0, umax = 0;
+  double operator()(double x) const {
+    if (x < r_cutoff) return umax;
+    if (x <= r.front()) return v.front();
+    if (x >= r.back()) return v.back();
+    const size_t j = std::upper_bound(r.begin(), r.end(), x) - r.begin();
+    const double f = (x - r[j - 1]) / (r[j] - r[j - 1]);
+    return v[j - 1] + f * (v[j] - v[j - 1]);
+  }
+};
+
+PairTable read_pair_table(const Input& in, const char* which) {
+  const std::string fn = trim(in.get<std::string>((std::string("table_") + which).c_str(), ""));
+  if (fn.empty()) stop(std::string("selec_") + which + "='table' needs table_" + which + " = a file name");
+  std::ifstream f(fn);
+  if (!f) stop("cannot open the potential table '" + fn + "'");
+  PairTable t;
+  t.r_cutoff = in.get<double>((std::string("r_cutoff_") + which).c_str(), 0.0);
+  t.umax = in.get<double>((std::string("umax_") + which).c_str(), 0.0);
+  fio::ListReader rd(f);
+  rd.skip_comments('#');
+  double a, b;
+  while (rd.real(a) && rd.real(b)) {
+    if (!t.r.empty() && !(a > t.r.back())) stop("potential table '" + fn + "': r must increase");
+    t.r.push_back(a);
+    t.v.push_back(b);
+  }
+  if (t.r.size() < 2) stop("potential table '" + fn + "' has fewer than two rows");
+  return t;
+}
+
+// potenimpini (potenimpini.f90:12-55) for tabulated pi / sigma channels:
+// V_Pi and V_Sigma - V_Pi on r_i = (i-1) rmax/(npot-1), npot = 100 max(n)+1,
+// rmax = 4 max(xmax, ymax, zmax), ends repeated.
+bool pair_tables(const Input& in, const ep_config& cfg, ep_ctx* ctx) {
+  const bool tpi = trim(in.get<std::string>("selec_pi", "")) == "table";
+  const bool tsg = trim(in.get<std::string>("selec_sigma", "")) == "table";
+  if (!tpi && !tsg) return false;
+  if (!(tpi && tsg)) stop("selec_pi and selec_sigma must both be 'table' when one is");
+  const PairTable vp = read_pair_table(in, "pi"), vs = read_pair_table(in, "sigma");
+  const int npot = 100 * std::max(cfg.nx, std::max(cfg.ny, cfg.nz)) + 1;
+  const double rmax = 4.0 * std::max(cfg.xmax, std::max(cfg.ymax, cfg.zmax));
+  const double del = rmax / (double)(npot - 1);
+  std::vector<double> tp(npot + 2), td(npot + 2);
+  for (int i = 1; i <= npot; ++i) {
+    const double r = (double)(i - 1) * del;
+    tp[i] = vp(r);
+    td[i] = vs(r) - tp[i];
+  }
+  tp[0] = tp[1];
+  tp[npot + 1] = tp[npot];
+  td[0] = td[1];
+  td[npot + 1] = td[npot];
+  check(ep_set_impurity_tables(ctx, tp.data(), td.data(), npot, del, vs.umax), ctx, "impurity tables");
+  return true;
 }
 
 // Echo of the namelist as read (DFT4He3d.f90:164-166).
@@ -465,6 +529,7 @@ int main(int argc, char** argv) {
     const ep_potential psg = potential_of(in, "sigma", "Ba_plus_2D0", 1.05, 9.674836e4);
     const ep_potential ppl = potential_of(in, "plus", "Ba_plus_2D2", 1.05, 6.260015e4);
     check(ep_set_impurity_potentials(ctx, &ppi, &psg, &ppl), ctx, "impurity potentials");
+    pair_tables(in, cfg, ctx);
 
     if (!scan.empty()) {
       // loop.sh + get_impurity_energy.sh in one job: every file's first energy
@@ -523,6 +588,7 @@ int main(int argc, char** argv) {
       ctx = nullptr;
       check(ep_create(&cfg, &ctx), nullptr, "ep_create");
       check(ep_set_impurity_potentials(ctx, &ppi, &psg, &ppl), ctx, "impurity potentials");
+    pair_tables(in, cfg, ctx);
       check(ep_upload_psi(ctx, keep.data()), ctx, "upload psi");
       check(ep_set_impurity_state(ctx, s.rimp, s.vimp, s.invar.data()), ctx, "impurity state");
       check(ep_potenimp(ctx), ctx, "potenimp");

@@ -245,3 +245,26 @@ def test_p_state_instate_matches_the_api(tmp_path):
             assert abs(float(v) - e[k]) < 2e-6, (instate, k, v, e[k])
         assert abs(eso - e["eso"]) < 2e-6
         assert abs(e["eso"] - 5.0 * (-1.0 if instate == 0 else 0.5)) < 0.3  # j = 1/2 vs 3/2 level
+
+
+def test_tabulated_pair_potentials_equal_the_formula(tmp_path):
+    """selec_* = 'table' with (r, V) files on potenimpini's knots gives the
+    energies of the same potential selected by name."""
+    psi = ep.woods_saxon_psi(N, N, N, XMAX, XMAX, XMAX, N4, seed=8)
+    write_density(tmp_path / "in.dat", np.abs(psi) ** 2, (0.2, 0.1, 0.4))
+    (tmp_path / "invar.dat").write_text("\n".join(["(0.d0,0.d0)"] * 10) + "\n")
+    npot = 100 * N + 1
+    dr = 4.0 * XMAX / (npot - 1)
+    r = np.arange(npot) * dr
+    v = 10.0 * (1.0 - np.exp(-1.2 * (r - 4.5))) ** 2 - 10.0
+    with open(tmp_path / "morse.tab", "w") as f:
+        f.write("# r (A)  V (K)\n")
+        for a, b in zip(r, v):
+            f.write(f"{a:.17E} {b:.17E}\n")
+    by_name = balance(run_driver(tmp_path, namelist(0, ", instate=5")))
+    tab = namelist(0, ", instate=5, selec_pi='table', selec_sigma='table', table_pi='morse.tab', "
+                      "table_sigma='morse.tab'")
+    by_table = balance(run_driver(tmp_path, tab))
+    for k in by_name:
+        assert abs(float(by_name[k]) - float(by_table[k])) <= 2e-6, (k, by_name[k], by_table[k])
+    assert abs(float(by_table["eHeX"])) > 1.0  # the impurity field is not trivial
