@@ -178,3 +178,24 @@ def test_nonfinite_input_is_reported_not_trapped(oracle):
         with pytest.raises(ep.EffPotError) as ei:
             g.steprk(1e-3)
         assert ei.value.status == 5
+
+
+def test_fp64_path_matches_the_committed_golden_vectors():
+    """The FP64 GPU path against the oracle's committed golden vectors of a
+    short OTC evolution (no oracle at run time)."""
+    import importlib.util
+    import json
+    import os
+    here = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
+    spec = importlib.util.spec_from_file_location("mk", os.path.join(here, "make_oracle_fixture.py"))
+    mk = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(mk)
+    want = json.load(open(os.path.join(here, "oracle_otc_32.json")))
+    got = mk.scenario(ep.Solver)
+    for part in ("start", "after"):
+        for k in ("etot", "etot4", "ekin4", "elj4", "ecor4", "ealphas", "eHeX"):
+            assert abs(got[part][k] - want[part][k]) <= 1e-10 * abs(want["start"]["etot4"]), (part, k)
+    assert abs(got["mu"] - want["mu"]) <= 1e-10 * abs(want["mu"])
+    for k in ("norm", "den_sum", "den_sq"):
+        assert abs(got[k] - want[k]) <= 1e-10 * abs(want[k]), k
+    assert np.allclose(got["den_samples"], want["den_samples"], rtol=0, atol=1e-9)

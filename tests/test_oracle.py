@@ -189,3 +189,24 @@ def test_imaginary_time_lowers_the_energy(oracle):
             energies.append(s.energy()["etot"])
         assert energies[0] < e0
         assert all(b < a for a, b in zip(energies, energies[1:]))
+
+
+def test_oracle_reproduces_its_golden_vectors(oracle):
+    """The committed golden vectors of a short OTC evolution
+    (tests/golden/make_oracle_fixture.py) pin the oracle against regressions."""
+    import importlib.util
+    import json
+    import os
+    here = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
+    spec = importlib.util.spec_from_file_location("mk", os.path.join(here, "make_oracle_fixture.py"))
+    mk = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(mk)
+    want = json.load(open(os.path.join(here, "oracle_otc_32.json")))
+    got = mk.scenario(oracle.OracleSolver)
+    for part in ("start", "after"):
+        for k, v in want[part].items():
+            assert abs(got[part][k] - v) <= 1e-11 * max(1.0, abs(v)), (part, k, got[part][k], v)
+    for k in ("mu", "norm", "den_sum", "den_sq", "den_xmom"):
+        assert abs(got[k] - want[k]) <= 1e-11 * max(1e-12, abs(want[k])), k
+    assert abs(got["errHe"] - want["errHe"]) <= 1e-9 * abs(want["errHe"])
+    assert np.allclose(got["den_samples"], want["den_samples"], rtol=1e-11, atol=1e-18)
