@@ -244,6 +244,10 @@ int ep_create(const ep_config* cfg, ep_ctx** out) {
   if (c.npd < 3 || c.npd > 25 || c.npd % 2 == 0) { g_create_error = "npd must be odd, 3..25"; return EP_ERR_INVALID_ARG; }
   if (c.npd > 13) { g_create_error = "stencils wider than 13 points are not built"; return EP_ERR_UNSUPPORTED; }
   if (c.nx < c.npd || c.ny < c.npd || c.nz < c.npd) { g_create_error = "grid smaller than the stencil"; return EP_ERR_BAD_GRID; }
+  if ((long long)c.nx * c.ny >= (1LL << 21)) {
+    g_create_error = "x-y planes of 2^21 points or more are not supported";
+    return EP_ERR_UNSUPPORTED;
+  }
   if (c.icon != EP_ICON_PERIODIC && c.icon != EP_ICON_ZERO_OUTSIDE) {
     g_create_error = "icon must be 8 (periodic) or 13 (zero outside)";
     return EP_ERR_UNSUPPORTED;

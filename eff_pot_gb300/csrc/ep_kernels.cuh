@@ -1213,16 +1213,19 @@ __global__ void __launch_bounds__(EP_TX* EP_TY, sizeof(T) == 4 ? 4 : 2) k_predic
   extern __shared__ __align__(16) unsigned char smraw[];
   constexpr int NT = EP_TX * EP_TY;
   const HCoef<T> hc(ph);
-  const T s3 = (T)sc->bscale[sl.a], s1 = (T)sc->bscale[sl.h1], s2 = (T)sc->bscale[sl.h2],
-          sp_ = (T)sc->bscale[sl.pc];
+  // buffer scales folded into the method's coefficients once per thread:
+  // pp = s3 po3 + f (2 H - s1 h1 + 2 s2 h2), pn = pp - c112 sp pc
+  const double f_ = (double)f;
+  const T s3 = (T)sc->bscale[sl.a], k2f = (T)(2.0 * f_), kh1 = (T)(f_ * sc->bscale[sl.h1]),
+          kh2 = (T)(2.0 * f_ * sc->bscale[sl.h2]), kpc = (T)((double)c112 * sc->bscale[sl.pc]);
   const C2<T>* cin[4] = {po3, h1, h2, pc};
   const T* rin[2] = {pot4, uimp};
   lap_march_async<T, R, 4, 2>(
       g, psi, fd, zc, smraw, cin, rin, (T)sc->bscale[sl.psi],
       [&](long long p, C2<T> c, C2<T> lap, const C2<T>* ic, const T* ir) {
         const C2<T> H = happly<T>(hc, lap, c, ir[0], ir[NT]);
-        const C2<T> pp = s3 * ic[0] + f * ((T(2) * H - s1 * ic[NT]) + T(2) * (s2 * ic[2 * NT]));
-        const C2<T> pn = pp - c112 * (sp_ * ic[3 * NT]);
+        const C2<T> pp = ((s3 * ic[0] + k2f * H) - kh1 * ic[NT]) + kh2 * ic[2 * NT];
+        const C2<T> pn = pp - kpc * ic[3 * NT];
         po3[p] = pn;
         pc[p] = pp;
         h2[p] = H;
@@ -1257,14 +1260,18 @@ __global__ void __launch_bounds__(EP_TX* EP_TY, sizeof(T) == 4 ? 3 : 2) k_correc
   constexpr int NT = EP_TX * EP_TY;
   const HCoef<T> hc(ph);
   Acc<T> acc[4];
-  const T s3 = (T)sc->bscale[sl.a], s2o = (T)sc->bscale[sl.b], s1 = (T)sc->bscale[sl.h1],
-          s2 = (T)sc->bscale[sl.h2], sp_ = (T)sc->bscale[sl.pc];
+  // buffer scales folded into the method's coefficients once per thread:
+  // p5 = (9 s3 po3 - s2o po2 + f3 (H + 2 s1 h1 - s2 h2)) / 8
+  const double f3_ = (double)f3;
+  const T k3 = (T)(1.125 * sc->bscale[sl.a]), k2o = (T)(0.125 * sc->bscale[sl.b]), kH = (T)(0.125 * f3_),
+          k1 = (T)(0.25 * f3_ * sc->bscale[sl.h1]), k2 = (T)(0.125 * f3_ * sc->bscale[sl.h2]),
+          sp_ = (T)sc->bscale[sl.pc];
   const C2<T>* cin[5] = {po3, po2, h1, h2, pc};
   const T* rin[2] = {pot4, uimp};
   lap_march_async<T, R, 5, 2>(g, psi, fd, zc, smraw, cin, rin, (T)sc->bscale[sl.psi],
                               [&](long long p, C2<T> c, C2<T> lap, const C2<T>* ic, const T* ir) {
     const C2<T> H = happly<T>(hc, lap, c, ir[0], ir[NT]);
-    const C2<T> p5 = T(0.125) * ((T(9) * (s3 * ic[0]) - s2o * ic[NT]) + f3 * ((H + T(2) * (s1 * ic[2 * NT])) - s2 * ic[3 * NT]));
+    const C2<T> p5 = (((k3 * ic[0] - k2o * ic[NT]) + kH * H) + k1 * ic[2 * NT]) - k2 * ic[3 * NT];
     const C2<T> pcn = sp_ * ic[4 * NT] - p5;
     pc[p] = pcn;
     const C2<T> po = p5 + c9 * pcn;
