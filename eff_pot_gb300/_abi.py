@@ -17,12 +17,13 @@ EP_IMAGINARY_TIME, EP_REAL_TIME = 0, 1
 EP_IMPURITY_NONE, EP_IMPURITY_FIXED, EP_IMPURITY_MOVING = 0, 1, 2
 EP_FP64, EP_FP32 = 0, 1
 EP_ICON_PERIODIC, EP_ICON_ZERO_OUTSIDE = 8, 13
+EP_STATE_P, EP_STATE_D = 0, 1
 EP_POT_NULL, EP_POT_MORSE = 0, 1
 
 FIELDS = {
     "den": 0, "pot4": 1, "uimp": 2, "dencg": 3, "delj4": 4, "dxden": 5,
     "dyden": 6, "dzden": 7, "falfs": 8, "intxalf": 9, "intyalf": 10,
-    "intzalf": 11, "ualphas": 12, "vpi": 13, "delta": 14,
+    "intzalf": 11, "ualphas": 12, "vpi": 13, "delta": 14, "sigdel": 15,
 }
 CFIELDS = {
     "psi": 0, "psiold1": 1, "psiold2": 2, "psiold3": 3, "hpsiold1": 4,
@@ -46,6 +47,7 @@ class EpConfig(C.Structure):
         ("als_p", C.c_double), ("ev0", C.c_double),
         ("z_exciplex_exclusion", C.c_double),
         ("precision", C.c_int), ("device", C.c_int),
+        ("state", C.c_int), ("als_d", C.c_double),
     ]
 
 
@@ -82,6 +84,10 @@ _prototypes = {
     "last_error": (C.c_char_p, [_P]),
     "set_impurity_potentials": (_I, [_P, C.POINTER(EpPotential), C.POINTER(EpPotential), C.POINTER(EpPotential)]),
     "set_impurity_tables": (_I, [_P, _D, _D, _I, C.c_double, C.c_double]),
+    "set_impurity_potentials_d": (_I, [_P, C.POINTER(EpPotential), C.POINTER(EpPotential),
+                                       C.POINTER(EpPotential), C.POINTER(EpPotential)]),
+    "set_impurity_tables_d": (_I, [_P, _D, _D, _D, _I, C.c_double, C.c_double, C.c_double]),
+    "impurity_matrix_d": (_I, [_P, _D]),
     "set_impurity_state": (_I, [_P, _D, _D, _D]),
     "get_impurity_state": (_I, [_P, _D, _D, _D, _D]),
     "upload_psi": (_I, [_P, _D]),

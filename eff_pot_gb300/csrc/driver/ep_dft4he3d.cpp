@@ -22,12 +22,13 @@
 // those scripts assemble (time, X-He centre-of-mass distance, Ekin(X), U*,
 // U+, E_SO per file).
 //
-// P-state internal variables (instate 0..2) are built as instates.f90 does
-// in its default branch (ep_instates.h); Lexcite_state_fix gives its fixed
-// vectors, instate 5 reads invar.dat.  Not built here (listed as next): the
-// D states and the Ldiag_jz / Laverage_P_value / Lmixture / exciplex
-// variants of instates.f90, and the tabulated Select_Pot potentials other
-// than 'null' (V_impur.f90:87-932).
+// The internal variables of the P (instate 0..2) and D (Lstate = 'D',
+// instate 0..4) states are built as instates.f90 does in its default branch
+// (ep_instates.h); Lexcite_state_fix gives the fixed P vectors, instate 5
+// reads invar.dat.  Not built here: the Ldiag_jz / Laverage_P_value /
+// Lmixture / exciplex variants of instates.f90, and the Select_Pot closed
+// forms other than 'null' and 'Morse' (V_impur.f90:87-932; any of them runs
+// as selec_* = 'table' from a file of (r, V) rows).
 #include <cmath>
 #include <complex>
 #include <cstdio>
@@ -152,12 +153,33 @@ PairTable read_pair_table(const Input& in, const char* which) {
 bool pair_tables(const Input& in, const ep_config& cfg, ep_ctx* ctx) {
   const bool tpi = trim(in.get<std::string>("selec_pi", "")) == "table";
   const bool tsg = trim(in.get<std::string>("selec_sigma", "")) == "table";
-  if (!tpi && !tsg) return false;
-  if (!(tpi && tsg)) stop("selec_pi and selec_sigma must both be 'table' when one is");
+  const bool dst = cfg.state == EP_STATE_D;
+  const bool tdl = dst && trim(in.get<std::string>("selec_delta", "")) == "table";
+  if (!tpi && !tsg && !tdl) return false;
+  if (!(tpi && tsg && (tdl || !dst)))
+    stop(dst ? "selec_pi, selec_sigma and selec_delta must all be 'table' when one is"
+             : "selec_pi and selec_sigma must both be 'table' when one is");
   const PairTable vp = read_pair_table(in, "pi"), vs = read_pair_table(in, "sigma");
   const int npot = 100 * std::max(cfg.nx, std::max(cfg.ny, cfg.nz)) + 1;
   const double rmax = 4.0 * std::max(cfg.xmax, std::max(cfg.ymax, cfg.zmax));
   const double del = rmax / (double)(npot - 1);
+  if (dst) {  // potenimpini.f90:28-50: V_Delta, V_Pi - V_Delta, V_Sigma - V_Delta
+    const PairTable vd = read_pair_table(in, "delta");
+    std::vector<double> td(npot + 2), tpd(npot + 2), tsd(npot + 2);
+    for (int i = 1; i <= npot; ++i) {
+      const double r = (double)(i - 1) * del;
+      td[i] = vd(r);
+      tpd[i] = vp(r) - td[i];
+      tsd[i] = vs(r) - td[i];
+    }
+    for (std::vector<double>* t : {&td, &tpd, &tsd}) {
+      (*t)[0] = (*t)[1];
+      (*t)[npot + 1] = (*t)[npot];
+    }
+    check(ep_set_impurity_tables_d(ctx, td.data(), tpd.data(), tsd.data(), npot, del, vp.umax, vs.umax), ctx,
+          "impurity tables");
+    return true;
+  }
   std::vector<double> tp(npot + 2), td(npot + 2);
   for (int i = 1; i <= npot; ++i) {
     const double r = (double)(i - 1) * del;
@@ -192,6 +214,7 @@ struct State {
   bool have_invar = false;
   double time_ps = 0.0;                       // from the file's comment lines
   int p_instate = -1;                         // P state to build from the field moments
+  int d_instate = -1;                         // D state to build from the field matrix
   double auxn4 = 0, xc = 0, yc = 0, zc = 0;   // helium number and centre of mass
 };
 
@@ -280,7 +303,12 @@ void prepare_invar(const Input& in, State& s) {
   }
   if (instate > 5) stop("instate value invalid " + std::to_string(instate));
   const std::string lstate = trim(in.get<std::string>("lstate", "P"));
-  if (lstate != "P") stop("Lstate='" + lstate + "': the D-state internal variables are not built in this driver");
+  if (lstate == "D") {  // instates.f90:440-647, default branch
+    if (in.get<bool>("ldiag_jz", false)) stop("ldiag_jz: this instates.f90 variant is not built in this driver");
+    s.d_instate = (int)instate;
+    return;
+  }
+  if (lstate != "P") stop("Lstate='" + lstate + "' is neither 'P' nor 'D'");
   if (in.get<bool>("lexcite_state_fix", false) && instate <= 2) {  // fixed P states, instates.f90:300-320
     std::fill(s.invar.begin(), s.invar.end(), 0.0);
     const int n = (int)instate + 1;
@@ -297,6 +325,14 @@ void prepare_invar(const Input& in, State& s) {
 // density give the 6x6 V + (Als/2) SO; its pair of eigenvectors selected by
 // instate gives invar, then the impurity field is recomputed with it.
 void build_p_state(ep_ctx* ctx, const ep_config& cfg, State& s) {
+  if (s.d_instate >= 0) {  // D state: the 5x5 field matrix, MatDSO, instate's pair
+    double M[25];
+    check(ep_impurity_matrix_d(ctx, M), ctx, "impurity matrix");
+    instates::d_state(M, cfg.als_d, s.d_instate, s.invar.data());
+    check(ep_set_impurity_state(ctx, s.rimp, s.vimp, s.invar.data()), ctx, "impurity state");
+    check(ep_potenimp(ctx), ctx, "potenimp");
+    return;
+  }
   if (s.p_instate < 0) return;
   double m[6];
   check(ep_impurity_moments(ctx, m), ctx, "impurity moments");
@@ -514,6 +550,12 @@ int main(int argc, char** argv) {
     cfg.mimpur = in.get<double>("mimpur", cfg.mimpur);
     cfg.fix_lambda = in.get<bool>("lfix_lambda", false) ? 1 : 0;
     cfg.als_p = in.get<double>("als_p", 0.0);
+    cfg.als_d = in.get<double>("als_d", 0.0);
+    {
+      const std::string ls = trim(in.get<std::string>("lstate", "P"));
+      if (ls != "P" && ls != "D") stop("Lstate='" + ls + "' is neither 'P' nor 'D'");
+      cfg.state = ls == "D" ? EP_STATE_D : EP_STATE_P;
+    }
     cfg.ev0 = in.get<double>("ev0", 0.0);
     cfg.z_exciplex_exclusion = in.get<double>("z_exciplex_exclusion", cfg.z_exciplex_exclusion);
     cfg.impurity = EP_IMPURITY_MOVING;
@@ -528,8 +570,16 @@ int main(int argc, char** argv) {
     const ep_potential ppi = potential_of(in, "pi", "Ba_plus_2D1", 1.05, 5.216077e4);
     const ep_potential psg = potential_of(in, "sigma", "Ba_plus_2D0", 1.05, 9.674836e4);
     const ep_potential ppl = potential_of(in, "plus", "Ba_plus_2D2", 1.05, 6.260015e4);
-    check(ep_set_impurity_potentials(ctx, &ppi, &psg, &ppl), ctx, "impurity potentials");
-    pair_tables(in, cfg, ctx);
+    const ep_potential pdl = cfg.state == EP_STATE_D ? potential_of(in, "delta", "Ba_plus_2D2", 1.05, 6.260015e4)
+                                                     : ep_potential{};
+    auto set_potentials = [&](ep_ctx* x) {
+      if (cfg.state == EP_STATE_D)
+        check(ep_set_impurity_potentials_d(x, &ppi, &psg, &pdl, &ppl), x, "impurity potentials");
+      else
+        check(ep_set_impurity_potentials(x, &ppi, &psg, &ppl), x, "impurity potentials");
+      pair_tables(in, cfg, x);
+    };
+    set_potentials(ctx);
 
     if (!scan.empty()) {
       // loop.sh + get_impurity_energy.sh in one job: every file's first energy
@@ -587,8 +637,7 @@ int main(int argc, char** argv) {
       check(ep_destroy(ctx), nullptr, "ep_destroy");
       ctx = nullptr;
       check(ep_create(&cfg, &ctx), nullptr, "ep_create");
-      check(ep_set_impurity_potentials(ctx, &ppi, &psg, &ppl), ctx, "impurity potentials");
-    pair_tables(in, cfg, ctx);
+      set_potentials(ctx);
       check(ep_upload_psi(ctx, keep.data()), ctx, "upload psi");
       check(ep_set_impurity_state(ctx, s.rimp, s.vimp, s.invar.data()), ctx, "impurity state");
       check(ep_potenimp(ctx), ctx, "potenimp");

@@ -1,5 +1,5 @@
-// ep_instates.h - the P-state internal variables of instates.f90 (Lstate
-// 'P', the default branch): the 6x6 matrix V + (Als/2) SO over
+// ep_instates.h - the internal variables of instates.f90 (default branch).
+// P state (Lstate 'P'): the 6x6 matrix V + (Als/2) SO over
 // (p_x up, p_x down, p_y up, p_y down, p_z up, p_z down) built from the
 // density-weighted moments of the impurity field (instates.f90:123-193), its
 // eigenvectors in ascending order of the eigenvalues, and the state
@@ -13,6 +13,8 @@
 #include <cmath>
 #include <complex>
 #include <vector>
+
+#include "../ep_dstate.h"
 
 namespace instates {
 
@@ -109,6 +111,29 @@ inline void p_state(const double* moments, double als, int instate, double* inva
   for (int i = 0; i < 10; ++i) invar[2 * i] = invar[2 * i + 1] = 0.0;
   for (int i = 0; i < 6; ++i) {
     const cd z = r * v[(size_t)i * 6 + il] + r * v[(size_t)i * 6 + il1];
+    invar[2 * i] = z.real();
+    invar[2 * i + 1] = z.imag();
+  }
+}
+
+// D state (instates.f90:440-612, default branch :642-647): MatDSO over the
+// ten internal variables from the 5x5 density-weighted field matrix M
+// (ep_impurity_matrix_d), its eigenvectors ascending, and
+//   invar = (v_il + v_il+1) / sqrt(2),  il = 2 * instate (0-based, instate 0..4).
+// Kramers pairs again make the choice of basis inside a pair immaterial.
+inline void d_state(const double* M, double als_d, int instate, double* invar) {
+  cd S[10][10];
+  dstate::sod(S);
+  std::vector<cd> A(100);
+  for (int i = 0; i < 10; ++i)
+    for (int j = 0; j < 10; ++j) A[(size_t)i * 10 + j] = dstate::matdso(M, S, als_d, i, j);
+  std::vector<double> w;
+  std::vector<cd> v;
+  hermitian_eigen(10, A, w, v);
+  const int il = 2 * instate, il1 = il + 1;
+  const double r = 1.0 / std::sqrt(2.0);
+  for (int i = 0; i < 10; ++i) {
+    const cd z = r * v[(size_t)i * 10 + il] + r * v[(size_t)i * 10 + il1];
     invar[2 * i] = z.real();
     invar[2 * i + 1] = z.imag();
   }

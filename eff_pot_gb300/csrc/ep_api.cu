@@ -227,6 +227,8 @@ int ep_config_init(ep_config* c) {
   c->z_exciplex_exclusion = 0.0;
   c->precision = EP_FP64;
   c->device = 0;
+  c->state = EP_STATE_P;
+  c->als_d = 0.0;
   return EP_OK;
 }
 
@@ -244,10 +246,6 @@ int ep_create(const ep_config* cfg, ep_ctx** out) {
   if (c.npd < 3 || c.npd > 25 || c.npd % 2 == 0) { g_create_error = "npd must be odd, 3..25"; return EP_ERR_INVALID_ARG; }
   if (c.npd > 13) { g_create_error = "stencils wider than 13 points are not built"; return EP_ERR_UNSUPPORTED; }
   if (c.nx < c.npd || c.ny < c.npd || c.nz < c.npd) { g_create_error = "grid smaller than the stencil"; return EP_ERR_BAD_GRID; }
-  if ((long long)c.nx * c.ny >= (1LL << 21)) {
-    g_create_error = "x-y planes of 2^21 points or more are not supported";
-    return EP_ERR_UNSUPPORTED;
-  }
   if (c.icon != EP_ICON_PERIODIC && c.icon != EP_ICON_ZERO_OUTSIDE) {
     g_create_error = "icon must be 8 (periodic) or 13 (zero outside)";
     return EP_ERR_UNSUPPORTED;
@@ -258,6 +256,7 @@ int ep_create(const ep_config* cfg, ep_ctx** out) {
     return EP_ERR_INVALID_ARG;
   }
   if (c.precision != EP_FP64 && c.precision != EP_FP32) { g_create_error = "unknown precision"; return EP_ERR_INVALID_ARG; }
+  if (c.state != EP_STATE_P && c.state != EP_STATE_D) { g_create_error = "state must be P or D"; return EP_ERR_INVALID_ARG; }
   int ndev = 0;
   if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) {
     cudaGetLastError();
@@ -300,6 +299,7 @@ int ep_destroy(ep_ctx* c) {
   if (c->e32) { c->e32->release(); delete c->e32; }
   if (c->imp.d_potpi) cudaFree(c->imp.d_potpi);
   if (c->imp.d_potdel) cudaFree(c->imp.d_potdel);
+  if (c->imp.d_potsigdel) cudaFree(c->imp.d_potsigdel);
   c->prof.release();
   for (cudaEvent_t e : c->ev)
     if (e) cudaEventDestroy(e);
@@ -313,6 +313,7 @@ const char* ep_last_error(const ep_ctx* c) { return c ? c->err.c_str() : "null c
 // potenimpini (potenimpini.f90:11-58), P state.
 int ep_set_impurity_potentials(ep_ctx* c, const ep_potential* pi, const ep_potential* sigma, const ep_potential* plus) {
   if (!c || !pi || !sigma) return EP_ERR_INVALID_ARG;
+  if (c->cfg.state != EP_STATE_P) return fail(c, EP_ERR_STATE, "D state: use ep_set_impurity_potentials_d");
   const ep_config& g = c->cfg;
   const int npot = 100 * std::max(g.nx, std::max(g.ny, g.nz)) + 1;
   const double rmax = 4.0 * std::max(g.xmax, std::max(g.ymax, g.zmax));
@@ -330,23 +331,79 @@ int ep_set_impurity_potentials(ep_ctx* c, const ep_potential* pi, const ep_poten
   return ep_set_impurity_tables(c, tp.data(), td.data(), npot, del, sigma->umax);
 }
 
+// Replaces the device tables (d_potpi, d_potdel, d_potsigdel) by tabs[0..2]
+// (NULL: none) of npot + 2 entries each.
+static int upload_tables(ep_ctx* c, const double* const tabs[3], int npot) {
+  cudaSetDevice(c->cfg.device);
+  double** dst[3] = {&c->imp.d_potpi, &c->imp.d_potdel, &c->imp.d_potsigdel};
+  for (double** d : dst) {
+    if (*d) cudaFree(*d);
+    *d = nullptr;
+  }
+  c->imp.have_tables = false;
+  const size_t n = (size_t)(npot + 2) * sizeof(double);
+  for (int i = 0; i < 3; ++i) {
+    if (!tabs[i]) continue;
+    if (cudaMalloc((void**)dst[i], n) != cudaSuccess) {
+      cudaGetLastError();
+      *dst[i] = nullptr;
+      return fail(c, EP_ERR_OOM, "table allocation failed");
+    }
+    cudaMemcpyAsync(*dst[i], tabs[i], n, cudaMemcpyHostToDevice, c->st);
+  }
+  if (cudaStreamSynchronize(c->st) != cudaSuccess) return fail(c, EP_ERR_CUDA, "table upload failed");
+  return EP_OK;
+}
+
 int ep_set_impurity_tables(ep_ctx* c, const double* potpi, const double* potdel, int npot, double delinter,
                            double umax_sigma) {
   if (!c || !potpi || !potdel || npot < 3 || !(delinter > 0)) return EP_ERR_INVALID_ARG;
-  cudaSetDevice(c->cfg.device);
-  if (c->imp.d_potpi) cudaFree(c->imp.d_potpi);
-  if (c->imp.d_potdel) cudaFree(c->imp.d_potdel);
-  c->imp.d_potpi = c->imp.d_potdel = nullptr;
-  const size_t n = (size_t)(npot + 2) * sizeof(double);
-  if (cudaMalloc((void**)&c->imp.d_potpi, n) != cudaSuccess || cudaMalloc((void**)&c->imp.d_potdel, n) != cudaSuccess) {
-    cudaGetLastError();
-    return fail(c, EP_ERR_OOM, "table allocation failed");
-  }
-  cudaMemcpyAsync(c->imp.d_potpi, potpi, n, cudaMemcpyHostToDevice, c->st);
-  cudaMemcpyAsync(c->imp.d_potdel, potdel, n, cudaMemcpyHostToDevice, c->st);
-  if (cudaStreamSynchronize(c->st) != cudaSuccess) return fail(c, EP_ERR_CUDA, "table upload failed");
+  if (c->cfg.state != EP_STATE_P) return fail(c, EP_ERR_STATE, "D state: use ep_set_impurity_tables_d");
+  const double* tabs[3] = {potpi, potdel, nullptr};
+  int r = upload_tables(c, tabs, npot);
+  if (r) return r;
   c->imp.npot = npot;
   c->imp.delinter = delinter;
+  c->imp.umax_sigma = umax_sigma;
+  c->imp.have_tables = true;
+  return EP_OK;
+}
+
+// potenimpini.f90:28-50, D state: V_Delta, V_Pi - V_Delta, V_Sigma - V_Delta
+// on r_i = (i-1)*delinter, end points repeated.
+int ep_set_impurity_potentials_d(ep_ctx* c, const ep_potential* pi, const ep_potential* sigma,
+                                 const ep_potential* delta, const ep_potential* plus) {
+  if (!c || !pi || !sigma || !delta) return EP_ERR_INVALID_ARG;
+  if (c->cfg.state != EP_STATE_D) return fail(c, EP_ERR_STATE, "D-state potentials need state = EP_STATE_D");
+  const ep_config& g = c->cfg;
+  const int npot = 100 * std::max(g.nx, std::max(g.ny, g.nz)) + 1;
+  const double rmax = 4.0 * std::max(g.xmax, std::max(g.ymax, g.zmax));
+  const double del = rmax / (double)(npot - 1);
+  std::vector<double> td(npot + 2), tpd(npot + 2), tsd(npot + 2);
+  for (int i = 1; i <= npot; ++i) {
+    const double r = (double)(i - 1) * del;
+    const double aux = select_pot(*delta, r);
+    td[i] = aux;
+    tpd[i] = select_pot(*pi, r) - aux;
+    tsd[i] = select_pot(*sigma, r) - aux;
+  }
+  td[0] = td[1]; td[npot + 1] = td[npot];
+  tpd[0] = tpd[1]; tpd[npot + 1] = tpd[npot];
+  tsd[0] = tsd[1]; tsd[npot + 1] = tsd[npot];
+  if (plus) c->imp.plus = *plus;
+  return ep_set_impurity_tables_d(c, td.data(), tpd.data(), tsd.data(), npot, del, pi->umax, sigma->umax);
+}
+
+int ep_set_impurity_tables_d(ep_ctx* c, const double* potdel, const double* potpidel, const double* potsigdel,
+                             int npot, double delinter, double umax_pi, double umax_sigma) {
+  if (!c || !potdel || !potpidel || !potsigdel || npot < 3 || !(delinter > 0)) return EP_ERR_INVALID_ARG;
+  if (c->cfg.state != EP_STATE_D) return fail(c, EP_ERR_STATE, "D-state tables need state = EP_STATE_D");
+  const double* tabs[3] = {potpidel, potdel, potsigdel};
+  int r = upload_tables(c, tabs, npot);
+  if (r) return r;
+  c->imp.npot = npot;
+  c->imp.delinter = delinter;
+  c->imp.umax_pi = umax_pi;
   c->imp.umax_sigma = umax_sigma;
   c->imp.have_tables = true;
   return EP_OK;
@@ -433,6 +490,17 @@ int ep_impurity_moments(ep_ctx* c, double* v6) {
     int r = e.ensure_materialized();
     if (!r) r = e.forceimp(F);
     if (!r) r = e.moments(v6);
+    return r;
+  });
+}
+
+int ep_impurity_matrix_d(ep_ctx* c, double* m25) {
+  if (!m25) return EP_ERR_INVALID_ARG;
+  return dispatch(c, [&](auto& e) -> int {
+    double F[3];
+    int r = e.ensure_materialized();
+    if (!r) r = e.forceimp(F);
+    if (!r) r = e.matrix_d(m25);
     return r;
   });
 }

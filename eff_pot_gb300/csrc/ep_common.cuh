@@ -38,7 +38,7 @@ template <class T2> EP_HD T2 mul_mi(T2 a) { T2 r; r.x = a.y; r.y = -a.x; return 
 // Device-side scalar block shared by all kernels of a context.  Reductions
 // are accumulated in FP64 whatever the field precision.
 struct DevScalars {
-  double sums[32];      // finalize outputs (named by the producing kernel)
+  double sums[40];      // finalize outputs (named by the producing kernel)
   double scale;         // pending imaginary-time renormalisation factor
   double errHe, norm, mu;
   unsigned int flags;   // bit 0: non-finite detected; bit 1: den <= 0

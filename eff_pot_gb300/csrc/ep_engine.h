@@ -40,10 +40,13 @@ struct ImpState {
   double pcr[3] = {0, 0, 0}, pcv[3] = {0, 0, 0};
   std::complex<double> qiv[10], invarold[10][3], hinvarold[10][2], pciv[10];
   // interpolation tables (module interpol), FP64 on the device
+  // P state: d_potpi = V_Pi, d_potdel = V_Sigma - V_Pi.  D state:
+  // d_potdel = V_Delta, d_potpi = V_Pi - V_Delta, d_potsigdel = V_Sigma - V_Delta.
   int npot = 0;
-  double delinter = 0, umax_sigma = 9.674836e3;
+  double delinter = 0, umax_sigma = 9.674836e3, umax_pi = 0.0;
   double* d_potpi = nullptr;
   double* d_potdel = nullptr;
+  double* d_potsigdel = nullptr;
   ep_potential plus{};
   bool have_tables = false;
 };
@@ -71,8 +74,10 @@ class Engine {
   int dev_sm = 0;
   int zc_pc = 16, zc_rk = 16, zc_d1 = 16;  // z planes per CTA of the stencil marches
   T* dyz = nullptr;                         // dy(gy) + dz(gz) of term_alfa
+  T* sigdel = nullptr;                      // Sig_Del of the D state (vpi holds Pi_Del)
   int d1march(int mode, const T* f, const T* f2, T* o0, T* o1, T* o2);
   int moments(double* v6);
+  int matrix_d(double* m25);
   // Step graphs (CUDA-graph replay of steppc): while capturing, cap_nodes
   // receives the predictor / corrector nodes; while replaying, upd_exec is the
   // executable graph whose nodes lap_predict / lap_correct update.

@@ -4,6 +4,7 @@
 #include <cmath>
 #include <cstring>
 
+#include "ep_dstate.h"
 #include "ep_engine.h"
 #include "ep_kernels_impl.cuh"
 #include "ep_rfft.cuh"
@@ -194,6 +195,7 @@ int Engine<T>::init(const ep_config& c, cudaStream_t s, Prof* p, ImpState* im, s
   T** rbufs[] = {&den, &pot4, &uimp, &dencg, &delj4, &dxd, &dyd, &dzd, &falfs, &intx, &inty, &intz,
                  &ualphas, &gy, &gz, &dgx, &vpi, &delta, &dyz};
   for (T** b : rbufs) if ((r = alloc((void**)b, N * sizeof(T)))) return r;
+  if (c.state == EP_STATE_D && (r = alloc((void**)&sigdel, N * sizeof(T)))) return r;
   for (int i = 0; i < 4; ++i) {
     if ((r = alloc((void**)&S[i], Nh * sizeof(CT)))) return r;
     if ((r = alloc((void**)&Tb[i], Nh * sizeof(CT)))) return r;
@@ -306,7 +308,7 @@ int Engine<T>::init(const ep_config& c, cudaStream_t s, Prof* p, ImpState* im, s
     const long long nxy = (long long)((c.nx + EP_TX - 1) / EP_TX) * ((c.ny + EP_TY - 1) / EP_TY);
     const int zmin = std::min(zc_pc, zc_rk);
     const long long nbs = nxy * ((c.nz + zmin - 1) / zmin);
-    npartials = std::max(nbs * 4, (long long)EP_RED_BLOCKS * 9);
+    npartials = std::max(nbs * 4, (long long)EP_RED_BLOCKS * 18);
     if ((r = alloc((void**)&partials, npartials * sizeof(double)))) return r;
   }
   return cuda_ok(cudaStreamSynchronize(st), "init");
@@ -323,9 +325,10 @@ template <class T>
 void Engine<T>::release() {
   void* bufs[] = {psi, spare, po[0], po[1], po[2], ph[0], ph[1], pc, q, den, pot4, uimp, dencg, delj4, dxd, dyd,
                   dzd, falfs, intx, inty, intz, ualphas, gy, gz, dgx, vpi, delta, dyz, S[0], S[1], S[2], S[3], Tb[0],
-                  Tb[1], Tb[2], Tb[3], fvlj4, wcgk, kalfs, twx, twy, twz, partials, sc};
+                  Tb[1], Tb[2], Tb[3], fvlj4, wcgk, kalfs, twx, twy, twz, partials, sc, sigdel};
   for (void* b : bufs)
     if (b) cudaFree(b);
+  sigdel = nullptr;
   psi = nullptr;
   bytes = 0;
 }
@@ -506,6 +509,22 @@ int Engine<T>::potenimp() {
     return EP_ERR_STATE;
   }
   const double rmax = (imp->npot - 1) * imp->delinter;
+  if (cfg.state == EP_STATE_D) {
+    // Re G_ij of the internal variables for the per-point quadratic form
+    DGram G{};
+    int k = 0;
+    for (int i = 0; i < 5; ++i)
+      for (int j = i; j < 5; ++j, ++k) {
+        const std::complex<double> gij = std::conj(imp->invar[2 * i]) * imp->invar[2 * j] +
+                                         std::conj(imp->invar[2 * i + 1]) * imp->invar[2 * j + 1];
+        G.g[k] = (i == j ? 1.0 : 2.0) * gij.real();
+      }
+    auto kd = k_potenimp_d<T>;
+    EP_LAUNCH("potenimp", kd, 4 * 152, 256, 0, g, cfg.xmax, cfg.ymax, cfg.zmax, hx, hy, hz, imp->rimp[0],
+              imp->rimp[1], imp->rimp[2], imp->d_potdel, imp->d_potpi, imp->d_potsigdel, imp->npot, rmax,
+              imp->umax_pi, imp->umax_sigma, G, delta, vpi, sigdel, uimp);
+    return EP_OK;
+  }
   double2 iv[6];
   for (int i = 0; i < 6; ++i) iv[i] = make_double2(imp->invar[i].real(), imp->invar[i].imag());
   auto k = k_potenimp<T>;
@@ -559,8 +578,21 @@ int Engine<T>::energy(ep_energies* e) {
   const std::complex<double>* iv = imp->invar;
   std::complex<double> ivs[10];
   for (int i = 0; i < 10; ++i) ivs[i] = std::conj(iv[i]);
-  e->eso = 0.5 * c.als_p * (2.0 * (ivs[0] * iv[5] - ivs[1] * iv[4]).real() +
-                            2.0 * (ivs[0] * iv[2] + ivs[3] * iv[1] + ivs[2] * iv[5] + ivs[3] * iv[4]).imag());
+  if (c.state == EP_STATE_D) {
+    // energy.f90:176-190: Als_D * 0.5 * sum_i conj(iv_i) (SOD iv)_i
+    std::complex<double> S[10][10];
+    dstate::sod(S);
+    std::complex<double> vls = 0.0;
+    for (int i = 0; i < 10; ++i) {
+      std::complex<double> t = 0.0;
+      for (int j = 0; j < 10; ++j) t += S[i][j] * iv[j];
+      vls += t * ivs[i];
+    }
+    e->eso = (0.5 * vls * c.als_d).real();
+  } else {
+    e->eso = 0.5 * c.als_p * (2.0 * (ivs[0] * iv[5] - ivs[1] * iv[4]).real() +
+                              2.0 * (ivs[0] * iv[2] + ivs[3] * iv[1] + ivs[2] * iv[5] + ivs[3] * iv[4]).imag());
+  }
   e->eimpu = e->ekinx + e->eHeX + e->eso;
   e->etot = e->etot4 + e->eimpu;
   e->n4 = s[7] * dxyz;
@@ -569,6 +601,17 @@ int Engine<T>::energy(ep_energies* e) {
 
 template <class T>
 int Engine<T>::forceimp(double* F) {
+  if (cfg.state == EP_STATE_D) {
+    auto kd = k_impmoments_d<T>;
+    EP_LAUNCH("impmoments", kd, EP_RED_BLOCKS, 256, 0, g, den, dxd, dyd, dzd, uimp, delta, vpi, sigdel, cfg.xmax,
+              cfg.ymax, cfg.zmax, hx, hy, hz, imp->rimp[0], imp->rimp[1], imp->rimp[2], partials);
+    int r;
+    if ((r = reduce_finalize(EP_RED_BLOCKS, 18, 16, 0))) return r;
+    double s[3];
+    if ((r = read_sums(s, 3, 16))) return r;
+    for (int i = 0; i < 3; ++i) F[i] = -s[i] * dxyz;
+    return EP_OK;
+  }
   auto k = k_impmoments<T>;
   EP_LAUNCH("impmoments", k, EP_RED_BLOCKS, 256, 0, g, den, dxd, dyd, dzd, uimp, vpi, delta, cfg.xmax, cfg.ymax,
             cfg.zmax, hx, hy, hz, imp->rimp[0], imp->rimp[1], imp->rimp[2], partials);
@@ -584,6 +627,7 @@ int Engine<T>::forceimp(double* F) {
 // by the last forceimp() call.
 template <class T>
 int Engine<T>::moments(double* v6) {
+  if (cfg.state != EP_STATE_P) { *err = "the six moments belong to the P state"; return EP_ERR_STATE; }
   double s[9];
   int r;
   if ((r = read_sums(s, 9, 16))) return r;
@@ -596,16 +640,46 @@ int Engine<T>::moments(double* v6) {
   return EP_OK;
 }
 
-// potinvar, P state (potenimp.f90:298-330, 487-492), from the moments left
-// by the last forceimp() call.
+// D state: the 5x5 matrix (MP + MS + sumVdel) dxyz of potinvar /
+// instates, from the sums left by the last forceimp() call.
+template <class T>
+int Engine<T>::matrix_d(double* m25) {
+  if (cfg.state != EP_STATE_D) { *err = "the D-state matrix needs state = EP_STATE_D"; return EP_ERR_STATE; }
+  double s[18];
+  int r;
+  if ((r = read_sums(s, 18, 16))) return r;
+  int k = 3;
+  for (int i = 0; i < 5; ++i)
+    for (int j = i; j < 5; ++j, ++k) m25[5 * i + j] = m25[5 * j + i] = s[k] * dxyz;
+  return EP_OK;
+}
+
+// potinvar (potenimp.f90:261-492), from the sums left by the last forceimp()
+// call.  D state: Hiv = (M (x) 1_2 + Als_D/2 SOD) iv; P state: the six
+// moments and the 6x6 spin-orbit block.  Then -i (Hiv - Ev0 iv).
 template <class T>
 int Engine<T>::potinvar(std::complex<double>* Hiv) {
+  const std::complex<double> uim(0.0, 1.0);
+  if (cfg.state == EP_STATE_D) {
+    double M[25];
+    int r;
+    if ((r = matrix_d(M))) return r;
+    std::complex<double> S[10][10];
+    dstate::sod(S);
+    const std::complex<double>* iv = imp->invar;
+    for (int i = 0; i < 10; ++i) {
+      std::complex<double> h = 0.0;
+      for (int j = 0; j < 10; ++j) h += dstate::matdso(M, S, cfg.als_d, i, j) * iv[j];
+      Hiv[i] = h;
+    }
+    for (int i = 0; i < 10; ++i) Hiv[i] = -uim * (Hiv[i] - cfg.ev0 * iv[i]);
+    return EP_OK;
+  }
   double s[9];
   int r;
   if ((r = read_sums(s, 9, 16))) return r;
   const double uxx = s[3], uxy = s[4], uxz = s[5], uyy = s[6], uyz = s[7], uzz = s[8];
   const std::complex<double>* iv = imp->invar;
-  const std::complex<double> uim(0.0, 1.0);
   const double A = cfg.als_p / 2.0;
   Hiv[0] = (uxx * iv[0] + uxy * iv[2] + uxz * iv[4]) * dxyz + A * (-uim * iv[2] + iv[5]);
   Hiv[1] = (uxx * iv[1] + uxy * iv[3] + uxz * iv[5]) * dxyz + A * (uim * iv[3] - iv[4]);
@@ -906,11 +980,13 @@ int Engine<T>::steppc(double dt, ep_step_errors* e) {
       std::complex<double> auxc[10];
       for (int k = 0; k < 10; ++k)
         auxc[k] = 0.125 * (9.0 * m.invarold[k][i3] - m.invarold[k][i2] + 3.0 * dt * (m.hinvar[k] + 2.0 * m.hinvarold[k][h1] - m.hinvarold[k][h2]));
-      for (int k = 0; k < 6; ++k) m.pciv[k] = m.pciv[k] - auxc[k];
+      // steppc.f90:199-217: P corrects components 1-6 (7-10 zeroed), D all ten
+      const int nc = cfg.state == EP_STATE_D ? 10 : 6;
+      for (int k = 0; k < nc; ++k) m.pciv[k] = m.pciv[k] - auxc[k];
       for (int k = 0; k < 10; ++k) m.invar[k] = 0.0;
-      for (int k = 0; k < 6; ++k) m.invar[k] = auxc[k] + c9 * m.pciv[k];
-      for (int k = 0; k < 6; ++k) erriv += std::abs(c9 * m.pciv[k]);
-      erriv *= 0.1666666666666;
+      for (int k = 0; k < nc; ++k) m.invar[k] = auxc[k] + c9 * m.pciv[k];
+      for (int k = 0; k < nc; ++k) erriv += std::abs(c9 * m.pciv[k]);
+      erriv *= nc == 10 ? 0.1 : 0.1666666666666;
     }
     { const int t = m.ioldv[2]; m.ioldv[2] = m.ioldv[1]; m.ioldv[1] = m.ioldv[0]; m.ioldv[0] = t; }
     { const int t = m.ioldiv[2]; m.ioldiv[2] = m.ioldiv[1]; m.ioldiv[1] = m.ioldiv[0]; m.ioldiv[0] = t; }
@@ -1037,6 +1113,10 @@ int Engine<T>::download_r(int which, double* h) {
     case EP_FIELD_UALPHAS: src = ualphas; break;
     case EP_FIELD_VPI: src = vpi; break;
     case EP_FIELD_DELTA: src = delta; break;
+    case EP_FIELD_SIGDEL:
+      if (!sigdel) { *err = "SIGDEL exists in the D state only"; return EP_ERR_INVALID_ARG; }
+      src = sigdel;
+      break;
     default: *err = "unknown field"; return EP_ERR_INVALID_ARG;
   }
   int r;
@@ -1100,6 +1180,10 @@ int Engine<T>::import_state(const Engine<U>& o) {
   for (int i = 0; i < 15; ++i) {
     auto k = k_convert<U, T>;
     EP_LAUNCH("convert", k, 4 * 152, 256, 0, rs[i], rd[i], g.N);
+  }
+  if (sigdel && o.sigdel) {
+    auto k = k_convert<U, T>;
+    EP_LAUNCH("convert", k, 4 * 152, 256, 0, o.sigdel, sigdel, g.N);
   }
   for (int i = 0; i < 3; ++i) ioldp[i] = o.ioldp[i];
   for (int i = 0; i < 2; ++i) ioldh[i] = o.ioldh[i];

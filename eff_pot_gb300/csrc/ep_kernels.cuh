@@ -1414,6 +1414,22 @@ __global__ void k_potenimp(Geo g, double xmax, double ymax, double zmax, double 
                            double2 iv0, double2 iv1, double2 iv2, double2 iv3, double2 iv4, double2 iv5,
                            T* __restrict__ vpi, T* __restrict__ delta, T* __restrict__ uimp);
 
+// D state (potenimp.f90:47-182, 545-566): Delta = V_Delta(r),
+// Pi_Del = (V_Pi - V_Delta)(r)/r^4, Sig_Del = (V_Sigma - V_Delta)(r)/r^4 and
+// uimp = sum_ij M_ij Re G_ij, M = Delta 1 + Pi_Del d d^T + Sig_Del P(x).
+// G holds Re G_ij = Re(conj(iv_2i) iv_2j + conj(iv_2i+1) iv_2j+1) over the
+// upper triangle (1,1),(1,2),..,(1,5),(2,2),..,(5,5), off-diagonal doubled.
+struct DGram {
+  double g[15];
+};
+template <class T>
+__global__ void k_potenimp_d(Geo g, double xmax, double ymax, double zmax, double hx, double hy, double hz,
+                             double r0, double r1, double r2, const double* __restrict__ potdel,
+                             const double* __restrict__ potpidel, const double* __restrict__ potsigdel, int npot,
+                             double rmax, double umax_pi, double umax_sigma, const __grid_constant__ DGram G,
+                             T* __restrict__ delta, T* __restrict__ pidel, T* __restrict__ sigdel,
+                             T* __restrict__ uimp);
+
 // Energy integrals of energy.f90:47-165 (8 sums, see the launcher).
 struct PotDev {
   int kind;
@@ -1435,6 +1451,16 @@ __global__ void k_impmoments(Geo g, const T* __restrict__ den, const T* __restri
                              const T* __restrict__ vpi, const T* __restrict__ delta, double xmax, double ymax,
                              double zmax, double hx, double hy, double hz, double r0, double r1, double r2,
                              double* __restrict__ partials);
+
+// forceimp sums + the D-state matrix (potenimp.f90:331-405): 3 + 15 sums,
+// the matrix's upper triangle in DGram's order.
+template <class T>
+__global__ void k_impmoments_d(Geo g, const T* __restrict__ den, const T* __restrict__ dxd,
+                               const T* __restrict__ dyd, const T* __restrict__ dzd, const T* __restrict__ uimp,
+                               const T* __restrict__ delta, const T* __restrict__ pidel,
+                               const T* __restrict__ sigdel, double xmax, double ymax, double zmax, double hx,
+                               double hy, double hz, double r0, double r1, double r2,
+                               double* __restrict__ partials);
 
 // Form factors on the device (fforma.f90:11-60, initcg.f90:314-331,
 // DFT4He3d.f90:396-400), FP64 evaluation, stored in T.

@@ -66,6 +66,108 @@ __global__ void k_potenimp(Geo g, double xmax, double ymax, double zmax, double 
   }
 }
 
+// D-state angular factors at x = r - rimp (potenimp.f90:68-117): the d
+// harmonics a = (d1..d5) and the upper triangle of P in DGram's order.
+EP_DEV void dstate_factors(double xx, double yy, double zz, double (&a)[5], double (&P)[15]) {
+  const double sqr3 = sqrt(3.0), sqr3o2 = sqrt(3.0) / 2.0, insqr3 = 1.0 / sqrt(3.0), in3 = 1.0 / 3.0;
+  const double d0 = xx * xx + yy * yy + zz * zz;
+  const double d1 = sqr3 * xx * yy, d2 = sqr3 * yy * zz, d3 = (-xx * xx - yy * yy + 2.0 * zz * zz) / 2.0;
+  const double d4 = sqr3 * xx * zz, d5 = sqr3o2 * (xx * xx - yy * yy);
+  a[0] = d1; a[1] = d2; a[2] = d3; a[3] = d4; a[4] = d5;
+  const double sd1 = d1 * d1, sd2 = d2 * d2, sd4 = d4 * d4, sd5 = d5 * d5;
+  const double s35 = d3 + insqr3 * d5, f35 = d3 - insqr3 * d5;
+  P[0] = in3 * (sd2 + sd4 + 4.0 * sd5);                 // (1,1)
+  P[1] = -4.0 * in3 * d1 * d2 + insqr3 * d4 * d0;       // (1,2)
+  P[2] = -2.0 * insqr3 * d2 * d4;                       // (1,3)
+  P[3] = -4.0 * in3 * d1 * d4 + insqr3 * d2 * d0;       // (1,4)
+  P[4] = -4.0 * in3 * d1 * d5;                          // (1,5)
+  P[5] = in3 * (sd1 + sd4) + s35 * s35;                 // (2,2)
+  P[6] = insqr3 * d1 * d4 - d2 * s35;                   // (2,3)
+  P[7] = -4.0 * in3 * d2 * d4 + insqr3 * d1 * d0;       // (2,4)
+  P[8] = -d1 * d4 - insqr3 * d2 * s35;                  // (2,5)
+  P[9] = sd4 + sd2;                                     // (3,3)
+  P[10] = insqr3 * d1 * d2 - d4 * f35;                  // (3,4)
+  P[11] = insqr3 * (sd2 - sd4);                         // (3,5)
+  P[12] = in3 * (sd1 + sd2) + f35 * f35;                // (4,4)
+  P[13] = d1 * d2 + insqr3 * d4 * f35;                  // (4,5)
+  P[14] = in3 * (sd2 + sd4 + 4.0 * sd1);                // (5,5)
+}
+
+template <class T>
+__global__ void k_potenimp_d(Geo g, double xmax, double ymax, double zmax, double hx, double hy, double hz,
+                             double r0, double r1, double r2, const double* __restrict__ potdel,
+                             const double* __restrict__ potpidel, const double* __restrict__ potsigdel, int npot,
+                             double rmax, double umax_pi, double umax_sigma, const __grid_constant__ DGram G,
+                             T* __restrict__ delta, T* __restrict__ pidel, T* __restrict__ sigdel,
+                             T* __restrict__ uimp) {
+  const double gtr = G.g[0] + G.g[5] + G.g[9] + G.g[12] + G.g[14];
+  for (long long p = blockIdx.x * (long long)blockDim.x + threadIdx.x; p < g.N; p += (long long)gridDim.x * blockDim.x) {
+    int ix, iy, iz;
+    idx3(g, p, ix, iy, iz);
+    const double xx = coord(xmax, hx, ix) - r0;
+    const double yy = coord(ymax, hy, iy) - r1;
+    const double zz = coord(zmax, hz, iz) - r2;
+    const double zt = zz * zz;
+    const double yt = yy * yy + zt;
+    const double rr2 = xx * xx + yt;
+    const double r4 = rr2 * rr2;
+    const double r = sqrt(rr2);
+    const double dl = interp_update(r, npot, rmax, potdel);
+    double pd = umax_pi, sd = umax_sigma;
+    if (r > 1e-3) {
+      pd = interp_update(r, npot, rmax, potpidel) / r4;
+      sd = interp_update(r, npot, rmax, potsigdel) / r4;
+    }
+    double a[5], P[15];
+    dstate_factors(xx, yy, zz, a, P);
+    double qs = 0.0, qp = 0.0;
+    int k = 0;
+#pragma unroll
+    for (int i = 0; i < 5; ++i)
+#pragma unroll
+      for (int j = i; j < 5; ++j, ++k) {
+        qs += a[i] * a[j] * G.g[k];
+        qp += P[k] * G.g[k];
+      }
+    const double u = dl * gtr + pd * qs + sd * qp;
+    delta[p] = (T)dl;
+    pidel[p] = (T)pd;
+    sigdel[p] = (T)sd;
+    uimp[p] = (T)fmin(u, 1000.0);
+  }
+}
+
+template <class T>
+__global__ void k_impmoments_d(Geo g, const T* __restrict__ den, const T* __restrict__ dxd,
+                               const T* __restrict__ dyd, const T* __restrict__ dzd, const T* __restrict__ uimp,
+                               const T* __restrict__ delta, const T* __restrict__ pidel,
+                               const T* __restrict__ sigdel, double xmax, double ymax, double zmax, double hx,
+                               double hy, double hz, double r0, double r1, double r2,
+                               double* __restrict__ partials) {
+  double acc[18];
+#pragma unroll
+  for (int q = 0; q < 18; ++q) acc[q] = 0.0;
+  for (long long p = blockIdx.x * (long long)blockDim.x + threadIdx.x; p < g.N; p += (long long)gridDim.x * blockDim.x) {
+    int ix, iy, iz;
+    idx3(g, p, ix, iy, iz);
+    const double u = uimp[p];
+    acc[0] += (double)dxd[p] * u;
+    acc[1] += (double)dyd[p] * u;
+    acc[2] += (double)dzd[p] * u;
+    const double xx = coord(xmax, hx, ix) - r0, yy = coord(ymax, hy, iy) - r1, zz = coord(zmax, hz, iz) - r2;
+    const double rho = den[p];
+    const double dvd = (double)delta[p] * rho, dv1 = (double)pidel[p] * rho, dv2 = (double)sigdel[p] * rho;
+    double a[5], P[15];
+    dstate_factors(xx, yy, zz, a, P);
+    int k = 0;
+#pragma unroll
+    for (int i = 0; i < 5; ++i)
+#pragma unroll
+      for (int j = i; j < 5; ++j, ++k) acc[3 + k] += P[k] * dv2 + a[i] * a[j] * dv1 + (i == j ? dvd : 0.0);
+  }
+  block_reduce_store<18>(acc, partials);
+}
+
 // Sum of |psi|^2 (block partials).
 template <class T>
 __global__ void k_normsum(const C2<T>* __restrict__ psi, long long N, double* __restrict__ partials) {

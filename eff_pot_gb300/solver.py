@@ -142,6 +142,24 @@ class Solver:
                                             len(potpi) - 2, delinter, umax_sigma)
         self._check(st, "set_impurity_tables")
 
+    def set_impurity_potentials_d(self, pi, sigma, delta, plus=None):
+        """D state (Lstate='D'): potenimpini's three tables from V_Pi, V_Sigma, V_Delta."""
+        st = self._f["set_impurity_potentials_d"](self._h, C.byref(pi), C.byref(sigma), C.byref(delta),
+                                                  C.byref(plus) if plus is not None else None)
+        self._check(st, "set_impurity_potentials_d")
+
+    def set_impurity_tables_d(self, potdel, potpidel, potsigdel, delinter, umax_pi, umax_sigma):
+        t = [np.ascontiguousarray(a, dtype=np.float64) for a in (potdel, potpidel, potsigdel)]
+        st = self._f["set_impurity_tables_d"](self._h, *(_abi.dptr(a) for a in t), len(t[0]) - 2, delinter,
+                                              umax_pi, umax_sigma)
+        self._check(st, "set_impurity_tables_d")
+
+    def impurity_matrix_d(self):
+        """The D-state 5x5 density-weighted field matrix (potinvar / instates)."""
+        m = np.zeros(25)
+        self._check(self._f["impurity_matrix_d"](self._h, _abi.dptr(m)), "impurity_matrix_d")
+        return m.reshape(5, 5)
+
     def set_impurity(self, rimp=None, vimp=None, invar=None):
         def arr(a, n):
             if a is None:

@@ -44,6 +44,8 @@ enum { EP_IMPURITY_NONE = 0, EP_IMPURITY_FIXED = 1, EP_IMPURITY_MOVING = 2 };
 enum { EP_FP64 = 0, EP_FP32 = 1 };
 /* ---- boundary modes of the finite differences (newder.f ICON) ---------- */
 enum { EP_ICON_PERIODIC = 8, EP_ICON_ZERO_OUTSIDE = 13 };
+/* ---- electronic state of the impurity (Lstate, modules.f90:303) -------- */
+enum { EP_STATE_P = 0, EP_STATE_D = 1 };
 
 /*
  * Solver configuration.  ep_config_init() fills every field with the
@@ -73,6 +75,8 @@ typedef struct ep_config {
   double z_exciplex_exclusion;
   int precision;             /* EP_FP64 / EP_FP32                           */
   int device;                /* CUDA device ordinal                         */
+  int state;                 /* Lstate: EP_STATE_P (default) / EP_STATE_D   */
+  double als_d;              /* spin-orbit splitting, D state (Als_D)       */
 } ep_config;
 
 /* Pair potentials (a subset of the Select_Pot registry, V_impur.f90:87-932,
@@ -110,8 +114,12 @@ enum {
   EP_FIELD_DELJ4 = 4, EP_FIELD_DXDEN = 5, EP_FIELD_DYDEN = 6, EP_FIELD_DZDEN = 7,
   EP_FIELD_FALFS = 8, EP_FIELD_INTXALF = 9, EP_FIELD_INTYALF = 10,
   EP_FIELD_INTZALF = 11, EP_FIELD_UALPHAS = 12, EP_FIELD_VPI = 13,
-  EP_FIELD_DELTA = 14, EP_FIELD_COUNT = 15
+  EP_FIELD_DELTA = 14, EP_FIELD_SIGDEL = 15, EP_FIELD_COUNT = 16
 };
+/* The impurity fields by state (updatepoten, potenimp.f90:531-566):
+ *   P: VPI = V_Pi(r), DELTA = (V_Sigma - V_Pi)(r) / r^2;
+ *   D: DELTA = V_Delta(r), VPI = Pi_Del = (V_Pi - V_Delta)(r) / r^4,
+ *      SIGDEL = Sig_Del = (V_Sigma - V_Delta)(r) / r^4 (D state only). */
 /* Complex-field identifiers for ep_download_cfield. */
 enum {
   EP_CFIELD_PSI = 0, EP_CFIELD_PSIOLD1 = 1, EP_CFIELD_PSIOLD2 = 2,
@@ -144,6 +152,19 @@ int ep_set_impurity_potentials(ep_ctx* ctx, const ep_potential* pi,
 int ep_set_impurity_tables(ep_ctx* ctx, const double* potpi,
                            const double* potdel, int npot, double delinter,
                            double umax_sigma);
+/* D state (Lstate = 'D'): the three tables of potenimpini's D branch
+ * (potenimpini.f90:28-50): potdel = V_Delta, potpidel = V_Pi - V_Delta,
+ * potsigdel = V_Sigma - V_Delta at r_i = (i-1)*delinter.  umax of pi and
+ * sigma are the values updatepoten stores at r <= 1e-3 (potenimp.f90:
+ * 555-562). */
+int ep_set_impurity_potentials_d(ep_ctx* ctx, const ep_potential* pi,
+                                 const ep_potential* sigma,
+                                 const ep_potential* delta,
+                                 const ep_potential* plus);
+int ep_set_impurity_tables_d(ep_ctx* ctx, const double* potdel,
+                             const double* potpidel, const double* potsigdel,
+                             int npot, double delinter, double umax_pi,
+                             double umax_sigma);
 /* rimp(3), vimp(3) (A, A*K), invar(10) complex as 20 doubles. */
 int ep_set_impurity_state(ep_ctx* ctx, const double* rimp, const double* vimp,
                           const double* invar);
@@ -167,11 +188,17 @@ int ep_energy(ep_ctx* ctx, ep_energies* e);
  * dxyz with x = r - rimp, from the fields of the last ep_potenimp: the
  * matrix of the P-state internal variables (instates.f90:123-147). */
 int ep_impurity_moments(ep_ctx* ctx, double* v6);
+/* D state: the 5x5 matrix m25 (row-major, symmetric) of the density-
+ * weighted impurity field, sum den (Delta delta_ij + Pi_Del d_i d_j +
+ * Sig_Del P_ij) dxyz over the d harmonics d_i of x = r - rimp, from the
+ * fields of the last ep_potenimp: the MP + MS + sumVdel of potinvar and
+ * instates (potenimp.f90:331-405, instates.f90:457-534). */
+int ep_impurity_matrix_d(ep_ctx* ctx, double* m25);
 /* forceimp(rimp,F) (potenimp.f90:193-258); for a moving impurity also
  * stores aimp = F / mAg_u, as every reference call site does next
  * (DFT4He3d.f90:454-455). */
 int ep_forceimp(ep_ctx* ctx, double* F);
-/* potinvar(rimp,invar,Hinvar), P state (potenimp.f90:261-492). */
+/* potinvar(rimp,invar,Hinvar), P and D states (potenimp.f90:261-492). */
 int ep_potinvar(ep_ctx* ctx, double* hinvar);
 
 /* steprk(deltat) (steprk.f90:1-191). */

@@ -380,7 +380,7 @@ struct oc_ctx {
   std::vector<cd> psi, psiold[3], hpsiold[2], pc, q;
   std::vector<double> den, pot4, uimp, dencg, delj4, dxden, dyden, dzden;
   std::vector<double> denalf, falfs, intx, inty, intz, ualphas, penalty;
-  std::vector<double> vpi, delta;
+  std::vector<double> vpi, delta, sigdel;  // D state: vpi = Pi_Del, delta = V_Delta, sigdel = Sig_Del
   std::vector<cd> fden, wk1, wk2, wk3;
   std::vector<double> sto1, sto2, sto3, sto4, sto5, sto6;
   std::vector<cd> lap;  // sum of the three second derivatives
@@ -396,8 +396,9 @@ struct oc_ctx {
   cd qiv[10], invarold[10][3], hinvarold[10][2], pciv[10];
   // interpolation tables (module interpol)
   int npot = 0;
-  double delinter = 0, umax_sigma = 9.674836e3;
-  std::vector<double> potpi, potdel;
+  double delinter = 0, umax_sigma = 9.674836e3, umax_pi = 0.0;
+  std::vector<double> potpi, potdel;  // D state: potpi = potpidel, potdel = V_Delta
+  std::vector<double> potsigdel;      // D state only
   ep_potential pot_plus;
   bool have_tables = false;
   double last_mu = 0, last_norm = 0;
@@ -588,6 +589,7 @@ int oc_create(const ep_config* cfg, oc_ctx** out) {
                   &c->denalf, &c->falfs, &c->intx, &c->inty, &c->intz, &c->ualphas, &c->penalty,
                   &c->vpi, &c->delta, &c->sto1, &c->sto2, &c->sto3, &c->sto4, &c->sto5, &c->sto6})
     v->assign(N, 0.0);
+  if (cfg->state == EP_STATE_D) c->sigdel.assign(N, 0.0);
   c->lap.assign(N, cd(0));
   c->fden.assign(Nh, cd(0)); c->wk1.assign(Nh, cd(0)); c->wk2.assign(Nh, cd(0)); c->wk3.assign(Nh, cd(0));
   for (int i = 0; i < 3; ++i) { c->ioldp[i] = i; c->ioldr[i] = i; c->ioldv[i] = i; c->ioldiv[i] = i; }
@@ -648,11 +650,51 @@ int oc_set_impurity_potentials(oc_ctx* c, const ep_potential* pi, const ep_poten
 int oc_set_impurity_tables(oc_ctx* c, const double* potpi, const double* potdel, int npot,
                            double delinter, double umax_sigma) {
   if (!c || !potpi || !potdel || npot < 3 || !(delinter > 0)) return EP_ERR_INVALID_ARG;
+  if (c->cfg.state != EP_STATE_P) return fail(c, EP_ERR_STATE, "P-state tables need state = EP_STATE_P");
   c->npot = npot;
   c->delinter = delinter;
   c->umax_sigma = umax_sigma;
   c->potpi.assign(potpi, potpi + npot + 2);
   c->potdel.assign(potdel, potdel + npot + 2);
+  c->have_tables = true;
+  return EP_OK;
+}
+
+// potenimpini.f90:28-50, D state: potdel = V_Delta, potpidel = V_Pi - V_Delta,
+// potsigdel = V_Sigma - V_Delta, end points repeated.
+int oc_set_impurity_potentials_d(oc_ctx* c, const ep_potential* pi, const ep_potential* sigma,
+                                 const ep_potential* delta, const ep_potential* plus) {
+  if (!c || !pi || !sigma || !delta) return EP_ERR_INVALID_ARG;
+  const ep_config& g = c->cfg;
+  const int npot = 100 * std::max(g.nx, std::max(g.ny, g.nz)) + 1;
+  const double rmax = 4.0 * std::max(g.xmax, std::max(g.ymax, g.zmax));
+  const double del = rmax / (double)(npot - 1);
+  std::vector<double> td(npot + 2), tpd(npot + 2), tsd(npot + 2);
+  for (int i = 1; i <= npot; ++i) {
+    const double r = (double)(i - 1) * del;
+    const double aux = select_pot(*delta, r);
+    td[i] = aux;
+    tpd[i] = select_pot(*pi, r) - aux;
+    tsd[i] = select_pot(*sigma, r) - aux;
+  }
+  td[0] = td[1]; td[npot + 1] = td[npot];
+  tpd[0] = tpd[1]; tpd[npot + 1] = tpd[npot];
+  tsd[0] = tsd[1]; tsd[npot + 1] = tsd[npot];
+  if (plus) c->pot_plus = *plus;
+  return oc_set_impurity_tables_d(c, td.data(), tpd.data(), tsd.data(), npot, del, pi->umax, sigma->umax);
+}
+
+int oc_set_impurity_tables_d(oc_ctx* c, const double* potdel, const double* potpidel, const double* potsigdel,
+                             int npot, double delinter, double umax_pi, double umax_sigma) {
+  if (!c || !potdel || !potpidel || !potsigdel || npot < 3 || !(delinter > 0)) return EP_ERR_INVALID_ARG;
+  if (c->cfg.state != EP_STATE_D) return fail(c, EP_ERR_STATE, "D-state tables need state = EP_STATE_D");
+  c->npot = npot;
+  c->delinter = delinter;
+  c->umax_pi = umax_pi;
+  c->umax_sigma = umax_sigma;
+  c->potdel.assign(potdel, potdel + npot + 2);
+  c->potpi.assign(potpidel, potpidel + npot + 2);
+  c->potsigdel.assign(potsigdel, potsigdel + npot + 2);
   c->have_tables = true;
   return EP_OK;
 }
@@ -743,13 +785,110 @@ int oc_download_field(oc_ctx* c, int which, double* out) {
     case EP_FIELD_UALPHAS: v = &c->ualphas; break;
     case EP_FIELD_VPI: v = &c->vpi; break;
     case EP_FIELD_DELTA: v = &c->delta; break;
+    case EP_FIELD_SIGDEL:
+      if (c->cfg.state != EP_STATE_D) return EP_ERR_INVALID_ARG;
+      v = &c->sigdel;
+      break;
     default: return EP_ERR_INVALID_ARG;
   }
   std::copy(v->begin(), v->end(), out);
   return EP_OK;
 }
 
-// updatepoten (potenimp.f90:515-585) + potenimp P state (:1-46, :184-186).
+// D-state angular factors at x = r - rimp (potenimp.f90:68-117, the same
+// algebra in potinvar :346-390 and instates.f90:478-527): the d harmonics
+// armonicd = (d1..d5, d0) and the symmetric matrix P whose upper triangle
+// the reference writes out (MP before the factor dV2).
+static void d_factors(double xx, double yy, double zz, double arm[6], double P[5][5]) {
+  const double sqr3 = std::sqrt(3.0), sqr3o2 = std::sqrt(3.0) / 2.0, insqr3 = 1.0 / std::sqrt(3.0), in3 = 1.0 / 3.0;
+  const double d0 = xx * xx + yy * yy + zz * zz;
+  const double d1 = sqr3 * xx * yy;
+  const double d2 = sqr3 * yy * zz;
+  const double d3 = (-xx * xx - yy * yy + 2 * zz * zz) / 2;
+  const double d4 = sqr3 * xx * zz;
+  const double d5 = sqr3o2 * (xx * xx - yy * yy);
+  arm[0] = d1; arm[1] = d2; arm[2] = d3; arm[3] = d4; arm[4] = d5; arm[5] = d0;
+  const double sd1 = d1 * d1, sd2 = d2 * d2, sd4 = d4 * d4, sd5 = d5 * d5;
+  const double sumd3d5 = d3 + insqr3 * d5, difd3d5 = d3 - insqr3 * d5;
+  P[0][0] = in3 * (sd2 + sd4 + 4.0 * sd5);
+  P[1][1] = in3 * (sd1 + sd4) + sumd3d5 * sumd3d5;
+  P[2][2] = sd4 + sd2;
+  P[3][3] = in3 * (sd1 + sd2) + difd3d5 * difd3d5;
+  P[4][4] = in3 * (sd2 + sd4 + 4.0 * sd1);
+  P[0][1] = -4.0 * in3 * d1 * d2 + insqr3 * d4 * d0;
+  P[0][2] = -2.0 * insqr3 * d2 * d4;
+  P[0][3] = -4.0 * in3 * d1 * d4 + insqr3 * d2 * d0;
+  P[0][4] = -4.0 * in3 * d1 * d5;
+  P[1][2] = insqr3 * d1 * d4 - d2 * sumd3d5;
+  P[1][3] = -4.0 * in3 * d2 * d4 + insqr3 * d1 * d0;
+  P[1][4] = -d1 * d4 - insqr3 * d2 * sumd3d5;
+  P[2][3] = insqr3 * d1 * d2 - d4 * difd3d5;
+  P[2][4] = insqr3 * (sd2 - sd4);
+  P[3][4] = d1 * d2 + insqr3 * d4 * difd3d5;
+  for (int i = 0; i < 5; ++i)
+    for (int j = i + 1; j < 5; ++j) P[j][i] = P[i][j];
+}
+
+// Spin-orbit matrix SOD of the D state (potenimp.f90:429-451,
+// instates.f90:549-571): upper triangle, then SOD(j,i) = conj(SOD(i,j)).
+static void sod_matrix(cd S[10][10]) {
+  const cd uim(0.0, 1.0);
+  const double sqr3 = std::sqrt(3.0);
+  for (int i = 0; i < 10; ++i)
+    for (int j = 0; j < 10; ++j) S[i][j] = cd(0);
+  S[0][3] = 1.0;  S[0][7] = -uim;  S[0][8] = 2.0 * uim;
+  S[1][2] = -1.0; S[1][6] = -uim;  S[1][9] = -2.0 * uim;
+  S[2][5] = -uim * sqr3; S[2][6] = uim; S[2][9] = -uim;
+  S[3][4] = -uim * sqr3; S[3][7] = -uim; S[3][8] = -uim;
+  S[4][7] = -sqr3; S[5][6] = sqr3; S[6][9] = -1.0; S[7][8] = 1.0;
+  for (int i = 0; i < 10; ++i)
+    for (int j = i; j < 10; ++j) S[j][i] = std::conj(S[i][j]);
+}
+
+// updatepoten D branch (potenimp.f90:545-566) + potenimp D state (:47-182).
+static void potenimp_d(oc_ctx* c) {
+  const double rmax = (c->npot - 1) * c->delinter;
+  const double zeror = 1e-3;
+  const int nx = c->nx, ny = c->ny;
+  const double* rr = c->rimp;
+  const cd* iv = c->invar;
+#pragma omp parallel for schedule(static)
+  for (long long p = 0; p < (long long)c->N; ++p) {
+    const int ix = (int)(p % nx), iy = (int)((p / nx) % ny), iz = (int)(p / ((long long)nx * ny));
+    const double zt = (c->z[iz] - rr[2]) * (c->z[iz] - rr[2]);
+    const double yt = (c->y[iy] - rr[1]) * (c->y[iy] - rr[1]) + zt;
+    const double r2 = (c->x[ix] - rr[0]) * (c->x[ix] - rr[0]) + yt;
+    const double r4 = r2 * r2;
+    const double r = std::sqrt(r2);
+    c->delta[p] = update_interp(r, c->npot, rmax, c->potdel.data());
+    if (r > zeror) {
+      c->vpi[p] = update_interp(r, c->npot, rmax, c->potpi.data()) / r4;
+      c->sigdel[p] = update_interp(r, c->npot, rmax, c->potsigdel.data()) / r4;
+    } else {
+      c->vpi[p] = c->umax_pi;
+      c->sigdel[p] = c->umax_sigma;
+    }
+    const double xx = c->x[ix] - rr[0], yy = c->y[iy] - rr[1], zz = c->z[iz] - rr[2];
+    const double dVdel = c->delta[p], dV1 = c->vpi[p], dV2 = c->sigdel[p];
+    double arm[6], P[5][5], MP[5][5];
+    d_factors(xx, yy, zz, arm, P);
+    // MP = sumVdel + MS + MP (the reference's names: MS = armonicd (x)
+    // armonicd * dV1, MP = P * dV2)
+    for (int i = 0; i < 5; ++i)
+      for (int j = 0; j < 5; ++j) MP[i][j] = (i == j ? dVdel : 0.0) + arm[i] * arm[j] * dV1 + P[i][j] * dV2;
+    // MatD = MP (x) 1_2; Aux = sum_i (MatD iv)_i conj(iv_i), real part
+    double aux = 0.0;
+    for (int i = 0; i < 10; ++i) {
+      cd ivs(0);
+      for (int j = 0; j < 10; ++j)
+        if ((i & 1) == (j & 1)) ivs += MP[i / 2][j / 2] * iv[j];
+      aux += (ivs * std::conj(iv[i])).real();
+    }
+    c->uimp[p] = std::min(aux, 1000.0);
+  }
+}
+
+// updatepoten (potenimp.f90:515-585) + potenimp (:1-189, cap :184-186).
 int oc_potenimp(oc_ctx* c) {
   if (!c) return EP_ERR_INVALID_ARG;
   if (c->cfg.impurity == EP_IMPURITY_NONE) {
@@ -757,6 +896,10 @@ int oc_potenimp(oc_ctx* c) {
     return EP_OK;
   }
   if (!c->have_tables) return fail(c, EP_ERR_STATE, "impurity tables not set");
+  if (c->cfg.state == EP_STATE_D) {
+    potenimp_d(c);
+    return EP_OK;
+  }
   const double rmax = (c->npot - 1) * c->delinter;
   const double zeror = 1e-3;
   const int nx = c->nx, ny = c->ny;
@@ -931,9 +1074,24 @@ int oc_energy(oc_ctx* c, ep_energies* e) {
   const cd* iv = c->invar;
   cd ivs[10];
   for (int i = 0; i < 10; ++i) ivs[i] = std::conj(iv[i]);
-  const double Also2 = 0.5 * g.als_p;
-  const double eso = Also2 * (2.0 * (ivs[0] * iv[5] - ivs[1] * iv[4]).real() +
-                              2.0 * (ivs[0] * iv[2] + ivs[3] * iv[1] + ivs[2] * iv[5] + ivs[3] * iv[4]).imag());
+  double eso;
+  if (g.state == EP_STATE_D) {
+    // energy.f90:176-190: eso = Als_D * 0.5 * sum_i (SOD iv)_i conj(iv_i), real part
+    cd S[10][10];
+    sod_matrix(S);
+    cd vls(0);
+    for (int i = 0; i < 10; ++i) {
+      cd t(0);
+      for (int j = 0; j < 10; ++j) t += S[i][j] * iv[j];
+      vls += t * std::conj(iv[i]);
+    }
+    vls *= 0.5;
+    eso = (vls * g.als_d).real();
+  } else {
+    const double Also2 = 0.5 * g.als_p;
+    eso = Also2 * (2.0 * (ivs[0] * iv[5] - ivs[1] * iv[4]).real() +
+                   2.0 * (ivs[0] * iv[2] + ivs[3] * iv[1] + ivs[2] * iv[5] + ivs[3] * iv[4]).imag());
+  }
   e->ekin4 = ekin4; e->elj4 = elj4; e->ecor4 = ecor4; e->ealphas = ealphas; e->esolid = esolid;
   e->etot4 = etot4; e->ekinx = ekinx; e->eHeX = eHeX; e->uplus = uplus; e->eso = eso;
   e->eimpu = ekinx + eHeX + eso;
@@ -955,9 +1113,96 @@ int oc_forceimp(oc_ctx* c, double* F) {
   return EP_OK;
 }
 
+// The density-weighted D-state matrix MP + MS + sumVdel, times dxyz
+// (potenimp.f90:331-405; instates.f90:457-534), summed as the reference
+// does: the three matrices separately, then added.
+static void dmatrix(oc_ctx* c, double M[5][5]) {
+  const int nx = c->nx, ny = c->ny;
+  const double* rr = c->rimp;
+  const size_t N = c->N;
+  int nt = 1;
+#ifdef _OPENMP
+  nt = omp_get_max_threads();
+#endif
+  // per thread: MP, MS upper triangles and sumVdel, compensated
+  std::vector<std::vector<Neu>> acc(nt, std::vector<Neu>(31));
+#pragma omp parallel
+  {
+    int t = 0;
+#ifdef _OPENMP
+    t = omp_get_thread_num();
+#endif
+    std::vector<Neu>& a = acc[t];
+#pragma omp for schedule(static)
+    for (long long p = 0; p < (long long)N; ++p) {
+      const int ix = (int)(p % nx), iy = (int)((p / nx) % ny), iz = (int)(p / ((long long)nx * ny));
+      const double xx = c->x[ix] - rr[0], yy = c->y[iy] - rr[1], zz = c->z[iz] - rr[2];
+      const double aux = c->den[p];
+      const double dVdel = c->delta[p] * aux, dV1 = c->vpi[p] * aux, dV2 = c->sigdel[p] * aux;
+      double arm[6], P[5][5];
+      d_factors(xx, yy, zz, arm, P);
+      int k = 0;
+      for (int i = 0; i < 5; ++i)
+        for (int j = i; j < 5; ++j, ++k) {
+          a[k].add(P[i][j] * dV2);
+          a[15 + k].add(arm[i] * arm[j] * dV1);
+        }
+      a[30].add(dVdel);
+    }
+  }
+  double tot[31];
+  for (int q = 0; q < 31; ++q) {
+    Neu s;
+    for (int t = 0; t < nt; ++t) s.add(acc[t][q].get());
+    tot[q] = s.get();
+  }
+  int k = 0;
+  for (int i = 0; i < 5; ++i)
+    for (int j = i; j < 5; ++j, ++k) {
+      const double v = tot[k] * c->dxyz + tot[15 + k] * c->dxyz + (i == j ? tot[30] * c->dxyz : 0.0);
+      M[i][j] = M[j][i] = v;
+    }
+}
+
+int oc_impurity_matrix_d(oc_ctx* c, double* m25) {
+  if (!c || !m25) return EP_ERR_INVALID_ARG;
+  if (c->cfg.state != EP_STATE_D) return fail(c, EP_ERR_STATE, "the D-state matrix needs state = EP_STATE_D");
+  double M[5][5];
+  dmatrix(c, M);
+  for (int i = 0; i < 5; ++i)
+    for (int j = 0; j < 5; ++j) m25[5 * i + j] = M[i][j];
+  return EP_OK;
+}
+
+// potinvar, D state (potenimp.f90:331-475, :487-492): Hiv = (MatD + Als_D/2
+// SOD) iv with MatD = M (x) 1_2, then -i (Hiv - Ev0 iv).
+static void potinvar_d(oc_ctx* c, cd* Hiv) {
+  const ep_config& g = c->cfg;
+  double M[5][5];
+  dmatrix(c, M);
+  cd S[10][10];
+  sod_matrix(S);
+  const cd uim(0.0, 1.0);
+  const double Also2 = g.als_d / 2.0;
+  const cd* iv = c->invar;
+  for (int i = 0; i < 10; ++i) {
+    cd h(0);
+    for (int j = 0; j < 10; ++j) {
+      const double md = ((i & 1) == (j & 1)) ? M[i / 2][j / 2] : 0.0;
+      h += (md + Also2 * S[i][j]) * iv[j];
+    }
+    Hiv[i] = h;
+  }
+  for (int i = 0; i < 10; ++i) Hiv[i] = -uim * (Hiv[i] - g.ev0 * iv[i]);
+}
+
 // potinvar, P state (potenimp.f90:261-330, :487-492).
 static void potinvar_(oc_ctx* c, cd* Hiv) {
   const ep_config& g = c->cfg;
+  if (g.state == EP_STATE_D) {
+    potinvar_d(c, Hiv);
+    return;
+  }
   const int nx = c->nx, ny = c->ny;
   const double* rr = c->rimp;
   auto X = [&](size_t p) { return c->x[(int)(p % nx)] - rr[0]; };
@@ -1251,11 +1496,14 @@ int oc_steppc(oc_ctx* c, double deltat, ep_step_errors* err) {
       for (int k = 0; k < 10; ++k)
         auxc[k] = 0.125 * (9.0 * c->invarold[k][i3] - c->invarold[k][i2] +
                            3.0 * deltat * (c->hinvar[k] + 2.0 * c->hinvarold[k][h1] - c->hinvarold[k][h2]));
-      for (int k = 0; k < 6; ++k) c->pciv[k] = c->pciv[k] - auxc[k];
+      // steppc.f90:199-217: the P state corrects components 1-6 and zeroes
+      // 7-10; the D state corrects all ten
+      const int nc = c->cfg.state == EP_STATE_D ? 10 : 6;
+      for (int k = 0; k < nc; ++k) c->pciv[k] = c->pciv[k] - auxc[k];
       for (int k = 0; k < 10; ++k) c->invar[k] = cd(0);
-      for (int k = 0; k < 6; ++k) c->invar[k] = auxc[k] + c9 * c->pciv[k];
-      for (int k = 0; k < 6; ++k) erriv += std::abs(c9 * c->pciv[k]);
-      erriv *= 0.1666666666666;
+      for (int k = 0; k < nc; ++k) c->invar[k] = auxc[k] + c9 * c->pciv[k];
+      for (int k = 0; k < nc; ++k) erriv += std::abs(c9 * c->pciv[k]);
+      erriv *= nc == 10 ? 0.1 : 0.1666666666666;
     }
     { int t = c->ioldv[2]; c->ioldv[2] = c->ioldv[1]; c->ioldv[1] = c->ioldv[0]; c->ioldv[0] = t; }
     { int t = c->ioldiv[2]; c->ioldiv[2] = c->ioldiv[1]; c->ioldiv[1] = c->ioldiv[0]; c->ioldiv[0] = t; }

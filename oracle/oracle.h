@@ -32,6 +32,15 @@ int oc_set_impurity_tables(oc_ctx* c, const double* potpi, const double* potdel,
                            int npot, double delinter, double umax_sigma);
 int oc_get_impurity_tables(oc_ctx* c, double* potpi, double* potdel, int* npot,
                            double* delinter);
+int oc_set_impurity_potentials_d(oc_ctx* c, const ep_potential* pi,
+                                 const ep_potential* sigma,
+                                 const ep_potential* delta,
+                                 const ep_potential* plus);
+int oc_set_impurity_tables_d(oc_ctx* c, const double* potdel,
+                             const double* potpidel, const double* potsigdel,
+                             int npot, double delinter, double umax_pi,
+                             double umax_sigma);
+int oc_impurity_matrix_d(oc_ctx* c, double* m25);
 int oc_set_impurity_state(oc_ctx* c, const double* rimp, const double* vimp,
                           const double* invar);
 int oc_get_impurity_state(oc_ctx* c, double* rimp, double* vimp, double* aimp,

@@ -268,3 +268,61 @@ def test_tabulated_pair_potentials_equal_the_formula(tmp_path):
     for k in by_name:
         assert abs(float(by_name[k]) - float(by_table[k])) <= 2e-6, (k, by_name[k], by_table[k])
     assert abs(float(by_table["eHeX"])) > 1.0  # the impurity field is not trivial
+
+
+def _sod():
+    """SOD of potenimp.f90:429-451, restated: the listed upper triangle plus
+    its conjugate transpose."""
+    S = np.zeros((10, 10), complex)
+    s3 = np.sqrt(3.0)
+    for (i, j), v in {(1, 4): 1, (1, 8): -1j, (1, 9): 2j, (2, 3): -1, (2, 7): -1j, (2, 10): -2j,
+                      (3, 6): -1j * s3, (3, 7): 1j, (3, 10): -1j, (4, 5): -1j * s3, (4, 8): -1j, (4, 9): -1j,
+                      (5, 8): -s3, (6, 7): s3, (7, 10): -1, (8, 9): 1}.items():
+        S[i - 1, j - 1] = v
+    return S + S.conj().T
+
+
+def test_d_state_instate_matches_the_api(tmp_path):
+    """Lstate='D': the driver builds invar from the field matrix and SOD
+    (instates.f90:440-647, default branch) as the host mirror does with
+    numpy; three different tabulated channels make the field anisotropic."""
+    psi = ep.woods_saxon_psi(N, N, N, XMAX, XMAX, XMAX, N4, seed=9)
+    den = np.abs(psi) ** 2
+    rimp = (0.4, -0.3, 0.9)
+    write_density(tmp_path / "in.dat", den, rimp)
+    npot = 100 * N + 1
+    r = np.arange(npot) * (4.0 * XMAX / (npot - 1))
+    chans = {"pi": (10.0, 4.5, 1.2), "sigma": (25.0, 4.0, 1.1), "delta": (6.0, 5.0, 1.0)}
+    for name, (de, re_, al) in chans.items():
+        e = np.exp(-al * (r - re_))
+        with open(tmp_path / f"{name}.tab", "w") as f:
+            for a, b in zip(r, de * (e * e - 2.0 * e)):
+                f.write(f"{a:.17E} {b:.17E}\n")
+    als = 4.0
+    extra = (", Lstate='D', Als_D=4.d0, selec_pi='table', selec_sigma='table', selec_delta='table', "
+             "table_pi='pi.tab', table_sigma='sigma.tab', table_delta='delta.tab', umax_delta=1000.d0")
+    for instate in (0, 2):
+        out = run_driver(tmp_path, namelist(0, f", instate={instate}" + extra))
+        got = balance(out)
+        eso = float(re.search(r"Spin-Orbit energy \(X\) \.*: +(-?\d+\.\d+) K", out).group(1))
+        cfg = ep.make_config(nx=N, ny=N, nz=N, xmax=XMAX, ymax=XMAX, zmax=XMAX, icon=_abi.EP_ICON_PERIODIC,
+                             core="OTC", n4=N4, impurity=_abi.EP_IMPURITY_MOVING, mimpur=40.0, fix_lambda=1,
+                             state=_abi.EP_STATE_D, als_d=als)
+        with ep.Solver(cfg) as s:
+            pots = [ep.morse(*chans[c], r_cutoff=0.0, umax=1000.0) for c in ("pi", "sigma", "delta")]
+            s.set_impurity_potentials_d(*pots, ep.null_potential())
+            s.set_impurity(rimp=rimp, invar=np.zeros(10, dtype=np.complex128))
+            s.upload_psi(np.sqrt(den).astype(np.complex128))
+            s.potenimp()
+            M = s.impurity_matrix_d()
+            w, V = np.linalg.eigh(np.kron(M, np.eye(2)) + 0.5 * als * _sod())
+            iv = (V[:, 2 * instate] + V[:, 2 * instate + 1]) / np.sqrt(2)
+            s.set_impurity(rimp=rimp, invar=iv)
+            s.potenimp()
+            s.poten()
+            e = s.energy()
+        assert abs(w[2 * instate] - w[2 * instate + 1]) < 1e-9 * max(1.0, abs(w).max())  # a Kramers pair
+        for k, v in got.items():
+            assert abs(float(v) - e[k]) < 2e-6, (instate, k, v, e[k])
+        assert abs(eso - e["eso"]) < 2e-6
+        assert abs(float(got["eHeX"])) > 1.0
