@@ -5,7 +5,7 @@ include/eff_pot.h does all the work on the GPU; this package binds it with
 ctypes and mirrors the reference's subroutine interface (Solver).
 """
 from . import _abi
-from .config import make_config, config_dict, morse, null_potential, DEFAULTS, KTOPS, MP_U
+from .config import make_config, config_dict, morse, koutselos, null_potential, DEFAULTS, KTOPS, MP_U
 from .solver import Solver, Batch, EffPotError, load_library, library_config_defaults, LIBPATH
 from .initial import woods_saxon_psi, grid_axes
 

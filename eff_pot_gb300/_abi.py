@@ -18,7 +18,7 @@ EP_IMPURITY_NONE, EP_IMPURITY_FIXED, EP_IMPURITY_MOVING = 0, 1, 2
 EP_FP64, EP_FP32 = 0, 1
 EP_ICON_PERIODIC, EP_ICON_ZERO_OUTSIDE = 8, 13
 EP_STATE_P, EP_STATE_D = 0, 1
-EP_POT_NULL, EP_POT_MORSE = 0, 1
+EP_POT_NULL, EP_POT_MORSE, EP_POT_KOUTSELOS = 0, 1, 2
 
 FIELDS = {
     "den": 0, "pot4": 1, "uimp": 2, "dencg": 3, "delj4": 4, "dxden": 5,

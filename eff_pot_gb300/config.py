@@ -58,6 +58,19 @@ def morse(De=10.0, re=4.5, alpha=1.2, r_cutoff=0.0, umax=1000.0):
     return p
 
 
+KOUTSELOS_IONS = {"Na": 0, "K": 1, "Rb": 2, "Cs": 3}
+
+
+def koutselos(ion="Rb", r_cutoff=0.0, umax=0.0):
+    """He-M+ of Koutselos et al. (selec = 'Na_plus_Koutselos' ... 'Cs_plus_Koutselos')."""
+    p = _abi.EpPotential()
+    p.kind = _abi.EP_POT_KOUTSELOS
+    p.r_cutoff = r_cutoff
+    p.umax = umax
+    p.par[0], p.par[1], p.par[2], p.par[3] = float(KOUTSELOS_IONS[ion]), 0.0, 0.0, 0.0
+    return p
+
+
 def null_potential():
     p = _abi.EpPotential()
     p.kind = _abi.EP_POT_NULL

@@ -27,8 +27,9 @@
 // (ep_instates.h); Lexcite_state_fix gives the fixed P vectors, instate 5
 // reads invar.dat.  Not built here: the Ldiag_jz / Laverage_P_value /
 // Lmixture / exciplex variants of instates.f90, and the Select_Pot closed
-// forms other than 'null' and 'Morse' (V_impur.f90:87-932; any of them runs
-// as selec_* = 'table' from a file of (r, V) rows).
+// forms other than 'null', 'Morse' and the four '*_plus_Koutselos'
+// (V_impur.f90:87-932; any of them runs as selec_* = 'table' from a file of
+// (r, V) rows).
 #include <cmath>
 #include <complex>
 #include <cstdio>
@@ -102,9 +103,14 @@ ep_potential potential_of(const Input& in, const char* which, const char* dflt_s
     p.par[0] = in.get<double>("morse_de", 10.0);
     p.par[1] = in.get<double>("morse_re", 4.5);
     p.par[2] = in.get<double>("morse_alpha", 1.2);
+  } else if (sel == "Na_plus_Koutselos" || sel == "K_plus_Koutselos" || sel == "Rb_plus_Koutselos" ||
+             sel == "Cs_plus_Koutselos") {  // V_impur.f90:232-290
+    p.kind = EP_POT_KOUTSELOS;
+    p.par[0] = sel[0] == 'N' ? 0 : sel[0] == 'K' ? 1 : sel[0] == 'R' ? 2 : 3;
   } else {
     stop("selec_" + std::string(which) + "='" + sel +
-         "': this potential of Select_Pot is not built into this driver (use 'null', 'Morse' or 'table' with "
+         "': this potential of Select_Pot is not built into this driver (use 'null', 'Morse', "
+         "'{Na,K,Rb,Cs}_plus_Koutselos' or 'table' with "
          "table_" + std::string(which) + " = a file of r (A), V (K) rows)");
   }
   return p;

@@ -13,6 +13,7 @@
 
 #include "../../include/eff_pot.h"
 #include "ep_engine.h"
+#include "ep_pairpot.h"
 
 // A captured steppc (one context, or one step of every context of a batch)
 // and, per context, its predictor / corrector nodes and the engine state the
@@ -80,13 +81,7 @@ int fail(ep_ctx* c, int code, const std::string& msg) {
 
 // Select_Pot subset (V_impur.f90:87-932) plus the Morse selector.
 double select_pot(const ep_potential& p, double r) {
-  if (p.kind == EP_POT_NULL) return 0.0;
-  if (r < p.r_cutoff) return p.umax;
-  if (p.kind == EP_POT_MORSE) {
-    const double e = std::exp(-p.par[2] * (r - p.par[1]));
-    return p.par[0] * (e * e - 2.0 * e);
-  }
-  return 0.0;
+  return ep_pair_potential(p.kind, p.r_cutoff, p.umax, p.par[0], p.par[1], p.par[2], r);
 }
 
 template <class F>

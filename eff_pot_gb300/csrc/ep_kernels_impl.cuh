@@ -1,6 +1,7 @@
 // ep_kernels_impl.cuh - bodies of the point-wise and reduction kernels.
 #pragma once
 #include "ep_kernels.cuh"
+#include "ep_pairpot.h"
 
 // Grid coordinate -xmax + h*i without contraction (x(i) of DFT4He3d.f90:248-256).
 EP_DEV double coord(double xmax, double h, int i) { return __dadd_rn(-xmax, __dmul_rn(h, (double)i)); }
@@ -33,10 +34,7 @@ EP_DEV double interp_update(double r, int nint, double rmax, const double* __res
 
 // Pair potential of the U+ integral (Select_Pot subset + Morse).
 EP_DEV double pot_eval(const PotDev& v, double r) {
-  if (v.kind == 0) return 0.0;
-  if (r < v.r_cutoff) return v.umax;
-  const double e = exp(-v.p2 * (r - v.p1));
-  return v.p0 * (e * e - 2.0 * e);
+  return ep_pair_potential(v.kind, v.r_cutoff, v.umax, v.p0, v.p1, v.p2, r);
 }
 
 template <class T>

@@ -80,12 +80,16 @@ typedef struct ep_config {
 } ep_config;
 
 /* Pair potentials (a subset of the Select_Pot registry, V_impur.f90:87-932,
- * plus the Morse selector this project adds).  r < r_cutoff -> umax.       */
-enum { EP_POT_NULL = 0, EP_POT_MORSE = 1 };
+ * plus the Morse selector this project adds).  r < r_cutoff -> umax.
+ * EP_POT_KOUTSELOS: the He-M+ potentials 'Na_plus_Koutselos',
+ * 'K_plus_Koutselos', 'Rb_plus_Koutselos', 'Cs_plus_Koutselos'
+ * (V_impur.f90:232-290,1704-1883), par[0] = 0, 1, 2, 3 for Na+, K+, Rb+, Cs+. */
+enum { EP_POT_NULL = 0, EP_POT_MORSE = 1, EP_POT_KOUTSELOS = 2 };
 typedef struct ep_potential {
   int kind;                  /* EP_POT_*                                    */
   double r_cutoff, umax;
-  double par[4];             /* Morse: De (K), re (A), alpha (1/A)          */
+  double par[4];             /* Morse: De (K), re (A), alpha (1/A);
+                                Koutselos: ion code                         */
 } ep_potential;
 
 /* Energies printed by DFT4He3d.f90:460-463 (module energies). */

@@ -334,6 +334,37 @@ static double bforce_(int core, double eps, double sigma, double hc) {
 }
 
 // Pair potentials: Select_Pot subset (V_impur.f90:87-932) + Morse.
+// V_Koutselos_{Na,K,Rb,Cs}_plus_gs (V_impur.f90:1704-1883), xx in A, result in K.
+static double v_koutselos(int ion, double xx) {
+  struct Ion { double v_0, rho, R_m, C4, C6, C8; };
+  static const Ion ions[4] = {{0.2063, 0.7640, 4.55, 0.0, 1.424, 13.17},   // Na+ :1771-1772
+                              {0.2690, 0.8589, 5.49, 0.0, 5.83, 72.05},    // K+  :1861-1862
+                              {0.3474, 0.8868, 5.85, 0.0, 8.8, 126.2},     // Rb+ :1817-1818
+                              {0.5092, 0.9241, 6.38, 0.0, 13.69, 236.4}};  // Cs+ :1727-1728
+  const Ion& p = ions[std::min(std::max(ion, 0), 3)];
+  const double a_bohr = 0.529177, Hartree = 27.2114, eV_K = 11604.448;
+  const double A = 146.98, a_a = 1.5024, B = 70.198, b_b = 1.4041;
+  const double a_d = 1.3831, a_q = 2.4434, a_o = 10.614;
+  const double CC4 = p.C4 + a_d / 2.0, CC6 = p.C6 + a_q / 2.0, CC8 = p.C8 + a_o / 2.0;
+  const double x = xx / a_bohr;
+  const double Rs = x / p.rho;
+  const double V_ex = p.v_0 * (A * std::exp(-a_a * Rs) - B * std::exp(-b_b * Rs));
+  const double Aux = p.R_m * 1.28;
+  double h_r;
+  if (x >= Aux) {
+    h_r = 1.0;
+  } else {
+    h_r = 0.0;
+    if (x != 0.0) h_r = std::exp(-std::pow(Aux / x - 1.0, 2));
+  }
+  double Sto = V_ex;
+  if (x != 0.0) {
+    const double x2 = x * x, x4 = x2 * x2, x6 = x4 * x2, x8 = x6 * x2;
+    Sto = Sto + (-CC4 / x4 - CC6 / x6 - CC8 / x8) * h_r;
+  }
+  return Sto * Hartree * eV_K;
+}
+
 static double select_pot(const ep_potential& p, double r) {
   if (p.kind == EP_POT_NULL) return 0.0;
   if (r < p.r_cutoff) return p.umax;
@@ -342,6 +373,7 @@ static double select_pot(const ep_potential& p, double r) {
     const double e = std::exp(-al * (r - re));
     return De * (e * e - 2.0 * e);
   }
+  if (p.kind == EP_POT_KOUTSELOS) return v_koutselos((int)p.par[0], r);
   return 0.0;
 }
 

@@ -326,3 +326,28 @@ def test_d_state_instate_matches_the_api(tmp_path):
             assert abs(float(v) - e[k]) < 2e-6, (instate, k, v, e[k])
         assert abs(eso - e["eso"]) < 2e-6
         assert abs(float(got["eHeX"])) > 1.0
+
+
+def test_scan_settings_of_prep_sh_give_the_api_uplus(tmp_path):
+    """selec_plus='Rb_plus_Koutselos', r_cutoff_plus=2, umax_plus=6110.59...
+    (the settings prep.sh writes) give the U+ the ABI computes."""
+    psi = ep.woods_saxon_psi(N, N, N, XMAX, XMAX, XMAX, N4, seed=10)
+    den = np.abs(psi) ** 2
+    rimp = (0.6, 0.2, -0.8)
+    write_density(tmp_path / "in.dat", den, rimp)
+    (tmp_path / "invar.dat").write_text("\n".join(["(0.d0,0.d0)"] * 10) + "\n")
+    text = namelist(0, ", instate=5").replace(
+        "selec_plus='null'", "selec_plus='Rb_plus_Koutselos', r_cutoff_plus=2.d0, umax_plus=6.1105922888E+03")
+    out = run_driver(tmp_path, text)
+    m = re.search(r"Interaction energy \(X\+-He\) \.*: +(-?\d+\.\d+) K", out)
+    assert m, out
+    s = solver(rimp, np.zeros(10, dtype=np.complex128))
+    with s:
+        m_ = ep.morse(10.0, 4.5, 1.2, r_cutoff=0.0, umax=1000.0)
+        s.set_impurity_potentials(m_, m_, ep.koutselos("Rb", r_cutoff=2.0, umax=6.1105922888e3))
+        s.upload_psi(np.sqrt(den).astype(np.complex128))
+        s.potenimp()
+        s.poten()
+        e = s.energy()
+    assert abs(float(m.group(1)) - e["uplus"]) < 2e-6
+    assert abs(e["uplus"]) > 1.0
