@@ -69,6 +69,7 @@ constexpr size_t smem_bytes() {
   return (size_t)(32 * (N + 1) + N) * sizeof(C2<T>);
 }
 
+
 // Line base address of line L of a LineSet-like description.
 EP_DEV long long line_base(long long L, long long Mi, long long So) { return (L % Mi) + (L / Mi) * So; }
 
@@ -76,9 +77,13 @@ EP_DEV long long line_base(long long L, long long Mi, long long So) { return (L 
 
 // Blocks per SM the launch bounds ask for (FP32 / FP64).
 template <class T, int N> struct Occ {
-  static constexpr int c2c = sizeof(T) == 4 ? (N <= 64 ? 4 : (N == 128 ? 3 : 2)) : (N <= 64 ? 2 : 1);
+  // the in-place Y pass fits 64 registers at N = 128 without spilling: four
+  // CTAs per SM keep more lines in flight (the pass is load-latency bound)
+  static constexpr int c2c = sizeof(T) == 4 ? (N <= 128 ? 4 : 2) : (N <= 64 ? 2 : 1);
   static constexpr int conv = sizeof(T) == 4 ? (N <= 64 ? 3 : (N == 128 ? 2 : 1)) : 1;
-  static constexpr int conv1 = c2c;  // one output per input: no spectrum kept
+  // one output per input (no spectrum kept): 3 CTAs per SM at N = 128 (64
+  // registers would spill)
+  static constexpr int conv1 = sizeof(T) == 4 ? (N <= 64 ? 4 : (N == 128 ? 3 : 2)) : (N <= 64 ? 2 : 1);
 };
 
 // In-place transforms along a strided axis of up to 8 arrays (blockIdx.y).

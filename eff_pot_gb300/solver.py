@@ -188,8 +188,14 @@ class Solver:
         st = self._f["upload_psi"](self._h, buf.ctypes.data_as(C.POINTER(C.c_double)))
         self._check(st, "upload_psi")
 
-    def psi(self):
-        out = np.empty(self.shape, dtype=np.complex128, order="F")
+    def psi(self, out=None):
+        """psi as a (nx, ny, nz) complex array in Fortran order.  out: an array
+        of that shape and layout to fill (e.g. in page-locked memory, which
+        the device copies into at full link speed) instead of a new one."""
+        if out is None:
+            out = np.empty(self.shape, dtype=np.complex128, order="F")
+        elif out.shape != self.shape or out.dtype != np.complex128 or not out.flags.f_contiguous:
+            raise ValueError("out must be a Fortran-ordered complex128 array of the grid's shape")
         self._check(self._f["download_psi"](self._h, out.ctypes.data_as(C.POINTER(C.c_double))), "download_psi")
         return out
 
