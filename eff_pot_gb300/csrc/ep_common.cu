@@ -65,6 +65,9 @@ __global__ void k_finalize(const double* __restrict__ partials, int nblocks, int
 }
 
 __global__ void k_reset_scales(DevScalars* sc) {
-  if (threadIdx.x < EP_NSLOTS) sc->bscale[threadIdx.x] = 1.0;
+  if (threadIdx.x < EP_NSLOTS) {
+    sc->bscale[threadIdx.x] = 1.0;
+    sc->bscale_f[threadIdx.x] = 1.0f;
+  }
   if (threadIdx.x == 0) sc->den_scale = 1.0;
 }

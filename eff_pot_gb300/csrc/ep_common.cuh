@@ -48,6 +48,10 @@ struct DevScalars {
   // stored * bscale[k]; den's logical value is stored * den_scale.
   double bscale[8];
   double den_scale;
+  // bscale rounded to FP32 once, by the thread that writes bscale: FP32
+  // kernels read these instead of converting bscale in every thread (a
+  // double -> float conversion runs on the FP64 pipe)
+  float bscale_f[8];
 };
 #define EP_NSLOTS 8
 enum { EP_FLAG_NONFINITE = 1u, EP_FLAG_DEN_NONPOS = 2u };

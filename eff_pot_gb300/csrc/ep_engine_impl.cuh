@@ -186,6 +186,10 @@ int Engine<T>::init(const ep_config& c, cudaStream_t s, Prof* p, ImpState* im, s
   phl.dxyz = dxyz;
   phl.core = c.core;
   phl.time_mode = c.time_mode;
+  phl.rden0s = 1.0 / c.den0s;
+  phl.f = PhysF{(float)phl.cp4, (float)phl.cpp4, (float)phl.a0, (float)phl.a1, (float)phl.rden0s,
+                (float)phl.h2o2m4, (float)phl.alphas, (float)phl.C, (float)phl.beta, (float)phl.den_m,
+                (float)phl.renor};
   phys = phl;
 
   const size_t N = (size_t)g.N, Nh = (size_t)g.Nh;

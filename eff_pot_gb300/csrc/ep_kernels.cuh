@@ -13,12 +13,41 @@ template <class T> struct FdW {
   int periodic;           // icon 8 (1) or icon 13 (0)
 };
 
+// The functional's constants in FP32, rounded once on the host.
+struct PhysF {
+  float cp4, cpp4, a0, a1, rden0s, h2o2m4, alphas, C, beta, den_m, renor;
+};
 struct Phys {
   double cp4, cpp4, a0, a1, den0s, h2o2m4, alphas, C, beta, den_m;
   double renor, dxyz;
+  double rden0s;          // 1 / den0s
   int core;               // EP_CORE_*
   int time_mode;          // 0 imaginary, 1 real
+  PhysF f;                // the same constants for the FP32 kernels
 };
+
+// Phys in the field precision T.  FP32 kernels take the host-rounded copies:
+// a double -> float conversion or a double division in every thread would
+// run on the FP64 pipe (1/64 of the FP32 rate on this part) before any
+// point is processed.
+template <class T> struct PConst;
+template <> struct PConst<double> {
+  double cp4, cpp4, a0, a1, rden0s, h2o2m4, alphas, C, beta, den_m, renor;
+  EP_DEV explicit PConst(const Phys& p)
+      : cp4(p.cp4), cpp4(p.cpp4), a0(p.a0), a1(p.a1), rden0s(p.rden0s), h2o2m4(p.h2o2m4), alphas(p.alphas),
+        C(p.C), beta(p.beta), den_m(p.den_m), renor(p.renor) {}
+};
+template <> struct PConst<float> {
+  float cp4, cpp4, a0, a1, rden0s, h2o2m4, alphas, C, beta, den_m, renor;
+  EP_DEV explicit PConst(const Phys& p)
+      : cp4(p.f.cp4), cpp4(p.f.cpp4), a0(p.f.a0), a1(p.f.a1), rden0s(p.f.rden0s), h2o2m4(p.f.h2o2m4),
+        alphas(p.f.alphas), C(p.f.C), beta(p.f.beta), den_m(p.f.den_m), renor(p.f.renor) {}
+};
+
+// Buffer scale k of the lazy renormalisation in the field precision.
+template <class T> EP_DEV T bscale_of(const DevScalars* sc, int k);
+template <> EP_DEV double bscale_of<double>(const DevScalars* sc, int k) { return sc->bscale[k]; }
+template <> EP_DEV float bscale_of<float>(const DevScalars* sc, int k) { return sc->bscale_f[k]; }
 
 // Lines of a strided pass: element k of line L lives at
 //   (L % Mi) + (L / Mi) * So + k * Sa.
@@ -89,7 +118,12 @@ EP_DEV T d1_line(const T* __restrict__ line, int i, int n, const T* w, int R, in
 // double -> float conversion per point would run on the FP64 pipe).
 template <class T> struct Pen {
   T C, beta, den_m;
-  EP_DEV explicit Pen(const Phys& ph) : C((T)ph.C), beta((T)ph.beta), den_m((T)ph.den_m) {}
+  EP_DEV explicit Pen(const Phys& ph) {
+    const PConst<T> k(ph);
+    C = k.C;
+    beta = k.beta;
+    den_m = k.den_m;
+  }
 };
 EP_DEV double penalty_of(const Pen<double>& pn, double den) {
   const double t = tanh(pn.beta * (den - pn.den_m));
@@ -110,7 +144,7 @@ EP_DEV float penalty_of(const Pen<float>& pn, float den) {
 template <class T> struct HCoef {
   T h;
   int real_time;
-  EP_DEV explicit HCoef(const Phys& ph) : h((T)ph.h2o2m4), real_time(ph.time_mode == 1) {}
+  EP_DEV explicit HCoef(const Phys& ph) : h(PConst<T>(ph).h2o2m4), real_time(ph.time_mode == 1) {}
 };
 template <class T>
 EP_DEV C2<T> happly(const HCoef<T>& hc, C2<T> lap, C2<T> psi, T pot4, T uimp) {
@@ -618,11 +652,12 @@ __global__ void k_x2(Geo g, Phys ph, const C2<T>* __restrict__ B0, const C2<T>* 
   T* Rcg = S.R;
   T* Rlj = S.R + nl * nx;
   T* Ral = S.R + 2 * nl * nx;
-  const T rn = (T)ph.renor;
+  const PConst<T> kc(ph);
+  const T rn = kc.renor;
   x_inverse<T, N2>(B0, line0, nlv, nl, nx, nxh, S, p2, rn, Rcg);
   x_inverse<T, N2>(B1, line0, nlv, nl, nx, nxh, S, p2, rn, Rlj);
   if (otc) x_inverse<T, N2>(B2, line0, nlv, nl, nx, nxh, S, p2, rn, Ral);
-  const T a0 = (T)ph.a0, a1 = (T)ph.a1, rden0s = (T)(1.0 / ph.den0s), cp4 = (T)ph.cp4, cpp4 = (T)ph.cpp4;
+  const T a0 = kc.a0, a1 = kc.a1, rden0s = kc.rden0s, cp4 = kc.cp4, cpp4 = kc.cpp4;
   for (int e = threadIdx.x; e < nlv * nx; e += blockDim.x) {
     const long long p = line0 * nx + e;
     const T cg = Rcg[e], lj = Rlj[e];
@@ -672,7 +707,7 @@ __global__ void k_x3(Geo g, Phys ph, const __grid_constant__ FdW<T> fd, const C2
   const int nlv = (int)min((long long)nl, nlines - line0);
   S.template load_twiddles<N2>(twx, nx);
   __syncthreads();
-  const T rn = (T)ph.renor;
+  const T rn = PConst<T>(ph).renor;
   T* Rc = S.R;
   x_inverse<T, N2>(D0, line0, nlv, nl, nx, nxh, S, p2, rn, Rc);
   if (!otc) {
@@ -730,8 +765,9 @@ __global__ void k_x4(Geo g, Phys ph, const C2<T>* __restrict__ F0, const T* __re
   S.template load_twiddles<N2>(twx, nx);
   __syncthreads();
   T* Ru = S.R;
-  x_inverse<T, N2>(F0, line0, nlv, nl, nx, nxh, S, p2, (T)ph.renor, Ru);
-  const T rden0s = (T)(1.0 / ph.den0s), h2 = (T)ph.h2o2m4, al = (T)ph.alphas;
+  const PConst<T> kc(ph);
+  x_inverse<T, N2>(F0, line0, nlv, nl, nx, nxh, S, p2, kc.renor, Ru);
+  const T rden0s = kc.rden0s, h2 = kc.h2o2m4, al = kc.alphas;
   const Pen<T> pn(ph);
   for (int e = threadIdx.x; e < nlv * nx; e += blockDim.x) {
     const long long p = line0 * nx + e;
@@ -1215,13 +1251,12 @@ __global__ void __launch_bounds__(EP_TX* EP_TY, sizeof(T) == 4 ? 4 : 2) k_predic
   const HCoef<T> hc(ph);
   // buffer scales folded into the method's coefficients once per thread:
   // pp = s3 po3 + f (2 H - s1 h1 + 2 s2 h2), pn = pp - c112 sp pc
-  const double f_ = (double)f;
-  const T s3 = (T)sc->bscale[sl.a], k2f = (T)(2.0 * f_), kh1 = (T)(f_ * sc->bscale[sl.h1]),
-          kh2 = (T)(2.0 * f_ * sc->bscale[sl.h2]), kpc = (T)((double)c112 * sc->bscale[sl.pc]);
+  const T s3 = bscale_of<T>(sc, sl.a), k2f = T(2) * f, kh1 = f * bscale_of<T>(sc, sl.h1),
+          kh2 = (T(2) * f) * bscale_of<T>(sc, sl.h2), kpc = c112 * bscale_of<T>(sc, sl.pc);
   const C2<T>* cin[4] = {po3, h1, h2, pc};
   const T* rin[2] = {pot4, uimp};
   lap_march_async<T, R, 4, 2>(
-      g, psi, fd, zc, smraw, cin, rin, (T)sc->bscale[sl.psi],
+      g, psi, fd, zc, smraw, cin, rin, bscale_of<T>(sc, sl.psi),
       [&](long long p, C2<T> c, C2<T> lap, const C2<T>* ic, const T* ir) {
         const C2<T> H = happly<T>(hc, lap, c, ir[0], ir[NT]);
         const C2<T> pp = ((s3 * ic[0] + k2f * H) - kh1 * ic[NT]) + kh2 * ic[2 * NT];
@@ -1236,6 +1271,9 @@ __global__ void __launch_bounds__(EP_TX* EP_TY, sizeof(T) == 4 ? 4 : 2) k_predic
       sc->bscale[sl.a] = 1.0;
       sc->bscale[sl.h2] = 1.0;
       sc->bscale[sl.pc] = 1.0;
+      sc->bscale_f[sl.a] = 1.0f;
+      sc->bscale_f[sl.h2] = 1.0f;
+      sc->bscale_f[sl.pc] = 1.0f;
       sc->den_scale = 1.0;
       sc->counter2 = 0u;
     }
@@ -1262,13 +1300,12 @@ __global__ void __launch_bounds__(EP_TX* EP_TY, sizeof(T) == 4 ? 3 : 2) k_correc
   Acc<T> acc[4];
   // buffer scales folded into the method's coefficients once per thread:
   // p5 = (9 s3 po3 - s2o po2 + f3 (H + 2 s1 h1 - s2 h2)) / 8
-  const double f3_ = (double)f3;
-  const T k3 = (T)(1.125 * sc->bscale[sl.a]), k2o = (T)(0.125 * sc->bscale[sl.b]), kH = (T)(0.125 * f3_),
-          k1 = (T)(0.25 * f3_ * sc->bscale[sl.h1]), k2 = (T)(0.125 * f3_ * sc->bscale[sl.h2]),
-          sp_ = (T)sc->bscale[sl.pc];
+  const T k3 = T(1.125) * bscale_of<T>(sc, sl.a), k2o = T(0.125) * bscale_of<T>(sc, sl.b), kH = T(0.125) * f3,
+          k1 = (T(0.25) * f3) * bscale_of<T>(sc, sl.h1), k2 = (T(0.125) * f3) * bscale_of<T>(sc, sl.h2),
+          sp_ = bscale_of<T>(sc, sl.pc);
   const C2<T>* cin[5] = {po3, po2, h1, h2, pc};
   const T* rin[2] = {pot4, uimp};
-  lap_march_async<T, R, 5, 2>(g, psi, fd, zc, smraw, cin, rin, (T)sc->bscale[sl.psi],
+  lap_march_async<T, R, 5, 2>(g, psi, fd, zc, smraw, cin, rin, bscale_of<T>(sc, sl.psi),
                               [&](long long p, C2<T> c, C2<T> lap, const C2<T>* ic, const T* ir) {
     const C2<T> H = happly<T>(hc, lap, c, ir[0], ir[NT]);
     const C2<T> p5 = (((k3 * ic[0] - k2o * ic[NT]) + kH * H) + k1 * ic[2 * NT]) - k2 * ic[3 * NT];
@@ -1305,6 +1342,7 @@ __global__ void __launch_bounds__(EP_TX* EP_TY, sizeof(T) == 4 ? 3 : 2) k_correc
       for (int k = 0; k < EP_NSLOTS; ++k) sc->bscale[k] *= s;
       sc->bscale[sl.pc] = s;
       sc->bscale[sl.out] = s;
+      for (int k = 0; k < EP_NSLOTS; ++k) sc->bscale_f[k] = (float)sc->bscale[k];
       sc->den_scale = s * s;
       sc->counter = 0u;
     }
