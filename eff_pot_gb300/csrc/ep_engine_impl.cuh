@@ -449,8 +449,8 @@ int Engine<T>::poten() {
   const long long nlines = (long long)g.ny * g.nz;
   int r;
   {
-    const int nl = x_lines(0, 1);
-    EP_XLAUNCH("x1_r2c_den", k_x1, (unsigned)((nlines + nl - 1) / nl), shp.xthr[0], x_smem(nl, 1), g, den, S[0], p2, twx,
+    const int nl = x_lines(0, 0);
+    EP_XLAUNCH("x1_r2c_den", k_x1, (unsigned)((nlines + nl - 1) / nl), shp.xthr[0], x_smem(nl, 0), g, den, S[0], p2, twx,
                nl);
   }
   if (grad && (r = d1march(0, den, nullptr, dxd, dyd, dzd))) return r;
@@ -1231,7 +1231,7 @@ int Engine<T>::autotune(std::string* report) {
   // poten gets faster by more than 1% (timing noise)
   {
     float cur = base;
-    const int xreal[4] = {1, 4, 4, 1};
+    const int xreal[4] = {0, 4, 4, 1};
     for (int round = 0; round < 2; ++round) {
       for (int cls = 0; cls < 6; ++cls) {
         if ((cls == 4 && rfft::supported(g.ny)) || (cls == 5 && rfft::supported(g.nz))) continue;

@@ -512,13 +512,22 @@ EP_DEV void x_inverse(const C2<T>* __restrict__ spec, long long line0, int nlv, 
   __syncthreads();
 }
 
+// The pair (f[i], f[i+1]) of a line at an even index i, as one 8- or 16-byte
+// load (rows of even length start aligned).
+template <class T>
+EP_DEV C2<T> ld2(const T* p) {
+  return *reinterpret_cast<const C2<T>*>(p);
+}
+
 // Register-resident r2c of half-lines (N2 > 0): thread t packs its own
-// z[m] = val(2m) + i val(2m+1), m = t + P a, runs xlines' two steps, fetches
+// z[m] = val(2m) + i val(2m+1) = pair(l, m), m = t + P a (one vector load
+// per element from the caller's arrays, all issued before the transform),
+// runs xlines' two steps, fetches
 // the partner Z[N2 - k] of each of its outputs with a warp shuffle (lane
 // P - t, register E - 1 - m; thread 0 holds its own partners) and writes
 // r2c_unpack's X[k] straight to global memory (thread 0 also X[N2]).
 template <class T, int N2, class F>
-EP_DEV void x_forward_reg(F val, C2<T>* __restrict__ out, long long line0, int nlv, int nl, int nxh,
+EP_DEV void x_forward_reg(F pair, C2<T>* __restrict__ out, long long line0, int nlv, int nl, int nxh,
                           const XSmem<T>& S) {
   constexpr int P = XShape<N2>::P, E = XShape<N2>::E, LPW = 32 / P, Q = P + 1;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
@@ -532,7 +541,7 @@ EP_DEV void x_forward_reg(F val, C2<T>* __restrict__ out, long long line0, int n
 #pragma unroll
     for (int a = 0; a < E; ++a) {
       const int m = t + P * a;
-      v[a] = act ? cmk<T>(val(l, 2 * m), val(l, 2 * m + 1)) : cmk<T>(T(0), T(0));
+      v[a] = act ? pair(l, m) : cmk<T>(T(0), T(0));
     }
     epfft::dft<T, E, -1>(v);
     if (t != 0) {
@@ -590,11 +599,13 @@ EP_DEV void x_forward_reg(F val, C2<T>* __restrict__ out, long long line0, int n
   __syncthreads();
 }
 
+// Forward r2c of nl x-lines whose values are pair(l, m) = (val(l, 2m),
+// val(l, 2m+1)).
 template <class T, int N2, class F>
-EP_DEV void x_forward(F val, C2<T>* __restrict__ out, long long line0, int nlv, int nl, int nx, int nxh,
+EP_DEV void x_forward(F pair, C2<T>* __restrict__ out, long long line0, int nlv, int nl, int nx, int nxh,
                       const XSmem<T>& S, const FftPlan& p2) {
   if constexpr (N2 != 0) {
-    x_forward_reg<T, N2>(val, out, line0, nlv, nl, nxh, S);
+    x_forward_reg<T, N2>(pair, out, line0, nlv, nl, nxh, S);
     return;
   }
   const int n2 = nx / 2, ld = S.ld;
@@ -603,7 +614,7 @@ EP_DEV void x_forward(F val, C2<T>* __restrict__ out, long long line0, int nlv, 
   for (int e = threadIdx.x; e < nl * n2; e += blockDim.x) {
     int m;
     const int l = epfft::fdivmod(e, n2, inv2, m);
-    P[l * ld + m] = l < nlv ? cmk<T>(val(l, 2 * m), val(l, 2 * m + 1)) : cmk<T>(T(0), T(0));
+    P[l * ld + m] = l < nlv ? pair(l, m) : cmk<T>(T(0), T(0));
   }
   __syncthreads();
   const C2<T>* Z = x_lines<T, N2, -1>(P, S.Q, nl, ld, p2, S.tw, S.twt);
@@ -624,10 +635,9 @@ __global__ void k_x1(Geo g, const T* __restrict__ den, C2<T>* __restrict__ out, 
   const long long line0 = (long long)blockIdx.x * nl;
   const int nlv = (int)min((long long)nl, nlines - line0);
   S.template load_twiddles<N2>(twx, nx);
-  T* R0 = S.R;
-  for (int e = threadIdx.x; e < nlv * nx; e += blockDim.x) R0[e] = den[line0 * nx + e];
   __syncthreads();
-  x_forward<T, N2>([&](int l, int i) { return R0[l * nx + i]; }, out, line0, nlv, nl, nx, g.nxh, S, p2);
+  x_forward<T, N2>([&](int l, int m) { return ld2(den + (line0 + l) * nx + 2 * m); }, out, line0, nlv, nl, nx,
+                   g.nxh, S, p2);
 }
 
 // X2: c2r of the three products of fden -> dencg, delj4 (and denalf for
@@ -672,18 +682,25 @@ __global__ void k_x2(Geo g, Phys ph, const C2<T>* __restrict__ B0, const C2<T>* 
   }
   __syncthreads();
   x_forward<T, N2>(
-      [&](int l, int i) {
-        const T cg = Rcg[l * nx + i];
-        return den[(line0 + l) * nx + i] * cg * (cp4 + cpp4 * cg);
+      [&](int l, int m) {
+        const C2<T> cg = ld2(Rcg + l * nx + 2 * m), d = ld2(den + (line0 + l) * nx + 2 * m);
+        return cmk<T>(d.x * cg.x * (cp4 + cpp4 * cg.x), d.y * cg.y * (cp4 + cpp4 * cg.y));
       },
       C0, line0, nlv, nl, nx, nxh, S, p2);
   if (otc) {
-    x_forward<T, N2>([&](int l, int i) { return Ral[l * nx + i] * dxd[(line0 + l) * nx + i]; },
-                 C1, line0, nlv, nl, nx, nxh, S, p2);
-    x_forward<T, N2>([&](int l, int i) { return Ral[l * nx + i] * dyd[(line0 + l) * nx + i]; },
-                 C2o, line0, nlv, nl, nx, nxh, S, p2);
-    x_forward<T, N2>([&](int l, int i) { return Ral[l * nx + i] * dzd[(line0 + l) * nx + i]; },
-                 C3, line0, nlv, nl, nx, nxh, S, p2);
+    // f * grad(den), one gradient component per transform
+    const T* grad[3] = {dxd, dyd, dzd};
+    C2<T>* outs[3] = {C1, C2o, C3};
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+      const T* gc = grad[c];
+      x_forward<T, N2>(
+          [&](int l, int m) {
+            const C2<T> f = ld2(Ral + l * nx + 2 * m), d = ld2(gc + (line0 + l) * nx + 2 * m);
+            return cmk<T>(f.x * d.x, f.y * d.y);
+          },
+          outs[c], line0, nlv, nl, nx, nxh, S, p2);
+    }
   }
 }
 
@@ -742,10 +759,12 @@ __global__ void k_x3(Geo g, Phys ph, const __grid_constant__ FdW<T> fd, const C2
     dgx[line0 * nx + e] = d1_line(Rc + l * nx, i, nx, fd.w1[0], fd.R, fd.periodic);
   }
   x_forward<T, N2>(
-      [&](int l, int i) {
-        const int e = l * nx + i;
+      [&](int l, int m) {
+        const int e = l * nx + 2 * m;
         const long long p = line0 * nx + e;
-        return (dxd[p] * Rx[e]) + (dyd[p] * Ry[e]) + (dzd[p] * Rz[e]);
+        const C2<T> gx = ld2(dxd + p), gy_ = ld2(dyd + p), gz_ = ld2(dzd + p);
+        const C2<T> ix = ld2(Rx + e), iy = ld2(Ry + e), iz = ld2(Rz + e);
+        return cmk<T>((gx.x * ix.x) + (gy_.x * iy.x) + (gz_.x * iz.x), (gx.y * ix.y) + (gy_.y * iy.y) + (gz_.y * iz.y));
       },
       E0, line0, nlv, nl, nx, nxh, S, p2);
 }
