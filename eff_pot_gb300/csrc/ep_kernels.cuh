@@ -474,8 +474,7 @@ EP_DEV void x_inverse_reg(const C2<T>* __restrict__ spec, long long line0, int n
 #pragma unroll
       for (int m = 0; m < E; ++m) {
         const int i = t + P * m;
-        Rout[l * nx + 2 * i] = v[m].x * scale;
-        Rout[l * nx + 2 * i + 1] = v[m].y * scale;
+        *reinterpret_cast<C2<T>*>(Rout + l * nx + 2 * i) = cmk<T>(v[m].x * scale, v[m].y * scale);
       }
     }
   }
@@ -510,6 +509,50 @@ EP_DEV void x_inverse(const C2<T>* __restrict__ spec, long long line0, int nlv, 
     Rout[l * nx + 2 * m + 1] = v.y * scale;
   }
   __syncthreads();
+}
+
+// K consecutive values, moved as one 16-byte access when K * sizeof(T) == 16.
+template <class T, int K> struct Pack {
+  T v[K];
+};
+template <int K> struct KC {
+  static constexpr int value = K;
+};
+template <class T, int K>
+EP_DEV Pack<T, K> ldk(const T* p) {
+  Pack<T, K> r;
+  if constexpr (K == 1) {
+    r.v[0] = *p;
+  } else if constexpr (sizeof(T) == 4) {
+    const float4 q = *reinterpret_cast<const float4*>(p);
+    r.v[0] = q.x; r.v[1] = q.y; r.v[2] = q.z; r.v[3] = q.w;
+  } else {
+    const double2 q = *reinterpret_cast<const double2*>(p);
+    r.v[0] = q.x; r.v[1] = q.y;
+  }
+  return r;
+}
+template <class T, int K>
+EP_DEV void stk(T* p, const Pack<T, K>& r) {
+  if constexpr (K == 1) {
+    *p = r.v[0];
+  } else if constexpr (sizeof(T) == 4) {
+    *reinterpret_cast<float4*>(p) = make_float4(r.v[0], r.v[1], r.v[2], r.v[3]);
+  } else {
+    *reinterpret_cast<double2*>(p) = make_double2(r.v[0], r.v[1]);
+  }
+}
+// Point-wise loop over the n contiguous points of an X-pass CTA:
+// body(e, KC<K>) handles points e .. e+K-1, K = 16 / sizeof(T) when vec (the
+// range and every array start 16-byte aligned: nx a multiple of K), else 1.
+template <class T, class F>
+EP_DEV void pointwise(int n, bool vec, F&& body) {
+  constexpr int K = 16 / (int)sizeof(T);
+  if (vec) {
+    for (int e = threadIdx.x * K; e < n; e += blockDim.x * K) body(e, KC<K>());
+  } else {
+    for (int e = threadIdx.x; e < n; e += blockDim.x) body(e, KC<1>());
+  }
 }
 
 // The pair (f[i], f[i+1]) of a line at an even index i, as one 8- or 16-byte
@@ -668,18 +711,25 @@ __global__ void k_x2(Geo g, Phys ph, const C2<T>* __restrict__ B0, const C2<T>* 
   x_inverse<T, N2>(B1, line0, nlv, nl, nx, nxh, S, p2, rn, Rlj);
   if (otc) x_inverse<T, N2>(B2, line0, nlv, nl, nx, nxh, S, p2, rn, Ral);
   const T a0 = kc.a0, a1 = kc.a1, rden0s = kc.rden0s, cp4 = kc.cp4, cpp4 = kc.cpp4;
-  for (int e = threadIdx.x; e < nlv * nx; e += blockDim.x) {
+  const bool vec = nx % (16 / (int)sizeof(T)) == 0;
+  pointwise<T>(nlv * nx, vec, [&](int e, auto kc) {
+    constexpr int K = decltype(kc)::value;
     const long long p = line0 * nx + e;
-    const T cg = Rcg[e], lj = Rlj[e];
-    dencg[p] = cg;
-    delj4[p] = lj;
-    pot4[p] = lj + cg * cg * (a0 + a1 * cg);
+    const Pack<T, K> cg = ldk<T, K>(Rcg + e), lj = ldk<T, K>(Rlj + e);
+    Pack<T, K> pt;
+#pragma unroll
+    for (int k = 0; k < K; ++k) pt.v[k] = lj.v[k] + cg.v[k] * cg.v[k] * (a0 + a1 * cg.v[k]);
+    stk<T, K>(dencg + p, cg);
+    stk<T, K>(delj4 + p, lj);
+    stk<T, K>(pot4 + p, pt);
     if (otc) {
-      const T f = T(1) - Ral[e] * rden0s;
-      falfs[p] = f;
-      Ral[e] = f;  // the f * grad(den) transforms below reuse it
+      Pack<T, K> f = ldk<T, K>(Ral + e);
+#pragma unroll
+      for (int k = 0; k < K; ++k) f.v[k] = T(1) - f.v[k] * rden0s;
+      stk<T, K>(falfs + p, f);
+      stk<T, K>(Ral + e, f);  // the f * grad(den) transforms below reuse it
     }
-  }
+  });
   __syncthreads();
   x_forward<T, N2>(
       [&](int l, int m) {
@@ -729,10 +779,15 @@ __global__ void k_x3(Geo g, Phys ph, const __grid_constant__ FdW<T> fd, const C2
   x_inverse<T, N2>(D0, line0, nlv, nl, nx, nxh, S, p2, rn, Rc);
   if (!otc) {
     const Pen<T> pn(ph);
-    for (int e = threadIdx.x; e < nlv * nx; e += blockDim.x) {
+    pointwise<T>(nlv * nx, nx % (16 / (int)sizeof(T)) == 0, [&](int e, auto kc) {
+      constexpr int K = decltype(kc)::value;
       const long long p = line0 * nx + e;
-      pot4[p] = (pot4[p] + Rc[e]) + penalty_of(pn, den[p]);
-    }
+      Pack<T, K> pt = ldk<T, K>(pot4 + p);
+      const Pack<T, K> rc = ldk<T, K>(Rc + e), dn = ldk<T, K>(den + p);
+#pragma unroll
+      for (int k = 0; k < K; ++k) pt.v[k] = (pt.v[k] + rc.v[k]) + penalty_of(pn, dn.v[k]);
+      stk<T, K>(pot4 + p, pt);
+    });
     return;
   }
   T* Rx = S.R + nl * nx;
@@ -741,17 +796,28 @@ __global__ void k_x3(Geo g, Phys ph, const __grid_constant__ FdW<T> fd, const C2
   x_inverse<T, N2>(D1, line0, nlv, nl, nx, nxh, S, p2, rn, Rx);
   x_inverse<T, N2>(D2, line0, nlv, nl, nx, nxh, S, p2, rn, Ry);
   x_inverse<T, N2>(D3, line0, nlv, nl, nx, nxh, S, p2, rn, Rz);
-  for (int e = threadIdx.x; e < nlv * nx; e += blockDim.x) {
+  pointwise<T>(nlv * nx, nx % (16 / (int)sizeof(T)) == 0, [&](int e, auto kc) {
+    constexpr int K = decltype(kc)::value;
     const long long p = line0 * nx + e;
-    pot4[p] = pot4[p] + Rc[e];
-    const T f = falfs[p];
-    intx[p] = Rx[e];
-    inty[p] = Ry[e];
-    intz[p] = Rz[e];
-    gy[p] = f * Ry[e];
-    gz[p] = f * Rz[e];
-    Rc[e] = f * Rx[e];
-  }
+    Pack<T, K> pt = ldk<T, K>(pot4 + p), rc = ldk<T, K>(Rc + e);
+    const Pack<T, K> f = ldk<T, K>(falfs + p), rx = ldk<T, K>(Rx + e), ry = ldk<T, K>(Ry + e),
+                     rz = ldk<T, K>(Rz + e);
+    Pack<T, K> fy, fz;
+#pragma unroll
+    for (int k = 0; k < K; ++k) {
+      pt.v[k] = pt.v[k] + rc.v[k];
+      fy.v[k] = f.v[k] * ry.v[k];
+      fz.v[k] = f.v[k] * rz.v[k];
+      rc.v[k] = f.v[k] * rx.v[k];
+    }
+    stk<T, K>(pot4 + p, pt);
+    stk<T, K>(intx + p, rx);
+    stk<T, K>(inty + p, ry);
+    stk<T, K>(intz + p, rz);
+    stk<T, K>(gy + p, fy);
+    stk<T, K>(gz + p, fz);
+    stk<T, K>(Rc + e, rc);
+  });
   __syncthreads();
   for (int e = threadIdx.x; e < nlv * nx; e += blockDim.x) {
     int i;
@@ -788,12 +854,20 @@ __global__ void k_x4(Geo g, Phys ph, const C2<T>* __restrict__ F0, const T* __re
   x_inverse<T, N2>(F0, line0, nlv, nl, nx, nxh, S, p2, kc.renor, Ru);
   const T rden0s = kc.rden0s, h2 = kc.h2o2m4, al = kc.alphas;
   const Pen<T> pn(ph);
-  for (int e = threadIdx.x; e < nlv * nx; e += blockDim.x) {
+  pointwise<T>(nlv * nx, nx % (16 / (int)sizeof(T)) == 0, [&](int e, auto kc) {
+    constexpr int K = decltype(kc)::value;
     const long long p = line0 * nx + e;
-    const T ua = ((Ru[e] * rden0s + dgx[p]) + dyz[p]) * h2 * al;
-    ualphas[p] = ua;
-    pot4[p] = (pot4[p] + ua) + penalty_of(pn, den[p]);
-  }
+    const Pack<T, K> ru = ldk<T, K>(Ru + e), gx = ldk<T, K>(dgx + p), yz = ldk<T, K>(dyz + p),
+                     dn = ldk<T, K>(den + p);
+    Pack<T, K> pt = ldk<T, K>(pot4 + p), ua;
+#pragma unroll
+    for (int k = 0; k < K; ++k) {
+      ua.v[k] = ((ru.v[k] * rden0s + gx.v[k]) + yz.v[k]) * h2 * al;
+      pt.v[k] = (pt.v[k] + ua.v[k]) + penalty_of(pn, dn.v[k]);
+    }
+    stk<T, K>(ualphas + p, ua);
+    stk<T, K>(pot4 + p, pt);
+  });
 }
 
 // ---------------------------------------------------------------------------
