@@ -88,7 +88,7 @@ class Engine {
   int launch_march(const void* fn, dim3 grid, dim3 blk, size_t smem, void** args, const char* name, int which);
   int steppc_update(double dt, cudaGraphExec_t x, cudaGraphNode_t np, cudaGraphNode_t nc);
   bool graph_ok() const { return cfg.impurity != EP_IMPURITY_MOVING && !prof->on; }
-  int march_zchunk(int blocks_per_sm) const;
+  int march_zchunk(int blocks_per_sm, int tile_x = EP_TX) const;
   long long bytes = 0;
   Phys phys{};
   FdW<T> fd{};

@@ -306,7 +306,7 @@ int Engine<T>::init(const ep_config& c, cudaStream_t s, Prof* p, ImpState* im, s
 #undef EP_OCC
     zc_pc = march_zchunk(occ_pc);
     zc_rk = march_zchunk(occ_rk);
-    zc_d1 = march_zchunk(occ_d1);
+    zc_d1 = march_zchunk(occ_d1, EP_D1_TX);
   }
   {
     const long long nxy = (long long)((c.nx + EP_TX - 1) / EP_TX) * ((c.ny + EP_TY - 1) / EP_TY);
@@ -319,8 +319,8 @@ int Engine<T>::init(const ep_config& c, cudaStream_t s, Prof* p, ImpState* im, s
 }
 
 template <class T>
-int Engine<T>::march_zchunk(int blocks_per_sm) const {
-  const long long nxy = (long long)((g.nx + EP_TX - 1) / EP_TX) * ((g.ny + EP_TY - 1) / EP_TY);
+int Engine<T>::march_zchunk(int blocks_per_sm, int tile_x) const {
+  const long long nxy = (long long)((g.nx + tile_x - 1) / tile_x) * ((g.ny + EP_TY - 1) / EP_TY);
   const long long slots = (long long)dev_sm * std::max(1, blocks_per_sm);
   return march_chunk(nxy, g.nz, slots, fd.R);
 }
@@ -421,7 +421,7 @@ int Engine<T>::zconv(const CT* const* in, CT* const (*out)[3], const T* const (*
 // First-derivative marches (k_d1march): mode 0 = grad f, mode 1 = dy f + dz f2.
 template <class T>
 int Engine<T>::d1march(int mode, const T* f, const T* f2, T* o0, T* o1, T* o2) {
-  dim3 grid((g.nx + EP_TX - 1) / EP_TX, (g.ny + EP_TY - 1) / EP_TY, (g.nz + zc_d1 - 1) / zc_d1);
+  dim3 grid((g.nx + EP_D1_TX - 1) / EP_D1_TX, (g.ny + EP_TY - 1) / EP_TY, (g.nz + zc_d1 - 1) / zc_d1);
   dim3 blk(EP_TX, EP_TY);
 #define EP_D1(RR)                                                                                  \
   case RR:                                                                                         \

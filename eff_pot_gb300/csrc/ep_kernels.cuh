@@ -1200,33 +1200,41 @@ EP_DEV void lap_march_async(const Geo& g, const C2<T>* __restrict__ psi, const F
 // the boundary handling and summation order of d1_global):
 //   MODE 0: o0, o1, o2 = d/dx, d/dy, d/dz of f   (derden, energy.f90:207-227)
 //   MODE 1: o0 = d/dy f + d/dz f2                (term_alfa.f90:220-230)
+// Each thread computes two x-neighbouring points (x even), so every
+// neighbour in shared memory, the z-queue and every store move as pairs
+// (8-byte FP32 / 16-byte FP64 accesses): the march is bound by its
+// load/store instructions, not its arithmetic.
+#define EP_D1_TX (2 * EP_TX)  // x points of a CTA row
 template <class T, int R, int MODE>
 __global__ void __launch_bounds__(EP_TX* EP_TY) k_d1march(Geo g, const __grid_constant__ FdW<T> fd, int zc,
                                                          const T* __restrict__ f, const T* __restrict__ f2,
                                                          T* __restrict__ o0, T* __restrict__ o1,
                                                          T* __restrict__ o2) {
+  typedef C2<T> PT;
   // The plane tile (x halo rounded up to whole 16-byte chunks) is fetched
   // chunk by chunk when nx is a multiple of the chunk; element by element
   // otherwise.  Offsets of chunks (or elements) are tabulated once per CTA.
   constexpr int CH = 16 / (int)sizeof(T);
   constexpr int HX = MODE == 0 ? ((R + CH - 1) / CH) * CH : 0;
-  constexpr int W = EP_TX + 2 * HX, H = EP_TY + 2 * R, PL = W * H, NT = EP_TX * EP_TY;
-  constexpr int WC = W / CH, PC = WC * H;
+  constexpr int W = EP_D1_TX + 2 * HX, H = EP_TY + 2 * R, PL = W * H, NT = EP_TX * EP_TY;
+  constexpr int WC = W / CH, PC = WC * H, WP = W / 2;
+  constexpr int JLO = -((R + 1) / 2), JHI = (R + 1) / 2, NE = 2 * (JHI - JLO + 1);
+  static_assert(HX >= -2 * JLO || MODE != 0, "x halo");
   __shared__ __align__(16) T sp[2][PL];
-  __shared__ __align__(16) T sq[2][NT];
+  __shared__ __align__(16) PT sq[2][NT];
   __shared__ int soff[PL];
   const T* fq = MODE == 0 ? f : f2;
   const int tx = threadIdx.x, ty = threadIdx.y, tid = ty * EP_TX + tx;
-  const int x = blockIdx.x * EP_TX + tx, y = blockIdx.y * EP_TY + ty;
+  const int x = blockIdx.x * EP_D1_TX + 2 * tx, y = blockIdx.y * EP_TY + ty;
   const int z0 = blockIdx.z * zc, z1 = min(z0 + zc, g.nz);
-  const bool valid = (x < g.nx) && (y < g.ny);
+  const bool valid = (x < g.nx) && (y < g.ny);  // nx is even: x + 1 < nx too
   const int per = fd.periodic;
   const bool vec = (g.nx % CH) == 0;
   const int nunits = vec ? PC : PL, ulen = vec ? CH : 1, uperrow = vec ? WC : W;
   const long long sxy = (long long)g.nx * g.ny;
   for (int e = tid; e < nunits; e += NT) {
     const int r = e / uperrow, c = (e - r * uperrow) * ulen;
-    const int xx = blockIdx.x * EP_TX - HX + c, yy = blockIdx.y * EP_TY - R + r;
+    const int xx = blockIdx.x * EP_D1_TX - HX + c, yy = blockIdx.y * EP_TY - R + r;
     int o = -1;
     if (xx >= 0 && xx < g.nx && yy >= 0 && yy < g.ny) o = xx + g.nx * yy;
     else if (per) o = wrapi(xx, g.nx) + g.nx * wrapi(yy, g.ny);
@@ -1237,11 +1245,11 @@ __global__ void __launch_bounds__(EP_TX* EP_TY) k_d1march(Geo g, const __grid_co
     return zz;
   };
   const long long pxy = (long long)x + (long long)g.nx * y;
-  T q[2 * R + 1];
+  PT q[2 * R + 1];
 #pragma unroll
   for (int k = 0; k < 2 * R; ++k) {
     const int zz = zwrap(z0 - R + k);
-    q[k] = (valid && zz >= 0) ? fq[pxy + sxy * zz] : T(0);
+    q[k] = (valid && zz >= 0) ? *reinterpret_cast<const PT*>(fq + pxy + sxy * zz) : cmk<T>(T(0), T(0));
   }
   __syncthreads();
   auto prefetch = [&](int z, int buf) {
@@ -1268,8 +1276,8 @@ __global__ void __launch_bounds__(EP_TX* EP_TY) k_d1march(Geo g, const __grid_co
     }
     if (valid) {
       const int zq = zwrap(z + R);
-      if (zq >= 0) cp_async<sizeof(T)>(&sq[buf][tid], fq + pxy + sxy * zq);
-      else sq[buf][tid] = T(0);
+      if (zq >= 0) cp_async<sizeof(PT)>(&sq[buf][tid], fq + pxy + sxy * zq);
+      else sq[buf][tid] = cmk<T>(T(0), T(0));
     }
     cp_commit();
   };
@@ -1285,22 +1293,42 @@ __global__ void __launch_bounds__(EP_TX* EP_TY) k_d1march(Geo g, const __grid_co
     __syncthreads();
     if (valid) {
       q[2 * R] = sq[buf][tid];
-      const T* row = &sp[buf][(ty + R) * W + (tx + HX)];
+      // row element x of this thread (even offset: W, HX and 2 tx are even)
+      const T* rowe = &sp[buf][(ty + R) * W + HX + 2 * tx];
+      const PT* rowp = reinterpret_cast<const PT*>(rowe);
       const long long p = pxy + sxy * z;
-      T dy = T(0), dz = T(0);
+      PT dy = cmk<T>(T(0), T(0)), dz = cmk<T>(T(0), T(0));
 #pragma unroll
-      for (int k = 1; k <= R; ++k) dy += fd.w1[1][k] * (row[k * W] - row[-k * W]);
+      for (int k = 1; k <= R; ++k) {
+        const PT a = rowp[k * WP], b = rowp[-k * WP];
+        dy.x += fd.w1[1][k] * (a.x - b.x);
+        dy.y += fd.w1[1][k] * (a.y - b.y);
+      }
 #pragma unroll
-      for (int k = 1; k <= R; ++k) dz += fd.w1[2][k] * (q[R + k] - q[R - k]);
+      for (int k = 1; k <= R; ++k) {
+        dz.x += fd.w1[2][k] * (q[R + k].x - q[R - k].x);
+        dz.y += fd.w1[2][k] * (q[R + k].y - q[R - k].y);
+      }
       if (MODE == 0) {
-        T dx = T(0);
+        // elements x + JLO*2 .. x + 2*JHI + 1 of the row, as pairs
+        T e[NE];
 #pragma unroll
-        for (int k = 1; k <= R; ++k) dx += fd.w1[0][k] * (row[k] - row[-k]);
-        o0[p] = dx;
-        o1[p] = dy;
-        o2[p] = dz;
+        for (int j = JLO; j <= JHI; ++j) {
+          const PT v = rowp[j];
+          e[2 * (j - JLO)] = v.x;
+          e[2 * (j - JLO) + 1] = v.y;
+        }
+        PT dx = cmk<T>(T(0), T(0));
+#pragma unroll
+        for (int k = 1; k <= R; ++k) {
+          dx.x += fd.w1[0][k] * (e[k - 2 * JLO] - e[-k - 2 * JLO]);
+          dx.y += fd.w1[0][k] * (e[1 + k - 2 * JLO] - e[1 - k - 2 * JLO]);
+        }
+        *reinterpret_cast<PT*>(o0 + p) = dx;
+        *reinterpret_cast<PT*>(o1 + p) = dy;
+        *reinterpret_cast<PT*>(o2 + p) = dz;
       } else {
-        o0[p] = dy + dz;
+        *reinterpret_cast<PT*>(o0 + p) = cmk<T>(dy.x + dz.x, dy.y + dz.y);
       }
     }
 #pragma unroll
