@@ -295,6 +295,8 @@ int ep_destroy(ep_ctx* c) {
   if (c->imp.d_potpi) cudaFree(c->imp.d_potpi);
   if (c->imp.d_potdel) cudaFree(c->imp.d_potdel);
   if (c->imp.d_potsigdel) cudaFree(c->imp.d_potsigdel);
+  if (c->imp.d_potpi_f) cudaFree(c->imp.d_potpi_f);
+  if (c->imp.d_potdel_f) cudaFree(c->imp.d_potdel_f);
   c->prof.release();
   for (cudaEvent_t e : c->ev)
     if (e) cudaEventDestroy(e);
@@ -335,6 +337,11 @@ static int upload_tables(ep_ctx* c, const double* const tabs[3], int npot) {
     if (*d) cudaFree(*d);
     *d = nullptr;
   }
+  float** dstf[2] = {&c->imp.d_potpi_f, &c->imp.d_potdel_f};
+  for (float** d : dstf) {
+    if (*d) cudaFree(*d);
+    *d = nullptr;
+  }
   c->imp.have_tables = false;
   const size_t n = (size_t)(npot + 2) * sizeof(double);
   for (int i = 0; i < 3; ++i) {
@@ -345,6 +352,18 @@ static int upload_tables(ep_ctx* c, const double* const tabs[3], int npot) {
       return fail(c, EP_ERR_OOM, "table allocation failed");
     }
     cudaMemcpyAsync(*dst[i], tabs[i], n, cudaMemcpyHostToDevice, c->st);
+  }
+  // P state: FP32 copies for the FP32 engine's field evaluation
+  std::vector<float> tf((size_t)npot + 2);
+  for (int i = 0; i < 2 && c->cfg.state == EP_STATE_P; ++i) {
+    for (size_t k = 0; k < tf.size(); ++k) tf[k] = (float)tabs[i][k];
+    if (cudaMalloc((void**)dstf[i], tf.size() * sizeof(float)) != cudaSuccess) {
+      cudaGetLastError();
+      *dstf[i] = nullptr;
+      return fail(c, EP_ERR_OOM, "table allocation failed");
+    }
+    if (cudaMemcpy(*dstf[i], tf.data(), tf.size() * sizeof(float), cudaMemcpyHostToDevice) != cudaSuccess)
+      return fail(c, EP_ERR_CUDA, "table upload failed");
   }
   if (cudaStreamSynchronize(c->st) != cudaSuccess) return fail(c, EP_ERR_CUDA, "table upload failed");
   return EP_OK;
@@ -573,6 +592,11 @@ int ep_set_precision(ep_ctx* c, int precision) {
     }
     if ((r = c->e32->ensure_materialized())) return r;
     if ((r = c->e64->import_state(*c->e32))) return r;
+    // the impurity field is recomputed in FP64 from the tables and the
+    // impurity state, not widened from its FP32 copy: a fixed impurity's
+    // field is never refreshed, so the refinement sweeps would otherwise
+    // carry its FP32 rounding to the end
+    if (c->cfg.impurity != EP_IMPURITY_NONE && c->imp.have_tables && (r = c->e64->potenimp())) return r;
   } else {
     if (!c->e32) {
       c->e32 = new Engine<float>();

@@ -47,6 +47,9 @@ struct ImpState {
   double* d_potpi = nullptr;
   double* d_potdel = nullptr;
   double* d_potsigdel = nullptr;
+  // P state: FP32 copies of d_potpi, d_potdel for the FP32 engine
+  float* d_potpi_f = nullptr;
+  float* d_potdel_f = nullptr;
   ep_potential plus{};
   bool have_tables = false;
 };

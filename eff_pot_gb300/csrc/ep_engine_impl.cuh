@@ -529,6 +529,19 @@ int Engine<T>::potenimp() {
               imp->umax_pi, imp->umax_sigma, G, delta, vpi, sigdel, uimp);
     return EP_OK;
   }
+  if constexpr (sizeof(T) == 4) {
+    if (imp->d_potpi_f) {
+      float2 fv[6];
+      for (int i = 0; i < 6; ++i) fv[i] = make_float2((float)imp->invar[i].real(), (float)imp->invar[i].imag());
+      const double h = rmax / (imp->npot - 1);
+      auto kf = k_potenimp_f;
+      EP_LAUNCH("potenimp", kf, 4 * 152, 256, 0, g, (float)cfg.xmax, (float)cfg.ymax, (float)cfg.zmax, (float)hx,
+                (float)hy, (float)hz, (float)imp->rimp[0], (float)imp->rimp[1], (float)imp->rimp[2], imp->d_potpi_f,
+                imp->d_potdel_f, imp->npot, (float)h, (float)(1.0 / h), (float)imp->umax_sigma, fv[0], fv[1], fv[2],
+                fv[3], fv[4], fv[5], vpi, delta, uimp);
+      return EP_OK;
+    }
+  }
   double2 iv[6];
   for (int i = 0; i < 6; ++i) iv[i] = make_double2(imp->invar[i].real(), imp->invar[i].imag());
   auto k = k_potenimp<T>;
@@ -616,9 +629,16 @@ int Engine<T>::forceimp(double* F) {
     for (int i = 0; i < 3; ++i) F[i] = -s[i] * dxyz;
     return EP_OK;
   }
-  auto k = k_impmoments<T>;
-  EP_LAUNCH("impmoments", k, EP_RED_BLOCKS, 256, 0, g, den, dxd, dyd, dzd, uimp, vpi, delta, cfg.xmax, cfg.ymax,
-            cfg.zmax, hx, hy, hz, imp->rimp[0], imp->rimp[1], imp->rimp[2], partials);
+  if constexpr (sizeof(T) == 4) {
+    auto kf = k_impmoments_f;
+    EP_LAUNCH("impmoments", kf, EP_RED_BLOCKS, 256, 0, g, den, dxd, dyd, dzd, uimp, vpi, delta, (float)cfg.xmax,
+              (float)cfg.ymax, (float)cfg.zmax, (float)hx, (float)hy, (float)hz, (float)imp->rimp[0],
+              (float)imp->rimp[1], (float)imp->rimp[2], partials);
+  } else {
+    auto k = k_impmoments<T>;
+    EP_LAUNCH("impmoments", k, EP_RED_BLOCKS, 256, 0, g, den, dxd, dyd, dzd, uimp, vpi, delta, cfg.xmax, cfg.ymax,
+              cfg.zmax, hx, hy, hz, imp->rimp[0], imp->rimp[1], imp->rimp[2], partials);
+  }
   int r;
   if ((r = reduce_finalize(EP_RED_BLOCKS, 9, 16, 0))) return r;
   double s[9];

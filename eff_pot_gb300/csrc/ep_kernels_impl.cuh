@@ -166,6 +166,75 @@ __global__ void k_impmoments_d(Geo g, const T* __restrict__ den, const T* __rest
   block_reduce_store<18>(acc, partials);
 }
 
+// FP32 engine, P state: the impurity field in FP32 arithmetic (float tables,
+// 1/h and the coordinates rounded once; a double per point would run on the
+// FP64 pipe at 1/64 of the FP32 rate).  update() (potenimp.f90:588-632)
+// evaluates, in both of its branches, the parabola through f(i0-1), f(i0),
+// f(i0+1); here it is evaluated about r0 = (i0-1) h, which avoids the
+// cancellation of its global coefficients in FP32.
+EP_DEV float interp_update_f(float r, int nint, float h, float rh, const float* __restrict__ f) {
+  int i0 = (int)(1.5f + r * rh);
+  i0 = min(max(i0, 1), nint);
+  const float r0 = (float)(i0 - 1) * h;
+  const float fm = f[i0 - 1], f0 = f[i0], fp = f[i0 + 1];
+  const float aa = (fp - 2.0f * f0 + fm) * (0.5f * rh * rh);
+  const float b = (fp - f0) * rh - aa * h;
+  const float d = r - r0;
+  return f0 + d * (b + aa * d);
+}
+
+static __global__ void k_potenimp_f(Geo g, float xmax, float ymax, float zmax, float hx, float hy, float hz, float r0,
+                             float r1, float r2, const float* __restrict__ potpi, const float* __restrict__ potdel,
+                             int npot, float h, float rh, float umax_sigma, float2 iv0, float2 iv1, float2 iv2,
+                             float2 iv3, float2 iv4, float2 iv5, float* __restrict__ vpi, float* __restrict__ delta,
+                             float* __restrict__ uimp) {
+  for (long long p = blockIdx.x * (long long)blockDim.x + threadIdx.x; p < g.N; p += (long long)gridDim.x * blockDim.x) {
+    int ix, iy, iz;
+    idx3(g, p, ix, iy, iz);
+    const float xx = ((float)ix * hx - xmax) - r0;
+    const float yy = ((float)iy * hy - ymax) - r1;
+    const float zz = ((float)iz * hz - zmax) - r2;
+    const float rr2 = xx * xx + (yy * yy + zz * zz);
+    const float r = sqrtf(rr2);
+    const float vp = interp_update_f(r, npot, h, rh, potpi);
+    const float dl = r > 1e-3f ? interp_update_f(r, npot, h, rh, potdel) / rr2 : umax_sigma;
+    const float ox = iv0.x * xx + iv2.x * yy + iv4.x * zz, oy = iv0.y * xx + iv2.y * yy + iv4.y * zz;
+    const float ex = iv1.x * xx + iv3.x * yy + iv5.x * zz, ey = iv1.y * xx + iv3.y * yy + iv5.y * zz;
+    const float u = vp + dl * ((ox * ox + oy * oy) + (ex * ex + ey * ey));
+    vpi[p] = vp;
+    delta[p] = dl;
+    uimp[p] = fminf(u, 1000.0f);
+  }
+}
+
+// FP32 engine, P state: forceimp sums and the six moments in compensated
+// FP32 per thread, FP64 across threads and blocks.
+static __global__ void k_impmoments_f(Geo g, const float* __restrict__ den, const float* __restrict__ dxd,
+                               const float* __restrict__ dyd, const float* __restrict__ dzd,
+                               const float* __restrict__ uimp, const float* __restrict__ vpi,
+                               const float* __restrict__ delta, float xmax, float ymax, float zmax, float hx, float hy,
+                               float hz, float r0, float r1, float r2, double* __restrict__ partials) {
+  Acc<float> acc[9];
+  for (long long p = blockIdx.x * (long long)blockDim.x + threadIdx.x; p < g.N; p += (long long)gridDim.x * blockDim.x) {
+    int ix, iy, iz;
+    idx3(g, p, ix, iy, iz);
+    const float u = uimp[p];
+    acc[0].add(dxd[p] * u);
+    acc[1].add(dyd[p] * u);
+    acc[2].add(dzd[p] * u);
+    const float xx = ((float)ix * hx - xmax) - r0, yy = ((float)iy * hy - ymax) - r1,
+                zz = ((float)iz * hz - zmax) - r2;
+    const float a1 = den[p], a2 = delta[p], a3 = vpi[p];
+    acc[3].add(a1 * (a2 * xx * xx + a3));
+    acc[4].add(a1 * a2 * xx * yy);
+    acc[5].add(a1 * a2 * xx * zz);
+    acc[6].add(a1 * (a2 * yy * yy + a3));
+    acc[7].add(a1 * a2 * yy * zz);
+    acc[8].add(a1 * (a2 * zz * zz + a3));
+  }
+  block_reduce_store_acc<9>(acc, partials);
+}
+
 // Sum of |psi|^2 (block partials).
 template <class T>
 __global__ void k_normsum(const C2<T>* __restrict__ psi, long long N, double* __restrict__ partials) {
