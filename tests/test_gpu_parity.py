@@ -199,3 +199,42 @@ def test_fp64_path_matches_the_committed_golden_vectors():
     for k in ("norm", "den_sum", "den_sq"):
         assert abs(got[k] - want[k]) <= 1e-10 * abs(want[k]), k
     assert np.allclose(got["den_samples"], want["den_samples"], rtol=0, atol=1e-9)
+
+
+def test_precision_switch_evaluates_the_impurity_field_in_fp64(oracle):
+    """FP32 -> FP64 recomputes u_imp from the tables in FP64 (a fixed
+    impurity's field is never refreshed afterwards): equal to the oracle's
+    field to FP64 rounding, not to the FP32 copy's 1e-7."""
+    cfg32, psi = droplet_case(precision=_abi.EP_FP32)
+    cfg64, _ = droplet_case()
+    g, o = pair(cfg32, psi, rimp=(0.37, -1.21, 0.66), oracle=oracle)
+    with g, o:
+        g.set_precision("fp64")
+        assert rel(g.field("uimp"), o.field("uimp")) < 1e-13
+        assert rel(g.field("delta"), o.field("delta")) < 1e-13
+
+
+def test_fp32_impurity_field_and_moments_track_fp64(oracle):
+    """The FP32 engine evaluates the P-state field, the force and the six
+    moments in FP32 arithmetic (float tables, compensated sums): within
+    FP32 accuracy of the FP64 oracle on the same density."""
+    cfg32, psi = droplet_case(precision=_abi.EP_FP32, impurity=_abi.EP_IMPURITY_MOVING, mimpur=40.0,
+                              fix_lambda=1)
+    cfg64, _ = droplet_case(impurity=_abi.EP_IMPURITY_MOVING, mimpur=40.0, fix_lambda=1)
+    g = ep.Solver(cfg32)
+    o = oracle.OracleSolver(cfg64)
+    m1 = ep.morse(10.0, 4.5, 1.2, r_cutoff=0.0, umax=1000.0)
+    m2 = ep.morse(25.0, 4.0, 1.1, r_cutoff=0.0, umax=1000.0)
+    inv = np.zeros(10, dtype=np.complex128)
+    inv[0], inv[3] = 0.6, 0.8j
+    for s in (g, o):
+        s.set_impurity_potentials(m1, m2, ep.null_potential())
+        s.set_impurity(rimp=(0.9, -0.4, 1.3), invar=inv)
+        s.start(psi)
+    with g, o:
+        for f in ("uimp", "vpi", "delta"):
+            assert rel(g.field(f), o.field(f)) < 2e-6, f
+        Fg, Fo = g.forceimp(), o.forceimp()
+        assert np.max(np.abs(Fg - Fo)) < 5e-4 * np.max(np.abs(Fo)), (Fg, Fo)
+        mg, mo = g.impurity_moments(), o.impurity_moments()
+        assert np.max(np.abs(mg - mo)) < 1e-5 * np.max(np.abs(mo)), (mg, mo)
