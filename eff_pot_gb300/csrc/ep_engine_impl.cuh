@@ -289,7 +289,8 @@ int Engine<T>::init(const ep_config& c, cudaStream_t s, Prof* p, ImpState* im, s
 #define EP_ATTR(RR)                                                                                      \
   cudaFuncSetAttribute(k_predict<T, RR>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)march_smem<T, RR, 4, 2>()); \
   cudaFuncSetAttribute(k_correct<T, RR, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)march_smem<T, RR, 5, 2>()); \
-  cudaFuncSetAttribute(k_correct<T, RR, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)march_smem<T, RR, 5, 2>());
+  cudaFuncSetAttribute(k_correct<T, RR, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)march_smem<T, RR, 5, 2>()); \
+  cudaFuncSetAttribute(k_rkstage<T, RR>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)march_smem<T, RR, 1, 2>());
   EP_ATTR(1) EP_ATTR(2) EP_ATTR(3) EP_ATTR(4) EP_ATTR(5) EP_ATTR(6)
 #undef EP_ATTR
   {
@@ -299,7 +300,7 @@ int Engine<T>::init(const ep_config& c, cudaStream_t s, Prof* p, ImpState* im, s
 #define EP_OCC(RR)                                                                                         \
   case RR:                                                                                                 \
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_pc, k_correct<T, RR, true>, nt, march_smem<T, RR, 5, 2>()); \
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_rk, k_rkstage<T, RR>, nt, 0);                       \
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_rk, k_rkstage<T, RR>, nt, march_smem<T, RR, 1, 2>()); \
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_d1, k_d1march<T, RR, 0>, nt, 0);                    \
     break;
     switch (fd.R) { EP_OCC(1) EP_OCC(2) EP_OCC(3) EP_OCC(4) EP_OCC(5) EP_OCC(6) default: break; }
@@ -870,7 +871,8 @@ int Engine<T>::rk_stage(int jr, double dt) {
 #define EP_RK(RR)                                                                                              \
   case RR: {                                                                                                   \
     auto k = k_rkstage<T, RR>;                                                                                 \
-    EP_LAUNCH("rkstage", k, grid, blk, 0, g, fd, phys, zc_rk, psi, pot4, uimp, q, out, hout, den, a, b, cr, d, sc); \
+    EP_LAUNCH("rkstage", k, grid, blk, (march_smem<T, RR, 1, 2>()), g, fd, phys, zc_rk, psi, pot4, uimp, q, out, hout, \
+              den, a, b, cr, d, sc);                                                                           \
   } break;
   switch (fd.R) {
     EP_RK(1) EP_RK(2) EP_RK(3) EP_RK(4) EP_RK(5) EP_RK(6)

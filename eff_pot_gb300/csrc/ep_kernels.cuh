@@ -1011,59 +1011,11 @@ __global__ void k_zconv(const __grid_constant__ ConvSpec<T> cs, LineSet ls, cons
 // ---------------------------------------------------------------------------
 // 2.5-D stencil march: a (TX x TY) tile of (x,y) columns walks z; the x/y
 // neighbours of each plane come from a shared-memory tile with halo R, the
-// z neighbours from a per-thread register queue.  f(p, psi, lap) is called
-// for every grid point with lap = d2x + d2y + d2z (Deriv3D_pc,
+// z neighbours from a per-thread register queue.  The callback gets every
+// grid point with lap = d2x + d2y + d2z (Deriv3D_pc,
 // init_deriv_parallel.f90:923-1197, summed as steppc.f90:53).
 #define EP_TX 32
 #define EP_TY 8
-
-template <class T, int R, class F>
-EP_DEV void lap_march(const Geo& g, const C2<T>* __restrict__ psi, const FdW<T>& fd, int zc, C2<T>* sp, F&& f,
-                      T scale = T(1)) {
-  const int tx = threadIdx.x, ty = threadIdx.y;
-  const int x = blockIdx.x * EP_TX + tx, y = blockIdx.y * EP_TY + ty;
-  const int z0 = blockIdx.z * zc, z1 = min(z0 + zc, g.nz);
-  const bool valid = (x < g.nx) && (y < g.ny);
-  const int per = fd.periodic;
-  const long long sxy = (long long)g.nx * g.ny;
-  auto at = [&](int xx, int yy, int zz) -> C2<T> {
-    if (xx < 0 || xx >= g.nx || yy < 0 || yy >= g.ny || zz < 0 || zz >= g.nz) {
-      if (!per) return cmk<T>(T(0), T(0));
-      xx = wrapi(xx, g.nx); yy = wrapi(yy, g.ny); zz = wrapi(zz, g.nz);
-    }
-    const C2<T> v = psi[xx + (long long)g.nx * yy + sxy * zz];
-    return cmk<T>(v.x * scale, v.y * scale);
-  };
-  C2<T> q[2 * R + 1];
-#pragma unroll
-  for (int k = 0; k < 2 * R; ++k) q[k] = valid ? at(x, y, z0 - R + k) : cmk<T>(T(0), T(0));
-  const int W = EP_TX + 2 * R, H = EP_TY + 2 * R;
-  const int tid = ty * EP_TX + tx;
-  for (int z = z0; z < z1; ++z) {
-    q[2 * R] = valid ? at(x, y, z + R) : cmk<T>(T(0), T(0));
-    __syncthreads();
-    for (int e = tid; e < W * H; e += EP_TX * EP_TY) {
-      const int r = e / W, c = e - r * W;
-      sp[e] = at(blockIdx.x * EP_TX - R + c, blockIdx.y * EP_TY - R + r, z);
-    }
-    __syncthreads();
-    if (valid) {
-      const C2<T>* row = sp + (ty + R) * W + (tx + R);
-      const C2<T> c = q[R];
-      C2<T> lx = fd.w2[0][0] * c, ly = fd.w2[1][0] * c, lz = fd.w2[2][0] * c;
-#pragma unroll
-      for (int k = 1; k <= R; ++k) {
-        lx = lx + fd.w2[0][k] * (row[-k] + row[k]);
-        ly = ly + fd.w2[1][k] * (row[-k * W] + row[k * W]);
-        lz = lz + fd.w2[2][k] * (q[R - k] + q[R + k]);
-      }
-      f((long long)x + (long long)g.nx * y + sxy * z, c, (lx + ly) + lz);
-    }
-#pragma unroll
-    for (int k = 0; k < 2 * R; ++k) q[k] = q[k + 1];
-  }
-}
-
 
 // Shared memory of the pipelined march: two planes with halo, two z-queue
 // slots, two copies of NC complex and NR real per-point inputs.
@@ -1074,7 +1026,7 @@ constexpr size_t march_smem() {
          (size_t)(EP_TX + 2 * R) * (EP_TY + 2 * R) * sizeof(int);
 }
 
-// The 2.5-D march of lap_march, software-pipelined: while plane z is
+// The 2.5-D march, software-pipelined: while plane z is
 // computed, cp.async brings plane z+1 (with halo), the z-queue element
 // (x, y, z+1+R) and the NC complex / NR real per-point inputs of plane z+1
 // into the other half of a double buffer.  f(p, psi, lap, ic, ir) gets the
@@ -1470,9 +1422,11 @@ __global__ void __launch_bounds__(EP_TX* EP_TY, sizeof(T) == 4 ? 3 : 2) k_correc
   }
 }
 
-// One Runge-Kutta-Gill stage of steprk.f90:71-89 (jrun-independent part);
-// first stage also records H into hout (the history shift itself is done
-// by rotating buffers).  den <= 0 raises a flag (steprk.f90:94-110).
+// One Runge-Kutta-Gill stage of steprk.f90:71-89 (jrun-independent part) on
+// the pipelined march (q, pot4 and uimp of the next plane arrive with its
+// halo); the first stage also records H into hout (the history shift itself
+// is done by rotating buffers).  den <= 0 raises a flag (steprk.f90:94-110).
+// psi is materialised before steprk (no pending renormalisation scale).
 template <class T, int R>
 __global__ void __launch_bounds__(EP_TX* EP_TY, sizeof(T) == 4 ? 4 : 2) k_rkstage(Geo g, FdW<T> fd, Phys ph, int zc,
                                                          const C2<T>* __restrict__ psi, const T* __restrict__ pot4,
@@ -1480,12 +1434,16 @@ __global__ void __launch_bounds__(EP_TX* EP_TY, sizeof(T) == 4 ? 4 : 2) k_rkstag
                                                          C2<T>* __restrict__ out, C2<T>* __restrict__ hout,
                                                          T* __restrict__ den, T a, T b, T cr, T dt,
                                                          DevScalars* sc) {
-  __shared__ C2<T> sp[(EP_TX + 2 * R) * (EP_TY + 2 * R)];
+  extern __shared__ __align__(16) unsigned char smraw[];
+  constexpr int NT = EP_TX * EP_TY;
   const HCoef<T> hc(ph);
   bool bad = false;
-  lap_march<T, R>(g, psi, fd, zc, sp, [&](long long p, C2<T> c, C2<T> lap) {
-    const C2<T> H = happly<T>(hc, lap, c, pot4[p], uimp[p]);
-    const C2<T> qq = q[p];
+  const C2<T>* cin[1] = {q};
+  const T* rin[2] = {pot4, uimp};
+  lap_march_async<T, R, 1, 2>(g, psi, fd, zc, smraw, cin, rin, T(1),
+                              [&](long long p, C2<T> c, C2<T> lap, const C2<T>* ic, const T* ir) {
+    const C2<T> H = happly<T>(hc, lap, c, ir[0], ir[NT]);
+    const C2<T> qq = ic[0];
     const C2<T> aux2 = a * (H - b * qq);
     q[p] = (qq + T(3) * aux2) - cr * H;
     if (hout) hout[p] = H;
