@@ -25,11 +25,12 @@
 // The internal variables of the P (instate 0..2) and D (Lstate = 'D',
 // instate 0..4) states are built as instates.f90 does in its default branch
 // (ep_instates.h); Lexcite_state_fix gives the fixed P vectors, instate 5
-// reads invar.dat.  Not built here: the Ldiag_jz / Laverage_P_value /
-// Lmixture / exciplex variants of instates.f90, and the Select_Pot closed
-// forms other than 'null', 'Morse' and the four '*_plus_Koutselos'
-// (V_impur.f90:87-932; any of them runs as selec_* = 'table' from a file of
-// (r, V) rows).
+// reads invar.dat, Ldiag_jz picks the state of given <Jz> in a j manifold.
+// Not built here: the Laverage_P_value / Lmixture / exciplex variants of
+// instates.f90 (they sum eigenvectors, so they depend on EISPACK's phase
+// convention), and the Select_Pot closed forms other than 'null', 'Morse'
+// and the four '*_plus_Koutselos' (V_impur.f90:87-932; any of them runs as
+// selec_* = 'table' from a file of (r, V) rows).
 #include <cmath>
 #include <complex>
 #include <cstdio>
@@ -221,6 +222,7 @@ struct State {
   double time_ps = 0.0;                       // from the file's comment lines
   int p_instate = -1;                         // P state to build from the field moments
   int d_instate = -1;                         // D state to build from the field matrix
+  int jz_ki = 0, jz_n = 0, jz_il = -1;        // Ldiag_jz: manifold and <Jz> index
   double auxn4 = 0, xc = 0, yc = 0, zc = 0;   // helium number and centre of mass
 };
 
@@ -309,19 +311,26 @@ void prepare_invar(const Input& in, State& s) {
   }
   if (instate > 5) stop("instate value invalid " + std::to_string(instate));
   const std::string lstate = trim(in.get<std::string>("lstate", "P"));
+  if (lstate != "P" && lstate != "D") stop("Lstate='" + lstate + "' is neither 'P' nor 'D'");
+  if (in.get<bool>("ldiag_jz", false)) {  // instates.f90:228-300 (P), :613-690 (D)
+    if (instate > (lstate == "D" ? 4 : 2)) stop("instate " + std::to_string(instate) + " has no Ldiag_jz state");
+    const std::string ljz = trim(in.get<std::string>("ljz", ""));
+    instates::jz_selection(lstate == "D", (int)instate, ljz, s.jz_ki, s.jz_n, s.jz_il);
+    if (s.jz_il < 0) stop("Wrong Ljz value...:" + ljz);
+    (lstate == "D" ? s.d_instate : s.p_instate) = (int)instate;
+    return;
+  }
   if (lstate == "D") {  // instates.f90:440-647, default branch
-    if (in.get<bool>("ldiag_jz", false)) stop("ldiag_jz: this instates.f90 variant is not built in this driver");
     s.d_instate = (int)instate;
     return;
   }
-  if (lstate != "P") stop("Lstate='" + lstate + "' is neither 'P' nor 'D'");
   if (in.get<bool>("lexcite_state_fix", false) && instate <= 2) {  // fixed P states, instates.f90:300-320
     std::fill(s.invar.begin(), s.invar.end(), 0.0);
     const int n = (int)instate + 1;
     for (int k = 0; k < n; ++k) s.invar[2 * (2 * k)] = 1.0 / std::sqrt((double)n);
     return;
   }
-  for (const char* k : {"ldiag_jz", "laverage_p_value", "lmixture", "lexciplex_state_fix"})
+  for (const char* k : {"laverage_p_value", "lmixture", "lexciplex_state_fix"})
     if (in.get<bool>(k, false)) stop(std::string(k) + ": this instates.f90 variant is not built in this driver");
   if (instate > 2) stop("instate " + std::to_string(instate) + " has no P state (0..2)");
   s.p_instate = (int)instate;  // built from the field moments once the density is on the GPU
@@ -334,7 +343,7 @@ void build_p_state(ep_ctx* ctx, const ep_config& cfg, State& s) {
   if (s.d_instate >= 0) {  // D state: the 5x5 field matrix, MatDSO, instate's pair
     double M[25];
     check(ep_impurity_matrix_d(ctx, M), ctx, "impurity matrix");
-    instates::d_state(M, cfg.als_d, s.d_instate, s.invar.data());
+    instates::d_state(M, cfg.als_d, s.d_instate, s.invar.data(), s.jz_ki, s.jz_n, s.jz_il);
     check(ep_set_impurity_state(ctx, s.rimp, s.vimp, s.invar.data()), ctx, "impurity state");
     check(ep_potenimp(ctx), ctx, "potenimp");
     return;
@@ -342,7 +351,7 @@ void build_p_state(ep_ctx* ctx, const ep_config& cfg, State& s) {
   if (s.p_instate < 0) return;
   double m[6];
   check(ep_impurity_moments(ctx, m), ctx, "impurity moments");
-  instates::p_state(m, cfg.als_p, s.p_instate, s.invar.data());
+  instates::p_state(m, cfg.als_p, s.p_instate, s.invar.data(), s.jz_ki, s.jz_n, s.jz_il);
   check(ep_set_impurity_state(ctx, s.rimp, s.vimp, s.invar.data()), ctx, "impurity state");
   check(ep_potenimp(ctx), ctx, "potenimp");
 }

@@ -12,6 +12,7 @@
 #include <algorithm>
 #include <cmath>
 #include <complex>
+#include <string>
 #include <vector>
 
 #include "../ep_dstate.h"
@@ -74,6 +75,82 @@ inline void hermitian_eigen(int n, std::vector<cd> a, std::vector<double>& w, st
   v.swap(vs);
 }
 
+// Jz = Lz + Sz over the internal variables, as instates.f90 writes its
+// matrix elements (P: :246-258, D: :632-651); row-major nd x nd.
+inline std::vector<cd> jz_matrix(int nd) {
+  const cd I(0.0, 1.0);
+  std::vector<cd> J((size_t)nd * nd, cd(0));
+  auto at = [&](int i, int j) -> cd& { return J[(size_t)(i - 1) * nd + (j - 1)]; };
+  if (nd == 6) {
+    at(1, 1) = 0.5; at(1, 3) = -I; at(2, 2) = -0.5; at(2, 4) = -I; at(3, 1) = I; at(3, 3) = 0.5;
+    at(4, 2) = I; at(4, 4) = -0.5; at(5, 5) = 0.5; at(6, 6) = -0.5;
+  } else {
+    at(9, 9) = 0.5; at(9, 1) = -2.0 * I; at(10, 10) = -0.5; at(10, 2) = -2.0 * I; at(3, 3) = 0.5;
+    at(3, 7) = I; at(4, 4) = -0.5; at(4, 8) = I; at(5, 5) = 0.5; at(6, 6) = -0.5; at(7, 3) = -I;
+    at(7, 7) = 0.5; at(8, 4) = -I; at(8, 8) = -0.5; at(1, 9) = 2.0 * I; at(1, 1) = 0.5;
+    at(2, 10) = 2.0 * I; at(2, 2) = -0.5;
+  }
+  return J;
+}
+
+// Ldiag_jz (instates.f90:228-300 P, :613-690 D): the eigenvectors ki ..
+// ki+njz-1 of the state matrix (columns of v, ascending) span one j
+// manifold; Jz restricted to it is diagonalised and its il-th eigenvector
+// (0-based, ascending <Jz>) taken back to the internal variables.  The
+// result depends on the manifold, not on the basis the solver chose in it.
+inline void diag_jz(int nd, const std::vector<cd>& v, int ki, int njz, int il, double* invar) {
+  const std::vector<cd> J = jz_matrix(nd);
+  std::vector<cd> M((size_t)njz * njz, cd(0));
+  for (int a = 0; a < njz; ++a)
+    for (int b = 0; b < njz; ++b) {
+      cd t = 0.0;
+      for (int i = 0; i < nd; ++i)
+        for (int j = 0; j < nd; ++j)
+          t += std::conj(v[(size_t)i * nd + ki + a]) * J[(size_t)i * nd + j] * v[(size_t)j * nd + ki + b];
+      M[(size_t)a * njz + b] = t;
+    }
+  std::vector<double> w;
+  std::vector<cd> z;
+  hermitian_eigen(njz, M, w, z);
+  for (int i = 0; i < 10; ++i) invar[2 * i] = invar[2 * i + 1] = 0.0;
+  for (int i = 0; i < nd; ++i) {
+    cd t = 0.0;
+    for (int a = 0; a < njz; ++a) t += z[(size_t)a * njz + il] * v[(size_t)i * nd + ki + a];
+    invar[2 * i] = t.real();
+    invar[2 * i + 1] = t.imag();
+  }
+}
+
+// Manifold (ki, njz) and Jz index il of Ldiag_jz from instate and Ljz
+// ('' = the reference's default per instate); il < 0 for a wrong Ljz.
+inline void jz_selection(bool d_state, int instate, std::string ljz, int& ki, int& njz, int& il) {
+  il = -1;
+  std::vector<std::string> names;
+  if (!d_state) {
+    if (instate == 0) {
+      ki = 0; njz = 2;
+      if (ljz.empty()) ljz = "-1/2";
+      names = {"-1/2", "+1/2"};
+    } else {
+      ki = 2; njz = 4;
+      if (ljz.empty()) ljz = instate == 1 ? "-3/2" : "-1/2";
+      names = {"-3/2", "-1/2", "+1/2", "+3/2"};
+    }
+  } else {
+    if (instate <= 1) {
+      ki = 0; njz = 4;
+      if (ljz.empty()) ljz = instate == 0 ? "-3/2" : "-1/2";
+      names = {"-3/2", "-1/2", "+1/2", "+3/2"};
+    } else {
+      ki = 4; njz = 6;
+      if (ljz.empty()) ljz = instate == 2 ? "-5/2" : instate == 3 ? "-3/2" : "-1/2";
+      names = {"-5/2", "-3/2", "-1/2", "+1/2", "+3/2", "+5/2"};
+    }
+  }
+  for (size_t k = 0; k < names.size(); ++k)
+    if (names[k] == ljz) il = (int)k;
+}
+
 // V + (Als/2) SO of instates.f90:150-193 from m = (Vx, Vy, Vz, Vxy, Vxz, Vyz).
 inline std::vector<cd> p_matrix(const double* m, double als) {
   const cd I(0.0, 1.0);
@@ -101,11 +178,17 @@ inline std::vector<cd> p_matrix(const double* m, double als) {
   return M;
 }
 
-// invar (10 complex as 20 doubles) for a P state instate 0..2.
-inline void p_state(const double* moments, double als, int instate, double* invar) {
+// invar (10 complex as 20 doubles) for a P state instate 0..2; jz_il >= 0:
+// the Ldiag_jz state (ki, njz, jz_il) instead of the default pair.
+inline void p_state(const double* moments, double als, int instate, double* invar, int ki = 0, int njz = 0,
+                    int jz_il = -1) {
   std::vector<double> w;
   std::vector<cd> v;
   hermitian_eigen(6, p_matrix(moments, als), w, v);
+  if (jz_il >= 0) {
+    diag_jz(6, v, ki, njz, jz_il, invar);
+    return;
+  }
   const int il = 2 * instate, il1 = il + 1;
   const double r = 1.0 / std::sqrt(2.0);
   for (int i = 0; i < 10; ++i) invar[2 * i] = invar[2 * i + 1] = 0.0;
@@ -121,7 +204,8 @@ inline void p_state(const double* moments, double als, int instate, double* inva
 // (ep_impurity_matrix_d), its eigenvectors ascending, and
 //   invar = (v_il + v_il+1) / sqrt(2),  il = 2 * instate (0-based, instate 0..4).
 // Kramers pairs again make the choice of basis inside a pair immaterial.
-inline void d_state(const double* M, double als_d, int instate, double* invar) {
+inline void d_state(const double* M, double als_d, int instate, double* invar, int ki = 0, int njz = 0,
+                    int jz_il = -1) {
   cd S[10][10];
   dstate::sod(S);
   std::vector<cd> A(100);
@@ -130,6 +214,10 @@ inline void d_state(const double* M, double als_d, int instate, double* invar) {
   std::vector<double> w;
   std::vector<cd> v;
   hermitian_eigen(10, A, w, v);
+  if (jz_il >= 0) {
+    diag_jz(10, v, ki, njz, jz_il, invar);
+    return;
+  }
   const int il = 2 * instate, il1 = il + 1;
   const double r = 1.0 / std::sqrt(2.0);
   for (int i = 0; i < 10; ++i) {

@@ -10,6 +10,8 @@ import struct
 import subprocess
 import textwrap
 
+import numpy as np
+
 import pytest
 
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
@@ -68,6 +70,22 @@ int main(int argc, char** argv) {
       for (double x : iv) std::printf("%.17g ", x);
       std::printf("\n");
     }
+  } else if (what == "jz") {
+    // argv: state (P|D), Als, instate, Ljz ('-' for the default), then the 6
+    // P moments or the 25 entries of the D field matrix; prints invar
+    const bool d = std::string(argv[2]) == "D";
+    const double als = std::atof(argv[3]);
+    const int st = std::atoi(argv[4]);
+    const std::string ljz = std::string(argv[5]) == "-" ? "" : argv[5];
+    int ki, njz, il;
+    instates::jz_selection(d, st, ljz, ki, njz, il);
+    if (il < 0) { std::printf("BAD\n"); return 0; }
+    double m[25]; for (int i = 0; i < (d ? 25 : 6); ++i) m[i] = std::atof(argv[6 + i]);
+    double iv[20];
+    if (d) instates::d_state(m, als, st, iv, ki, njz, il);
+    else instates::p_state(m, als, st, iv, ki, njz, il);
+    for (double x : iv) std::printf("%.17g ", x);
+    std::printf("\n");
   } else if (what == "rec") {
     std::ofstream o(argv[2], std::ios::binary);
     double v[3] = {1.5, -2.25, 3.0}; int k = 7;
@@ -199,3 +217,82 @@ def test_p_state_eigenvectors(harness):
             assert np.allclose(M @ iv[:6], w[2 * st] * iv[:6], atol=1e-12)
         if m[3] == 0.0:
             assert np.allclose(w, [m[0] - als] * 2 + [m[0] + als / 2] * 4, atol=1e-12)
+
+
+def _jz(nd):
+    """Jz = Lz + Sz over the internal variables, restated from the matrix
+    elements instates.f90 writes (P :246-258, D :632-651)."""
+    J = np.zeros((nd, nd), complex)
+    ent = ({(1, 1): .5, (1, 3): -1j, (2, 2): -.5, (2, 4): -1j, (3, 1): 1j, (3, 3): .5, (4, 2): 1j, (4, 4): -.5,
+            (5, 5): .5, (6, 6): -.5} if nd == 6 else
+           {(9, 9): .5, (9, 1): -2j, (10, 10): -.5, (10, 2): -2j, (3, 3): .5, (3, 7): 1j, (4, 4): -.5, (4, 8): 1j,
+            (5, 5): .5, (6, 6): -.5, (7, 3): -1j, (7, 7): .5, (8, 4): -1j, (8, 8): -.5, (1, 9): 2j, (1, 1): .5,
+            (2, 10): 2j, (2, 2): -.5})
+    for (i, j), v in ent.items():
+        J[i - 1, j - 1] = v
+    return J
+
+
+def _state_matrix(d, m, als):
+    """P: V + (Als/2) SO (instates.f90:150-193); D: M (x) 1_2 + (Als/2) SOD."""
+    if not d:
+        vx, vy, vz, vxy, vxz, vyz = m
+        M = np.zeros((6, 6), complex)
+        for (i, j), v in {(0, 0): vx, (1, 1): vx, (2, 2): vy, (3, 3): vy, (4, 4): vz, (5, 5): vz, (0, 2): vxy,
+                          (1, 3): vxy, (0, 4): vxz, (1, 5): vxz, (2, 4): vyz, (3, 5): vyz}.items():
+            M[i, j] = M[j, i] = v
+        for (i, j), v in {(0, 2): -1j, (1, 3): 1j, (1, 4): -1, (0, 5): 1, (3, 4): -1j, (2, 5): -1j}.items():
+            M[i, j] += 0.5 * als * v
+            M[j, i] += 0.5 * als * np.conj(v)
+        return M
+    S = np.zeros((10, 10), complex)
+    s3 = np.sqrt(3.0)
+    for (i, j), v in {(1, 4): 1, (1, 8): -1j, (1, 9): 2j, (2, 3): -1, (2, 7): -1j, (2, 10): -2j, (3, 6): -1j * s3,
+                      (3, 7): 1j, (3, 10): -1j, (4, 5): -1j * s3, (4, 8): -1j, (4, 9): -1j, (5, 8): -s3,
+                      (6, 7): s3, (7, 10): -1, (8, 9): 1}.items():
+        S[i - 1, j - 1] = v
+    S = S + S.conj().T
+    return np.kron(np.asarray(m).reshape(5, 5), np.eye(2)) + 0.5 * als * S
+
+
+@pytest.mark.parametrize("d", [False, True])
+def test_ldiag_jz_picks_the_requested_jz_state(harness, d):
+    """Ldiag_jz (instates.f90:228-300, :613-690): the state is the eigenvector
+    of Jz restricted to the selected j manifold of the state matrix with the
+    requested <Jz>; in an isotropic field it is an exact Jz eigenstate with
+    <Jz> = m_j.  Checked against numpy for both states, isotropic and
+    anisotropic fields, every Ljz and the reference's defaults."""
+    rng = np.random.default_rng(3)
+    nd = 10 if d else 6
+    if d:
+        A = rng.normal(size=(5, 5))
+        fields = [list(np.diag([-4.0] * 5).ravel()), list((np.diag([-4.0] * 5) + 0.3 * (A + A.T)).ravel())]
+        cases = [(0, "-"), (1, "-"), (0, "+3/2"), (2, "-"), (3, "-"), (4, "+5/2"), (4, "-1/2")]
+        names = {0: ["-3/2", "-1/2", "+1/2", "+3/2"], 1: ["-5/2", "-3/2", "-1/2", "+1/2", "+3/2", "+5/2"]}
+        dflt = {0: "-3/2", 1: "-1/2", 2: "-5/2", 3: "-3/2", 4: "-1/2"}
+    else:
+        fields = [[-3.0, -3.0, -3.0, 0.0, 0.0, 0.0], [-3.0, -2.5, -2.0, 0.3, -0.2, 0.1]]
+        cases = [(0, "-"), (0, "+1/2"), (1, "-"), (2, "-"), (1, "+3/2"), (2, "+1/2")]
+        names = {0: ["-1/2", "+1/2"], 1: ["-3/2", "-1/2", "+1/2", "+3/2"]}
+        dflt = {0: "-1/2", 1: "-3/2", 2: "-1/2"}
+    J = _jz(nd)
+    als = 3.0
+    for iso, m in enumerate(fields):
+        H = _state_matrix(d, m, als)
+        w, V = np.linalg.eigh(H)
+        for st, ljz in cases:
+            out = run(harness, "jz", "D" if d else "P", als, st, ljz, *m).split()
+            iv = np.array([float(x) for x in out]).view(np.complex128)[:nd]
+            man = (0 if st <= 1 else 1) if d else (0 if st == 0 else 1)
+            ki, njz = ((0, 4) if man == 0 else (4, 6)) if d else ((0, 2) if man == 0 else (2, 4))
+            want_name = dflt[st] if ljz == "-" else ljz
+            il = names[man].index(want_name)
+            Vm = V[:, ki:ki + njz]
+            jw, Z = np.linalg.eigh(Vm.conj().T @ J @ Vm)
+            expect = Vm @ Z[:, il]
+            assert abs(np.vdot(iv, iv) - 1.0) < 1e-12
+            assert abs(abs(np.vdot(expect, iv)) - 1.0) < 1e-10, (d, iso, st, ljz)
+            if iso == 0:  # exact Jz eigenstate with m_j = the requested value
+                mj = float(want_name.replace("/2", "")) / 2.0
+                assert np.allclose(J @ iv, mj * iv, atol=1e-10), (d, st, ljz)
+    assert run(harness, "jz", "D" if d else "P", als, 1, "+9/2", *fields[0]).strip() == "BAD"

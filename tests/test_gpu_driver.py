@@ -351,3 +351,21 @@ def test_scan_settings_of_prep_sh_give_the_api_uplus(tmp_path):
         e = s.energy()
     assert abs(float(m.group(1)) - e["uplus"]) < 2e-6
     assert abs(e["uplus"]) > 1.0
+
+
+def test_ldiag_jz_namelist_selects_the_jz_state(tmp_path):
+    """Ldiag_jz=.true., Ljz='+3/2' in an isotropic field (V_Sigma = V_Pi):
+    the internal variables the driver writes (printoutc, frozen by
+    Lfix_lambda) are the Jz = +3/2 member of the j = 3/2 level."""
+    psi = ep.woods_saxon_psi(N, N, N, XMAX, XMAX, XMAX, N4, seed=11)
+    write_density(tmp_path / "in.dat", np.abs(psi) ** 2, (0.3, -0.2, 0.5))
+    run_driver(tmp_path, namelist(0, ", instate=1, Als_P=4.d0, Ldiag_jz=.true., Ljz='+3/2', niter=1"))
+    text = (tmp_path / "out.dat").read_text()
+    z = re.findall(r"\(([-+0-9.E]+),([-+0-9.E]+)\)", text)[:10]
+    iv = np.array([complex(float(a), float(b)) for a, b in z])
+    J = np.zeros((6, 6), complex)
+    for (i, j), v in {(1, 1): .5, (1, 3): -1j, (2, 2): -.5, (2, 4): -1j, (3, 1): 1j, (3, 3): .5, (4, 2): 1j,
+                      (4, 4): -.5, (5, 5): .5, (6, 6): -.5}.items():
+        J[i - 1, j - 1] = v
+    assert abs(np.vdot(iv, iv) - 1.0) < 1e-10 and np.all(iv[6:] == 0)
+    assert np.allclose(J @ iv[:6], 1.5 * iv[:6], atol=1e-9)
