@@ -238,3 +238,32 @@ def test_fp32_impurity_field_and_moments_track_fp64(oracle):
         assert np.max(np.abs(Fg - Fo)) < 5e-4 * np.max(np.abs(Fo)), (Fg, Fo)
         mg, mo = g.impurity_moments(), o.impurity_moments()
         assert np.max(np.abs(mg - mo)) < 1e-5 * np.max(np.abs(mo)), (mg, mo)
+
+
+@pytest.mark.parametrize("prec", [_abi.EP_FP64, _abi.EP_FP32])
+def test_uneven_mixed_radix_grid_matches_oracle(oracle, prec):
+    """30 x 36 x 40 (radix 3 and 5 on every axis): the shared-memory FFT
+    engine on all three passes, and the element-wise fallbacks of the
+    vector paths (FP32 rows of 30 points are not a multiple of 4: chunked
+    plane fetches, 16-byte point-wise packs and pair loads fall back)."""
+    cfg = ep.make_config(nx=30, ny=36, nz=40, xmax=15.0, ymax=18.0, zmax=20.0, icon=_abi.EP_ICON_PERIODIC,
+                         core="OTC", n4=150.0, impurity=_abi.EP_IMPURITY_FIXED, precision=prec)
+    cfg64 = ep.make_config(nx=30, ny=36, nz=40, xmax=15.0, ymax=18.0, zmax=20.0, icon=_abi.EP_ICON_PERIODIC,
+                           core="OTC", n4=150.0, impurity=_abi.EP_IMPURITY_FIXED)
+    psi = ep.woods_saxon_psi(30, 36, 40, 15.0, 18.0, 20.0, 150.0, seed=12)
+    g, o = ep.Solver(cfg), oracle.OracleSolver(cfg64)
+    pot = ep.morse(10.0, 4.5, 1.2, r_cutoff=0.0, umax=1000.0)
+    for s in (g, o):
+        s.set_impurity_potentials(pot, pot, ep.morse(12.0, 4.0, 1.1))
+        s.set_impurity(rimp=(0.4, -0.7, 1.1), invar=np.zeros(10, dtype=np.complex128))
+        s.start(psi)
+    ftol = 1e-11 if prec == _abi.EP_FP64 else 2e-5
+    with g, o:
+        for f in FIELDS_ALL:
+            assert rel(g.field(f), o.field(f)) < ftol, (f, rel(g.field(f), o.field(f)))
+        for _ in range(3):
+            g.steprk(5e-4)
+            o.steprk(5e-4)
+        g.run(6, 5e-4)
+        o.run(6, 5e-4)
+        assert rel(g.psi(), o.psi()) < (1e-10 if prec == _abi.EP_FP64 else 1e-4)
