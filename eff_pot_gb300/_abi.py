@@ -47,7 +47,7 @@ class EpConfig(C.Structure):
         ("als_p", C.c_double), ("ev0", C.c_double),
         ("z_exciplex_exclusion", C.c_double),
         ("precision", C.c_int), ("device", C.c_int),
-        ("state", C.c_int), ("als_d", C.c_double),
+        ("state", C.c_int), ("als_d", C.c_double), ("filter_exciplex_force", C.c_int),
     ]
 
 

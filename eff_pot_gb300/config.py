@@ -14,7 +14,7 @@ DEFAULTS = dict(
     time_mode=_abi.EP_IMAGINARY_TIME, renormalize=1, n4=300.0,
     impurity=_abi.EP_IMPURITY_NONE, mimpur=0.0, fix_lambda=0, als_p=0.0,
     ev0=0.0, z_exciplex_exclusion=0.0, precision=_abi.EP_FP64, device=0,
-    state=_abi.EP_STATE_P, als_d=0.0,
+    state=_abi.EP_STATE_P, als_d=0.0, filter_exciplex_force=0,
 )
 
 CORES = {"OT": _abi.EP_CORE_OT, "OT ": _abi.EP_CORE_OT, "OTC": _abi.EP_CORE_OTC,

@@ -573,6 +573,7 @@ int main(int argc, char** argv) {
     }
     cfg.ev0 = in.get<double>("ev0", 0.0);
     cfg.z_exciplex_exclusion = in.get<double>("z_exciplex_exclusion", cfg.z_exciplex_exclusion);
+    cfg.filter_exciplex_force = in.get<bool>("lfilter_exciplex_force", false) ? 1 : 0;
     cfg.impurity = EP_IMPURITY_MOVING;
     const std::string tm = trim(in.get<std::string>("timemode", "imaginary"));
     cfg.time_mode = (tm == "real") ? EP_REAL_TIME : EP_IMAGINARY_TIME;

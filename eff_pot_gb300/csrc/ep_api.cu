@@ -224,6 +224,7 @@ int ep_config_init(ep_config* c) {
   c->device = 0;
   c->state = EP_STATE_P;
   c->als_d = 0.0;
+  c->filter_exciplex_force = 0;
   return EP_OK;
 }
 

@@ -617,12 +617,32 @@ int Engine<T>::energy(ep_energies* e) {
   return check_flags();
 }
 
+// Planes [lo, hi) of the F_z sum: all of them, or with the exciplex filter
+// those beyond z_exciplex_exclusion on the far side of the impurity
+// (potenimp.f90:211-248: iz0 / nz0 truncated as Fortran's integer
+// assignment does, 1-based there).
+inline void fz_planes(const ep_config& c, double rz, double hz, int nz, int& lo, int& hi) {
+  lo = 0;
+  hi = nz;
+  if (!c.filter_exciplex_force) return;
+  const double z1 = -c.zmax;
+  if (rz < 0.0) {
+    const int iz0 = std::max(1, (int)((rz - z1 + c.z_exciplex_exclusion) / hz + 1.5));
+    lo = std::min(iz0 - 1, nz);
+  } else {
+    const int nz0 = std::min(nz, (int)((rz - z1 - c.z_exciplex_exclusion) / hz + 1.5));
+    hi = std::max(nz0, 0);
+  }
+}
+
 template <class T>
 int Engine<T>::forceimp(double* F) {
+  int izlo, izhi;
+  fz_planes(cfg, imp->rimp[2], hz, g.nz, izlo, izhi);
   if (cfg.state == EP_STATE_D) {
     auto kd = k_impmoments_d<T>;
     EP_LAUNCH("impmoments", kd, EP_RED_BLOCKS, 256, 0, g, den, dxd, dyd, dzd, uimp, delta, vpi, sigdel, cfg.xmax,
-              cfg.ymax, cfg.zmax, hx, hy, hz, imp->rimp[0], imp->rimp[1], imp->rimp[2], partials);
+              cfg.ymax, cfg.zmax, hx, hy, hz, imp->rimp[0], imp->rimp[1], imp->rimp[2], izlo, izhi, partials);
     int r;
     if ((r = reduce_finalize(EP_RED_BLOCKS, 18, 16, 0))) return r;
     double s[3];
@@ -634,11 +654,11 @@ int Engine<T>::forceimp(double* F) {
     auto kf = k_impmoments_f;
     EP_LAUNCH("impmoments", kf, EP_RED_BLOCKS, 256, 0, g, den, dxd, dyd, dzd, uimp, vpi, delta, (float)cfg.xmax,
               (float)cfg.ymax, (float)cfg.zmax, (float)hx, (float)hy, (float)hz, (float)imp->rimp[0],
-              (float)imp->rimp[1], (float)imp->rimp[2], partials);
+              (float)imp->rimp[1], (float)imp->rimp[2], izlo, izhi, partials);
   } else {
     auto k = k_impmoments<T>;
     EP_LAUNCH("impmoments", k, EP_RED_BLOCKS, 256, 0, g, den, dxd, dyd, dzd, uimp, vpi, delta, cfg.xmax, cfg.ymax,
-              cfg.zmax, hx, hy, hz, imp->rimp[0], imp->rimp[1], imp->rimp[2], partials);
+              cfg.zmax, hx, hy, hz, imp->rimp[0], imp->rimp[1], imp->rimp[2], izlo, izhi, partials);
   }
   int r;
   if ((r = reduce_finalize(EP_RED_BLOCKS, 9, 16, 0))) return r;

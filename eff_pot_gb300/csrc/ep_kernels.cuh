@@ -1561,13 +1561,14 @@ __global__ void k_energy(Geo g, FdW<T> fd, Phys ph, const C2<T>* __restrict__ ps
                          double hz, double r0, double r1, double r2, double zexc, PotDev vplus, int impurity,
                          double* __restrict__ partials);
 
-// forceimp / potinvar moments (potenimp.f90:193-258, 298-317).
+// forceimp / potinvar moments (potenimp.f90:193-258, 298-317); the F_z sum
+// runs over the planes izlo <= iz < izhi (the exciplex filter, :211-248).
 template <class T>
 __global__ void k_impmoments(Geo g, const T* __restrict__ den, const T* __restrict__ dxd,
                              const T* __restrict__ dyd, const T* __restrict__ dzd, const T* __restrict__ uimp,
                              const T* __restrict__ vpi, const T* __restrict__ delta, double xmax, double ymax,
                              double zmax, double hx, double hy, double hz, double r0, double r1, double r2,
-                             double* __restrict__ partials);
+                             int izlo, int izhi, double* __restrict__ partials);
 
 // forceimp sums + the D-state matrix (potenimp.f90:331-405): 3 + 15 sums,
 // the matrix's upper triangle in DGram's order.
@@ -1576,7 +1577,7 @@ __global__ void k_impmoments_d(Geo g, const T* __restrict__ den, const T* __rest
                                const T* __restrict__ dyd, const T* __restrict__ dzd, const T* __restrict__ uimp,
                                const T* __restrict__ delta, const T* __restrict__ pidel,
                                const T* __restrict__ sigdel, double xmax, double ymax, double zmax, double hx,
-                               double hy, double hz, double r0, double r1, double r2,
+                               double hy, double hz, double r0, double r1, double r2, int izlo, int izhi,
                                double* __restrict__ partials);
 
 // Form factors on the device (fforma.f90:11-60, initcg.f90:314-331,

@@ -140,7 +140,7 @@ __global__ void k_impmoments_d(Geo g, const T* __restrict__ den, const T* __rest
                                const T* __restrict__ dyd, const T* __restrict__ dzd, const T* __restrict__ uimp,
                                const T* __restrict__ delta, const T* __restrict__ pidel,
                                const T* __restrict__ sigdel, double xmax, double ymax, double zmax, double hx,
-                               double hy, double hz, double r0, double r1, double r2,
+                               double hy, double hz, double r0, double r1, double r2, int izlo, int izhi,
                                double* __restrict__ partials) {
   double acc[18];
 #pragma unroll
@@ -151,7 +151,7 @@ __global__ void k_impmoments_d(Geo g, const T* __restrict__ den, const T* __rest
     const double u = uimp[p];
     acc[0] += (double)dxd[p] * u;
     acc[1] += (double)dyd[p] * u;
-    acc[2] += (double)dzd[p] * u;
+    if (iz >= izlo && iz < izhi) acc[2] += (double)dzd[p] * u;
     const double xx = coord(xmax, hx, ix) - r0, yy = coord(ymax, hy, iy) - r1, zz = coord(zmax, hz, iz) - r2;
     const double rho = den[p];
     const double dvd = (double)delta[p] * rho, dv1 = (double)pidel[p] * rho, dv2 = (double)sigdel[p] * rho;
@@ -213,7 +213,8 @@ static __global__ void k_impmoments_f(Geo g, const float* __restrict__ den, cons
                                const float* __restrict__ dyd, const float* __restrict__ dzd,
                                const float* __restrict__ uimp, const float* __restrict__ vpi,
                                const float* __restrict__ delta, float xmax, float ymax, float zmax, float hx, float hy,
-                               float hz, float r0, float r1, float r2, double* __restrict__ partials) {
+                               float hz, float r0, float r1, float r2, int izlo, int izhi,
+                               double* __restrict__ partials) {
   Acc<float> acc[9];
   for (long long p = blockIdx.x * (long long)blockDim.x + threadIdx.x; p < g.N; p += (long long)gridDim.x * blockDim.x) {
     int ix, iy, iz;
@@ -221,7 +222,7 @@ static __global__ void k_impmoments_f(Geo g, const float* __restrict__ den, cons
     const float u = uimp[p];
     acc[0].add(dxd[p] * u);
     acc[1].add(dyd[p] * u);
-    acc[2].add(dzd[p] * u);
+    if (iz >= izlo && iz < izhi) acc[2].add(dzd[p] * u);
     const float xx = ((float)ix * hx - xmax) - r0, yy = ((float)iy * hy - ymax) - r1,
                 zz = ((float)iz * hz - zmax) - r2;
     const float a1 = den[p], a2 = delta[p], a3 = vpi[p];
@@ -306,7 +307,7 @@ __global__ void k_impmoments(Geo g, const T* __restrict__ den, const T* __restri
                              const T* __restrict__ dyd, const T* __restrict__ dzd, const T* __restrict__ uimp,
                              const T* __restrict__ vpi, const T* __restrict__ delta, double xmax, double ymax,
                              double zmax, double hx, double hy, double hz, double r0, double r1, double r2,
-                             double* __restrict__ partials) {
+                             int izlo, int izhi, double* __restrict__ partials) {
   double acc[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
   for (long long p = blockIdx.x * (long long)blockDim.x + threadIdx.x; p < g.N; p += (long long)gridDim.x * blockDim.x) {
     int ix, iy, iz;
@@ -314,7 +315,7 @@ __global__ void k_impmoments(Geo g, const T* __restrict__ den, const T* __restri
     const double u = uimp[p];
     acc[0] += (double)dxd[p] * u;
     acc[1] += (double)dyd[p] * u;
-    acc[2] += (double)dzd[p] * u;
+    if (iz >= izlo && iz < izhi) acc[2] += (double)dzd[p] * u;
     const double xx = coord(xmax, hx, ix) - r0, yy = coord(ymax, hy, iy) - r1, zz = coord(zmax, hz, iz) - r2;
     const double a1 = den[p], a2 = delta[p], a3 = vpi[p];
     acc[3] += a1 * (a2 * xx * xx + a3);

@@ -77,6 +77,9 @@ typedef struct ep_config {
   int device;                /* CUDA device ordinal                         */
   int state;                 /* Lstate: EP_STATE_P (default) / EP_STATE_D   */
   double als_d;              /* spin-orbit splitting, D state (Als_D)       */
+  int filter_exciplex_force; /* Lfilter_exciplex_force: F_z of forceimp only
+                                over the planes beyond z_exciplex_exclusion
+                                on the far side (potenimp.f90:211-248)      */
 } ep_config;
 
 /* Pair potentials (a subset of the Select_Pot registry, V_impur.f90:87-932,

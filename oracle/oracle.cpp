@@ -1132,13 +1132,34 @@ int oc_energy(oc_ctx* c, ep_energies* e) {
   return EP_OK;
 }
 
-// forceimp (potenimp.f90:193-258), exciplex filter off.
+// forceimp (potenimp.f90:193-258).  With Lfilter_exciplex_force the z
+// component sums the planes iz0..nz (impurity below z = 0) or 1..nz0
+// (:211-248); aux2, the He-He correction, is commented out there.
 int oc_forceimp(oc_ctx* c, double* F) {
   if (!c || !F) return EP_ERR_INVALID_ARG;
   const size_t N = c->N;
+  const ep_config& g = c->cfg;
   F[0] = -par_sum(N, [&](size_t i) { return c->dxden[i] * c->uimp[i]; }) * c->dxyz;
   F[1] = -par_sum(N, [&](size_t i) { return c->dyden[i] * c->uimp[i]; }) * c->dxyz;
-  F[2] = -par_sum(N, [&](size_t i) { return c->dzden[i] * c->uimp[i]; }) * c->dxyz;
+  if (g.filter_exciplex_force) {
+    int izfirst = 1, izlast = c->nz;  // 1-based, inclusive
+    if (c->rimp[2] < 0.0) {
+      int iz0 = (int)((c->rimp[2] - c->z[0] + g.z_exciplex_exclusion) / c->hz + 1.5);
+      izfirst = std::max(1, iz0);
+    } else {
+      int nz0 = (int)((c->rimp[2] - c->z[0] - g.z_exciplex_exclusion) / c->hz + 1.5);
+      izlast = std::min(c->nz, nz0);
+    }
+    const size_t nxy = (size_t)c->nx * c->ny;
+    double aux1 = par_sum(N, [&](size_t i) {
+      const int iz = (int)(i / nxy) + 1;
+      return (iz >= izfirst && iz <= izlast) ? c->dzden[i] * c->uimp[i] : 0.0;
+    });
+    const double aux2 = 0.0;
+    F[2] = -aux1 * c->dxyz + -aux2 * c->dxyz;
+  } else {
+    F[2] = -par_sum(N, [&](size_t i) { return c->dzden[i] * c->uimp[i]; }) * c->dxyz;
+  }
   // the callers' aimp = F / mAg_u (DFT4He3d.f90:454-455, steppc.f90:114-115)
   if (c->cfg.impurity == EP_IMPURITY_MOVING)
     for (int i = 0; i < 3; ++i) c->aimp[i] = F[i] / (c->cfg.mimpur * 0.0207569277);
