@@ -27,11 +27,14 @@
 // length of this grid (0: general engine).
 #define EP_XLAUNCH(name, KER, grid, block, smem, ...)                  \
   do {                                                                 \
-    switch (x_reg_n2(g.nx / 2)) {                                      \
+    switch (x_reg_n2<T>(g.nx / 2)) {                                   \
       case 16: { auto k = KER<T, 16>; EP_LAUNCH(name, k, grid, block, smem, __VA_ARGS__); } break;   \
       case 32: { auto k = KER<T, 32>; EP_LAUNCH(name, k, grid, block, smem, __VA_ARGS__); } break;   \
       case 64: { auto k = KER<T, 64>; EP_LAUNCH(name, k, grid, block, smem, __VA_ARGS__); } break;   \
       case 128: { auto k = KER<T, 128>; EP_LAUNCH(name, k, grid, block, smem, __VA_ARGS__); } break; \
+      case 48: if constexpr (sizeof(T) == 4) { auto k = KER<T, 48>; EP_LAUNCH(name, k, grid, block, smem, __VA_ARGS__); } break; \
+      case 80: if constexpr (sizeof(T) == 4) { auto k = KER<T, 80>; EP_LAUNCH(name, k, grid, block, smem, __VA_ARGS__); } break; \
+      case 96: if constexpr (sizeof(T) == 4) { auto k = KER<T, 96>; EP_LAUNCH(name, k, grid, block, smem, __VA_ARGS__); } break; \
       default: { auto k = KER<T, 0>; EP_LAUNCH(name, k, grid, block, smem, __VA_ARGS__); } break;    \
     }                                                                  \
   } while (0)
@@ -269,6 +272,7 @@ int Engine<T>::init(const ep_config& c, cudaStream_t s, Prof* p, ImpState* im, s
   cudaFuncSetAttribute(k_x3<T, NN>, cudaFuncAttributeMaxDynamicSharedMemorySize, big); \
   cudaFuncSetAttribute(k_x4<T, NN>, cudaFuncAttributeMaxDynamicSharedMemorySize, big);
   EP_XATTR(0) EP_XATTR(16) EP_XATTR(32) EP_XATTR(64) EP_XATTR(128)
+  if constexpr (sizeof(T) == 4) { EP_XATTR(48) EP_XATTR(80) EP_XATTR(96) }
 #undef EP_XATTR
   cudaFuncSetAttribute(k_c2c<T, -1>, cudaFuncAttributeMaxDynamicSharedMemorySize, big);
   cudaFuncSetAttribute(k_c2c<T, +1>, cudaFuncAttributeMaxDynamicSharedMemorySize, big);
@@ -279,6 +283,7 @@ int Engine<T>::init(const ep_config& c, cudaStream_t s, Prof* p, ImpState* im, s
   cudaFuncSetAttribute(k_zconv_r<T, NN, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)rfft::smem_bytes<T, NN>()); \
   cudaFuncSetAttribute(k_zconv_r<T, NN, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)rfft::smem_bytes<T, NN>());
   EP_RFFT_ATTR(32) EP_RFFT_ATTR(64) EP_RFFT_ATTR(128) EP_RFFT_ATTR(256)
+  if constexpr (sizeof(T) == 4) { EP_RFFT_ATTR(96) EP_RFFT_ATTR(192) }
 #undef EP_RFFT_ATTR
   {
     int dev = 0;
@@ -381,6 +386,8 @@ int Engine<T>::fft_y(CT** arrs, int n, int dir) {
     case 64: return rfft_y<64>(a, n, ls, dir);
     case 128: return rfft_y<128>(a, n, ls, dir);
     case 256: return rfft_y<256>(a, n, ls, dir);
+    case 96: if constexpr (sizeof(T) == 4) return rfft_y<96>(a, n, ls, dir); break;
+    case 192: if constexpr (sizeof(T) == 4) return rfft_y<192>(a, n, ls, dir); break;
     default: break;
   }
   const int LT = l_lines(g.ny, 2);
@@ -410,6 +417,8 @@ int Engine<T>::zconv(const CT* const* in, CT* const (*out)[3], const T* const (*
     case 64: return rfft_z<64>(cs, nin, ls);
     case 128: return rfft_z<128>(cs, nin, ls);
     case 256: return rfft_z<256>(cs, nin, ls);
+    case 96: if constexpr (sizeof(T) == 4) return rfft_z<96>(cs, nin, ls); break;
+    case 192: if constexpr (sizeof(T) == 4) return rfft_z<192>(cs, nin, ls); break;
     default: break;
   }
   const int LT = l_lines(g.nz, 3);
@@ -1276,7 +1285,7 @@ int Engine<T>::autotune(std::string* report) {
     const int xreal[4] = {0, 4, 4, 1};
     for (int round = 0; round < 2; ++round) {
       for (int cls = 0; cls < 6; ++cls) {
-        if ((cls == 4 && rfft::supported(g.ny)) || (cls == 5 && rfft::supported(g.nz))) continue;
+        if ((cls == 4 && rfft::supported<T>(g.ny)) || (cls == 5 && rfft::supported<T>(g.nz))) continue;
         const Shapes keep = shp;
         Shapes bestS = shp;
         float best = cur;

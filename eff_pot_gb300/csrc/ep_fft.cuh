@@ -150,11 +150,107 @@ template <class T, int DIR> EP_DEV void dft16(C2<T>* v) {
   }
 }
 
+// cos(2 pi m / n) (c = 0) and sin(2 pi m / n) (c = 1) as compile-time
+// constants: the angle is reduced by its quadrant to q pi/2 + phi with
+// phi in [0, pi/2), phi above pi/4 is taken as the complement, and the
+// Taylor series of sin and cos are summed at |x| <= pi/4 (terms to x^29,
+// far below double rounding there).
+namespace ctw {
+constexpr double kPi = 3.14159265358979323846264338327950288;
+__host__ __device__ constexpr double sin_t(double x) {
+  double t = x, s = x;
+  for (int i = 1; i < 15; ++i) {
+    t *= -x * x / ((2.0 * i) * (2.0 * i + 1.0));
+    s += t;
+  }
+  return s;
+}
+__host__ __device__ constexpr double cos_t(double x) {
+  double t = 1.0, s = 1.0;
+  for (int i = 1; i < 15; ++i) {
+    t *= -x * x / ((2.0 * i - 1.0) * (2.0 * i));
+    s += t;
+  }
+  return s;
+}
+__host__ __device__ constexpr double cs2pi(int m, int n, int c) {
+  const int mm = ((m % n) + n) % n;
+  const int q = (4 * mm) / n, r = 4 * mm - q * n;  // angle = q pi/2 + (pi/2) r/n
+  double co = 0.0, si = 0.0;
+  if (2 * r <= n) {
+    const double x = 0.5 * kPi * r / n;
+    co = cos_t(x);
+    si = sin_t(x);
+  } else {
+    const double x = 0.5 * kPi * (n - r) / n;
+    co = sin_t(x);
+    si = cos_t(x);
+  }
+  const double C[4] = {co, -si, -co, si}, S[4] = {si, co, -si, -co};
+  return c == 0 ? C[q] : S[q];
+}
+}  // namespace ctw
+
+// y[I] *= w_N^(DIR (I / A)(I % A)) for I = I0 .. N-1, w_N = exp(2 pi i / N):
+// the inner twiddles of dft_ab, as constants (multiples of pi/2 as swaps)
+template <class T, int N, int A, int DIR, int I>
+EP_DEV void tw_ab(C2<T>* y) {
+  if constexpr (I < N) {
+    constexpr int e = (I / A) * (I % A) % N;
+    if constexpr (e != 0) {
+      if constexpr ((4 * e) % N == 0) {
+        constexpr int q = 4 * e / N;
+        if constexpr (q == 1) y[I] = rot<DIR>(y[I]);
+        else if constexpr (q == 2) y[I] = cmk<T>(-y[I].x, -y[I].y);
+        else y[I] = rot<-DIR>(y[I]);
+      } else {
+        constexpr double c = ctw::cs2pi(e, N, 0), s = ctw::cs2pi(e, N, 1);
+        y[I] = rotc<T, DIR>(y[I], T(c), T(s));
+      }
+    }
+    tw_ab<T, N, A, DIR, I + 1>(y);
+  }
+}
+
+// N = A B point DFT (A, B in {2, 3, 4, 5, 8}) in registers:
+//   n = B n1 + n2, k = k1 + A k2,
+//   X[k1 + A k2] = sum_n2 w_B^(n2 k2) w_N^(n2 k1) sum_n1 x[B n1 + n2] w_A^(n1 k1)
+template <class T, int A, int B, int DIR> EP_DEV void dft_ab(C2<T>* v) {
+  constexpr int N = A * B;
+  C2<T> y[N];
+#pragma unroll
+  for (int n2 = 0; n2 < B; ++n2) {
+    C2<T> a[A];
+#pragma unroll
+    for (int n1 = 0; n1 < A; ++n1) a[n1] = v[B * n1 + n2];
+    dftR<T, A, DIR>(a);
+#pragma unroll
+    for (int k1 = 0; k1 < A; ++k1) y[A * n2 + k1] = a[k1];
+  }
+  tw_ab<T, N, A, DIR, 0>(y);
+#pragma unroll
+  for (int k1 = 0; k1 < A; ++k1) {
+    C2<T> b[B];
+#pragma unroll
+    for (int n2 = 0; n2 < B; ++n2) b[n2] = y[A * n2 + k1];
+    dftR<T, B, DIR>(b);
+#pragma unroll
+    for (int k2 = 0; k2 < B; ++k2) v[k1 + A * k2] = b[k2];
+  }
+}
+
+// Register DFT of R points, R in {2, 4, 8, 12, 16, 20, 24}.
 template <class T, int R, int DIR> EP_DEV void dft(C2<T>* v) {
-  if (R == 16) dft16<T, DIR>(v);
-  else if (R == 8) dft8<T, DIR>(v);
-  else if (R == 4) dft4<T, DIR>(v);
-  else dft2<T, DIR>(v);
+  if constexpr (R == 16) dft16<T, DIR>(v);
+  else if constexpr (R == 8) dft8<T, DIR>(v);
+  else if constexpr (R == 4) dft4<T, DIR>(v);
+  else if constexpr (R == 12) dft_ab<T, 4, 3, DIR>(v);
+  else if constexpr (R == 20) dft_ab<T, 4, 5, DIR>(v);
+  else if constexpr (R == 24) dft_ab<T, 8, 3, DIR>(v);
+  else {
+    static_assert(R == 2, "register DFT length");
+    dft2<T, DIR>(v);
+  }
 }
 
 // q = a / d, r = a - q d for 0 <= a < 2^22 through a float reciprocal

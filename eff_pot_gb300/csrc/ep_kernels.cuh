@@ -307,7 +307,8 @@ EP_DEV void block_reduce_store_acc(Acc<float> (&acc)[NQ], double* __restrict__ p
 // ---------------------------------------------------------------------------
 // X pass helpers (lines along x are contiguous; nl lines per CTA).
 //
-// Half-line transforms of N2 = nx/2 points.  N2 in {16, 32, 64, 128} use
+// Half-line transforms of N2 = nx/2 points.  N2 in {16, 32, 64, 128} (and
+// in FP32 also 48, 80, 96) use
 // xlines: P threads of one warp per line, E = N2/P points per thread, the
 // two-factor decomposition of ep_rfft.cuh with the exchange done in place in
 // the line's own shared-memory row (stride P+1 for the exchange), fenced by
@@ -319,21 +320,31 @@ template <> struct XShape<16> { static constexpr int P = 4, E = 4; };
 template <> struct XShape<32> { static constexpr int P = 4, E = 8; };
 template <> struct XShape<64> { static constexpr int P = 8, E = 8; };
 template <> struct XShape<128> { static constexpr int P = 8, E = 16; };
+template <> struct XShape<48> { static constexpr int P = 4, E = 12; };
+template <> struct XShape<80> { static constexpr int P = 4, E = 20; };
+template <> struct XShape<96> { static constexpr int P = 4, E = 24; };
 
+// the register transform length of half-lines of n2 points (0: the general
+// engine); the mixed-radix lengths only in FP32, where the FP64 engine is
+// bound by its arithmetic pipe either way
+template <class T>
 __host__ __device__ constexpr int x_reg_n2(int n2) {
-  return (n2 == 16 || n2 == 32 || n2 == 64 || n2 == 128) ? n2 : 0;
+  return (n2 == 16 || n2 == 32 || n2 == 64 || n2 == 128) ? n2
+         : (sizeof(T) == 4 && (n2 == 48 || n2 == 80 || n2 == 96)) ? n2
+                                                                    : 0;
 }
 // row stride (complex elements): >= n2 + 1 and >= E (P + 1), and congruent
 // to P modulo 16 so that the lines sharing a half-warp fall on distinct banks
 __host__ __device__ constexpr int x_row(int n2, int reg) {
-  return !reg ? n2 + 1 : (n2 == 16 ? 20 : n2 == 32 ? 52 : n2 == 64 ? 72 : 152);
+  return !reg ? n2 + 1
+              : (n2 == 16 ? 20 : n2 == 32 ? 52 : n2 == 48 ? 68 : n2 == 64 ? 72 : n2 == 80 ? 100 : n2 == 96 ? 132 : 152);
 }
 // shared memory of an X kernel: two line buffers, the twiddles exp(-2 pi i
 // k/nx), the [ka][t] twiddle table of xlines, nreal real arrays
 template <class T>
 __host__ __device__ constexpr size_t x_smem_bytes(int nl, int nx, int nreal) {
-  return 2 * (size_t)nl * x_row(nx / 2, x_reg_n2(nx / 2)) * sizeof(C2<T>) + (size_t)nx * sizeof(C2<T>) +
-         (size_t)(x_reg_n2(nx / 2) ? nx / 2 : 0) * sizeof(C2<T>) + (size_t)nreal * nl * nx * sizeof(T);
+  return 2 * (size_t)nl * x_row(nx / 2, x_reg_n2<T>(nx / 2)) * sizeof(C2<T>) + (size_t)nx * sizeof(C2<T>) +
+         (size_t)(x_reg_n2<T>(nx / 2) ? nx / 2 : 0) * sizeof(C2<T>) + (size_t)nreal * nl * nx * sizeof(T);
 }
 
 template <class T, int N2, int DIR>

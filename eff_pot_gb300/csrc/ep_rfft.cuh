@@ -1,5 +1,5 @@
 // ep_rfft.cuh - register-resident FFTs of strided lines (the Y and Z passes)
-// for line lengths N in {32, 64, 128, 256}.
+// for line lengths N in {32, 64, 128, 256} and, in FP32, {96, 192}.
 //
 // A CTA owns 32 lines whose first elements are (nearly) contiguous in memory
 // (the x index runs fastest) and P threads per line: lane = line, warp = t.
@@ -32,8 +32,15 @@ template <> struct Shape<32> { static constexpr int P = 4, E = 8; };
 template <> struct Shape<64> { static constexpr int P = 8, E = 8; };
 template <> struct Shape<128> { static constexpr int P = 8, E = 16; };
 template <> struct Shape<256> { static constexpr int P = 16, E = 16; };
+template <> struct Shape<96> { static constexpr int P = 4, E = 24; };
+template <> struct Shape<192> { static constexpr int P = 8, E = 24; };
 
-inline constexpr bool supported(int n) { return n == 32 || n == 64 || n == 128 || n == 256; }
+// the mixed-radix lengths only in FP32 (the FP64 passes are bound by the
+// arithmetic pipe, where the shared-memory engine does as well)
+template <class T>
+constexpr bool supported(int n) {
+  return n == 32 || n == 64 || n == 128 || n == 256 || (sizeof(T) == 4 && (n == 96 || n == 192));
+}
 
 // Transform of the CTA's lines: on entry v[a] = x[t + P a], on return
 // v[m] = X[t + P m].  S: this line's exchange row (N + 1 entries); tw: the
@@ -80,10 +87,10 @@ template <class T, int N> struct Occ {
   // the in-place Y pass fits 64 registers at N = 128 without spilling: four
   // CTAs per SM keep more lines in flight (the pass is load-latency bound)
   static constexpr int c2c = sizeof(T) == 4 ? (N <= 128 ? 4 : 2) : (N <= 64 ? 2 : 1);
-  static constexpr int conv = sizeof(T) == 4 ? (N <= 64 ? 3 : (N == 128 ? 2 : 1)) : 1;
+  static constexpr int conv = sizeof(T) == 4 ? (N <= 96 ? 3 : (N <= 192 ? 2 : 1)) : 1;
   // one output per input (no spectrum kept): 3 CTAs per SM at N = 128 (64
   // registers would spill)
-  static constexpr int conv1 = sizeof(T) == 4 ? (N <= 64 ? 4 : (N == 128 ? 3 : 2)) : (N <= 64 ? 2 : 1);
+  static constexpr int conv1 = sizeof(T) == 4 ? (N <= 96 ? 4 : (N == 128 ? 3 : 2)) : (N <= 64 ? 2 : 1);
 };
 
 // In-place transforms along a strided axis of up to 8 arrays (blockIdx.y).

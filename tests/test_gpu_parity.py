@@ -267,3 +267,36 @@ def test_uneven_mixed_radix_grid_matches_oracle(oracle, prec):
         g.run(6, 5e-4)
         o.run(6, 5e-4)
         assert rel(g.psi(), o.psi()) < (1e-10 if prec == _abi.EP_FP64 else 1e-4)
+
+
+@pytest.mark.parametrize("dims", [(96, 192, 32), (160, 32, 96), (192, 32, 192)])
+def test_fp32_mixed_radix_register_transforms_match_oracle(oracle, dims):
+    """FP32 grids whose axes take the mixed-radix register transforms: X
+    half-lines of 48, 80 and 96 points (12-, 20- and 24-point codelets, 4
+    threads per line) and Y/Z lines of 96 and 192 points (24-point codelets,
+    4 and 8 threads per line), against the FP64 oracle at FP32 tolerance:
+    every field of poten, then RK and predictor-corrector steps."""
+    nx, ny, nz = dims
+    h = 0.8
+
+    def cfg(prec):
+        return ep.make_config(nx=nx, ny=ny, nz=nz, xmax=nx * h / 2, ymax=ny * h / 2, zmax=nz * h / 2,
+                              icon=_abi.EP_ICON_PERIODIC, core="OTC", n4=100.0, impurity=_abi.EP_IMPURITY_FIXED,
+                              precision=prec)
+
+    psi = ep.woods_saxon_psi(nx, ny, nz, nx * h / 2, ny * h / 2, nz * h / 2, 100.0, seed=21)
+    g, o = ep.Solver(cfg(_abi.EP_FP32)), oracle.OracleSolver(cfg(_abi.EP_FP64))
+    pot = ep.morse(10.0, 4.5, 1.2, r_cutoff=0.0, umax=1000.0)
+    for s in (g, o):
+        s.set_impurity_potentials(pot, pot, ep.morse(12.0, 4.0, 1.1))
+        s.set_impurity(rimp=(0.4, -0.7, 1.1), invar=np.zeros(10, dtype=np.complex128))
+        s.start(psi)
+    with g, o:
+        for f in FIELDS_ALL:
+            assert rel(g.field(f), o.field(f)) < 2e-5, (f, rel(g.field(f), o.field(f)))
+        for _ in range(3):
+            g.steprk(5e-4)
+            o.steprk(5e-4)
+        g.run(3, 5e-4)
+        o.run(3, 5e-4)
+        assert rel(g.psi(), o.psi()) < 1e-4
