@@ -19,6 +19,8 @@ EP_FP64, EP_FP32 = 0, 1
 EP_ICON_PERIODIC, EP_ICON_ZERO_OUTSIDE = 8, 13
 EP_STATE_P, EP_STATE_D = 0, 1
 EP_POT_NULL, EP_POT_MORSE, EP_POT_KOUTSELOS = 0, 1, 2
+EP_POT_PATIL, EP_POT_AZIZ, EP_POT_TANG_TOENNIES, EP_POT_SERIES = 3, 4, 5, 6
+EP_SERIES_MAX = 24
 
 FIELDS = {
     "den": 0, "pot4": 1, "uimp": 2, "dencg": 3, "delj4": 4, "dxden": 5,
@@ -51,9 +53,17 @@ class EpConfig(C.Structure):
     ]
 
 
+class EpSeries(C.Structure):
+    _fields_ = [("r_core", C.c_double), ("f_core", C.c_double), ("r0", C.c_double),
+                ("aa", C.c_double), ("bb", C.c_double), ("cc", C.c_double),
+                ("k0", C.c_int), ("n", C.c_int), ("quad", C.c_int),
+                ("c_hi", C.c_double * EP_SERIES_MAX), ("c_lo", C.c_double * EP_SERIES_MAX)]
+
+
 class EpPotential(C.Structure):
     _fields_ = [("kind", C.c_int), ("r_cutoff", C.c_double),
-                ("umax", C.c_double), ("par", C.c_double * 4)]
+                ("umax", C.c_double), ("par", C.c_double * 4),
+                ("series", C.POINTER(EpSeries))]
 
 
 class EpEnergies(C.Structure):
@@ -104,8 +114,11 @@ _prototypes = {
     "steppc": (_I, [_P, C.c_double, C.POINTER(EpStepErrors)]),
     "run": (_I, [_P, _I, C.c_double, C.POINTER(EpRunStats)]),
     "renormalize": (_I, [_P, _D]),
+    "potential_values": (_I, [C.POINTER(EpPotential), _D, _D, _I]),
 }
 _product_only = {
+    "select_pot": (_I, [C.c_char_p, C.c_double, C.c_double, C.c_char_p, C.POINTER(EpPotential),
+                        C.POINTER(EpSeries), C.c_char_p, _I]),
     "create_error": (C.c_char_p, []),
     "synchronize": (_I, [_P]),
     "stream": (_P, [_P]),

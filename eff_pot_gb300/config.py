@@ -3,6 +3,8 @@
 Defaults follow modules.f90 (deriva :15,19; grid :75-84; he4 :124-133;
 lenard4 :191-196), V_impur.f90:1-16 and DFT4He3d.f90:78 (n4=300).
 """
+import ctypes as C
+
 from . import _abi
 
 DEFAULTS = dict(
@@ -74,4 +76,54 @@ def koutselos(ion="Rb", r_cutoff=0.0, umax=0.0):
 def null_potential():
     p = _abi.EpPotential()
     p.kind = _abi.EP_POT_NULL
+    return p
+
+
+PATIL_ATOMS = {"LI": 0, "NA": 1, "K": 2, "RB": 3, "CS": 4}
+TANG_TOENNIES_ATOMS = {"Ar": 0, "Xe": 1}
+
+
+def _closed(kind, atom=0.0, r_cutoff=0.0, umax=0.0):
+    p = _abi.EpPotential()
+    p.kind = kind
+    p.r_cutoff = r_cutoff
+    p.umax = umax
+    p.par[0] = float(atom)
+    return p
+
+
+def patil(atom="RB", r_cutoff=0.0, umax=0.0):
+    """Patil's alkali-He potential (selec = 'LI', 'NA', 'K', 'RB', 'CS')."""
+    return _closed(_abi.EP_POT_PATIL, PATIL_ATOMS[atom], r_cutoff, umax)
+
+
+def aziz_he(r_cutoff=0.0, umax=0.0):
+    """The He-He potential of Aziz et al. (selec = 'Aziz_He')."""
+    return _closed(_abi.EP_POT_AZIZ, 0, r_cutoff, umax)
+
+
+def tang_toennies(atom="Xe", r_cutoff=0.0, umax=0.0):
+    """Tang-Toennies rare-gas-He potentials (selec = 'Ar_He', 'Xe_He')."""
+    return _closed(_abi.EP_POT_TANG_TOENNIES, TANG_TOENNIES_ATOMS[atom], r_cutoff, umax)
+
+
+def series_potential(coef, k0, r_core, f_core, r0, aa, bb, cc, quad=True, r_cutoff=0.0, umax=0.0):
+    """An inverse-power fit with a parabolic core (the Param_LJ_* form of
+    V_impur.f90): f_core for x <= r_core, |aa x^2 + bb x + cc| for x <= r0,
+    sum_k coef[k-1] x^-(k+k0) beyond.  coef entries are floats or (hi, lo)
+    pairs (a double-double coefficient); quad sums in double-double.  The
+    returned EpPotential holds a reference to its EpSeries."""
+    if not 1 <= len(coef) <= _abi.EP_SERIES_MAX:
+        raise ValueError(f"1 <= len(coef) <= {_abi.EP_SERIES_MAX}")
+    s = _abi.EpSeries()
+    s.r_core, s.f_core, s.r0, s.aa, s.bb, s.cc = r_core, f_core, r0, aa, bb, cc
+    s.k0, s.n, s.quad = int(k0), len(coef), 1 if quad else 0
+    for k, c in enumerate(coef):
+        hi, lo = (c, 0.0) if not isinstance(c, (tuple, list)) else c
+        s.c_hi[k], s.c_lo[k] = float(hi), float(lo)
+    p = _abi.EpPotential()
+    p.kind = _abi.EP_POT_SERIES
+    p.r_cutoff, p.umax = r_cutoff, umax
+    p.series = C.pointer(s)
+    p._series = s
     return p

@@ -13,7 +13,8 @@
 // real time, printing mu and the energy every `pener` steps, and writes
 // `filedenout` in the printoutc layout (printoutc.f90:85-125; binary when
 // iprint < 0).  Namelist keys the reference does not know: morse_de,
-// morse_re, morse_alpha (selec_* = 'Morse'), precision ('fp64' | 'fp32'),
+// morse_re, morse_alpha (selec_* = 'Morse'), potentials_source (the
+// V_impur.f90 whose fits selec_* may name), precision ('fp64' | 'fp32'),
 // refine (final FP64 steps of an FP32 run), timemode, iprint.
 //
 // `ep_dft4he3d --scan file...` (namelist on standard input) is the U*/U+
@@ -26,11 +27,14 @@
 // instate 0..4) states are built as instates.f90 does in its default branch
 // (ep_instates.h); Lexcite_state_fix gives the fixed P vectors, instate 5
 // reads invar.dat, Ldiag_jz picks the state of given <Jz> in a j manifold.
-// Not built here: the Laverage_P_value / Lmixture / exciplex variants of
-// instates.f90 (they sum eigenvectors, so they depend on EISPACK's phase
-// convention), and the Select_Pot closed forms other than 'null', 'Morse'
-// and the four '*_plus_Koutselos' (V_impur.f90:87-932; any of them runs as
-// selec_* = 'table' from a file of (r, V) rows).
+// Pair potentials: Select_Pot by name through ep_select_pot (the closed
+// forms built into the library; the inverse-power fits of V_impur.f90 read
+// from the file named by the key potentials_source), 'Morse', or 'table'
+// from a file of (r, V) rows.  Not built here: the Laverage_P_value /
+// Lmixture / exciplex variants of instates.f90 (they sum eigenvectors, so
+// they depend on EISPACK's phase convention), and the Select_Pot forms that
+// are neither built in nor inverse-power fits (Ag, Ba_gs, CH3I, Cs_7s, the
+// surface potentials); they run as 'table'.
 #include <cmath>
 #include <complex>
 #include <cstdio>
@@ -89,30 +93,35 @@ void check(int st, ep_ctx* c, const char* what) {
   if (st != EP_OK) stop(std::string(what) + " failed: " + (c ? ep_last_error(c) : ep_create_error()), 2);
 }
 
-// selec_* -> ep_potential ('null', 'Morse'); anything else is not tabulated here.
+// selec_* -> ep_potential: 'Morse' (this project's selector), 'table'
+// (tabulated by pair_tables below), everything else through Select_Pot by
+// name (ep_select_pot: the built-in closed forms, and the inverse-power fits
+// read from the reference's V_impur.f90 named by potentials_source).  *store
+// holds a fit for as long as the potential is used.
 ep_potential potential_of(const Input& in, const char* which, const char* dflt_sel, double dflt_rc,
-                          double dflt_umax) {
+                          double dflt_umax, ep_series* store) {
   const std::string key = std::string("selec_") + which;
   const std::string sel = trim(in.get<std::string>(key.c_str(), dflt_sel));
   ep_potential p{};
   p.r_cutoff = in.get<double>((std::string("r_cutoff_") + which).c_str(), dflt_rc);
   p.umax = in.get<double>((std::string("umax_") + which).c_str(), dflt_umax);
-  if (sel == "null" || sel == "table") {  // 'table': tabulated by pair_tables below
+  if (sel == "table") {
     p.kind = EP_POT_NULL;
   } else if (sel == "Morse" || sel == "morse") {
     p.kind = EP_POT_MORSE;
     p.par[0] = in.get<double>("morse_de", 10.0);
     p.par[1] = in.get<double>("morse_re", 4.5);
     p.par[2] = in.get<double>("morse_alpha", 1.2);
-  } else if (sel == "Na_plus_Koutselos" || sel == "K_plus_Koutselos" || sel == "Rb_plus_Koutselos" ||
-             sel == "Cs_plus_Koutselos") {  // V_impur.f90:232-290
-    p.kind = EP_POT_KOUTSELOS;
-    p.par[0] = sel[0] == 'N' ? 0 : sel[0] == 'K' ? 1 : sel[0] == 'R' ? 2 : 3;
   } else {
-    stop("selec_" + std::string(which) + "='" + sel +
-         "': this potential of Select_Pot is not built into this driver (use 'null', 'Morse', "
-         "'{Na,K,Rb,Cs}_plus_Koutselos' or 'table' with "
-         "table_" + std::string(which) + " = a file of r (A), V (K) rows)");
+    const std::string src = trim(in.get<std::string>("potentials_source", ""));
+    char err[512];
+    if (ep_select_pot(sel.c_str(), p.r_cutoff, p.umax, src.empty() ? nullptr : src.c_str(), &p, store, err,
+                      (int)sizeof err) != EP_OK)
+      stop("selec_" + std::string(which) + "='" + sel + "': " + err +
+           " (built in: 'null', 'Morse', '{Na,K,Rb,Cs}_plus_Koutselos', 'LI', 'NA', 'K', 'RB', 'CS', "
+           "'Aziz_He', 'Ar_He', 'Xe_He'; the inverse-power fits of V_impur.f90 with potentials_source = "
+           "its path; any potential as 'table' with table_" + std::string(which) +
+           " = a file of r (A), V (K) rows)");
   }
   return p;
 }
@@ -583,11 +592,13 @@ int main(int argc, char** argv) {
 
     ep_ctx* ctx = nullptr;
     check(ep_create(&cfg, &ctx), nullptr, "ep_create");
-    const ep_potential ppi = potential_of(in, "pi", "Ba_plus_2D1", 1.05, 5.216077e4);
-    const ep_potential psg = potential_of(in, "sigma", "Ba_plus_2D0", 1.05, 9.674836e4);
-    const ep_potential ppl = potential_of(in, "plus", "Ba_plus_2D2", 1.05, 6.260015e4);
-    const ep_potential pdl = cfg.state == EP_STATE_D ? potential_of(in, "delta", "Ba_plus_2D2", 1.05, 6.260015e4)
-                                                     : ep_potential{};
+    ep_series fits[4] = {};
+    const ep_potential ppi = potential_of(in, "pi", "Ba_plus_2D1", 1.05, 5.216077e4, &fits[0]);
+    const ep_potential psg = potential_of(in, "sigma", "Ba_plus_2D0", 1.05, 9.674836e4, &fits[1]);
+    const ep_potential ppl = potential_of(in, "plus", "Ba_plus_2D2", 1.05, 6.260015e4, &fits[2]);
+    const ep_potential pdl = cfg.state == EP_STATE_D
+                                 ? potential_of(in, "delta", "Ba_plus_2D2", 1.05, 6.260015e4, &fits[3])
+                                 : ep_potential{};
     auto set_potentials = [&](ep_ctx* x) {
       if (cfg.state == EP_STATE_D)
         check(ep_set_impurity_potentials_d(x, &ppi, &psg, &pdl, &ppl), x, "impurity potentials");

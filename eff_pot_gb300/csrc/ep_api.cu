@@ -79,9 +79,29 @@ int fail(ep_ctx* c, int code, const std::string& msg) {
   return code;
 }
 
-// Select_Pot subset (V_impur.f90:87-932) plus the Morse selector.
+// Select_Pot (V_impur.f90:87-932) plus the Morse selector.
 double select_pot(const ep_potential& p, double r) {
-  return ep_pair_potential(p.kind, p.r_cutoff, p.umax, p.par[0], p.par[1], p.par[2], r);
+  return ep_pair_potential(p.kind, p.r_cutoff, p.umax, p.par, p.series, r);
+}
+
+// A potential the evaluator knows; a series fit with 0 < n <= EP_SERIES_MAX.
+const char* bad_potential(const ep_potential* p) {
+  if (!p) return "null potential";
+  if (p->kind < EP_POT_NULL || p->kind > EP_POT_SERIES) return "unknown potential kind";
+  if (p->kind == EP_POT_SERIES) {
+    if (!p->series) return "EP_POT_SERIES without its fit";
+    if (p->series->n < 1 || p->series->n > EP_SERIES_MAX) return "series fit: n outside 1..EP_SERIES_MAX";
+    if (p->series->k0 < 0 || p->series->k0 > 64) return "series fit: k0 outside 0..64";
+  }
+  return nullptr;
+}
+
+// Keeps plus for energy(): the fit is copied, the borrowed pointer dropped.
+void keep_plus(ImpState& imp, const ep_potential* plus) {
+  imp.plus = *plus;
+  imp.plus.series = nullptr;
+  imp.plus_series = ep_series{};
+  if (plus->kind == EP_POT_SERIES) imp.plus_series = *plus->series;
 }
 
 template <class F>
@@ -308,10 +328,18 @@ int ep_destroy(ep_ctx* c) {
 
 const char* ep_last_error(const ep_ctx* c) { return c ? c->err.c_str() : "null context"; }
 
+int ep_potential_values(const ep_potential* p, const double* r, double* v, int n) {
+  if (!p || (n > 0 && (!r || !v)) || n < 0 || bad_potential(p)) return EP_ERR_INVALID_ARG;
+  for (int i = 0; i < n; ++i) v[i] = select_pot(*p, r[i]);
+  return EP_OK;
+}
+
 // potenimpini (potenimpini.f90:11-58), P state.
 int ep_set_impurity_potentials(ep_ctx* c, const ep_potential* pi, const ep_potential* sigma, const ep_potential* plus) {
   if (!c || !pi || !sigma) return EP_ERR_INVALID_ARG;
   if (c->cfg.state != EP_STATE_P) return fail(c, EP_ERR_STATE, "D state: use ep_set_impurity_potentials_d");
+  for (const ep_potential* q : {pi, sigma, plus})
+    if (q && bad_potential(q)) return fail(c, EP_ERR_INVALID_ARG, bad_potential(q));
   const ep_config& g = c->cfg;
   const int npot = 100 * std::max(g.nx, std::max(g.ny, g.nz)) + 1;
   const double rmax = 4.0 * std::max(g.xmax, std::max(g.ymax, g.zmax));
@@ -325,7 +353,7 @@ int ep_set_impurity_potentials(ep_ctx* c, const ep_potential* pi, const ep_poten
   }
   tp[0] = tp[1]; tp[npot + 1] = tp[npot];
   td[0] = td[1]; td[npot + 1] = td[npot];
-  if (plus) c->imp.plus = *plus;
+  if (plus) keep_plus(c->imp, plus);
   return ep_set_impurity_tables(c, tp.data(), td.data(), npot, del, sigma->umax);
 }
 
@@ -390,6 +418,8 @@ int ep_set_impurity_potentials_d(ep_ctx* c, const ep_potential* pi, const ep_pot
                                  const ep_potential* delta, const ep_potential* plus) {
   if (!c || !pi || !sigma || !delta) return EP_ERR_INVALID_ARG;
   if (c->cfg.state != EP_STATE_D) return fail(c, EP_ERR_STATE, "D-state potentials need state = EP_STATE_D");
+  for (const ep_potential* q : {pi, sigma, delta, plus})
+    if (q && bad_potential(q)) return fail(c, EP_ERR_INVALID_ARG, bad_potential(q));
   const ep_config& g = c->cfg;
   const int npot = 100 * std::max(g.nx, std::max(g.ny, g.nz)) + 1;
   const double rmax = 4.0 * std::max(g.xmax, std::max(g.ymax, g.zmax));
@@ -405,7 +435,7 @@ int ep_set_impurity_potentials_d(ep_ctx* c, const ep_potential* pi, const ep_pot
   td[0] = td[1]; td[npot + 1] = td[npot];
   tpd[0] = tpd[1]; tpd[npot + 1] = tpd[npot];
   tsd[0] = tsd[1]; tsd[npot + 1] = tsd[npot];
-  if (plus) c->imp.plus = *plus;
+  if (plus) keep_plus(c->imp, plus);
   return ep_set_impurity_tables_d(c, td.data(), tpd.data(), tsd.data(), npot, del, pi->umax, sigma->umax);
 }
 

@@ -50,7 +50,8 @@ struct ImpState {
   // P state: FP32 copies of d_potpi, d_potdel for the FP32 engine
   float* d_potpi_f = nullptr;
   float* d_potdel_f = nullptr;
-  ep_potential plus{};
+  ep_potential plus{};  // series pointer cleared: the fit lives in plus_series
+  ep_series plus_series{};
   bool have_tables = false;
 };
 

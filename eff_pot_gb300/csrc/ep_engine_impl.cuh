@@ -581,7 +581,12 @@ int Engine<T>::energy(ep_energies* e) {
   if (!have_field) { *err = "poten() must run before energy()"; return EP_ERR_STATE; }
   int r0 = ensure_materialized();
   if (r0) return r0;
-  PotDev vp{imp->plus.kind, imp->plus.r_cutoff, imp->plus.umax, imp->plus.par[0], imp->plus.par[1], imp->plus.par[2]};
+  PotDev vp{};
+  vp.kind = imp->plus.kind;
+  vp.r_cutoff = imp->plus.r_cutoff;
+  vp.umax = imp->plus.umax;
+  for (int i = 0; i < 4; ++i) vp.par[i] = imp->plus.par[i];
+  vp.s = imp->plus_series;
   auto k = k_energy<T>;
   EP_LAUNCH("energy", k, EP_RED_BLOCKS, 256, 0, g, fd, phys, psi, den, dencg, delj4, falfs, dxd, dyd, dzd, intx,
             inty, intz, uimp, cfg.xmax, cfg.ymax, cfg.zmax, hx, hy, hz, imp->rimp[0], imp->rimp[1], imp->rimp[2],

@@ -3,6 +3,7 @@
 #pragma once
 #include "ep_common.cuh"
 #include "ep_fft.cuh"
+#include "ep_pairpot.h"
 
 // ---------------------------------------------------------------------------
 // Kernel parameter blocks.
@@ -1561,7 +1562,8 @@ __global__ void k_potenimp_d(Geo g, double xmax, double ymax, double zmax, doubl
 // Energy integrals of energy.f90:47-165 (8 sums, see the launcher).
 struct PotDev {
   int kind;
-  double r_cutoff, umax, p0, p1, p2;
+  double r_cutoff, umax, par[4];
+  ep_series s;  // EP_POT_SERIES
 };
 template <class T>
 __global__ void k_energy(Geo g, FdW<T> fd, Phys ph, const C2<T>* __restrict__ psi, const T* __restrict__ den,
@@ -1569,8 +1571,8 @@ __global__ void k_energy(Geo g, FdW<T> fd, Phys ph, const C2<T>* __restrict__ ps
                          const T* __restrict__ dxd, const T* __restrict__ dyd, const T* __restrict__ dzd,
                          const T* __restrict__ ix, const T* __restrict__ iy, const T* __restrict__ iz,
                          const T* __restrict__ uimp, double xmax, double ymax, double zmax, double hx, double hy,
-                         double hz, double r0, double r1, double r2, double zexc, PotDev vplus, int impurity,
-                         double* __restrict__ partials);
+                         double hz, double r0, double r1, double r2, double zexc, const __grid_constant__ PotDev vplus,
+                         int impurity, double* __restrict__ partials);
 
 // forceimp / potinvar moments (potenimp.f90:193-258, 298-317); the F_z sum
 // runs over the planes izlo <= iz < izhi (the exciplex filter, :211-248).

@@ -34,7 +34,7 @@ EP_DEV double interp_update(double r, int nint, double rmax, const double* __res
 
 // Pair potential of the U+ integral (Select_Pot subset + Morse).
 EP_DEV double pot_eval(const PotDev& v, double r) {
-  return ep_pair_potential(v.kind, v.r_cutoff, v.umax, v.p0, v.p1, v.p2, r);
+  return ep_pair_potential(v.kind, v.r_cutoff, v.umax, v.par, &v.s, r);
 }
 
 template <class T>
@@ -270,8 +270,8 @@ __global__ void k_energy(Geo g, FdW<T> fd, Phys ph, const C2<T>* __restrict__ ps
                          const T* __restrict__ dxd, const T* __restrict__ dyd, const T* __restrict__ dzd,
                          const T* __restrict__ ix_, const T* __restrict__ iy_, const T* __restrict__ iz_,
                          const T* __restrict__ uimp, double xmax, double ymax, double zmax, double hx, double hy,
-                         double hz, double r0, double r1, double r2, double zexc, PotDev vplus, int impurity,
-                         double* __restrict__ partials) {
+                         double hz, double r0, double r1, double r2, double zexc, const __grid_constant__ PotDev vplus,
+                         int impurity, double* __restrict__ partials) {
   double acc[8] = {0, 0, 0, 0, 0, 0, 0, 0};
   const bool otc = ph.core == 1;
   const double aux1 = 0.5 * ph.cp4, aux2 = (1.0 / 3.0) * ph.cpp4;

@@ -1,4 +1,4 @@
-// ep_pairpot.h - the He-X pair potentials of the Select_Pot subset this
+// ep_pairpot.h - the He-X pair potentials of the Select_Pot registry this
 // library evaluates itself (V_impur.f90:87-932), for host and device code.
 #pragma once
 #include <math.h>
@@ -49,16 +49,179 @@ EP_PP_HD double ep_koutselos(int ion, double r_angstrom) {
   return v * hartree * ev_k;
 }
 
-// Select_Pot for kind (EP_POT_*), its cutoff rule r < r_cutoff -> umax and
-// parameters p0..p2 (Morse: De, re, alpha; Koutselos: the ion code).
-EP_PP_HD double ep_pair_potential(int kind, double r_cutoff, double umax, double p0, double p1, double p2,
+// Patil's alkali-He potential, S. H. Patil, J. Chem. Phys. 94, 8089 (1991),
+// as V_alka (V_impur.f90:1097-1192): an exchange term from the alkali's
+// valence density at the He (asymptotic form agran d^(2u) (1 + v/d)^2
+// e^(-2d/a), u = a - 1, v = -a^2 u / 2) times the He moments r2, r4, r6,
+// minus the damped dispersion c6 f_9(d)/d^6 + c8 f_11(d)/d^8, f_m = 1 -
+// e^(-d/abar) sum_{n<=m} (d/abar)^n/n!, abar = (a + b)/4; d in bohr, result
+// in K.  atom: 0 Li, 1 Na, 2 K, 3 Rb, 4 Cs.
+EP_PP_HD double ep_patil(int atom, double r_angstrom) {
+  // per atom: a, c6, c8, agran (b = 0.744, r2 = 2.37, r4 = 7.78, r6 = 50.5 for all)
+  const double tab[5][4] = {{1.588, 22.5, 1.06e3, 0.0519},
+                            {1.627, 24.7, 1.29e3, 0.0450},
+                            {1.771, 38.9, 2.66e3, 0.0259},
+                            {1.805, 44.6, 3.18e3, 0.0226},
+                            {1.869, 51.2, 4.34e3, 0.0173}};
+  const double* t = tab[atom < 0 ? 0 : (atom > 4 ? 4 : atom)];
+  const double a = t[0], b = 0.744, c6 = t[1], c8 = t[2], agran = t[3];
+  const double r2 = 2.37, r4 = 7.78, r6 = 50.5;
+  const double bohr = 0.529177249, factor = 11604.448 * 27.211608;
+  const double pi = 4.0 * atan(1.0);
+  const double d = r_angstrom / bohr;
+  const double abar = (a + b) / 4.0, u = a - 1.0, v = -0.5 * (a * a) * u;
+  const double q = 1.0 + v / d;
+  const double roa = agran * pow(d, 2.0 * u) * (q * q) * exp(-2.0 * d / a);
+  double f[2];
+  for (int l = 1; l <= 2; ++l) {
+    double sum = 0.0, term = 1.0, fact = 1.0;
+    const double y = d / abar;
+    for (int n = 0; n <= 2 * l + 7; ++n) {
+      if (n >= 2) fact *= (double)n;
+      sum += term / fact;
+      term *= y;
+    }
+    f[l - 1] = 1.0 - sum * exp(-d / abar);
+  }
+  const double a2 = a * a, d2 = d * d, d6 = d2 * d2 * d2;
+  const double vimp = 4.0 * pi / 3.0 * roa * (r2 + 37.0 / 90.0 * r4 / a2 + 28.0 / 525.0 * r6 / (a2 * a2)) -
+                      c6 * f[0] / d6 - c8 * f[1] / (d6 * d2);
+  return vimp * factor;
+}
+
+// He-He of Aziz et al. (HFD form), as V_Aziz_He (V_impur.f90:970-990):
+// eps (A e^(-alpha x + beta x^2) - F(x) (C6/x^6 + C8/x^8 + C10/x^10)),
+// x = r / rm, F = e^(-(D/x - 1)^2) for x <= D, 1 beyond.
+EP_PP_HD double ep_aziz_he(double rr) {
+  const double eps = 10.948, A = 1.8443101e5, alpha = 10.43329537, beta = -2.27965105, D = 1.4826;
+  const double C6 = 1.36745214, C8 = 0.42123807, C10 = 0.17473318, rm = 2.963;
+  const double x = rr / rm;
+  if (x == 0.0) return A * eps;
+  double ff = 1.0;
+  if (x <= D) {
+    const double q = D / x - 1.0;
+    ff = exp(-(q * q));
+  }
+  const double x2 = x * x, x6 = x2 * x2 * x2, x8 = x6 * x2, x10 = x8 * x2;
+  return (A * exp(-alpha * x + beta * x2) - ff * (C6 / x6 + C8 / x8 + C10 / x10)) * eps;
+}
+
+// Tang-Toennies rare-gas-He potential, K. T. Tang and J. P. Toennies,
+// Z. Phys. D 1, 91 (1986), as V_Ar_He / V_Xe_He (V_impur.f90:2681-2782):
+// A e^(-b x) - sum_{n=3..9} f_2n(b x) C_2n / x^2n, with the damping f_2n =
+// 1 - e^(-bx) sum_{k<=2n} (bx)^k / k! and C_12.. from the recursion C_2n =
+// (C_2n-2 / C_2n-4)^3 C_2n-6; x in bohr, result in K.  atom: 0 Ar, 1 Xe.
+EP_PP_HD double ep_tang_toennies(int atom, double r) {
+  const double tab[2][5] = {{75.8953, 2.0589, 9.7697, 152.8468, 3249.728},
+                            {74.9002, 1.8175, 21.5674, 430.148, 10610.21}};
+  const double* t = tab[atom <= 0 ? 0 : 1];
+  const double AA = t[0], BB = t[1];
+  const double rbohr = 0.5292, to_k = 27.21 * 11604.0;
+  double B[18], C[7], S[18];
+  B[0] = BB;
+  for (int i = 1; i < 18; ++i) B[i] = B[i - 1] * BB / (double)(i + 1);
+  C[0] = t[2];
+  C[1] = t[3];
+  C[2] = t[4];
+  for (int i = 3; i < 7; ++i) {
+    const double q = C[i - 1] / C[i - 2];
+    C[i] = q * q * q * C[i - 3];
+  }
+  const double rr = r / rbohr;
+  const double e = exp(-BB * rr);
+  double p = rr;
+  S[0] = B[0] * p;
+  for (int i = 1; i < 18; ++i) {
+    p = p * rr;
+    S[i] = S[i - 1] + B[i] * p;
+  }
+  double v = AA * e;
+  const double s1 = 1.0 / (rr * rr);
+  double sp = s1 * s1 * s1;
+  for (int i = 0; i < 7; ++i) {
+    const int kmax = 2 * i + 5;  // S(2i + 6) of the 1-based recursion
+    v = v + ((S[kmax] + 1.0) * e - 1.0) * C[i] * sp;
+    sp = sp * s1;
+  }
+  return v * to_k;
+}
+
+// Double-double arithmetic (Knuth's two-sum, the fused-multiply-add product
+// error, and the normalisations of Dekker's and Bailey's double-double
+// algorithms): 106-bit sums for the Real*16 fits.
+struct ep_dd {
+  double hi, lo;
+};
+EP_PP_HD ep_dd ep_dd_quick(double a, double b) {  // |a| >= |b|
+  const double s = a + b;
+  return ep_dd{s, b - (s - a)};
+}
+EP_PP_HD ep_dd ep_dd_sum2(double a, double b) {
+  const double s = a + b, bb = s - a;
+  return ep_dd{s, (a - (s - bb)) + (b - bb)};
+}
+EP_PP_HD ep_dd ep_dd_add(ep_dd a, ep_dd b) {
+  ep_dd s = ep_dd_sum2(a.hi, b.hi);
+  const ep_dd t = ep_dd_sum2(a.lo, b.lo);
+  s = ep_dd_quick(s.hi, s.lo + t.hi);
+  return ep_dd_quick(s.hi, s.lo + t.lo);
+}
+EP_PP_HD ep_dd ep_dd_mul(ep_dd a, ep_dd b) {
+  const double p = a.hi * b.hi;
+  const double e = fma(a.hi, b.hi, -p) + (a.hi * b.lo + a.lo * b.hi);
+  return ep_dd_quick(p, e);
+}
+EP_PP_HD ep_dd ep_dd_recip(double x) {
+  const double q = 1.0 / x;
+  const double rem = fma(-q, x, 1.0);  // exact
+  return ep_dd_quick(q, rem / x);
+}
+
+// The inverse-power fit s at x (the Param_LJ_* functions of V_impur.f90,
+// e.g. V_Fausto_Rb_gs :2206-2250): core constant, parabola, then the sum
+// over k in ascending order with x^-(k0+1) advanced by one factor 1/x per
+// term.
+EP_PP_HD double ep_series_value(const ep_series* s, double x) {
+  if (x <= s->r_core) return s->f_core;
+  if (x <= s->r0) return fabs(s->aa * (x * x) + s->bb * x + s->cc);
+  const int n = s->n < EP_SERIES_MAX ? s->n : EP_SERIES_MAX;
+  if (s->quad) {
+    const ep_dd xq = ep_dd_recip(x);
+    ep_dd p = xq;
+    for (int i = 0; i < s->k0; ++i) p = ep_dd_mul(p, xq);
+    ep_dd acc{0.0, 0.0};
+    for (int k = 0; k < n; ++k) {
+      acc = ep_dd_add(acc, ep_dd_mul(ep_dd{s->c_hi[k], s->c_lo[k]}, p));
+      p = ep_dd_mul(p, xq);
+    }
+    return acc.hi + acc.lo;
+  }
+  const double xq = 1.0 / x;
+  double p = xq;
+  for (int i = 0; i < s->k0; ++i) p = p * xq;
+  double acc = 0.0;
+  for (int k = 0; k < n; ++k) {
+    acc = acc + s->c_hi[k] * p;
+    p = p * xq;
+  }
+  return acc;
+}
+
+// Select_Pot for kind (EP_POT_*), its cutoff rule r < r_cutoff -> umax,
+// parameters par (Morse: De, re, alpha; Koutselos, Patil, Tang-Toennies:
+// the atom) and, for EP_POT_SERIES, the fit s.
+EP_PP_HD double ep_pair_potential(int kind, double r_cutoff, double umax, const double* par, const ep_series* s,
                                   double r) {
   if (kind == EP_POT_NULL) return 0.0;
   if (r < r_cutoff) return umax;
   if (kind == EP_POT_MORSE) {
-    const double e = exp(-p2 * (r - p1));
-    return p0 * (e * e - 2.0 * e);
+    const double e = exp(-par[2] * (r - par[1]));
+    return par[0] * (e * e - 2.0 * e);
   }
-  if (kind == EP_POT_KOUTSELOS) return ep_koutselos((int)p0, r);
+  if (kind == EP_POT_KOUTSELOS) return ep_koutselos((int)par[0], r);
+  if (kind == EP_POT_PATIL) return ep_patil((int)par[0], r);
+  if (kind == EP_POT_AZIZ) return ep_aziz_he(r);
+  if (kind == EP_POT_TANG_TOENNIES) return ep_tang_toennies((int)par[0], r);
+  if (kind == EP_POT_SERIES && s) return ep_series_value(s, r);
   return 0.0;
 }

@@ -45,6 +45,34 @@ def load_library(path=None):
     return lib, funcs
 
 
+def select_pot(selec, r_cutoff=0.0, umax=0.0, source=None):
+    """Select_Pot by name (V_impur.f90:87-932) through ep_select_pot: the
+    closed forms built into the library, or an inverse-power fit read from
+    the reference's V_impur.f90 at `source`.  Host only (no GPU)."""
+    _, f = load_library()
+    p, s = _abi.EpPotential(), _abi.EpSeries()
+    err = C.create_string_buffer(512)
+    st = f["select_pot"](selec.encode(), float(r_cutoff), float(umax),
+                         None if source is None else os.fsencode(source), C.byref(p), C.byref(s), err, 512)
+    if st != _abi.EP_OK:
+        raise EffPotError(st, err.value.decode())
+    if p.kind == _abi.EP_POT_SERIES:
+        p.series = C.pointer(s)
+        p._series = s
+    return p
+
+
+def potential_values(pot, r):
+    """V(r) of an EpPotential in the library's host arithmetic (ep_potential_values)."""
+    _, f = load_library()
+    r = np.ascontiguousarray(r, dtype=np.float64)
+    v = np.empty_like(r)
+    st = f["potential_values"](C.byref(pot), _abi.dptr(r), _abi.dptr(v), r.size)
+    if st != _abi.EP_OK:
+        raise EffPotError(st, "ep_potential_values")
+    return v
+
+
 def library_config_defaults():
     """ep_config_init() of the library, as a dict."""
     _, f = load_library()

@@ -82,18 +82,71 @@ typedef struct ep_config {
                                 on the far side (potenimp.f90:211-248)      */
 } ep_config;
 
-/* Pair potentials (a subset of the Select_Pot registry, V_impur.f90:87-932,
- * plus the Morse selector this project adds).  r < r_cutoff -> umax.
+/* Pair potentials (the Select_Pot registry, V_impur.f90:87-932, plus the
+ * Morse selector this project adds).  r < r_cutoff -> umax.
  * EP_POT_KOUTSELOS: the He-M+ potentials 'Na_plus_Koutselos',
- * 'K_plus_Koutselos', 'Rb_plus_Koutselos', 'Cs_plus_Koutselos'
- * (V_impur.f90:232-290,1704-1883), par[0] = 0, 1, 2, 3 for Na+, K+, Rb+, Cs+. */
-enum { EP_POT_NULL = 0, EP_POT_MORSE = 1, EP_POT_KOUTSELOS = 2 };
+ *   'K_plus_Koutselos', 'Rb_plus_Koutselos', 'Cs_plus_Koutselos'
+ *   (V_impur.f90:232-290,1704-1883), par[0] = 0, 1, 2, 3 for Na+, K+, Rb+, Cs+.
+ * EP_POT_PATIL: Patil's alkali-He potentials 'LI', 'NA', 'K', 'RB', 'CS'
+ *   (V_alka, V_impur.f90:1097-1192), par[0] = 0 .. 4 for Li .. Cs.
+ * EP_POT_AZIZ: the He-He potential 'Aziz_He' (V_impur.f90:970-990).
+ * EP_POT_TANG_TOENNIES: 'Ar_He', 'Xe_He' (V_impur.f90:2681-2782),
+ *   par[0] = 0 Ar, 1 Xe.
+ * EP_POT_SERIES: the inverse-power fits of V_impur.f90 ('Rb_gs_Fausto',
+ *   'Ba_plus_gs', 'He2S_fci', 'LJ_OT', ...): the fit in *series. */
+enum {
+  EP_POT_NULL = 0,
+  EP_POT_MORSE = 1,
+  EP_POT_KOUTSELOS = 2,
+  EP_POT_PATIL = 3,
+  EP_POT_AZIZ = 4,
+  EP_POT_TANG_TOENNIES = 5,
+  EP_POT_SERIES = 6
+};
+
+#define EP_SERIES_MAX 24
+/* An inverse-power fit with a parabolic core (the Param_LJ_* blocks of
+ * V_impur.f90), x in A, V in K:
+ *   V = f_core                         x <= r_core
+ *   V = |aa x^2 + bb x + cc|           x <= r0
+ *   V = sum_{k=1..n} c_k x^-(k + k0)   beyond,
+ * c_k = c_hi[k-1] + c_lo[k-1].  quad = 1 forms the sum in double-double
+ * arithmetic (106-bit: the fits the reference sums in Real*16), 0 in
+ * double. */
+typedef struct ep_series {
+  double r_core, f_core, r0, aa, bb, cc;
+  int k0, n, quad;
+  double c_hi[EP_SERIES_MAX], c_lo[EP_SERIES_MAX];
+} ep_series;
+
 typedef struct ep_potential {
   int kind;                  /* EP_POT_*                                    */
   double r_cutoff, umax;
   double par[4];             /* Morse: De (K), re (A), alpha (1/A);
-                                Koutselos: ion code                         */
+                                Koutselos, Patil, Tang-Toennies: the atom   */
+  const ep_series* series;   /* EP_POT_SERIES: the fit (read during the
+                                call that takes the potential, not kept)    */
 } ep_potential;
+
+/* V(r_i), i < n, of p in the library's host arithmetic (no GPU needed): the
+ * values potenimpini tabulates and energy() sums for U+. */
+int ep_potential_values(const ep_potential* p, const double* r, double* v,
+                        int n);
+
+/* Select_Pot by name (V_impur.f90:87-932): selec as the namelist gives it,
+ * with its r_cutoff and umax.  The closed forms are built in ('null',
+ * '*_plus_Koutselos', 'LI' .. 'CS', 'Aziz_He', 'Ar_He', 'Xe_He'); the
+ * inverse-power fits are read from the reference's V_impur.f90 at
+ * source_path (NULL: closed forms only): its Select_Pot chain names the
+ * function, whose COMMON block names the BLOCK DATA with the coefficients.
+ * Fortran literal kinds are kept: a constant without exponent letter or
+ * with E is default REAL (rounded to binary32 before it is widened), D is
+ * double, Q is Real*16.  *series receives the fit (p->series points to
+ * it).  EP_ERR_INVALID_ARG with a message in err (cap bytes) for unknown
+ * names, forms this library does not evaluate, or unreadable sources. */
+int ep_select_pot(const char* selec, double r_cutoff, double umax,
+                  const char* source_path, ep_potential* p, ep_series* series,
+                  char* err, int cap);
 
 /* Energies printed by DFT4He3d.f90:460-463 (module energies). */
 typedef struct ep_energies {

@@ -365,6 +365,131 @@ static double v_koutselos(int ion, double xx) {
   return Sto * Hartree * eV_K;
 }
 
+// V_alka (V_impur.f90:1097-1192): Patil's alkali-He potential; atom 0..4 =
+// LI, NA, K, RB, CS (the order of celem).
+static double v_alka(int atom, double dist) {
+  static const double av[5] = {1.588, 1.627, 1.771, 1.805, 1.869};          // :1127
+  static const double c6v[5] = {22.5, 24.7, 38.9, 44.6, 51.2};              // :1129
+  static const double c8v[5] = {1.06e3, 1.29e3, 2.66e3, 3.18e3, 4.34e3};    // :1130
+  static const double agranv[5] = {0.0519, 0.0450, 0.0259, 0.0226, 0.0173};  // :1134
+  const int ie = std::min(std::max(atom, 0), 4);
+  const double evk = 11604.448, bohr = 0.529177249, hartree = 27.211608, factor = evk * hartree;
+  const double a = av[ie], b = 0.744, c6 = c6v[ie], c8 = c8v[ie], agran = agranv[ie];
+  const double r2 = 2.37, r4 = 7.78, r6 = 50.5;
+  const double d = dist / bohr;
+  const double pi = 4.0 * std::atan(1.0);
+  const double abar = (a + b) / 4.0, u = a - 1.0, v = -0.5 * std::pow(a, 2) * u;
+  const double roa = agran * std::pow(d, 2.0 * u) * std::pow(1.0 + v / d, 2) * std::exp(-2.0 * d / a);
+  double f[2];
+  for (int l = 1; l <= 2; ++l) {
+    double sum = 0.0;
+    const int l7 = 2 * l + 7;
+    for (int n = 0; n <= l7; ++n) {
+      double fac = 1.0;
+      for (int i = 2; i <= n; ++i) fac *= i;
+      sum += std::pow(d / abar, n) / fac;
+    }
+    f[l - 1] = 1.0 - sum * std::exp(-d / abar);
+  }
+  const double vimp = 4.0 * pi / 3.0 * roa * (r2 + 37.0 / 90.0 * r4 / std::pow(a, 2) + 28.0 / 525.0 * r6 / std::pow(a, 4)) -
+                      c6 * f[0] / std::pow(d, 6) - c8 * f[1] / std::pow(d, 8);
+  return vimp * factor;
+}
+
+// V_Aziz_He (V_impur.f90:970-990).
+static double v_aziz_he(double rr) {
+  const double Eps = 10.948, A = 1.8443101e5, alpha = 10.43329537, beta = -2.27965105, D = 1.4826;
+  const double C6 = 1.36745214, C8 = 0.42123807, C10 = 0.17473318, rm = 2.963;
+  double ff = 1.0;
+  const double r = rr / rm;
+  if (r <= D) ff = std::exp(-std::pow(D / r - 1.0, 2));
+  if (r == 0.0) return A * Eps;
+  return (A * std::exp(-alpha * r + beta * std::pow(r, 2)) -
+          ff * (C6 / std::pow(r, 6) + C8 / std::pow(r, 8) + C10 / std::pow(r, 10))) *
+         Eps;
+}
+
+// V_Ar_He / V_Xe_He (V_impur.f90:2681-2782), atom 0 = Ar, 1 = Xe.
+static double v_tang_toennies(int atom, double r) {
+  const double AA = atom ? 74.9002 : 75.8953, BB = atom ? 1.8175 : 2.0589;
+  const double C6 = atom ? 21.5674 : 9.7697, C8 = atom ? 430.148 : 152.8468, C10 = atom ? 10610.21 : 3249.728;
+  const double rbohr = 0.5292, Hartree_to_K = 27.21 * 11604.0;
+  double B[19], C[8], S[19];  // 1-based as the reference
+  B[1] = BB;
+  for (int i = 2; i <= 18; ++i) B[i] = B[i - 1] * BB / (double)i;
+  C[1] = C6;
+  C[2] = C8;
+  C[3] = C10;
+  for (int i = 4; i <= 7; ++i) C[i] = std::pow(C[i - 1] / C[i - 2], 3) * C[i - 3];
+  const double rr = r / rbohr;
+  const double Stoe = std::exp(-BB * rr);
+  double Stor = rr;
+  S[1] = B[1] * Stor;
+  for (int i = 2; i <= 18; ++i) {
+    Stor = Stor * rr;
+    S[i] = S[i - 1] + B[i] * Stor;
+  }
+  double Aux = AA * Stoe;
+  const double Sto1 = 1.0 / std::pow(rr, 2);
+  Stor = std::pow(Sto1, 3);
+  for (int i = 1; i <= 7; ++i) {
+    const int kmax = 2 * i + 4;
+    Aux = Aux + ((S[kmax] + 1.0) * Stoe - 1.0) * C[i] * Stor;
+    Stor = Stor * Sto1;
+  }
+  return Aux * Hartree_to_K;
+}
+
+// The inverse-power fits with a parabolic core (e.g. V_Fausto_Rb_gs,
+// V_impur.f90:2206-2250: Sto = sum_k Pg(k) Aux, Aux = xq**(k0+1) times xq
+// per term, xq = 1/x, all in Real*16).  The Real*16 arithmetic is restated
+// as an unevaluated sum of two doubles: hi + lo with |lo| <= ulp(hi)/2.
+namespace qd {
+struct Q {
+  double hi, lo;
+};
+static Q renorm(double a, double b) {
+  const double s = a + b;
+  return Q{s, b - (s - a)};
+}
+static Q plus(Q a, Q b) {
+  double s = a.hi + b.hi, v = s - a.hi;
+  double e = (a.hi - (s - v)) + (b.hi - v);
+  double t = a.lo + b.lo, w = t - a.lo;
+  double f = (a.lo - (t - w)) + (b.lo - w);
+  Q r = renorm(s, e + t);
+  return renorm(r.hi, r.lo + f);
+}
+static Q times(Q a, Q b) {
+  const double p = a.hi * b.hi;
+  return renorm(p, std::fma(a.hi, b.hi, -p) + a.hi * b.lo + a.lo * b.hi);
+}
+static Q inverse(double x) {
+  const double q = 1.0 / x;
+  return renorm(q, std::fma(-q, x, 1.0) / x);
+}
+}  // namespace qd
+
+static double v_series(const ep_series& s, double x) {
+  if (x <= s.r_core) return s.f_core;
+  if (x <= s.r0) return std::fabs(s.aa * std::pow(x, 2) + s.bb * x + s.cc);
+  if (!s.quad) {  // Real*8 Pg, Sto, xq (V_LJ_OT, :1021-1036)
+    const double xq = 1.0 / x;
+    double Sto = 0.0;
+    for (int k = 1; k <= s.n; ++k) Sto = Sto + s.c_hi[k - 1] * std::pow(xq, k + s.k0);
+    return Sto;
+  }
+  const qd::Q xq = qd::inverse(x);
+  qd::Q Aux{1.0, 0.0};
+  for (int i = 0; i < s.k0 + 1; ++i) Aux = qd::times(Aux, xq);
+  qd::Q Sto{0.0, 0.0};
+  for (int k = 1; k <= s.n; ++k) {
+    Sto = qd::plus(Sto, qd::times(qd::Q{s.c_hi[k - 1], s.c_lo[k - 1]}, Aux));
+    Aux = qd::times(Aux, xq);
+  }
+  return Sto.hi + Sto.lo;
+}
+
 static double select_pot(const ep_potential& p, double r) {
   if (p.kind == EP_POT_NULL) return 0.0;
   if (r < p.r_cutoff) return p.umax;
@@ -374,8 +499,26 @@ static double select_pot(const ep_potential& p, double r) {
     return De * (e * e - 2.0 * e);
   }
   if (p.kind == EP_POT_KOUTSELOS) return v_koutselos((int)p.par[0], r);
+  if (p.kind == EP_POT_PATIL) return v_alka((int)p.par[0], r);
+  if (p.kind == EP_POT_AZIZ) return v_aziz_he(r);
+  if (p.kind == EP_POT_TANG_TOENNIES) return v_tang_toennies((int)p.par[0], r);
+  if (p.kind == EP_POT_SERIES && p.series) return v_series(*p.series, r);
   return 0.0;
 }
+
+// The potential and its fit, kept beyond the call that passed them.
+struct KeptPot {
+  ep_potential p{};
+  ep_series s{};
+  void keep(const ep_potential& q) {
+    p = q;
+    p.series = nullptr;
+    if (q.kind == EP_POT_SERIES && q.series) {
+      s = *q.series;
+      p.series = &s;
+    }
+  }
+};
 
 // potenimp.f90:588-632 (update): parabolic interpolation in f(0:nint+1).
 static double update_interp(double r, int nint, double rmax, const double* f) {
@@ -431,7 +574,7 @@ struct oc_ctx {
   double delinter = 0, umax_sigma = 9.674836e3, umax_pi = 0.0;
   std::vector<double> potpi, potdel;  // D state: potpi = potpidel, potdel = V_Delta
   std::vector<double> potsigdel;      // D state only
-  ep_potential pot_plus;
+  KeptPot plus;
   bool have_tables = false;
   double last_mu = 0, last_norm = 0;
   std::string err;
@@ -494,6 +637,14 @@ static void deriv(const oc_ctx* c, int id, int axis, const T* f, T* df) {
 }
 
 extern "C" {
+
+int oc_potential_values(const ep_potential* p, const double* r, double* v, int n) {
+  if (!p || n < 0 || (n > 0 && (!r || !v))) return EP_ERR_INVALID_ARG;
+  if (p->kind == EP_POT_SERIES && (!p->series || p->series->n < 1 || p->series->n > EP_SERIES_MAX))
+    return EP_ERR_INVALID_ARG;
+  for (int i = 0; i < n; ++i) v[i] = select_pot(*p, r[i]);
+  return EP_OK;
+}
 
 int oc_set_threads(int n) {
 #ifdef _OPENMP
@@ -631,7 +782,7 @@ int oc_create(const ep_config* cfg, oc_ctx** out) {
     for (int j = 0; j < 3; ++j) c->invarold[i][j] = cd(0);
     for (int j = 0; j < 2; ++j) c->hinvarold[i][j] = cd(0);
   }
-  c->pot_plus.kind = EP_POT_NULL;
+  c->plus.p.kind = EP_POT_NULL;
   *out = c;
   return EP_OK;
 }
@@ -675,7 +826,7 @@ int oc_set_impurity_potentials(oc_ctx* c, const ep_potential* pi, const ep_poten
   }
   td[0] = td[1]; td[npot + 1] = td[npot];
   tp[0] = tp[1]; tp[npot + 1] = tp[npot];
-  if (plus) c->pot_plus = *plus;
+  if (plus) c->plus.keep(*plus);
   return oc_set_impurity_tables(c, tp.data(), td.data(), npot, del, sigma->umax);
 }
 
@@ -712,7 +863,7 @@ int oc_set_impurity_potentials_d(oc_ctx* c, const ep_potential* pi, const ep_pot
   td[0] = td[1]; td[npot + 1] = td[npot];
   tpd[0] = tpd[1]; tpd[npot + 1] = tpd[npot];
   tsd[0] = tsd[1]; tsd[npot + 1] = tsd[npot];
-  if (plus) c->pot_plus = *plus;
+  if (plus) c->plus.keep(*plus);
   return oc_set_impurity_tables_d(c, td.data(), tpd.data(), tsd.data(), npot, del, pi->umax, sigma->umax);
 }
 
@@ -1100,7 +1251,7 @@ int oc_energy(oc_ctx* c, ep_energies* e) {
     eHeX = par_sum(N, [&](size_t p) { return rof(p) >= g.z_exciplex_exclusion ? c->den[p] * c->uimp[p] : 0.0; }) * c->dxyz;
     uplus = par_sum(N, [&](size_t p) {
       const double r = rof(p);
-      return r >= g.z_exciplex_exclusion ? c->den[p] * select_pot(c->pot_plus, r) : 0.0;
+      return r >= g.z_exciplex_exclusion ? c->den[p] * select_pot(c->plus.p, r) : 0.0;
     }) * c->dxyz;
   }
   const cd* iv = c->invar;

@@ -24,6 +24,7 @@ int oc_create(const ep_config* cfg, oc_ctx** out);
 int oc_destroy(oc_ctx* c);
 const char* oc_last_error(const oc_ctx* c);
 int oc_set_threads(int n);
+int oc_potential_values(const ep_potential* p, const double* r, double* v, int n);
 
 int oc_set_impurity_potentials(oc_ctx* c, const ep_potential* pi,
                                const ep_potential* sigma,

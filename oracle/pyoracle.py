@@ -83,6 +83,17 @@ def fd_weights(npd, order):
     return w
 
 
+def potential_values(pot, r):
+    """The oracle's Select_Pot restatement at the radii r (oc_potential_values)."""
+    _, f = load()
+    r = np.ascontiguousarray(r, dtype=np.float64)
+    v = np.empty_like(r)
+    st = f["potential_values"](C.byref(pot), _abi.dptr(r), _abi.dptr(v), r.size)
+    if st != 0:
+        raise EffPotError(st, "oc_potential_values")
+    return v
+
+
 def sinint(x):
     return load()[0].oc_sinint(float(x))
 

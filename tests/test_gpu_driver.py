@@ -353,6 +353,38 @@ def test_scan_settings_of_prep_sh_give_the_api_uplus(tmp_path):
     assert abs(e["uplus"]) > 1.0
 
 
+def test_named_potentials_through_the_namelist(tmp_path):
+    """selec_pi='Xe_He', selec_sigma='RB' (closed forms built into the
+    library) and selec_plus='Test_fit', an inverse-power fit read from the
+    file named by potentials_source: the driver's eHeX and U+ equal the ABI's
+    with the same potentials built through the Python API."""
+    from test_select_pot import SYNTHETIC, synthetic_fit
+    psi = ep.woods_saxon_psi(N, N, N, XMAX, XMAX, XMAX, N4, seed=12)
+    den = np.abs(psi) ** 2
+    rimp = (0.4, -0.3, 0.6)
+    write_density(tmp_path / "in.dat", den, rimp)
+    (tmp_path / "invar.dat").write_text("\n".join(["(0.d0,0.d0)"] * 10) + "\n")
+    text = namelist(0, f", instate=5, potentials_source='{SYNTHETIC}'").replace(
+        "selec_pi='Morse', selec_sigma='Morse', selec_plus='null', umax_pi=1000.d0, umax_sigma=1000.d0,\n"
+        " r_cutoff_pi=0.d0, r_cutoff_sigma=0.d0,",
+        "selec_pi='Xe_He', selec_sigma='RB', selec_plus='Test_fit', umax_pi=2.1450E+04, umax_sigma=5.d3,\n"
+        " r_cutoff_pi=2.d0, r_cutoff_sigma=2.5d0, r_cutoff_plus=0.d0, umax_plus=0.d0,")
+    out = run_driver(tmp_path, text)
+    m = re.search(r"Interaction energy \(X\+-He\) \.*: +(-?\d+\.\d+) K", out)
+    assert m, out
+    got = balance(out)
+    s = solver(rimp, np.zeros(10, dtype=np.complex128))
+    with s:
+        s.set_impurity_potentials(ep.tang_toennies("Xe", r_cutoff=2.0, umax=2.1450e4),
+                                  ep.patil("RB", r_cutoff=2.5, umax=5.0e3), synthetic_fit()[0])
+        s.upload_psi(np.sqrt(den).astype(np.complex128))
+        s.potenimp()
+        s.poten()
+        e = s.energy()
+    assert abs(float(m.group(1)) - e["uplus"]) < 2e-6 and abs(e["uplus"]) > 1e-3
+    assert abs(float(got["eHeX"]) - e["eHeX"]) < 2e-6 and abs(e["eHeX"]) > 1e-3
+
+
 def test_ldiag_jz_namelist_selects_the_jz_state(tmp_path):
     """Ldiag_jz=.true., Ljz='+3/2' in an isotropic field (V_Sigma = V_Pi):
     the internal variables the driver writes (printoutc, frozen by
