@@ -694,6 +694,7 @@ ep_ctx* ep_batch_ctx(ep_batch* b, int i) {
 int ep_batch_run(ep_batch* b, int nsteps, double dt, ep_run_stats* stats) {
   if (!b || nsteps < 0) return EP_ERR_INVALID_ARG;
   cudaSetDevice(b->device);
+  batch_join(b);  // work the caller left on the instance streams comes first
   int s0 = 0;
   const int ng = nsteps - (stats ? 1 : 0);
   bool eligible = b->use_graphs && ng >= 2;
@@ -741,10 +742,23 @@ int ep_batch_run(ep_batch* b, int nsteps, double dt, ep_run_stats* stats) {
   return EP_OK;
 }
 
+// The instances' Runge-Kutta steps are enqueued on their streams first and
+// checked afterwards, so that they overlap on the GPU; an instance with a
+// moving impurity reads its force every stage and runs on its own.
 int ep_batch_steprk(ep_batch* b, double dt) {
   if (!b) return EP_ERR_INVALID_ARG;
-  for (ep_ctx* c : b->ctx) {
-    int r = ep_steprk(c, dt);
+  cudaSetDevice(b->device);
+  std::vector<char> queued(b->ctx.size(), 0);
+  for (size_t i = 0; i < b->ctx.size(); ++i) {
+    ep_ctx* c = b->ctx[i];
+    const bool mov = c->cfg.impurity == EP_IMPURITY_MOVING;
+    int r = dispatch(c, [&](auto& e) -> int { return e.steprk(dt, mov); });
+    if (r) return r;
+    queued[i] = !mov;
+  }
+  for (size_t i = 0; i < b->ctx.size(); ++i) {
+    if (!queued[i]) continue;
+    int r = dispatch(b->ctx[i], [&](auto& e) -> int { return e.check_flags(); });
     if (r) return r;
   }
   return EP_OK;

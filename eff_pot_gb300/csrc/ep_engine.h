@@ -132,7 +132,10 @@ class Engine {
   int energy(ep_energies* out);
   int forceimp(double* F);
   int potinvar(std::complex<double>* H);
-  int steprk(double dt);
+  // wait = false: return once the step is enqueued (no stream synchronise,
+  // no flag check -- the caller runs check_flags() later); only for an
+  // impurity that does not move (a moving one reads its force each stage)
+  int steprk(double dt, bool wait = true);
   int steppc(double dt, ep_step_errors* err);
   int renormalize(double* norm_before, bool wait);
   int upload_psi(const double* h);

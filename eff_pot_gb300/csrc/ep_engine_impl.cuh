@@ -932,7 +932,7 @@ int Engine<T>::rk_stage(int jr, double dt) {
 
 // steprk (steprk.f90:1-191).
 template <class T>
-int Engine<T>::steprk(double dt) {
+int Engine<T>::steprk(double dt, bool wait) {
   if (!have_field) { *err = "poten() must run before steprk()"; return EP_ERR_STATE; }
   {
     int r0 = ensure_materialized();
@@ -980,6 +980,7 @@ int Engine<T>::steprk(double dt) {
   }
   for (int i = 0; i < 3; ++i) { ioldp[i] = i; imp->ioldr[i] = i; imp->ioldv[i] = i; imp->ioldiv[i] = i; }
   for (int i = 0; i < 2; ++i) { ioldh[i] = i; imp->iolda[i] = i; imp->ioldhiv[i] = i; }
+  if (!wait && !mov) return EP_OK;
   if ((r = cuda_ok(cudaStreamSynchronize(st), "steprk"))) return r;
   return check_flags();
 }
