@@ -146,6 +146,64 @@ EP_PP_HD double ep_tang_toennies(int atom, double r) {
   return v * to_k;
 }
 
+// He-Ag (V_Ag_gs / V_Ag_Pi / V_Ag_Sig, V_impur.f90:1038-1096): an HFD form
+// A e^(-alpha r - beta r^2) - F(r) (C6/r^6 + C8/r^8 + C10/r^10 + C12/r^12),
+// F = e^(-(D/r - 1)^2) for r <= D, 1 beyond; r in A, V in K.  The constants
+// the reference writes without an exponent letter are default REAL there
+// and enter as binary32 values (the float literals below).
+EP_PP_HD double ep_ag(int which, double r) {
+  double A, al, be, D, C6, C8, C10, C12;
+  if (which <= 0) {
+    A = (double)78741.3877f; al = (double)0.65299f; be = (double)0.36367f; D = (double)12.093f;
+    C6 = 137042.07; C8 = 189386.217; C10 = 111358462.0; C12 = 1.17670377e10;
+  } else if (which == 1) {
+    A = 0.7095092e6; al = (double)1.9928f; be = (double)0.45500f; D = (double)4.0562f;
+    C6 = 0.21661134e6; C8 = (double)123454.7952f; C10 = 0.307155024e6; C12 = 0.740464032e-10;
+  } else {
+    A = (double)40005.2f; al = (double)0.41529f; be = (double)0.14888f; D = (double)25.730f;
+    C6 = 1.97443e-9; C8 = 3.37393e-6; C10 = (double)0.00788363f; C12 = 7.52624e12;
+  }
+  if (r == 0.0) return A;
+  double ff = 1.0;
+  if (r <= D) {
+    const double q = D / r - 1.0;
+    ff = exp(-(q * q));
+  }
+  const double r2 = r * r, r6 = r2 * r2 * r2, r8 = r6 * r2, r10 = r8 * r2, r12 = r10 * r2;
+  return A * exp(-al * r - be * r2) - ff * (C6 / r6 + C8 / r8 + C10 / r10 + C12 / r12);
+}
+
+// He-Ba of Lovallo's fit (V_Ba_gs, V_impur.f90:1197-1210): 1297.1 K up to
+// 3.7 A, beyond it even inverse powers 6 .. 18, summed from the highest.
+EP_PP_HD double ep_ba_gs(double x) {
+  if (x <= 3.7) return 1297.1;
+  const double x2 = x * x, x6 = x2 * x2 * x2, x8 = x6 * x2, x10 = x8 * x2, x12 = x10 * x2, x14 = x12 * x2,
+               x16 = x14 * x2, x18 = x16 * x2;
+  return -6.146426949008034e14 / x18 + 1.6797251118695925e14 / x16 - 1.6513058293510484e13 / x14 +
+         7.015334514979032e11 / x12 - 1.1066880774828484e10 / x10 + 4.900282758445466e7 / x8 -
+         450294.6878721156 / x6;
+}
+
+// He-CH3I, Legendre component l of the m = 0 ground-state potential
+// (V_CH3I_l and radpot, V_impur.f90:3079-3243): a Morse function d (1 -
+// e^(-b (x - c)))^2 - d in hartree of x in bohr, and its own cutoff (umax_l
+// for r <= 3.6 A).  The Morse parameters and two cutoff radii are default
+// REAL literals in the reference (binary32 values).
+EP_PP_HD double ep_ch3i(int l, double r) {
+  const float dd[5] = {0.000185445f, -4.51657e-05f, 2.53688e-05f, -6.51825e-06f, 1.5032e-06f};
+  const float bb[5] = {0.782913f, 0.837569f, 0.849398f, 0.779254f, 0.787553f};
+  const float cc[5] = {9.5243f, 10.3772f, 10.6988f, 11.454f, 12.236f};
+  const double umax[5] = {3.1648655845e3, -5.1115736616e3, 5.5581502684e3, -2.7398540818e3, 2.4025334047e3};
+  const double rcut[5] = {3.6, (double)3.6f, 3.6, 3.6, (double)3.6f};
+  const int k = l < 0 ? 0 : (l > 4 ? 4 : l);
+  if (r <= rcut[k]) return umax[k];
+  const double a_bohr = 0.529177, hartree = 27.2114, ev_k = 11604.448;
+  const double x = r / a_bohr;
+  const double d = (double)dd[k], b = (double)bb[k], c = (double)cc[k];
+  const double e = 1.0 - exp(-b * (x - c));
+  return (d * (e * e) - d) * hartree * ev_k;
+}
+
 // Double-double arithmetic (Knuth's two-sum, the fused-multiply-add product
 // error, and the normalisations of Dekker's and Bailey's double-double
 // algorithms): 106-bit sums for the Real*16 fits.
@@ -223,5 +281,8 @@ EP_PP_HD double ep_pair_potential(int kind, double r_cutoff, double umax, const 
   if (kind == EP_POT_AZIZ) return ep_aziz_he(r);
   if (kind == EP_POT_TANG_TOENNIES) return ep_tang_toennies((int)par[0], r);
   if (kind == EP_POT_SERIES && s) return ep_series_value(s, r);
+  if (kind == EP_POT_AG) return ep_ag((int)par[0], r);
+  if (kind == EP_POT_BA_GS) return ep_ba_gs(r);
+  if (kind == EP_POT_CH3I) return ep_ch3i((int)par[0], r);
   return 0.0;
 }

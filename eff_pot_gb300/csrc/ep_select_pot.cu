@@ -288,6 +288,22 @@ int builtin(const std::string& sel, ep_potential* p) {
     p->par[0] = sel == "Ar_He" ? 0 : 1;
     return 1;
   }
+  static const char* ag[3] = {"Ag_gs", "Ag_Pi", "Ag_Sig"};
+  for (int i = 0; i < 3; ++i)
+    if (sel == ag[i]) {
+      p->kind = EP_POT_AG;
+      p->par[0] = i;
+      return 1;
+    }
+  if (sel == "Ba_gs") {
+    p->kind = EP_POT_BA_GS;
+    return 1;
+  }
+  if (sel.size() == 6 && sel.compare(0, 5, "CH3I_") == 0 && sel[5] >= '0' && sel[5] <= '4') {
+    p->kind = EP_POT_CH3I;
+    p->par[0] = sel[5] - '0';
+    return 1;
+  }
   return 0;
 }
 

@@ -93,7 +93,11 @@ typedef struct ep_config {
  * EP_POT_TANG_TOENNIES: 'Ar_He', 'Xe_He' (V_impur.f90:2681-2782),
  *   par[0] = 0 Ar, 1 Xe.
  * EP_POT_SERIES: the inverse-power fits of V_impur.f90 ('Rb_gs_Fausto',
- *   'Ba_plus_gs', 'He2S_fci', 'LJ_OT', ...): the fit in *series. */
+ *   'Ba_plus_gs', 'He2S_fci', 'LJ_OT', ...): the fit in *series.
+ * EP_POT_AG: 'Ag_gs', 'Ag_Pi', 'Ag_Sig' (V_impur.f90:1038-1096),
+ *   par[0] = 0, 1, 2.
+ * EP_POT_BA_GS: 'Ba_gs' (V_impur.f90:1197-1210).
+ * EP_POT_CH3I: 'CH3I_0' .. 'CH3I_4' (V_impur.f90:3079-3243), par[0] = l. */
 enum {
   EP_POT_NULL = 0,
   EP_POT_MORSE = 1,
@@ -101,7 +105,10 @@ enum {
   EP_POT_PATIL = 3,
   EP_POT_AZIZ = 4,
   EP_POT_TANG_TOENNIES = 5,
-  EP_POT_SERIES = 6
+  EP_POT_SERIES = 6,
+  EP_POT_AG = 7,
+  EP_POT_BA_GS = 8,
+  EP_POT_CH3I = 9
 };
 
 #define EP_SERIES_MAX 24
@@ -135,7 +142,8 @@ int ep_potential_values(const ep_potential* p, const double* r, double* v,
 
 /* Select_Pot by name (V_impur.f90:87-932): selec as the namelist gives it,
  * with its r_cutoff and umax.  The closed forms are built in ('null',
- * '*_plus_Koutselos', 'LI' .. 'CS', 'Aziz_He', 'Ar_He', 'Xe_He'); the
+ * '*_plus_Koutselos', 'LI' .. 'CS', 'Aziz_He', 'Ar_He', 'Xe_He', 'Ag_gs',
+ * 'Ag_Pi', 'Ag_Sig', 'Ba_gs', 'CH3I_0' .. 'CH3I_4'); the
  * inverse-power fits are read from the reference's V_impur.f90 at
  * source_path (NULL: closed forms only): its Select_Pot chain names the
  * function, whose COMMON block names the BLOCK DATA with the coefficients.

@@ -440,6 +440,46 @@ static double v_tang_toennies(int atom, double r) {
   return Aux * Hartree_to_K;
 }
 
+// V_Ag_gs / V_Ag_Pi / V_Ag_Sig (V_impur.f90:1038-1096); the literals the
+// reference writes without exponent letter are default REAL (binary32).
+static double v_ag(int which, double r) {
+  struct Ag { double A, alpha, beta, D, C6, C8, C10, C12; };
+  static const Ag t[3] = {
+      {78741.3877f, 0.65299f, 0.36367f, 12.093f, 137042.07, 189386.217, 111358462.0, 1.17670377e10},      // :1040-1047
+      {0.7095092e6, 1.9928f, 0.45500f, 4.0562f, 0.21661134e6, 123454.7952f, 0.307155024e6, 0.740464032e-10},  // :1060-1067
+      {40005.2f, 0.41529f, 0.14888f, 25.730f, 1.97443e-9, 3.37393e-6, 0.00788363f, 7.52624e12}};          // :1080-1087
+  const Ag& p = t[std::min(std::max(which, 0), 2)];
+  double ff = 1.0;
+  if (r <= p.D) ff = std::exp(-std::pow(p.D / r - 1.0, 2));
+  if (r == 0.0) return p.A;
+  return p.A * std::exp(-p.alpha * r - p.beta * std::pow(r, 2)) -
+         ff * (p.C6 / std::pow(r, 6) + p.C8 / std::pow(r, 8) + p.C10 / std::pow(r, 10) + p.C12 / std::pow(r, 12));
+}
+
+// V_Ba_gs (V_impur.f90:1197-1210).
+static double v_ba_gs(double x) {
+  if (x <= 3.7) return 1297.1;
+  return -6.146426949008034e14 / std::pow(x, 18) + 1.6797251118695925e14 / std::pow(x, 16) -
+         1.6513058293510484e13 / std::pow(x, 14) + 7.015334514979032e11 / std::pow(x, 12) -
+         1.1066880774828484e10 / std::pow(x, 10) + 4.900282758445466e7 / std::pow(x, 8) -
+         450294.6878721156 / std::pow(x, 6);
+}
+
+// V_CH3I_l with radpot(l, r) (V_impur.f90:3079-3243).
+static double v_ch3i(int l, double r) {
+  static const double r_cutoff[5] = {3.6, 3.6f, 3.6, 3.6, 3.6f};
+  static const double umax[5] = {3.1648655845e3, -5.1115736616e3, 5.5581502684e3, -2.7398540818e3, 2.4025334047e3};
+  static const double d[5] = {0.000185445f, -4.51657e-05f, 2.53688e-05f, -6.51825e-06f, 1.5032e-06f};
+  static const double b[5] = {0.782913f, 0.837569f, 0.849398f, 0.779254f, 0.787553f};
+  static const double c[5] = {9.5243f, 10.3772f, 10.6988f, 11.454f, 12.236f};
+  const int k = std::min(std::max(l, 0), 4);
+  const double a_bohr = 0.529177, Hartree = 27.2114, eV_K = 11604.448;
+  if (r <= r_cutoff[k]) return umax[k];
+  const double r_au = r / a_bohr;
+  const double radpot = d[k] * std::pow(1.0 - std::exp(-b[k] * (r_au - c[k])), 2) - d[k];
+  return radpot * Hartree * eV_K;
+}
+
 // The inverse-power fits with a parabolic core (e.g. V_Fausto_Rb_gs,
 // V_impur.f90:2206-2250: Sto = sum_k Pg(k) Aux, Aux = xq**(k0+1) times xq
 // per term, xq = 1/x, all in Real*16).  The Real*16 arithmetic is restated
@@ -503,6 +543,9 @@ static double select_pot(const ep_potential& p, double r) {
   if (p.kind == EP_POT_AZIZ) return v_aziz_he(r);
   if (p.kind == EP_POT_TANG_TOENNIES) return v_tang_toennies((int)p.par[0], r);
   if (p.kind == EP_POT_SERIES && p.series) return v_series(*p.series, r);
+  if (p.kind == EP_POT_AG) return v_ag((int)p.par[0], r);
+  if (p.kind == EP_POT_BA_GS) return v_ba_gs(r);
+  if (p.kind == EP_POT_CH3I) return v_ch3i((int)p.par[0], r);
   return 0.0;
 }
 

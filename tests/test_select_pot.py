@@ -41,6 +41,12 @@ def lib():
 def closed_forms():
     out = [(f"patil-{a}", ep.patil(a)) for a in ep.config.PATIL_ATOMS]
     out += [("aziz", ep.aziz_he()), ("tt-Ar", ep.tang_toennies("Ar")), ("tt-Xe", ep.tang_toennies("Xe"))]
+    for name, kind, par in [("Ag_gs", _abi.EP_POT_AG, 0), ("Ag_Pi", _abi.EP_POT_AG, 1),
+                            ("Ag_Sig", _abi.EP_POT_AG, 2), ("Ba_gs", _abi.EP_POT_BA_GS, 0)] + \
+            [(f"CH3I_{l}", _abi.EP_POT_CH3I, l) for l in range(5)]:
+        p = _abi.EpPotential()
+        p.kind, p.par[0] = kind, float(par)
+        out.append((name, p))
     return out
 
 
@@ -92,6 +98,104 @@ def test_tang_toennies_tail(lib, atom, consts):
     x = r / 0.5292
     want = -sum(C[i] / x ** (2 * i + 6) for i in range(7)) * 27.21 * 11604.0
     assert np.allclose(ep.potential_values(ep.tang_toennies(atom), r), want, rtol=1e-12, atol=0)
+
+
+# ------------------------------------------- closed forms vs the reference source
+def _function_body(text, name):
+    m = re.search(r"(?is)function\s+" + name + r"\s*\((.*?)\n\s*end(?:\s*function)?\b", text)
+    assert m, name
+    return m.group(1)
+
+
+def _decl(body):
+    """name -> value of the `name = literal` initialisations and assignments
+    of a function body, each literal with its Fortran kind."""
+    out = {}
+    for name, lit in re.findall(r"(?i)\b(\w+)\s*=\s*([-+]?(?:\d+\.?\d*|\.\d+)(?:[edq][-+]?\d+)?)(?![\w.])", body):
+        out.setdefault(name.lower(), float(literal(lit)[0]))
+    return out
+
+
+@pytest.fixture(scope="module")
+def source_text():
+    if not os.path.exists(SOURCE):
+        pytest.skip("the reference's V_impur.f90 is not present here")
+    with open(SOURCE, encoding="latin-1") as f:
+        return re.sub(r"![^\n]*", "", f.read())
+
+
+def test_ag_ba_ch3i_constants_and_forms_match_the_reference_source(lib, source_text):
+    """The He-Ag HFD forms, Lovallo's He-Ba and the He-CH3I Morse components
+    restated here in numpy with the constants read from V_impur.f90 (each
+    literal with its kind) equal the library's evaluator."""
+    r = np.linspace(0.5, 30.0, 600)
+    for i, (fn, suf) in enumerate((("V_Ag_gs", "gs"), ("V_Ag_Pi", "pi"), ("V_Ag_Sig", "si"))):
+        k = _decl(_function_body(source_text, fn))
+        A, al, be, D = (k[n + suf] for n in ("a", "alpha", "beta", "d"))
+        C = [k[f"c{j}{suf}"] for j in (6, 8, 10, 12)]
+        ff = np.where(r <= D, np.exp(-(D / r - 1.0) ** 2), 1.0)
+        want = A * np.exp(-al * r - be * r ** 2) - ff * sum(c / r ** p for c, p in zip(C, (6, 8, 10, 12)))
+        got = ep.potential_values(ep.select_pot(fn[2:]), r)
+        assert np.allclose(got, want, rtol=1e-13, atol=1e-13 * np.max(np.abs(want))), fn
+    body = _function_body(source_text, "V_Ba_gs")
+    terms = re.findall(r"([-+]?\s*\d+\.\d*d\d+)\s*/\s*x\*\*(\d+)", body.replace("&\n", " "))
+    assert len(terms) == 7
+    x = r[r > 3.7]
+    want = sum(float(literal(c.replace(" ", ""))[0]) / x ** int(p) for c, p in terms)
+    got = ep.potential_values(ep.select_pot("Ba_gs"), x)
+    assert np.allclose(got, want, rtol=1e-12, atol=1e-12 * np.max(np.abs(want)))
+    assert np.all(ep.potential_values(ep.select_pot("Ba_gs"), r[r <= 3.7]) == 1297.1)
+    rad = _function_body(source_text, "radpot")
+    cases = re.split(r"(?i)case\s*\(", rad)[2:7]
+    for l in range(5):
+        k = _decl(cases[l])
+        kf = _decl(_function_body(source_text, f"V_CH3I_{l}"))
+        xa = r / kf["a_bohr"]
+        want = (k["d"] * (1.0 - np.exp(-k["b"] * (xa - k["c"]))) ** 2 - k["d"]) * kf["hartree"] * kf["ev_k"]
+        want = np.where(r <= kf["r_cutoff"], kf["umax"], want)
+        got = ep.potential_values(ep.select_pot(f"CH3I_{l}"), r)
+        assert np.allclose(got, want, rtol=1e-13, atol=1e-15), l
+
+
+def test_patil_aziz_tang_toennies_constants_match_the_reference_source(lib, source_text):
+    """The constants of V_alka, V_Aziz_He, V_Ar_He and V_Xe_He as read from
+    the source give the library's values through numpy restatements."""
+    r = np.linspace(1.0, 30.0, 400)
+    k = _decl(_function_body(source_text, "V_Aziz_He"))
+    x = r / k["rm"]
+    ff = np.where(x <= k["d"], np.exp(-(k["d"] / x - 1.0) ** 2), 1.0)
+    want = (k["a"] * np.exp(-k["alpha"] * x + k["beta"] * x ** 2) -
+            ff * (k["c6"] / x ** 6 + k["c8"] / x ** 8 + k["c10"] / x ** 10)) * k["eps"]
+    assert np.allclose(ep.potential_values(ep.aziz_he(), r), want, rtol=1e-13, atol=1e-12)
+    for atom, fn in (("Ar", "V_Ar_He"), ("Xe", "V_Xe_He")):
+        k = _decl(_function_body(source_text, fn))
+        B = [k["bb"]]
+        for i in range(2, 19):
+            B.append(B[-1] * k["bb"] / i)
+        C = [k["c6"], k["c8"], k["c10"]]
+        for i in range(3, 7):
+            C.append((C[i - 1] / C[i - 2]) ** 3 * C[i - 3])
+        rr = r / k["rbohr"]
+        e = np.exp(-k["bb"] * rr)
+        S = np.cumsum([B[i] * rr ** (i + 1) for i in range(18)], axis=0)
+        v = k["aa"] * e + sum(((S[2 * i + 5] + 1.0) * e - 1.0) * C[i] / rr ** (2 * i + 6) for i in range(7))
+        assert np.allclose(ep.potential_values(ep.tang_toennies(atom), r), v * 27.21 * 11604.0, rtol=1e-11,
+                           atol=1e-9), atom
+    body = _function_body(source_text, "V_alka")
+    data = {n.lower(): [float(literal(v)[0]) for v in vals.split(",")]
+            for n, vals in re.findall(r"(?i)data\s+(\w+)\s*/([^/]*)/", body) if n.lower() != "celem"}
+    d = r / 0.529177249
+    for i, atom in enumerate(("LI", "NA", "K", "RB", "CS")):
+        a, b, c6, c8 = data["av"][i], data["bv"][i], data["c6v"][i], data["c8v"][i]
+        r2, r4, r6, ag = data["r2v"][i], data["r4v"][i], data["r6v"][i], data["agranv"][i]
+        abar, u = (a + b) / 4.0, a - 1.0
+        v = -0.5 * a ** 2 * u
+        roa = ag * d ** (2.0 * u) * (1.0 + v / d) ** 2 * np.exp(-2.0 * d / a)
+        f = [1.0 - np.exp(-d / abar) * sum((d / abar) ** n / math.factorial(n) for n in range(2 * l + 8))
+             for l in (1, 2)]
+        want = (4.0 * math.pi / 3.0 * roa * (r2 + 37.0 / 90.0 * r4 / a ** 2 + 28.0 / 525.0 * r6 / a ** 4) -
+                c6 * f[0] / d ** 6 - c8 * f[1] / d ** 8) * 11604.448 * 27.211608
+        assert np.allclose(ep.potential_values(ep.patil(atom), r), want, rtol=1e-12, atol=1e-9), atom
 
 
 # --------------------------------------------------------------- series fits
@@ -317,7 +421,7 @@ def test_select_pot_errors(lib):
         ep.select_pot("Rb_gs_Fausto", 0.0, 0.0, None)  # a fit needs its source
     if os.path.exists(SOURCE):
         with pytest.raises(ep.EffPotError, match="inverse-power"):
-            ep.select_pot("Ag_gs", 0.0, 0.0, SOURCE)
+            ep.select_pot("Cs_7s", 0.0, 0.0, SOURCE)
     p = ep.select_pot("Xe_He", 2.0, 21450.4867067095, None)
     assert p.kind == _abi.EP_POT_TANG_TOENNIES and p.r_cutoff == 2.0
     assert ep.potential_values(p, np.array([1.0]))[0] == 21450.4867067095
@@ -341,7 +445,9 @@ def test_gpu_uplus_of_the_new_forms_matches_oracle(oracle):
     build()
     cfg, psi = _case()
     pluses = {"patil": ep.patil("RB", r_cutoff=2.0, umax=5000.0), "aziz": ep.aziz_he(r_cutoff=1.5, umax=2000.0),
-              "tt": ep.tang_toennies("Xe", r_cutoff=2.0, umax=21450.4867067095), "series": _fit()}
+              "tt": ep.tang_toennies("Xe", r_cutoff=2.0, umax=21450.4867067095), "series": _fit(),
+              "ag": ep.select_pot("Ag_Pi", 1.0, 3000.0), "ba": ep.select_pot("Ba_gs"),
+              "ch3i": ep.select_pot("CH3I_2")}
     for name, plus in pluses.items():
         res = []
         for S in (ep.Solver, oracle.OracleSolver):
