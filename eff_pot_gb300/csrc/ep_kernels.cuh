@@ -1093,8 +1093,10 @@ EP_DEV void lap_march_async(const Geo& g, const C2<T>* __restrict__ psi, const F
     if (zz < 0 || zz >= g.nz) zz = per ? wrapi(zz, g.nz) : -1;
     const CT* pz = psi + sxy * (zz < 0 ? 0 : zz);
     if (CHUNKED && vec) {
-      for (int e = tid; e < nunits; e += NT) {
-        const int r = e / uperrow, c = (e - r * uperrow) * CH;
+      // chunks per row as a compile-time divisor (a multiply and a shift)
+      constexpr int UPR = W / CH, NU = UPR * H;
+      for (int e = tid; e < NU; e += NT) {
+        const int r = e / UPR, c = (e - r * UPR) * CH;
         CT* dst = P + r * W + c;
         const int o = zz < 0 ? -1 : soff[e];
         if (o >= 0) {
