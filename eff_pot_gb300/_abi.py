@@ -20,7 +20,7 @@ EP_ICON_PERIODIC, EP_ICON_ZERO_OUTSIDE = 8, 13
 EP_STATE_P, EP_STATE_D = 0, 1
 EP_POT_NULL, EP_POT_MORSE, EP_POT_KOUTSELOS = 0, 1, 2
 EP_POT_PATIL, EP_POT_AZIZ, EP_POT_TANG_TOENNIES, EP_POT_SERIES = 3, 4, 5, 6
-EP_POT_AG, EP_POT_BA_GS, EP_POT_CH3I = 7, 8, 9
+EP_POT_AG, EP_POT_BA_GS, EP_POT_CH3I, EP_POT_SURFACE = 7, 8, 9, 10
 EP_SERIES_MAX = 24
 
 FIELDS = {

@@ -32,9 +32,9 @@
 // from the file named by the key potentials_source), 'Morse', or 'table'
 // from a file of (r, V) rows.  Not built here: the Laverage_P_value /
 // Lmixture / exciplex variants of instates.f90 (they sum eigenvectors, so
-// they depend on EISPACK's phase convention), and the Select_Pot forms that
-// are neither built in nor inverse-power fits (Cs_7s, Ba_plus_old_gs, the
-// surface potentials); they run as 'table'.
+// they depend on EISPACK's phase convention), and the two Select_Pot forms
+// that are neither built in nor inverse-power fits (Cs_7s, Ba_plus_old_gs);
+// they run as 'table'.
 #include <cmath>
 #include <complex>
 #include <cstdio>
@@ -119,7 +119,8 @@ ep_potential potential_of(const Input& in, const char* which, const char* dflt_s
                       (int)sizeof err) != EP_OK)
       stop("selec_" + std::string(which) + "='" + sel + "': " + err +
            " (built in: 'null', 'Morse', '{Na,K,Rb,Cs}_plus_Koutselos', 'LI', 'NA', 'K', 'RB', 'CS', "
-           "'Aziz_He', 'Ar_He', 'Xe_He', 'Ag_gs', 'Ag_Pi', 'Ag_Sig', 'Ba_gs', 'CH3I_0'..'CH3I_4'; "
+           "'Aziz_He', 'Ar_He', 'Xe_He', 'Ag_gs', 'Ag_Pi', 'Ag_Sig', 'Ba_gs', 'CH3I_0'..'CH3I_4', "
+           "the graphene/TiO2/Au surface names; "
            "the inverse-power fits of V_impur.f90 with potentials_source = "
            "its path; any potential as 'table' with table_" + std::string(which) +
            " = a file of r (A), V (K) rows)");

@@ -87,7 +87,7 @@ double select_pot(const ep_potential& p, double r) {
 // A potential the evaluator knows; a series fit with 0 < n <= EP_SERIES_MAX.
 const char* bad_potential(const ep_potential* p) {
   if (!p) return "null potential";
-  if (p->kind < EP_POT_NULL || p->kind > EP_POT_CH3I) return "unknown potential kind";
+  if (p->kind < EP_POT_NULL || p->kind > EP_POT_SURFACE) return "unknown potential kind";
   if (p->kind == EP_POT_SERIES) {
     if (!p->series) return "EP_POT_SERIES without its fit";
     if (p->series->n < 1 || p->series->n > EP_SERIES_MAX) return "series fit: n outside 1..EP_SERIES_MAX";

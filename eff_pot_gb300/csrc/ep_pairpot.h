@@ -204,6 +204,68 @@ EP_PP_HD double ep_ch3i(int l, double r) {
   return (d * (e * e) - d) * hartree * ev_k;
 }
 
+// The He-surface and adatom potentials of the registry (V_impur.f90:939-965,
+// 2417-2554, 3013-3030), V in K of one distance z in A:
+//   0 graphene (V_grafeno): (A e^(-alpha z) - C4/z^4 - C6/z^6) meV
+//   1 graphene without dispersion: Morse D (1 - e^(-alpha (z - Ze)))^2 - D, meV
+//   2 TiO2: Morse in cm^-1 plus -1/2 (1 + tanh((z - z0)/a) c3 (c3/z)^3)
+//   3 Au (V_Au): -De (1 + sum_k a_k r^k) e^(-a1 r), r = z - Re (Horner form)
+//   4, 5 Au on TiO2 and its z derivative: even inverse powers 6..14 in meV
+//        (Horner in 1/z^2), a constant for z <= 2
+//   6, 7 Ag on graphene and its derivative: (A e^(-beta z) - C4/z^4) kcal/mol
+//   8, 9 Au on graphene and its derivative: the same form in meV
+EP_PP_HD double ep_surface(int which, double z) {
+  const double mev_k = 11.604448;
+  switch (which) {
+    case 0: {
+      const double z2 = z * z;
+      return (554811.0 * exp(-3.21193 * z) - 1531.83 / (z2 * z2) - 22259.0 / (z2 * z2 * z2)) * mev_k;
+    }
+    case 1: {
+      const double D = 0.493191, e = 1.0 - exp(-1.54605 * (z - 4.34871));
+      return (D * (e * e) - D) * mev_k;
+    }
+    case 2: {
+      const double de = 95.9583, e = 1.0 - exp(-1.47089 * (z - 4.22534));
+      const double vz = de * (e * e) - de;
+      const double c3 = 8.85163, q = c3 / z;
+      const double vzd = -0.5 * (1.0 + tanh((z - 4.77765) / 1.06161) * c3 * (q * q * q));
+      return (vz + vzd) * 1.4387770;
+    }
+    case 3: {
+      const double a1 = 1.6417, a2 = -0.6164, a3 = 0.3770, a4 = -0.0549, a5 = 0.0018, a6 = 0.0046, a7 = -0.0010,
+                   a8 = 0.0001, a9 = 2.7e-6, Re = 4.124, De = 20.301143;
+      const double r = z - Re;
+      return -De * (1.0 + r * (a1 + r * (a2 + r * (a3 + r * (a4 + r * (a5 + r * (a6 + r * (a7 + r * (a8 + r * a9))))))))) *
+             exp(-a1 * r);
+    }
+    case 4:
+    case 5: {
+      const double C6 = -4.18518e6, C8 = 6.54459e7, C10 = -3.73112e8, C12 = 9.44942e8, C14 = -8.97265e8;
+      if (!(z > 2.0)) return (which == 4 ? 1821.44287109375 : -5415.35400390625) * mev_k;
+      const double a = 1.0 / z, a2 = a * a;
+      if (which == 4)
+        return (((((C14 * a2 + C12) * a2 + C10) * a2 + C8) * a2 + C6) * (a2 * a2 * a2)) * mev_k;
+      return (((((-14.0 * C14 * a2 - 12.0 * C12) * a2 - 10.0 * C10) * a2 - 8.0 * C8) * a2 - 6.0 * C6) *
+              (a2 * a2 * a2 * a)) *
+             mev_k;
+    }
+    case 6:
+    case 7: {
+      const double A = 11557.3, beta = 2.33671, C4 = 1143.0, kcal_k = 5.03216592455e2;
+      const double z2 = z * z, z4 = z2 * z2;
+      if (which == 6) return (A * exp(-beta * z) - C4 / z4) * kcal_k;
+      return (-A * beta * exp(-beta * z) + 4.0 * C4 / (z4 * z)) * kcal_k;
+    }
+    default: {
+      const double A = 448058.0, beta = 2.12336, C4 = 83077.3;
+      const double z2 = z * z, z4 = z2 * z2;
+      if (which == 8) return (A * exp(-beta * z) - C4 / z4) * mev_k;
+      return (-A * beta * exp(-beta * z) + 4.0 * C4 / (z4 * z)) * mev_k;
+    }
+  }
+}
+
 // Double-double arithmetic (Knuth's two-sum, the fused-multiply-add product
 // error, and the normalisations of Dekker's and Bailey's double-double
 // algorithms): 106-bit sums for the Real*16 fits.
@@ -284,5 +346,6 @@ EP_PP_HD double ep_pair_potential(int kind, double r_cutoff, double umax, const 
   if (kind == EP_POT_AG) return ep_ag((int)par[0], r);
   if (kind == EP_POT_BA_GS) return ep_ba_gs(r);
   if (kind == EP_POT_CH3I) return ep_ch3i((int)par[0], r);
+  if (kind == EP_POT_SURFACE) return ep_surface((int)par[0], r);
   return 0.0;
 }

@@ -299,6 +299,14 @@ int builtin(const std::string& sel, ep_potential* p) {
     p->kind = EP_POT_BA_GS;
     return 1;
   }
+  static const char* surf[10] = {"Grafeno", "Grafeno_sin_dispersion", "TiO2", "Au", "Au_TiO2",
+                                 "dAu_TiO2", "Ag_Graphene", "dz_Ag_Graphene", "Au_Graphene", "dz_Au_Graphene"};
+  for (int i = 0; i < 10; ++i)
+    if (sel == surf[i]) {
+      p->kind = EP_POT_SURFACE;
+      p->par[0] = i;
+      return 1;
+    }
   if (sel.size() == 6 && sel.compare(0, 5, "CH3I_") == 0 && sel[5] >= '0' && sel[5] <= '4') {
     p->kind = EP_POT_CH3I;
     p->par[0] = sel[5] - '0';

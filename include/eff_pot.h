@@ -97,7 +97,12 @@ typedef struct ep_config {
  * EP_POT_AG: 'Ag_gs', 'Ag_Pi', 'Ag_Sig' (V_impur.f90:1038-1096),
  *   par[0] = 0, 1, 2.
  * EP_POT_BA_GS: 'Ba_gs' (V_impur.f90:1197-1210).
- * EP_POT_CH3I: 'CH3I_0' .. 'CH3I_4' (V_impur.f90:3079-3243), par[0] = l. */
+ * EP_POT_CH3I: 'CH3I_0' .. 'CH3I_4' (V_impur.f90:3079-3243), par[0] = l.
+ * EP_POT_SURFACE: the He-surface and adatom potentials of the registry,
+ *   functions of one distance like the rest: par[0] = 0 'Grafeno',
+ *   1 'Grafeno_sin_dispersion', 2 'TiO2', 3 'Au', 4 'Au_TiO2', 5 'dAu_TiO2',
+ *   6 'Ag_Graphene', 7 'dz_Ag_Graphene', 8 'Au_Graphene', 9 'dz_Au_Graphene'
+ *   (V_impur.f90:939-965,2417-2554,3013-3030). */
 enum {
   EP_POT_NULL = 0,
   EP_POT_MORSE = 1,
@@ -108,7 +113,8 @@ enum {
   EP_POT_SERIES = 6,
   EP_POT_AG = 7,
   EP_POT_BA_GS = 8,
-  EP_POT_CH3I = 9
+  EP_POT_CH3I = 9,
+  EP_POT_SURFACE = 10
 };
 
 #define EP_SERIES_MAX 24
@@ -143,7 +149,8 @@ int ep_potential_values(const ep_potential* p, const double* r, double* v,
 /* Select_Pot by name (V_impur.f90:87-932): selec as the namelist gives it,
  * with its r_cutoff and umax.  The closed forms are built in ('null',
  * '*_plus_Koutselos', 'LI' .. 'CS', 'Aziz_He', 'Ar_He', 'Xe_He', 'Ag_gs',
- * 'Ag_Pi', 'Ag_Sig', 'Ba_gs', 'CH3I_0' .. 'CH3I_4'); the
+ * 'Ag_Pi', 'Ag_Sig', 'Ba_gs', 'CH3I_0' .. 'CH3I_4' and the ten surface
+ * names of EP_POT_SURFACE); the
  * inverse-power fits are read from the reference's V_impur.f90 at
  * source_path (NULL: closed forms only): its Select_Pot chain names the
  * function, whose COMMON block names the BLOCK DATA with the coefficients.

@@ -480,6 +480,49 @@ static double v_ch3i(int l, double r) {
   return radpot * Hartree * eV_K;
 }
 
+// The surface and adatom potentials (V_grafeno, V_grafeno_sin_dispersion,
+// V_TiO2, V_Au, V_Au_TiO2, V_dAu_TiO2, Ag_Graphene, dz_Ag_Graphene,
+// Au_Graphene, dz_Au_Graphene; V_impur.f90:939-965,2417-2554,3013-3030).
+static double v_surface(int which, double z) {
+  const double C_meV_to_K = 11.604448;
+  if (which == 0) {
+    const double A = 554811.0, alpha = 3.21193, C4 = 1531.83, C6 = 22259.0;
+    return (A * std::exp(-alpha * z) - C4 / std::pow(z, 4) - C6 / std::pow(z, 6)) * C_meV_to_K;
+  }
+  if (which == 1) {
+    const double D = 0.493191, alpha = 1.54605, Ze = 4.34871;
+    return (D * std::pow(1.0 - std::exp(-alpha * (z - Ze)), 2) - D) * C_meV_to_K;
+  }
+  if (which == 2) {
+    const double cmm1toK = 1.4387770, de = 95.9583, alpha = 1.47089, ze = 4.22534, z0 = 4.77765, c3 = 8.85163,
+                 aa = 1.06161;
+    const double vz = de * std::pow(1.0 - std::exp(-alpha * (z - ze)), 2) - de;
+    const double vzd = -0.5 * (1.0 + std::tanh((z - z0) / aa) * c3 * std::pow(c3 / z, 3));
+    return (vz + vzd) * cmm1toK;
+  }
+  if (which == 3) {
+    const double a[10] = {0.0, 1.6417, -0.6164, 0.3770, -0.0549, 0.0018, 0.0046, -0.0010, 0.0001, 2.7e-6};
+    const double Re = 4.124, De = 20.301143, r = z - Re;
+    double h = a[9];
+    for (int k = 8; k >= 1; --k) h = a[k] + r * h;
+    return -De * (1.0 + r * h) * std::exp(-a[1] * r);
+  }
+  if (which == 4 || which == 5) {
+    const double C6 = -4.18518e6, C8 = 6.54459e7, C10 = -3.73112e8, C12 = 9.44942e8, C14 = -8.97265e8;
+    if (!(z > 2.0)) return (which == 4 ? 1821.44287109375 : -5415.35400390625) * C_meV_to_K;
+    const double Aux = 1.0 / z, Aux2 = std::pow(Aux, 2);
+    if (which == 4) return (((((C14 * Aux2 + C12) * Aux2 + C10) * Aux2 + C8) * Aux2 + C6) * std::pow(Aux2, 3)) * C_meV_to_K;
+    return (((((-14.0 * C14 * Aux2 - 12.0 * C12) * Aux2 - 10.0 * C10) * Aux2 - 8.0 * C8) * Aux2 - 6.0 * C6) *
+            (std::pow(Aux2, 3) * Aux)) *
+           C_meV_to_K;
+  }
+  const bool ag = which == 6 || which == 7, deriv = which == 7 || which == 9;
+  const double A = ag ? 11557.3 : 448058.0, beta = ag ? 2.33671 : 2.12336, C4 = ag ? 1143.0 : 83077.3;
+  const double unit = ag ? 5.03216592455e2 : C_meV_to_K;
+  if (!deriv) return (A * std::exp(-beta * z) - C4 / std::pow(z, 4)) * unit;
+  return (-A * beta * std::exp(-beta * z) + 4.0 * C4 / std::pow(z, 5)) * unit;
+}
+
 // The inverse-power fits with a parabolic core (e.g. V_Fausto_Rb_gs,
 // V_impur.f90:2206-2250: Sto = sum_k Pg(k) Aux, Aux = xq**(k0+1) times xq
 // per term, xq = 1/x, all in Real*16).  The Real*16 arithmetic is restated
@@ -546,6 +589,7 @@ static double select_pot(const ep_potential& p, double r) {
   if (p.kind == EP_POT_AG) return v_ag((int)p.par[0], r);
   if (p.kind == EP_POT_BA_GS) return v_ba_gs(r);
   if (p.kind == EP_POT_CH3I) return v_ch3i((int)p.par[0], r);
+  if (p.kind == EP_POT_SURFACE) return v_surface((int)p.par[0], r);
   return 0.0;
 }
 

@@ -38,12 +38,17 @@ def lib():
         pytest.skip(f"libeffpot.so not loadable: {e}")
 
 
+SURFACES = ["Grafeno", "Grafeno_sin_dispersion", "TiO2", "Au", "Au_TiO2", "dAu_TiO2", "Ag_Graphene",
+            "dz_Ag_Graphene", "Au_Graphene", "dz_Au_Graphene"]
+
+
 def closed_forms():
     out = [(f"patil-{a}", ep.patil(a)) for a in ep.config.PATIL_ATOMS]
     out += [("aziz", ep.aziz_he()), ("tt-Ar", ep.tang_toennies("Ar")), ("tt-Xe", ep.tang_toennies("Xe"))]
     for name, kind, par in [("Ag_gs", _abi.EP_POT_AG, 0), ("Ag_Pi", _abi.EP_POT_AG, 1),
                             ("Ag_Sig", _abi.EP_POT_AG, 2), ("Ba_gs", _abi.EP_POT_BA_GS, 0)] + \
-            [(f"CH3I_{l}", _abi.EP_POT_CH3I, l) for l in range(5)]:
+            [(f"CH3I_{l}", _abi.EP_POT_CH3I, l) for l in range(5)] + \
+            [(n, _abi.EP_POT_SURFACE, i) for i, n in enumerate(SURFACES)]:
         p = _abi.EpPotential()
         p.kind, p.par[0] = kind, float(par)
         out.append((name, p))
@@ -155,6 +160,46 @@ def test_ag_ba_ch3i_constants_and_forms_match_the_reference_source(lib, source_t
         want = np.where(r <= kf["r_cutoff"], kf["umax"], want)
         got = ep.potential_values(ep.select_pot(f"CH3I_{l}"), r)
         assert np.allclose(got, want, rtol=1e-13, atol=1e-15), l
+
+
+def _data(body):
+    """name -> value of the DATA statements of a function body."""
+    out = {}
+    for stmt in re.findall(r"(?i)\bdata\b([^\n]*)", body):
+        for name, lit in re.findall(r"(\w+)\s*/\s*([^/,]+?)\s*/", stmt):
+            out[name.lower()] = float(literal(lit)[0])
+    return out
+
+
+def test_surface_potentials_match_the_reference_source(lib, source_text):
+    """The ten surface and adatom entries restated in numpy with the
+    constants read from V_impur.f90 equal the library's evaluator."""
+    z = np.linspace(1.0, 20.0, 500)
+    k = _data(_function_body(source_text, "V_grafeno"))
+    want = {"Grafeno": (k["a"] * np.exp(-k["alpha"] * z) - k["c4"] / z ** 4 - k["c6"] / z ** 6) * k["c_mev_to_k"]}
+    k = _data(_function_body(source_text, "V_grafeno_sin_dispersion"))
+    want["Grafeno_sin_dispersion"] = (k["d"] * (1 - np.exp(-k["alpha"] * (z - k["ze"]))) ** 2 - k["d"]) * k["c_mev_to_k"]
+    k = _data(_function_body(source_text, "V_TiO2"))
+    vz = k["de"] * (1 - np.exp(-k["alpha"] * (z - k["ze"]))) ** 2 - k["de"]
+    vzd = -0.5 * (1 + np.tanh((z - k["z0"]) / k["aa"]) * k["c3"] * (k["c3"] / z) ** 3)
+    want["TiO2"] = (vz + vzd) * k["cmm1tok"]
+    k = _data(_function_body(source_text, "V_Au"))
+    r = z - k["re"]
+    poly = 1.0 + sum(k[f"a{j}"] * r ** j for j in range(1, 10))
+    want["Au"] = -k["de"] * poly * np.exp(-k["a1"] * r)
+    k = _decl(_function_body(source_text, "V_Au_TiO2"))
+    a2 = 1.0 / z ** 2
+    v = sum(k[f"c{n}"] * a2 ** (n // 2) for n in (6, 8, 10, 12, 14)) * k["cmev_to_k"]
+    want["Au_TiO2"] = np.where(z > 2, v, 1821.44287109375 * k["cmev_to_k"])
+    dv = sum(-n * k[f"c{n}"] * a2 ** (n // 2) / z for n in (6, 8, 10, 12, 14)) * k["cmev_to_k"]
+    want["dAu_TiO2"] = np.where(z > 2, dv, -5415.35400390625 * k["cmev_to_k"])
+    for name, fn, unit in (("Ag_Graphene", "Ag_Graphene", "ckcal_to_k"), ("Au_Graphene", "Au_Graphene", "xmev_to_k")):
+        k = _data(_function_body(source_text, fn))
+        want[name] = (k["a"] * np.exp(-k["beta"] * z) - k["c4"] / z ** 4) * k[unit]
+        want["dz_" + name] = (-k["a"] * k["beta"] * np.exp(-k["beta"] * z) + 4 * k["c4"] / z ** 5) * k[unit]
+    for name in SURFACES:
+        got = ep.potential_values(ep.select_pot(name), z)
+        assert np.allclose(got, want[name], rtol=1e-12, atol=1e-10), name
 
 
 def test_patil_aziz_tang_toennies_constants_match_the_reference_source(lib, source_text):
@@ -447,7 +492,8 @@ def test_gpu_uplus_of_the_new_forms_matches_oracle(oracle):
     pluses = {"patil": ep.patil("RB", r_cutoff=2.0, umax=5000.0), "aziz": ep.aziz_he(r_cutoff=1.5, umax=2000.0),
               "tt": ep.tang_toennies("Xe", r_cutoff=2.0, umax=21450.4867067095), "series": _fit(),
               "ag": ep.select_pot("Ag_Pi", 1.0, 3000.0), "ba": ep.select_pot("Ba_gs"),
-              "ch3i": ep.select_pot("CH3I_2")}
+              "ch3i": ep.select_pot("CH3I_2"), "tio2": ep.select_pot("TiO2", 2.5, 1.887964e4),
+              "au": ep.select_pot("Au", 1.0, 6.645232e4)}
     for name, plus in pluses.items():
         res = []
         for S in (ep.Solver, oracle.OracleSolver):
