@@ -21,6 +21,7 @@ EP_STATE_P, EP_STATE_D = 0, 1
 EP_POT_NULL, EP_POT_MORSE, EP_POT_KOUTSELOS = 0, 1, 2
 EP_POT_PATIL, EP_POT_AZIZ, EP_POT_TANG_TOENNIES, EP_POT_SERIES = 3, 4, 5, 6
 EP_POT_AG, EP_POT_BA_GS, EP_POT_CH3I, EP_POT_SURFACE = 7, 8, 9, 10
+EP_POT_EVENPOW, EP_POT_EXPFIT = 11, 12
 EP_SERIES_MAX = 24
 
 FIELDS = {

@@ -32,9 +32,7 @@
 // from the file named by the key potentials_source), 'Morse', or 'table'
 // from a file of (r, V) rows.  Not built here: the Laverage_P_value /
 // Lmixture / exciplex variants of instates.f90 (they sum eigenvectors, so
-// they depend on EISPACK's phase convention), and the two Select_Pot forms
-// that are neither built in nor inverse-power fits (Cs_7s, Ba_plus_old_gs);
-// they run as 'table'.
+// they depend on EISPACK's phase convention).
 #include <cmath>
 #include <complex>
 #include <cstdio>

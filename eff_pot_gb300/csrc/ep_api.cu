@@ -87,9 +87,9 @@ double select_pot(const ep_potential& p, double r) {
 // A potential the evaluator knows; a series fit with 0 < n <= EP_SERIES_MAX.
 const char* bad_potential(const ep_potential* p) {
   if (!p) return "null potential";
-  if (p->kind < EP_POT_NULL || p->kind > EP_POT_SURFACE) return "unknown potential kind";
-  if (p->kind == EP_POT_SERIES) {
-    if (!p->series) return "EP_POT_SERIES without its fit";
+  if (p->kind < EP_POT_NULL || p->kind > EP_POT_EXPFIT) return "unknown potential kind";
+  if (p->kind == EP_POT_SERIES || p->kind == EP_POT_EVENPOW || p->kind == EP_POT_EXPFIT) {
+    if (!p->series) return "a fitted potential without its fit";
     if (p->series->n < 1 || p->series->n > EP_SERIES_MAX) return "series fit: n outside 1..EP_SERIES_MAX";
     if (p->series->k0 < 0 || p->series->k0 > 64) return "series fit: k0 outside 0..64";
   }
@@ -101,7 +101,7 @@ void keep_plus(ImpState& imp, const ep_potential* plus) {
   imp.plus = *plus;
   imp.plus.series = nullptr;
   imp.plus_series = ep_series{};
-  if (plus->kind == EP_POT_SERIES) imp.plus_series = *plus->series;
+  if (plus->series) imp.plus_series = *plus->series;
 }
 
 template <class F>

@@ -327,6 +327,35 @@ EP_PP_HD double ep_series_value(const ep_series* s, double x) {
   return acc;
 }
 
+// Func_Ba_plus_gs (V_impur.f90:1479-1497): the plain parabola up to r0, then
+// even inverse powers x^-6, x^-8, ... in double.
+EP_PP_HD double ep_evenpow_value(const ep_series* s, double x) {
+  if (x <= s->r0) return s->aa * (x * x) + s->bb * x + s->cc;
+  const int n = s->n < EP_SERIES_MAX ? s->n : EP_SERIES_MAX;
+  const double x2 = x * x;
+  double p = x2 * x2 * x2, sto = 0.0;
+  for (int k = 0; k < n; ++k) {
+    sto = sto + s->c_hi[k] / p;
+    p = p * x2;
+  }
+  return sto;
+}
+
+// V_Cs_7s (V_impur.f90:1682-1702): x clamped below at x0 (r_core), the plain
+// parabola up to r0, then Pg(1) e^(-Ps(1) x)/x + sum_{k>=2} Pg(k) x^(k-1)
+// e^(-Ps(k) x) (Pg in c_hi, Ps in c_lo).
+EP_PP_HD double ep_expfit_value(const ep_series* s, double xx) {
+  const double x = xx < s->r_core ? s->r_core : xx;
+  if (x <= s->r0) return s->aa * (x * x) + s->bb * x + s->cc;
+  const int n = s->n < EP_SERIES_MAX ? s->n : EP_SERIES_MAX;
+  double sto = s->c_hi[0] * exp(-s->c_lo[0] * x) / x, p = 1.0;
+  for (int k = 1; k < n; ++k) {
+    p = p * x;
+    sto = sto + s->c_hi[k] * p * exp(-s->c_lo[k] * x);
+  }
+  return sto;
+}
+
 // Select_Pot for kind (EP_POT_*), its cutoff rule r < r_cutoff -> umax,
 // parameters par (Morse: De, re, alpha; Koutselos, Patil, Tang-Toennies:
 // the atom) and, for EP_POT_SERIES, the fit s.
@@ -347,5 +376,7 @@ EP_PP_HD double ep_pair_potential(int kind, double r_cutoff, double umax, const 
   if (kind == EP_POT_BA_GS) return ep_ba_gs(r);
   if (kind == EP_POT_CH3I) return ep_ch3i((int)par[0], r);
   if (kind == EP_POT_SURFACE) return ep_surface((int)par[0], r);
+  if (kind == EP_POT_EVENPOW && s) return ep_evenpow_value(s, r);
+  if (kind == EP_POT_EXPFIT && s) return ep_expfit_value(s, r);
   return 0.0;
 }

@@ -10,7 +10,9 @@
 // it writes x**(k+5), the exponent offset.  Every literal keeps its Fortran
 // kind: without exponent letter or with E it is default REAL (binary32)
 // before DATA widens it, D is double, Q is Real*16 (kept here as a
-// double-double pair, 106 bits).
+// double-double pair, 106 bits).  Two fits of their own form are read the
+// same way: Func_Ba_plus_gs behind 'Ba_plus_old_gs' (even inverse powers)
+// and V_Cs_7s (exponentials times powers of x).
 #include <stdint.h>
 #include <stdio.h>
 #include <string.h>
@@ -367,35 +369,73 @@ extern "C" int ep_select_pot(const char* selec, double r_cutoff, double umax, co
   }
   if (func.empty()) return put_err(err, cap, "selec '" + sel + "' is not in the Select_Pot chain of " + source_path);
 
-  // 2. the function: its COMMON block, the precision of Sto, the exponent offset
+  // 2. the function: its COMMON block and its form -- the inverse-power fit
+  // (core constant, |parabola|, sum of Pg(k) x^-(k+k0), Real*16 or Real*8
+  // Sto), Func_Ba_plus_gs's even powers, or V_Cs_7s's exponential fit; a
+  // function that only returns another one (V_Ba_plus_old_gs) is followed
+  enum { F_SERIES, F_EVENPOW, F_EXPFIT, F_NONE };
   std::string common;
   bool quad = false, has_core = false, has_par = false, has_sum = false;
+  bool even_sum = false, plain_par = false, exp_first = false, exp_sum = false, clamp = false;
   int k0_lit = -1;
-  {
+  Lit x0;
+  for (int hop = 0; hop < 2; ++hop) {
     size_t i = 0;
     for (; i < st.size(); ++i)
       if (function_name(st[i].cl) == func) break;
     if (i == st.size()) return put_err(err, cap, "function " + func + " not found");
+    std::string forward;
+    int stmts = 0;
     for (++i; i < st.size() && !is_end(st[i].cl); ++i) {
       const std::string& c = st[i].cl;
+      if (starts(c, "implicit") || starts(c, "parameter") || starts(c, "real") || starts(c, "integer") ||
+          c == "return")
+        continue;
+      ++stmts;
+      if (starts(c, (func + "=").c_str()) && c.size() > func.size() + 4 &&
+          c.compare(c.size() - 3, 3, "(x)") == 0)
+        forward = c.substr(func.size() + 1, c.size() - func.size() - 4);
       if (starts(c, "common/")) common = c.substr(7, c.find('/', 7) - 7);
-      if (starts(c, "real*16") && c.find("sto") != std::string::npos) quad = true;
       if (c.find("x.le.rcutoff") != std::string::npos) has_core = true;
       if (c.find("abs(aa*x**2+bb*x+cc)") != std::string::npos) has_par = true;
-      if (c.find("sto=sto+pg(k)") != std::string::npos) {
+      if (c.find("=aa*x**2+bb*x+cc") != std::string::npos) plain_par = true;
+      if (c.find("sto=sto+pg(k)/x**(2*(k-1)+6)") != std::string::npos) even_sum = true;
+      else if (c.find("sto=sto+pg(k)*x**(k-1)*dexp(-ps(k)*x)") != std::string::npos) exp_sum = true;
+      else if (c.find("sto=sto+pg(k)") != std::string::npos) {
         has_sum = true;
         size_t q = c.find("x**(k+");
         if (q != std::string::npos) k0_lit = std::atoi(c.c_str() + q + 6);
       }
+      if (c.find("sto=pg(1)*dexp(-ps(1)*x)/x") != std::string::npos) exp_first = true;
+      if (c.find("if(xx.lt.x0)") != std::string::npos) clamp = true;
+      if (starts(c, "data")) {
+        for (const DataItem& d : data_items(st[i].raw))
+          if (d.name == "x0" && d.vals.size() == 1) x0 = literal(d.vals[0]);
+      }
     }
+    // function bodies hold their statements between a declaration and END;
+    // the Real*16 / Real*8 declaration of Sto decides the sum's precision
+    if (forward.empty() || stmts != 1) break;
+    func = forward;
   }
-  if (common.empty() || !has_core || !has_par || !has_sum)
+  {
+    size_t i = 0;
+    for (; i < st.size(); ++i)
+      if (function_name(st[i].cl) == func) break;
+    for (++i; i < st.size() && !is_end(st[i].cl); ++i)
+      if (starts(st[i].cl, "real*16") && st[i].cl.find("sto") != std::string::npos) quad = true;
+  }
+  const int form = (has_core && has_par && has_sum) ? F_SERIES
+                   : (even_sum && plain_par)        ? F_EVENPOW
+                   : (exp_first && exp_sum && plain_par && clamp && x0.ok) ? F_EXPFIT
+                                                                            : F_NONE;
+  if (common.empty() || form == F_NONE)
     return put_err(err, cap, "'" + sel + "' (" + func + ") is not an inverse-power fit with a parabolic core");
 
   // 3. the BLOCK DATA holding that COMMON
   int npg = -1;
   bool pg16 = false;
-  std::vector<std::string> pg;
+  std::vector<std::string> pg, ps;
   Lit sc[6];
   const char* scn[6] = {"rcutoff", "fcutoff", "r0", "aa", "bb", "cc"};
   int k0 = -1;
@@ -418,6 +458,7 @@ extern "C" int ep_select_pot(const char* selec, double r_cutoff, double umax, co
       if (!starts(c, "data")) continue;
       for (const DataItem& d : data_items(st[j].raw)) {
         if (d.name == "pg") pg = d.vals;
+        if (d.name == "ps") ps = d.vals;
         for (int q = 0; q < 6; ++q)
           if (d.name == scn[q] && d.vals.size() == 1) sc[q] = literal(d.vals[0]);
         if (d.name == "k0" && d.vals.size() == 1) k0 = (int)literal(d.vals[0]).ival;
@@ -425,20 +466,22 @@ extern "C" int ep_select_pot(const char* selec, double r_cutoff, double umax, co
     }
   }
   if (k0_lit >= 0) k0 = k0_lit;
-  if (npg < 1 || npg > EP_SERIES_MAX || (int)pg.size() != npg || k0 < 0)
-    return put_err(err, cap, "BLOCK DATA of /" + common + "/: Npg, Pg or k0 unreadable or above EP_SERIES_MAX");
-  for (int q = 0; q < 6; ++q)
+  if (form != F_SERIES) k0 = 0;
+  if (npg < 1 || npg > EP_SERIES_MAX || (int)pg.size() != npg || k0 < 0 ||
+      (form == F_EXPFIT && (int)ps.size() != npg))
+    return put_err(err, cap, "BLOCK DATA of /" + common + "/: Npg, Pg, Ps or k0 unreadable or above EP_SERIES_MAX");
+  for (int q = form == F_SERIES ? 0 : 2; q < 6; ++q)
     if (!sc[q].ok) return put_err(err, cap, std::string("BLOCK DATA of /") + common + "/: no " + scn[q]);
   ep_series s{};
-  s.r_core = sc[0].hi;
-  s.f_core = sc[1].hi;
+  s.r_core = form == F_SERIES ? sc[0].hi : (form == F_EXPFIT ? x0.hi : 0.0);
+  s.f_core = form == F_SERIES ? sc[1].hi : 0.0;
   s.r0 = sc[2].hi;
   s.aa = sc[3].hi;
   s.bb = sc[4].hi;
   s.cc = sc[5].hi;
   s.k0 = k0;
   s.n = npg;
-  s.quad = quad ? 1 : 0;
+  s.quad = (form == F_SERIES && quad) ? 1 : 0;
   for (int k = 0; k < npg; ++k) {
     const Lit L = literal(pg[k]);
     if (!L.ok) return put_err(err, cap, "Pg(" + std::to_string(k + 1) + ") of /" + common + "/ unreadable");
@@ -446,9 +489,14 @@ extern "C" int ep_select_pot(const char* selec, double r_cutoff, double umax, co
     // a Real*8 Pg keeps the literal rounded to double; Real*16 keeps its kind
     s.c_lo[k] = (pg16 && L.kind == 16) ? L.lo : 0.0;
     if (!pg16 && L.kind == 16) s.c_hi[k] = L.hi + L.lo;
+    if (form == F_EXPFIT) {
+      const Lit M = literal(ps[k]);
+      if (!M.ok) return put_err(err, cap, "Ps(" + std::to_string(k + 1) + ") of /" + common + "/ unreadable");
+      s.c_lo[k] = M.hi + M.lo;
+    }
   }
   *series = s;
-  p->kind = EP_POT_SERIES;
+  p->kind = form == F_SERIES ? EP_POT_SERIES : (form == F_EVENPOW ? EP_POT_EVENPOW : EP_POT_EXPFIT);
   p->series = series;
   return EP_OK;
 }

@@ -56,7 +56,7 @@ def select_pot(selec, r_cutoff=0.0, umax=0.0, source=None):
                          None if source is None else os.fsencode(source), C.byref(p), C.byref(s), err, 512)
     if st != _abi.EP_OK:
         raise EffPotError(st, err.value.decode())
-    if p.kind == _abi.EP_POT_SERIES:
+    if p.kind in (_abi.EP_POT_SERIES, _abi.EP_POT_EVENPOW, _abi.EP_POT_EXPFIT):
         p.series = C.pointer(s)
         p._series = s
     return p

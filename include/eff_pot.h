@@ -102,7 +102,14 @@ typedef struct ep_config {
  *   functions of one distance like the rest: par[0] = 0 'Grafeno',
  *   1 'Grafeno_sin_dispersion', 2 'TiO2', 3 'Au', 4 'Au_TiO2', 5 'dAu_TiO2',
  *   6 'Ag_Graphene', 7 'dz_Ag_Graphene', 8 'Au_Graphene', 9 'dz_Au_Graphene'
- *   (V_impur.f90:939-965,2417-2554,3013-3030). */
+ *   (V_impur.f90:939-965,2417-2554,3013-3030).
+ * EP_POT_EVENPOW: 'Ba_plus_old_gs' (Func_Ba_plus_gs, V_impur.f90:1440-1497):
+ *   aa x^2 + bb x + cc for x <= r0, sum_k c_hi[k-1] x^-(2k+4) beyond, in
+ *   *series (r0, aa, bb, cc, n, c_hi).
+ * EP_POT_EXPFIT: 'Cs_7s' (V_Cs_7s, V_impur.f90:1660-1702): x = max(r, x0);
+ *   aa x^2 + bb x + cc for x <= r0, else Pg(1) e^(-Ps(1) x)/x + sum_{k>=2}
+ *   Pg(k) x^(k-1) e^(-Ps(k) x), in *series (r_core = x0, r0, aa, bb, cc,
+ *   n, c_hi = Pg, c_lo = Ps). */
 enum {
   EP_POT_NULL = 0,
   EP_POT_MORSE = 1,
@@ -114,7 +121,9 @@ enum {
   EP_POT_AG = 7,
   EP_POT_BA_GS = 8,
   EP_POT_CH3I = 9,
-  EP_POT_SURFACE = 10
+  EP_POT_SURFACE = 10,
+  EP_POT_EVENPOW = 11,
+  EP_POT_EXPFIT = 12
 };
 
 #define EP_SERIES_MAX 24
@@ -137,8 +146,9 @@ typedef struct ep_potential {
   double r_cutoff, umax;
   double par[4];             /* Morse: De (K), re (A), alpha (1/A);
                                 Koutselos, Patil, Tang-Toennies: the atom   */
-  const ep_series* series;   /* EP_POT_SERIES: the fit (read during the
-                                call that takes the potential, not kept)    */
+  const ep_series* series;   /* EP_POT_SERIES, _EVENPOW, _EXPFIT: the fit
+                                (read during the call that takes the
+                                potential, not kept)                        */
 } ep_potential;
 
 /* V(r_i), i < n, of p in the library's host arithmetic (no GPU needed): the
@@ -151,7 +161,8 @@ int ep_potential_values(const ep_potential* p, const double* r, double* v,
  * '*_plus_Koutselos', 'LI' .. 'CS', 'Aziz_He', 'Ar_He', 'Xe_He', 'Ag_gs',
  * 'Ag_Pi', 'Ag_Sig', 'Ba_gs', 'CH3I_0' .. 'CH3I_4' and the ten surface
  * names of EP_POT_SURFACE); the
- * inverse-power fits are read from the reference's V_impur.f90 at
+ * inverse-power fits (and the two fits of their own form, 'Ba_plus_old_gs'
+ * and 'Cs_7s') are read from the reference's V_impur.f90 at
  * source_path (NULL: closed forms only): its Select_Pot chain names the
  * function, whose COMMON block names the BLOCK DATA with the coefficients.
  * Fortran literal kinds are kept: a constant without exponent letter or

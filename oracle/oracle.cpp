@@ -573,6 +573,23 @@ static double v_series(const ep_series& s, double x) {
   return Sto.hi + Sto.lo;
 }
 
+// Func_Ba_plus_gs (V_impur.f90:1479-1497), behind 'Ba_plus_old_gs'.
+static double v_evenpow(const ep_series& s, double x) {
+  if (x <= s.r0) return s.aa * std::pow(x, 2) + s.bb * x + s.cc;
+  double Sto = 0.0;
+  for (int k = 1; k <= s.n; ++k) Sto = Sto + s.c_hi[k - 1] / std::pow(x, 2 * (k - 1) + 6);
+  return Sto;
+}
+
+// V_Cs_7s (V_impur.f90:1682-1702): Pg in c_hi, Ps in c_lo, x0 in r_core.
+static double v_expfit(const ep_series& s, double xx) {
+  const double x = xx < s.r_core ? s.r_core : xx;
+  if (x <= s.r0) return s.aa * std::pow(x, 2) + s.bb * x + s.cc;
+  double Sto = s.c_hi[0] * std::exp(-s.c_lo[0] * x) / x;
+  for (int k = 2; k <= s.n; ++k) Sto = Sto + s.c_hi[k - 1] * std::pow(x, k - 1) * std::exp(-s.c_lo[k - 1] * x);
+  return Sto;
+}
+
 static double select_pot(const ep_potential& p, double r) {
   if (p.kind == EP_POT_NULL) return 0.0;
   if (r < p.r_cutoff) return p.umax;
@@ -590,6 +607,8 @@ static double select_pot(const ep_potential& p, double r) {
   if (p.kind == EP_POT_BA_GS) return v_ba_gs(r);
   if (p.kind == EP_POT_CH3I) return v_ch3i((int)p.par[0], r);
   if (p.kind == EP_POT_SURFACE) return v_surface((int)p.par[0], r);
+  if (p.kind == EP_POT_EVENPOW && p.series) return v_evenpow(*p.series, r);
+  if (p.kind == EP_POT_EXPFIT && p.series) return v_expfit(*p.series, r);
   return 0.0;
 }
 
@@ -600,7 +619,7 @@ struct KeptPot {
   void keep(const ep_potential& q) {
     p = q;
     p.series = nullptr;
-    if (q.kind == EP_POT_SERIES && q.series) {
+    if ((q.kind == EP_POT_SERIES || q.kind == EP_POT_EVENPOW || q.kind == EP_POT_EXPFIT) && q.series) {
       s = *q.series;
       p.series = &s;
     }
@@ -727,7 +746,8 @@ extern "C" {
 
 int oc_potential_values(const ep_potential* p, const double* r, double* v, int n) {
   if (!p || n < 0 || (n > 0 && (!r || !v))) return EP_ERR_INVALID_ARG;
-  if (p->kind == EP_POT_SERIES && (!p->series || p->series->n < 1 || p->series->n > EP_SERIES_MAX))
+  if ((p->kind == EP_POT_SERIES || p->kind == EP_POT_EVENPOW || p->kind == EP_POT_EXPFIT) &&
+      (!p->series || p->series->n < 1 || p->series->n > EP_SERIES_MAX))
     return EP_ERR_INVALID_ARG;
   for (int i = 0; i < n; ++i) v[i] = select_pot(*p, r[i]);
   return EP_OK;

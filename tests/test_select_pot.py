@@ -379,6 +379,54 @@ def test_every_reference_fit_matches_exact_arithmetic(lib, oracle, reference_fit
                 assert abs(g - float(want)) <= 1e-14 * scale, (name, x)
 
 
+def _block(text, common):
+    """The DATA of the BLOCK DATA holding COMMON /common/ (name -> literals)."""
+    t = re.sub(r"&\s*\n\s*&?", " ", text)
+    for m in re.finditer(r"(?is)\n\s*block\s*data\s+\w+(.*?)\n\s*end\b", t):
+        if re.search(r"(?i)common/" + common + "/", m.group(1)):
+            return {k.lower(): [v for v in vals.split(",") if v.strip()]
+                    for k, vals in re.findall(r"(?i)data\s+(\w+)\s*/([^/]*)/", m.group(1))}
+    raise AssertionError(common)
+
+
+def test_old_ba_plus_and_cs_7s_fits(lib, oracle, source_text):
+    """'Ba_plus_old_gs' (through Func_Ba_plus_gs: a plain parabola, then even
+    inverse powers 6..36) against exact rational arithmetic, and 'Cs_7s' (x
+    clamped at 2.5 A, a parabola, then Pg(1) e^(-Ps(1) x)/x + sum Pg(k)
+    x^(k-1) e^(-Ps(k) x)) against a numpy restatement, both with the
+    coefficients read here from the BLOCK DATA."""
+    d = _block(source_text, "Param_LJ_Ba_plus_gs")
+    pg = [literal(v)[0] for v in d["pg"]]
+    r0, aa, bb, cc = (literal(d[k][0])[0] for k in ("r0", "aa", "bb", "cc"))
+    p = ep.select_pot("Ba_plus_old_gs", 0.0, 0.0, SOURCE)
+    assert p.kind == _abi.EP_POT_EVENPOW
+    x = np.linspace(1.0, 25.0, 300)
+    got = ep.potential_values(p, x)
+    for v, g in zip(x, got):
+        X = Fraction(v)
+        if X <= r0:
+            want = aa * X * X + bb * X + cc
+            scale = abs(aa) * X * X + abs(bb) * X + abs(cc)
+        else:
+            want = sum(c / X ** (2 * k + 6) for k, c in enumerate(pg))
+            scale = sum(abs(c) / X ** (2 * k + 6) for k, c in enumerate(pg))
+        assert abs(g - float(want)) <= 1e-14 * float(scale), v
+    assert np.allclose(oracle.potential_values(p, x), got, rtol=0, atol=1e-13 * np.max(np.abs(got)))
+    d = _block(source_text, "Param_AP_Fit_APG_Cs_7s0")
+    pg = [float(literal(v)[0]) for v in d["pg"]]
+    ps = [float(literal(v)[0]) for v in d["ps"]]
+    r0, aa, bb, cc = (float(literal(d[k][0])[0]) for k in ("r0", "aa", "bb", "cc"))
+    p = ep.select_pot("Cs_7s", 0.0, 0.0, SOURCE)
+    assert p.kind == _abi.EP_POT_EXPFIT and p.series.contents.r_core == 2.5
+    xc = np.maximum(x, 2.5)
+    series = pg[0] * np.exp(-ps[0] * xc) / xc + sum(pg[k] * xc ** k * np.exp(-ps[k] * xc) for k in range(1, 12))
+    want = np.where(xc <= r0, aa * xc ** 2 + bb * xc + cc, series)
+    scale = np.abs(pg[0] * np.exp(-ps[0] * xc) / xc) + sum(np.abs(pg[k] * xc ** k * np.exp(-ps[k] * xc))
+                                                           for k in range(1, 12))
+    assert np.all(np.abs(ep.potential_values(p, x) - want) <= 1e-13 * scale)
+    assert np.all(np.abs(oracle.potential_values(p, x) - want) <= 1e-13 * scale)
+
+
 def test_real16_fits_need_the_double_double_sum(lib, reference_fits):
     """Near the core the terms of the Fausto fits cancel by ten orders of
     magnitude: the same coefficients summed in double miss the exact value by
@@ -465,8 +513,8 @@ def test_select_pot_errors(lib):
     with pytest.raises(ep.EffPotError):
         ep.select_pot("Rb_gs_Fausto", 0.0, 0.0, None)  # a fit needs its source
     if os.path.exists(SOURCE):
-        with pytest.raises(ep.EffPotError, match="inverse-power"):
-            ep.select_pot("Cs_7s", 0.0, 0.0, SOURCE)
+        with pytest.raises(ep.EffPotError, match="not in the Select_Pot chain"):
+            ep.select_pot("Cs_8s", 0.0, 0.0, SOURCE)
     p = ep.select_pot("Xe_He", 2.0, 21450.4867067095, None)
     assert p.kind == _abi.EP_POT_TANG_TOENNIES and p.r_cutoff == 2.0
     assert ep.potential_values(p, np.array([1.0]))[0] == 21450.4867067095
