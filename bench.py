@@ -22,6 +22,7 @@ import json
 import os
 import statistics
 import subprocess
+import tempfile
 import sys
 import time
 
@@ -69,10 +70,10 @@ class ClockSampler:
          "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
          "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
 
-    def __init__(self, device, tag):
+    def __init__(self, device, tag, directory=None):
         self.device = device
         self.proc = None
-        self.path = os.path.join(ROOT, "gpurun_out", f"clocks_{tag}_{device}.csv")
+        self.path = os.path.join(directory or tempfile.gettempdir(), f"clocks_{tag}_{device}.csv")
 
     def __enter__(self):
         try:
@@ -279,7 +280,7 @@ def run_ours(args):
     b.synchronize()
     barrier(dist)
     l0 = b.kernel_launches()
-    with ClockSampler(local, "batch") as clk:
+    with ClockSampler(local, "batch", args.clocks_dir) as clk:
         b.event_record(0)
         b.run(k32, DT, wait=False)
         b.set_precision("fp64")
@@ -405,6 +406,8 @@ def main():
     ap.add_argument("--batch", type=int, default=32)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--clocks-dir", default=None, help="where the nvidia-smi samples of the timed region go "
+                                                      "(default: the temporary directory)")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     if args.impl == "reference":
