@@ -507,6 +507,31 @@ def test_reader_on_a_synthetic_source(lib):
         ep.select_pot("Other", 0.0, 0.0, SYNTHETIC)
 
 
+def test_reader_survives_damaged_sources(lib, tmp_path):
+    """Cut or gapped copies of a source (the synthetic one, and the
+    reference's where present) give a potential or EP_ERR_INVALID_ARG, never
+    a crash: every index the reader takes is checked against its statement."""
+    import random
+    rng = random.Random(7)
+    texts = [(open(SYNTHETIC).read(), ["Test_fit", "Other"])]
+    if os.path.exists(SOURCE):
+        texts.append((open(SOURCE, encoding="latin-1").read(), ["Rb_gs_Fausto", "Cs_7s", "Ba_plus_old_gs"]))
+    f = tmp_path / "v.f90"
+    for text, names in texts:
+        for trial in range(40):
+            i = rng.randrange(len(text))
+            j = min(len(text), i + rng.randrange(1, 400))
+            cut = (text[:i], text[i:], text[:i] + text[j:])[trial % 3]
+            f.write_text(cut, encoding="latin-1")
+            for n in names:
+                try:
+                    p = ep.select_pot(n, 0.0, 0.0, str(f))
+                    assert p.kind in (_abi.EP_POT_SERIES, _abi.EP_POT_EVENPOW, _abi.EP_POT_EXPFIT)
+                    assert 1 <= p.series.contents.n <= _abi.EP_SERIES_MAX
+                except ep.EffPotError as e:
+                    assert e.status == 1
+
+
 def test_select_pot_errors(lib):
     with pytest.raises(ep.EffPotError):
         ep.select_pot("No_such_potential", 0.0, 0.0, None)
