@@ -232,12 +232,10 @@ struct DataItem {
 };
 std::vector<DataItem> data_items(const std::string& raw) {
   std::vector<DataItem> out;
-  size_t p = lower_compact(raw.substr(0, 8)).find("data");
-  std::string s = raw;
+  const std::string& s = raw;
   size_t k = 0;
   while (k < s.size() && isspace((unsigned char)s[k])) ++k;
   k += 4;  // "data"
-  (void)p;
   while (k < s.size()) {
     size_t sl = s.find('/', k);
     if (sl == std::string::npos) break;
