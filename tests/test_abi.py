@@ -29,6 +29,42 @@ def test_header_and_binding_agree():
     assert header_symbols() == _abi.HEADER_SYMBOLS
 
 
+def test_header_enums_and_struct_sizes_match_the_binding():
+    """Every EP_* enumerator and #define of the header has the binding's
+    value, and the ctypes structs have the C layout's size (a C compile of
+    the header reports sizeof)."""
+    src = open(os.path.join(ROOT, "include", "eff_pot.h")).read()
+    src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
+    vals = {}
+    for body in re.findall(r"enum\s*\{([^}]*)\}", src):
+        for name, v in re.findall(r"\b(EP_[A-Z0-9_]+)\s*=\s*(-?\d+)", body):
+            vals[name] = int(v)
+    for name, v in re.findall(r"#define\s+(EP_[A-Z0-9_]+)\s+(\d+)", src):
+        vals[name] = int(v)
+    checked = 0
+    for name, v in vals.items():
+        if hasattr(_abi, name):
+            assert getattr(_abi, name) == v, name
+            checked += 1
+    assert checked >= 25
+    import shutil
+    import subprocess
+    import tempfile
+    cc = shutil.which("gcc") or shutil.which("cc")
+    if cc is None:
+        pytest.skip("no C compiler")
+    with tempfile.TemporaryDirectory() as d:
+        c = os.path.join(d, "s.c")
+        open(c, "w").write('#include <stdio.h>\n#include "eff_pot.h"\nint main(void){printf("%zu %zu %zu %zu\\n",'
+                           " sizeof(ep_config), sizeof(ep_potential), sizeof(ep_series), sizeof(ep_energies));"
+                           "return 0;}\n")
+        exe = os.path.join(d, "s")
+        subprocess.run([cc, "-I", os.path.join(ROOT, "include"), c, "-o", exe], check=True)
+        sizes = [int(x) for x in subprocess.run([exe], capture_output=True, text=True, check=True).stdout.split()]
+    assert sizes == [C.sizeof(_abi.EpConfig), C.sizeof(_abi.EpPotential), C.sizeof(_abi.EpSeries),
+                     C.sizeof(_abi.EpEnergies)]
+
+
 def test_library_exports_every_declared_symbol(lib):
     cdll, _ = lib
     missing = [s for s in header_symbols() if not hasattr(cdll, s)]
