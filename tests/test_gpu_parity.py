@@ -300,3 +300,35 @@ def test_fp32_mixed_radix_register_transforms_match_oracle(oracle, dims):
         g.run(3, 5e-4)
         o.run(3, 5e-4)
         assert rel(g.psi(), o.psi()) < 1e-4
+
+
+@pytest.mark.parametrize("prec", [_abi.EP_FP64, _abi.EP_FP32])
+def test_real_time_conserves_norm_and_energy_on_the_gpu(oracle, prec):
+    """The library's real-time evolution (no impurity, 24^3, 3 RK-Gill + 60
+    Hamming steps): the FP64 engine keeps the norm to 1e-12 and the energy
+    to 2e-5 like the oracle and tracks the oracle's state; the FP32 engine
+    keeps the norm to 1e-5 and the energy to 1e-4."""
+    n, xmax, n4 = 24, 12.0, 100.0
+
+    def cfg(p):
+        return ep.make_config(nx=n, ny=n, nz=n, xmax=xmax, ymax=xmax, zmax=xmax, icon=_abi.EP_ICON_PERIODIC,
+                              core="OTC", n4=n4, time_mode=_abi.EP_REAL_TIME, renormalize=0, precision=p)
+
+    psi = ep.woods_saxon_psi(n, n, n, xmax, xmax, xmax, n4, seed=5)
+    h3 = (2 * xmax / n) ** 3
+    out = []
+    for S, p in ((ep.Solver, prec), (oracle.OracleSolver, _abi.EP_FP64)):
+        with S(cfg(p)) as s:
+            s.start(psi)
+            e0 = s.energy()["etot"]
+            n0 = np.sum(np.abs(s.psi()) ** 2) * h3
+            for _ in range(3):
+                s.steprk(2e-4)
+            s.run(60, 2e-4)
+            s.poten()
+            out.append((e0, s.energy()["etot"], n0, np.sum(np.abs(s.psi()) ** 2) * h3, s.psi()))
+    (e0, e1, n0, n1, pg), (_, _, _, _, po) = out
+    ntol, etol = (1e-12, 2e-5) if prec == _abi.EP_FP64 else (1e-5, 1e-4)
+    assert abs(n1 - n0) < ntol * n0
+    assert abs(e1 - e0) < etol * abs(e0)
+    assert rel(pg, po) < (1e-10 if prec == _abi.EP_FP64 else 1e-4)
