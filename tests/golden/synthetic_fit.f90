@@ -19,6 +19,12 @@ ElseIf(Trim(selec).Eq.'Test_fit'.Or.   &
      Select_pot = V_test_fit(r)
    Endif
    Return
+ElseIf(Trim(selec).Eq.'Test_even')Then
+   Select_pot = V_test_even(r)
+   Return
+ElseIf(Trim(selec).Eq.'Test_exp')Then
+   Select_pot = V_test_exp(r)
+   Return
 Endif
 End Function Select_Pot
 Block Data Inicio_LJ_test_fit
@@ -67,3 +73,65 @@ Implicit None
 Real (Kind=8) :: r
 V_other = 1.d0/r
 End
+      Double Precision Function V_test_even(x)
+      Implicit Real*8(A-H,O-Z)
+      V_test_even=Func_test_even(x)
+      Return
+      End
+      Block Data Inicio_test_even
+      Implicit Real*8(A-H,O-Z)
+      Parameter(Npg=3)
+      Common/Param_test_even/r0,aa,bb,cc,Pg(Npg)
+      Data Pg/ -2.0D+03, 5.0D+04, -1.0D+05 /
+      Data r0/ 2.0D0/
+      Data aa/ 10.0D0/
+      Data bb/ -5.0D0/
+      Data cc/ 100.0D0/
+      End
+      Double Precision Function Func_test_even(x)
+      Parameter(Npg=3)
+      Implicit Real*8(A-H,O-Z)
+      Common/Param_test_even/r0,aa,bb,cc,Pg(Npg)
+      If(x.le.r0)Then
+        Func_test_even=aa*x**2+bb*x+cc
+        Return
+      Endif
+      Sto=0.0d0
+      Do k=1,Npg
+        Sto=Sto+pg(k)/x**(2*(k-1)+6)
+      EndDo
+      Func_test_even=Sto
+      Return
+      End
+      Block Data Inicio_test_exp
+      Implicit Real*8(A-H,O-Z)
+      Parameter(Npg=3)
+      Common/Param_test_exp/r0,aa,bb,cc,Pg(Npg),Ps(Npg)
+      Data Pg/ 3.0D+03, -1.0D+01, 2.0D-01 /
+      Data Ps/ 1.5D+00, 0.5D+00, 0.25D+00 /
+      Data r0/ 2.5D0/
+      Data aa/ 1.0D0/
+      Data bb/ 0.0D0/
+      Data cc/ 50.0D0/
+      End
+      Double Precision Function V_test_exp(xx)
+      Parameter(Npg=3)
+      Implicit Real*8(A-H,O-Z)
+      Common/Param_test_exp/r0,aa,bb,cc,Pg(Npg),Ps(Npg)
+      data x0/2.0d0/
+      If(xx.lt.x0)then
+        x=x0
+      Else
+         x=xx
+      Endif
+      If(x.le.r0)Then
+        V_test_exp=aa*x**2+bb*x+cc
+        Return
+      Endif
+      Sto=pg(1)*Dexp(-Ps(1)*x)/x
+      Do k=2,Npg
+        Sto=Sto+pg(k)*x**(k-1)*Dexp(-Ps(k)*x)
+      EndDo
+      V_test_exp=Sto
+      Return
+      End

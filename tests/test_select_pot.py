@@ -507,6 +507,26 @@ def test_reader_on_a_synthetic_source(lib):
         ep.select_pot("Other", 0.0, 0.0, SYNTHETIC)
 
 
+def test_reader_on_the_other_two_forms(lib, oracle):
+    """The synthetic file's even-power fit behind a forwarding function and
+    its exponential fit with the x0 clamp (the forms of 'Ba_plus_old_gs' and
+    'Cs_7s'), against their formulas."""
+    p = ep.select_pot("Test_even", 0.0, 0.0, SYNTHETIC)
+    assert p.kind == _abi.EP_POT_EVENPOW and p.series.contents.n == 3
+    x = np.linspace(1.0, 12.0, 200)
+    pg = [-2.0e3, 5.0e4, -1.0e5]
+    want = np.where(x <= 2.0, 10.0 * x ** 2 - 5.0 * x + 100.0, sum(c / x ** (2 * k + 6) for k, c in enumerate(pg)))
+    assert np.allclose(ep.potential_values(p, x), want, rtol=1e-14, atol=1e-13)
+    assert np.allclose(oracle.potential_values(p, x), want, rtol=1e-14, atol=1e-13)
+    p = ep.select_pot("Test_exp", 0.0, 0.0, SYNTHETIC)
+    assert p.kind == _abi.EP_POT_EXPFIT and p.series.contents.r_core == 2.0
+    xc = np.maximum(x, 2.0)
+    ser = 3.0e3 * np.exp(-1.5 * xc) / xc - 10.0 * xc * np.exp(-0.5 * xc) + 0.2 * xc ** 2 * np.exp(-0.25 * xc)
+    want = np.where(xc <= 2.5, xc ** 2 + 50.0, ser)
+    assert np.allclose(ep.potential_values(p, x), want, rtol=1e-13, atol=1e-12)
+    assert np.allclose(oracle.potential_values(p, x), want, rtol=1e-13, atol=1e-12)
+
+
 def test_reader_survives_damaged_sources(lib, tmp_path):
     """Cut or gapped copies of a source (the synthetic one, and the
     reference's where present) give a potential or EP_ERR_INVALID_ARG, never
