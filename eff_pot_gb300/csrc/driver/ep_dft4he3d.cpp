@@ -590,8 +590,8 @@ int main(int argc, char** argv) {
     const std::string prec = trim(in.get<std::string>("precision", "fp64"));
     cfg.precision = prec == "fp32" ? EP_FP32 : EP_FP64;
 
-    ep_ctx* ctx = nullptr;
-    check(ep_create(&cfg, &ctx), nullptr, "ep_create");
+    // the pair potentials first: a name the registry does not know stops the
+    // run before any device work
     ep_series fits[4] = {};
     const ep_potential ppi = potential_of(in, "pi", "Ba_plus_2D1", 1.05, 5.216077e4, &fits[0]);
     const ep_potential psg = potential_of(in, "sigma", "Ba_plus_2D0", 1.05, 9.674836e4, &fits[1]);
@@ -599,6 +599,8 @@ int main(int argc, char** argv) {
     const ep_potential pdl = cfg.state == EP_STATE_D
                                  ? potential_of(in, "delta", "Ba_plus_2D2", 1.05, 6.260015e4, &fits[3])
                                  : ep_potential{};
+    ep_ctx* ctx = nullptr;
+    check(ep_create(&cfg, &ctx), nullptr, "ep_create");
     auto set_potentials = [&](ep_ctx* x) {
       if (cfg.state == EP_STATE_D)
         check(ep_set_impurity_potentials_d(x, &ppi, &psg, &pdl, &ppl), x, "impurity potentials");

@@ -195,6 +195,22 @@ def test_driver_rejects_unknown_core_and_bad_namelist(driver, tmp_path):
     assert r.returncode == 1 and "Error in input master file" in r.stdout
 
 
+def test_driver_resolves_pair_potentials_before_the_gpu(driver, tmp_path):
+    """selec_* names go through Select_Pot's registry before any device
+    work: unknown names, fits without potentials_source and unknown names in
+    a given source stop the run with the registry's message."""
+    base = "&input deltat=1.d-4, selec_pi='Morse', selec_sigma='Morse', selec_plus='null', {} /\n"
+    r = drive(driver, tmp_path, base.format("selec_plus='No_such_pot'"))
+    assert r.returncode == 1 and "selec_plus='No_such_pot'" in r.stdout and "built in:" in r.stdout
+    r = drive(driver, tmp_path, base.format("selec_pi='Rb_gs_Fausto'"))
+    assert r.returncode == 1 and "give the V_impur.f90 source" in r.stdout
+    src = os.path.join(os.path.dirname(__file__), "golden", "synthetic_fit.f90")
+    r = drive(driver, tmp_path, base.format(f"selec_sigma='Other', potentials_source='{src}'"))
+    assert r.returncode == 1 and "is not an inverse-power fit" in r.stdout
+    r = drive(driver, tmp_path, base.format("potentials_source='/nonexistent/V_impur.f90', selec_pi='Test_fit'"))
+    assert r.returncode == 1 and "cannot read" in r.stdout
+
+
 def test_p_state_eigenvectors(harness):
     """The Jacobi eigen-solver of the P-state matrix V + (Als/2) SO
     (instates.f90:150-193): eigenpairs of the Hermitian matrix, Kramers
