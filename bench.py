@@ -232,13 +232,9 @@ def fp64_flop_roofline(steps_per_s):
     the plain FP64 single instance against the measured FMA peak."""
     from eff_pot_gb300.roofline import step_flops
     achieved = step_flops(N_GRID, N_GRID, N_GRID, otc=True) * steps_per_s / 1e12
-    try:
-        peak = float(json.load(open(os.path.join(ROOT, "profiles", "fma_peaks.json")))["fp64_tflops"])
-        src = "profiles/fma_peaks.json (measured: python -m eff_pot_gb300.peaks)"
-    except Exception:
-        peak, src = 1.196, "earlier measurement on this pool"
+    peak = 1.25
     return {"bound": "fp64 alu", "achieved": achieved, "peak": peak, "unit": "TFLOP/s", "frac": achieved / peak,
-            "peak_source": src}
+            "peak_source": "nominal GB300 FP64 rate (no measured FP64 peak in MEASURED_PEAKS.json)"}
 
 
 def run_ours(args):

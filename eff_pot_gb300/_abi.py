@@ -12,6 +12,8 @@ STATUS_NAMES = {
     4: "EP_ERR_OOM", 5: "EP_ERR_NONFINITE", 6: "EP_ERR_STATE",
     7: "EP_ERR_NO_DEVICE", 8: "EP_ERR_UNSUPPORTED", 9: "EP_ERR_TIMEOUT",
 }
+(EP_ERR_INVALID_ARG, EP_ERR_BAD_GRID, EP_ERR_CUDA, EP_ERR_OOM, EP_ERR_NONFINITE, EP_ERR_STATE,
+ EP_ERR_NO_DEVICE, EP_ERR_UNSUPPORTED, EP_ERR_TIMEOUT) = range(1, 10)
 EP_CORE_OT, EP_CORE_OTC, EP_CORE_OP = 0, 1, 2
 EP_IMAGINARY_TIME, EP_REAL_TIME = 0, 1
 EP_IMPURITY_NONE, EP_IMPURITY_FIXED, EP_IMPURITY_MOVING = 0, 1, 2

@@ -64,6 +64,24 @@ struct FftPlan {
   int rad[12];
 };
 
+// Radix sequence for n = 2^a 3^b 5^c: as many 8s as possible, a 4 or 2 for
+// the rest of the power of two (two 4s instead of 8*2), then 3s and 5s.
+inline bool make_plan(int n, FftPlan& p) {
+  p.n = n;
+  p.nst = 0;
+  int m = n, e = 0;
+  while (m % 2 == 0) { m /= 2; ++e; }
+  int n8 = e / 3, rem = e % 3;
+  if (rem == 1 && n8 > 0) { --n8; rem = 4; }
+  for (int i = 0; i < n8; ++i) p.rad[p.nst++] = 8;
+  if (rem == 4) { p.rad[p.nst++] = 4; p.rad[p.nst++] = 4; }
+  else if (rem == 2) p.rad[p.nst++] = 4;
+  else if (rem == 1) p.rad[p.nst++] = 2;
+  while (m % 3 == 0) { m /= 3; p.rad[p.nst++] = 3; }
+  while (m % 5 == 0) { m /= 5; p.rad[p.nst++] = 5; }
+  return m == 1 && p.nst <= 12;
+}
+
 // Geometry of a grid (passed by value to kernels).
 struct Geo {
   int nx, ny, nz, nxh;

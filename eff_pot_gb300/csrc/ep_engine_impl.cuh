@@ -58,24 +58,6 @@ inline int march_chunk(long long nxy, int nz, long long slots, int R) {
   return best;
 }
 
-// Radix sequence for n = 2^a 3^b 5^c: as many 8s as possible, a 4 or 2 for
-// the rest of the power of two (two 4s instead of 8*2), then 3s and 5s.
-inline bool make_plan(int n, FftPlan& p) {
-  p.n = n;
-  p.nst = 0;
-  int m = n, e = 0;
-  while (m % 2 == 0) { m /= 2; ++e; }
-  int n8 = e / 3, rem = e % 3;
-  if (rem == 1 && n8 > 0) { --n8; rem = 4; }
-  for (int i = 0; i < n8; ++i) p.rad[p.nst++] = 8;
-  if (rem == 4) { p.rad[p.nst++] = 4; p.rad[p.nst++] = 4; }
-  else if (rem == 2) p.rad[p.nst++] = 4;
-  else if (rem == 1) p.rad[p.nst++] = 2;
-  while (m % 3 == 0) { m /= 3; p.rad[p.nst++] = 3; }
-  while (m % 5 == 0) { m /= 5; p.rad[p.nst++] = 5; }
-  return m == 1 && p.nst <= 12;
-}
-
 // Central-row weights of the (2R+1)-point stencils (closed forms of the
 // Bickley/Lagrange coefficients), at +k.
 inline void fd_weights(int R, long double* w1, long double* w2) {
@@ -318,7 +300,9 @@ int Engine<T>::init(const ep_config& c, cudaStream_t s, Prof* p, ImpState* im, s
     const long long nxy = (long long)((c.nx + EP_TX - 1) / EP_TX) * ((c.ny + EP_TY - 1) / EP_TY);
     const int zmin = std::min(zc_pc, zc_rk);
     const long long nbs = nxy * ((c.nz + zmin - 1) / zmin);
-    npartials = std::max(nbs * 4, (long long)EP_RED_BLOCKS * 18);
+    // block partials are compensated (hi, lo) pairs: the hi parts of a
+    // reduction's nblocks*nq sums, then their lo parts
+    npartials = 2 * std::max(nbs * 4, (long long)EP_RED_BLOCKS * 18);
     if ((r = alloc((void**)&partials, npartials * sizeof(double)))) return r;
   }
   return cuda_ok(cudaStreamSynchronize(st), "init");

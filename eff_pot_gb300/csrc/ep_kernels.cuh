@@ -3,6 +3,7 @@
 #pragma once
 #include "ep_common.cuh"
 #include "ep_fft.cuh"
+#include "ep_reduce.cuh"
 #include "ep_pairpot.h"
 
 // ---------------------------------------------------------------------------
@@ -166,143 +167,6 @@ template <class T>
 EP_DEV T hexp_t(const Phys& ph, C2<T> psi, C2<T> H) {
   if (ph.time_mode == 1) return -psi.x * H.y + psi.y * H.x;
   return -(psi.x * H.x + psi.y * H.y);
-}
-
-// Per-thread accumulator: FP64 sums for FP64 fields; compensated (Kahan)
-// FP32 sums for FP32 fields, widened to FP64 once per thread.
-template <class T> struct Acc {
-  double s = 0.0;
-  EP_DEV void add(T v) { s += (double)v; }
-  EP_DEV double get() const { return s; }
-};
-template <> struct Acc<float> {
-  float s = 0.f, c = 0.f;
-  EP_DEV void add(float v) {
-    const float y = v - c;
-    const float t = s + y;
-    c = (t - s) - y;
-    s = t;
-  }
-  EP_DEV double get() const { return (double)s - (double)c; }
-};
-
-EP_DEV void neu_add_d(double& s, double& c, double v) {
-  const double t = s + v;
-  if (fabs(s) >= fabs(v)) c += (s - t) + v; else c += (v - t) + s;
-  s = t;
-}
-
-// Sum of block partials (fixed order, compensated) by one block of 256
-// threads -> sc->sums[out0 + q]; mode 1: corrector epilogue (norm, mu,
-// renormalisation factor), mode 2: norm only.
-EP_DEV void finalize_block(const double* partials, int nblocks, int nq, DevScalars* sc, int out0, int mode,
-                           double N, double dxyz, double n4, int renorm, int stats = 1) {
-  __shared__ double ss[256];
-  const int tid = threadIdx.x + blockDim.x * threadIdx.y;
-  const int nth = blockDim.x * blockDim.y;
-  // partials are already FP64 block sums: a fixed-order pairwise tree keeps
-  // the relative error near log2(nblocks) ulp with few FP64 operations
-  for (int q = 0; q < nq; ++q) {
-    double s = 0.0;
-    for (int b = tid; b < nblocks; b += nth) s += __ldcg(partials + (long long)b * nq + q);
-    ss[tid] = s;
-    __syncthreads();
-    for (int off = nth / 2; off > 0; off >>= 1) {
-      if (tid < off) ss[tid] += ss[tid + off];
-      __syncthreads();
-    }
-    if (tid == 0) sc->sums[out0 + q] = ss[0];
-    __syncthreads();
-  }
-  if (tid == 0) {
-    bool bad = false;
-    for (int q = 0; q < nq; ++q) bad |= !isfinite(sc->sums[out0 + q]);
-    if (mode == 1) {
-      const double norm = sc->sums[out0 + 1] * dxyz;
-      sc->norm = norm;
-      if (stats) {
-        sc->mu = sc->sums[out0 + 2] / sc->sums[out0 + 3];
-        sc->errHe = sc->sums[out0] / N;
-      }
-      sc->scale = (renorm && norm > 0.0) ? sqrt(n4 / norm) : 1.0;
-    } else if (mode == 2) {
-      const double norm = sc->sums[out0] * dxyz;
-      sc->norm = norm;
-      sc->scale = norm > 0.0 ? sqrt(n4 / norm) : 1.0;
-      bad |= !(norm > 0.0);
-    }
-    if (bad) atomicOr(&sc->flags, (unsigned)EP_FLAG_NONFINITE);
-  }
-}
-
-// Block reduction of NQ doubles into partials[block * NQ + q].
-template <int NQ>
-EP_DEV void block_reduce_store(double (&v)[NQ], double* __restrict__ partials) {
-  __shared__ double red[NQ][32];
-  const int tid = threadIdx.x + blockDim.x * (threadIdx.y + blockDim.y * threadIdx.z);
-  const int nth = blockDim.x * blockDim.y * blockDim.z;
-  const int lane = tid & 31, warp = tid >> 5, nw = (nth + 31) >> 5;
-#pragma unroll
-  for (int q = 0; q < NQ; ++q) {
-    double s = v[q];
-    for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
-    if (lane == 0) red[q][warp] = s;
-  }
-  __syncthreads();
-  if (warp == 0) {
-#pragma unroll
-    for (int q = 0; q < NQ; ++q) {
-      double s = lane < nw ? red[q][lane] : 0.0;
-      for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
-      if (lane == 0) {
-        const long long b = blockIdx.x + (long long)gridDim.x * (blockIdx.y + (long long)gridDim.y * blockIdx.z);
-        partials[b * NQ + q] = s;
-      }
-    }
-  }
-}
-
-// Block reduction of per-thread accumulators into partials[block * NQ + q].
-// FP32 accumulators (s, c) are summed across the warp as unevaluated pairs
-// with the error-free two-sum, so only one lane per warp widens to FP64
-// (the FP64 pipe is ~1/64 of the FP32 rate here).
-template <int NQ>
-EP_DEV void block_reduce_store_acc(Acc<double> (&acc)[NQ], double* __restrict__ partials) {
-  double v[NQ];
-#pragma unroll
-  for (int q = 0; q < NQ; ++q) v[q] = acc[q].get();
-  block_reduce_store<NQ>(v, partials);
-}
-template <int NQ>
-EP_DEV void block_reduce_store_acc(Acc<float> (&acc)[NQ], double* __restrict__ partials) {
-  __shared__ double red[NQ][32];
-  const int tid = threadIdx.x + blockDim.x * (threadIdx.y + blockDim.y * threadIdx.z);
-  const int nth = blockDim.x * blockDim.y * blockDim.z;
-  const int lane = tid & 31, warp = tid >> 5, nw = (nth + 31) >> 5;
-#pragma unroll
-  for (int q = 0; q < NQ; ++q) {
-    float hi = acc[q].s, lo = -acc[q].c;
-    for (int o = 16; o > 0; o >>= 1) {
-      const float h2 = __shfl_down_sync(0xffffffffu, hi, o), l2 = __shfl_down_sync(0xffffffffu, lo, o);
-      const float t = hi + h2, bb = t - hi;
-      const float e = (hi - (t - bb)) + (h2 - bb);
-      hi = t;
-      lo = (lo + l2) + e;
-    }
-    if (lane == 0) red[q][warp] = (double)hi + (double)lo;
-  }
-  __syncthreads();
-  if (warp == 0) {
-#pragma unroll
-    for (int q = 0; q < NQ; ++q) {
-      double s = lane < nw ? red[q][lane] : 0.0;
-      for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
-      if (lane == 0) {
-        const long long b = blockIdx.x + (long long)gridDim.x * (blockIdx.y + (long long)gridDim.y * blockIdx.z);
-        partials[b * NQ + q] = s;
-      }
-    }
-  }
 }
 
 // ---------------------------------------------------------------------------

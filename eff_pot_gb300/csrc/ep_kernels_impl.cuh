@@ -6,6 +6,15 @@
 // Grid coordinate -xmax + h*i without contraction (x(i) of DFT4He3d.f90:248-256).
 EP_DEV double coord(double xmax, double h, int i) { return __dadd_rn(-xmax, __dmul_rn(h, (double)i)); }
 
+// |x - r_imp|^2 in potenimp.f90's order (zt = z^2, yt = y^2 + zt, x^2 + yt)
+// without contraction: the table index int(1.5 + r/h) of update() then falls
+// on the same side of a node as in an uncontracted FP64 evaluation (an FMA
+// here moves r by an ulp, and where r/h sits on a node the parabola switches
+// to the neighbouring three table points, a 1e-9 relative change of u_imp).
+EP_DEV double rr2_nc(double xx, double yy, double zz) {
+  return __dadd_rn(__dmul_rn(xx, xx), __dadd_rn(__dmul_rn(yy, yy), __dmul_rn(zz, zz)));
+}
+
 EP_DEV void idx3(const Geo& g, long long p, int& ix, int& iy, int& iz) {
   ix = (int)(p % g.nx);
   const long long r = p / g.nx;
@@ -49,9 +58,7 @@ __global__ void k_potenimp(Geo g, double xmax, double ymax, double zmax, double 
     const double xx = coord(xmax, hx, ix) - r0;
     const double yy = coord(ymax, hy, iy) - r1;
     const double zz = coord(zmax, hz, iz) - r2;
-    const double zt = zz * zz;
-    const double yt = yy * yy + zt;
-    const double rr2 = xx * xx + yt;
+    const double rr2 = rr2_nc(xx, yy, zz);
     const double r = sqrt(rr2);
     const double vp = interp_update(r, npot, rmax, potpi);
     const double dl = r > 1e-3 ? interp_update(r, npot, rmax, potdel) / rr2 : umax_sigma;
@@ -105,9 +112,7 @@ __global__ void k_potenimp_d(Geo g, double xmax, double ymax, double zmax, doubl
     const double xx = coord(xmax, hx, ix) - r0;
     const double yy = coord(ymax, hy, iy) - r1;
     const double zz = coord(zmax, hz, iz) - r2;
-    const double zt = zz * zz;
-    const double yt = yy * yy + zt;
-    const double rr2 = xx * xx + yt;
+    const double rr2 = rr2_nc(xx, yy, zz);
     const double r4 = rr2 * rr2;
     const double r = sqrt(rr2);
     const double dl = interp_update(r, npot, rmax, potdel);
@@ -142,16 +147,14 @@ __global__ void k_impmoments_d(Geo g, const T* __restrict__ den, const T* __rest
                                const T* __restrict__ sigdel, double xmax, double ymax, double zmax, double hx,
                                double hy, double hz, double r0, double r1, double r2, int izlo, int izhi,
                                double* __restrict__ partials) {
-  double acc[18];
-#pragma unroll
-  for (int q = 0; q < 18; ++q) acc[q] = 0.0;
+  Acc<double> acc[18];
   for (long long p = blockIdx.x * (long long)blockDim.x + threadIdx.x; p < g.N; p += (long long)gridDim.x * blockDim.x) {
     int ix, iy, iz;
     idx3(g, p, ix, iy, iz);
     const double u = uimp[p];
-    acc[0] += (double)dxd[p] * u;
-    acc[1] += (double)dyd[p] * u;
-    if (iz >= izlo && iz < izhi) acc[2] += (double)dzd[p] * u;
+    acc[0].add((double)dxd[p] * u);
+    acc[1].add((double)dyd[p] * u);
+    if (iz >= izlo && iz < izhi) acc[2].add((double)dzd[p] * u);
     const double xx = coord(xmax, hx, ix) - r0, yy = coord(ymax, hy, iy) - r1, zz = coord(zmax, hz, iz) - r2;
     const double rho = den[p];
     const double dvd = (double)delta[p] * rho, dv1 = (double)pidel[p] * rho, dv2 = (double)sigdel[p] * rho;
@@ -161,9 +164,9 @@ __global__ void k_impmoments_d(Geo g, const T* __restrict__ den, const T* __rest
 #pragma unroll
     for (int i = 0; i < 5; ++i)
 #pragma unroll
-      for (int j = i; j < 5; ++j, ++k) acc[3 + k] += P[k] * dv2 + a[i] * a[j] * dv1 + (i == j ? dvd : 0.0);
+      for (int j = i; j < 5; ++j, ++k) acc[3 + k].add(P[k] * dv2 + a[i] * a[j] * dv1 + (i == j ? dvd : 0.0));
   }
-  block_reduce_store<18>(acc, partials);
+  block_reduce_store_acc<18>(acc, partials);
 }
 
 // FP32 engine, P state: the impurity field in FP32 arithmetic (float tables,
@@ -239,12 +242,12 @@ static __global__ void k_impmoments_f(Geo g, const float* __restrict__ den, cons
 // Sum of |psi|^2 (block partials).
 template <class T>
 __global__ void k_normsum(const C2<T>* __restrict__ psi, long long N, double* __restrict__ partials) {
-  double acc[1] = {0.0};
+  Acc<double> acc[1];
   for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < N; i += (long long)gridDim.x * blockDim.x) {
     const C2<T> v = psi[i];
-    acc[0] += (double)v.x * v.x + (double)v.y * v.y;
+    acc[0].add((double)v.x * v.x + (double)v.y * v.y);
   }
-  block_reduce_store<1>(acc, partials);
+  block_reduce_store_acc<1>(acc, partials);
 }
 
 // Complex first derivative from global memory.
@@ -272,7 +275,7 @@ __global__ void k_energy(Geo g, FdW<T> fd, Phys ph, const C2<T>* __restrict__ ps
                          const T* __restrict__ uimp, double xmax, double ymax, double zmax, double hx, double hy,
                          double hz, double r0, double r1, double r2, double zexc, const __grid_constant__ PotDev vplus,
                          int impurity, double* __restrict__ partials) {
-  double acc[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+  Acc<double> acc[8];
   const bool otc = ph.core == 1;
   const double aux1 = 0.5 * ph.cp4, aux2 = (1.0 / 3.0) * ph.cpp4;
   for (long long p = blockIdx.x * (long long)blockDim.x + threadIdx.x; p < g.N; p += (long long)gridDim.x * blockDim.x) {
@@ -282,24 +285,24 @@ __global__ void k_energy(Geo g, FdW<T> fd, Phys ph, const C2<T>* __restrict__ ps
     const C2<T> dy = d1c_global(psi, p, iy, g.ny, (long long)g.nx, fd.w1[1], fd.R, fd.periodic);
     const C2<T> dz = d1c_global(psi, p, iz, g.nz, (long long)g.nx * g.ny, fd.w1[2], fd.R, fd.periodic);
     const double dn = den[p], cg = dencg[p];
-    acc[0] += ((double)dx.x * dx.x + (double)dx.y * dx.y) + ((double)dy.x * dy.x + (double)dy.y * dy.y) +
-              ((double)dz.x * dz.x + (double)dz.y * dz.y);
-    acc[1] += (double)delj4[p] * dn;
-    acc[2] += dn * (cg * cg) * (aux1 + aux2 * cg);
+    acc[0].add(((double)dx.x * dx.x + (double)dx.y * dx.y) + ((double)dy.x * dy.x + (double)dy.y * dy.y) +
+               ((double)dz.x * dz.x + (double)dz.y * dz.y));
+    acc[1].add((double)delj4[p] * dn);
+    acc[2].add(dn * (cg * cg) * (aux1 + aux2 * cg));
     if (otc)
-      acc[3] += (double)falfs[p] * ((double)dxd[p] * ix_[p] + (double)dyd[p] * iy_[p] + (double)dzd[p] * iz_[p]);
-    acc[4] += dn * (1.0 + tanh(ph.beta * (dn - ph.den_m)));
+      acc[3].add((double)falfs[p] * ((double)dxd[p] * ix_[p] + (double)dyd[p] * iy_[p] + (double)dzd[p] * iz_[p]));
+    acc[4].add(dn * (1.0 + tanh(ph.beta * (dn - ph.den_m))));
     if (impurity) {
       const double a = r0 - coord(xmax, hx, ix), b = r1 - coord(ymax, hy, iy), c = r2 - coord(zmax, hz, iz);
-      const double r = sqrt(a * a + b * b + c * c);
+      const double r = sqrt(__dadd_rn(__dadd_rn(__dmul_rn(a, a), __dmul_rn(b, b)), __dmul_rn(c, c)));
       if (r >= zexc) {
-        acc[5] += dn * (double)uimp[p];
-        acc[6] += dn * pot_eval(vplus, r);
+        acc[5].add(dn * (double)uimp[p]);
+        acc[6].add(dn * pot_eval(vplus, r));
       }
     }
-    acc[7] += dn;
+    acc[7].add(dn);
   }
-  block_reduce_store<8>(acc, partials);
+  block_reduce_store_acc<8>(acc, partials);
 }
 
 template <class T>
@@ -308,24 +311,24 @@ __global__ void k_impmoments(Geo g, const T* __restrict__ den, const T* __restri
                              const T* __restrict__ vpi, const T* __restrict__ delta, double xmax, double ymax,
                              double zmax, double hx, double hy, double hz, double r0, double r1, double r2,
                              int izlo, int izhi, double* __restrict__ partials) {
-  double acc[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
+  Acc<double> acc[9];
   for (long long p = blockIdx.x * (long long)blockDim.x + threadIdx.x; p < g.N; p += (long long)gridDim.x * blockDim.x) {
     int ix, iy, iz;
     idx3(g, p, ix, iy, iz);
     const double u = uimp[p];
-    acc[0] += (double)dxd[p] * u;
-    acc[1] += (double)dyd[p] * u;
-    if (iz >= izlo && iz < izhi) acc[2] += (double)dzd[p] * u;
+    acc[0].add((double)dxd[p] * u);
+    acc[1].add((double)dyd[p] * u);
+    if (iz >= izlo && iz < izhi) acc[2].add((double)dzd[p] * u);
     const double xx = coord(xmax, hx, ix) - r0, yy = coord(ymax, hy, iy) - r1, zz = coord(zmax, hz, iz) - r2;
     const double a1 = den[p], a2 = delta[p], a3 = vpi[p];
-    acc[3] += a1 * (a2 * xx * xx + a3);
-    acc[4] += a1 * a2 * xx * yy;
-    acc[5] += a1 * a2 * xx * zz;
-    acc[6] += a1 * (a2 * yy * yy + a3);
-    acc[7] += a1 * a2 * yy * zz;
-    acc[8] += a1 * (a2 * zz * zz + a3);
+    acc[3].add(a1 * (a2 * xx * xx + a3));
+    acc[4].add(a1 * a2 * xx * yy);
+    acc[5].add(a1 * a2 * xx * zz);
+    acc[6].add(a1 * (a2 * yy * yy + a3));
+    acc[7].add(a1 * a2 * yy * zz);
+    acc[8].add(a1 * (a2 * zz * zz + a3));
   }
-  block_reduce_store<9>(acc, partials);
+  block_reduce_store_acc<9>(acc, partials);
 }
 
 // ---------------------------------------------------------------------------

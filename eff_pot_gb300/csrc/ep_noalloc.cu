@@ -35,28 +35,14 @@ constexpr int kMaxDevices = 64;
 std::mutex g_setup_mutex;
 double2* g_scratch_addr[kMaxDevices] = {};
 
+// n >= 2 with no prime factor other than 2, 3 and 5 (any length; the
+// scratch limit on the length is checked apart).
 bool axis_ok(int n) {
-  if (n < 2 || n > kMaxAxis) return false;
+  if (n < 2) return false;
   while (n % 2 == 0) n /= 2;
   while (n % 3 == 0) n /= 3;
   while (n % 5 == 0) n /= 5;
   return n == 1;
-}
-
-bool plan_for(int n, FftPlan& p) {
-  p.n = n;
-  p.nst = 0;
-  int m = n, e = 0;
-  while (m % 2 == 0) { m /= 2; ++e; }
-  int n8 = e / 3, rem = e % 3;
-  if (rem == 1 && n8 > 0) { --n8; rem = 4; }
-  for (int i = 0; i < n8; ++i) p.rad[p.nst++] = 8;
-  if (rem == 4) { p.rad[p.nst++] = 4; p.rad[p.nst++] = 4; }
-  else if (rem == 2) p.rad[p.nst++] = 4;
-  else if (rem == 1) p.rad[p.nst++] = 2;
-  while (m % 3 == 0) { m /= 3; p.rad[p.nst++] = 3; }
-  while (m % 5 == 0) { m /= 5; p.rad[p.nst++] = 5; }
-  return m == 1;
 }
 
 // Roots exp(-2 pi i k / n), k < n.
@@ -124,7 +110,7 @@ extern "C" int ep_convolve_noalloc(const double* d_in, const double* d_kernel, d
   if (!d_in || !d_kernel || !d_out) return EP_ERR_INVALID_ARG;
   if (nx % 2 || !axis_ok(nx) || !axis_ok(ny) || !axis_ok(nz)) return EP_ERR_BAD_GRID;
   const long long half = (long long)(nx / 2 + 1) * ny * nz;
-  if (half > kMaxHalf) return EP_ERR_UNSUPPORTED;
+  if (half > kMaxHalf || nx > kMaxAxis || ny > kMaxAxis || nz > kMaxAxis) return EP_ERR_UNSUPPORTED;
   int dev = 0;
   if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kMaxDevices) {
     cudaGetLastError();
@@ -140,9 +126,9 @@ extern "C" int ep_convolve_noalloc(const double* d_in, const double* d_kernel, d
   double2* twy = twx + kMaxAxis;
   double2* twz = twy + kMaxAxis;
   FftPlan p2{}, pY{}, pZ{};
-  plan_for(nx / 2, p2);
-  plan_for(ny, pY);
-  plan_for(nz, pZ);
+  make_plan(nx / 2, p2);
+  make_plan(ny, pY);
+  make_plan(nz, pZ);
   Geo g{nx, ny, nz, nx / 2 + 1, (long long)nx * ny * nz, half};
   k_noalloc_twiddles<<<1, 320, 0, st>>>(twx, nx);
   k_noalloc_twiddles<<<1, 320, 0, st>>>(twy, ny);

@@ -4,9 +4,11 @@ Reads the DATA statements of BLOCK DATA BLKDS in the reference's
 src/mates.f (COMMON /SDERA/ A(25792), layout unpacked by NEWDER ICON=1,
 newder.f:84-127) and writes, for every odd M = 3..25 and derivative order
 K = 1, 2, the M weights of the central row as the table's 25-digit decimal
-strings.  Run here, where the reference is mounted:
+strings.  Run where the reference is checked out (the path defaults to
+$EP_REFERENCE_ROOT/src/mates.f, else to a "reference" directory beside this
+repository):
 
-    python tests/golden/make_fd_fixture.py /root/reference/src/mates.f
+    python tests/golden/make_fd_fixture.py [path/to/src/mates.f]
 """
 import json
 import os
@@ -62,7 +64,9 @@ def central_row(A, M, K):
 
 
 def main():
-    path = sys.argv[1] if len(sys.argv) > 1 else "/root/reference/src/mates.f"
+    root = os.environ.get("EP_REFERENCE_ROOT") or os.path.join(os.path.dirname(os.path.dirname(HERE)), "..",
+                                                                "reference")
+    path = sys.argv[1] if len(sys.argv) > 1 else os.path.join(root, "src", "mates.f")
     A = parse(path)
     out = {}
     for M in range(3, 26, 2):

@@ -101,3 +101,20 @@ def test_widened_grid_validator_accepts_320(lib):
     if st == a.EP_OK:
         f["destroy"](h)
     assert st in (a.EP_OK, 7)  # 7: no device on this host
+
+
+def test_noalloc_grid_checks_come_before_any_device_work(lib):
+    """ep_convolve_noalloc refuses grids on the host: sizes past its fixed
+    scratch (a half spectrum above 33*64*64, an axis above 320) with
+    EP_ERR_UNSUPPORTED, odd nx or prime factors other than 2, 3, 5 with
+    EP_ERR_BAD_GRID, null buffers with EP_ERR_INVALID_ARG.  The pointers are
+    never dereferenced on these paths."""
+    _, f = lib
+    p = 4096  # a dummy address: refused calls touch no memory
+    assert f["convolve_noalloc"](p, p, p, 128, 128, 128, None) == _abi.EP_ERR_UNSUPPORTED
+    assert f["convolve_noalloc"](p, p, p, 32, 384, 8, None) == _abi.EP_ERR_UNSUPPORTED
+    assert f["convolve_noalloc"](p, p, p, 640, 2, 2, None) == _abi.EP_ERR_UNSUPPORTED
+    assert f["convolve_noalloc"](p, p, p, 33, 24, 40, None) == _abi.EP_ERR_BAD_GRID
+    assert f["convolve_noalloc"](p, p, p, 32, 28, 40, None) == _abi.EP_ERR_BAD_GRID
+    assert f["convolve_noalloc"](p, p, p, 32, 24, 0, None) == _abi.EP_ERR_BAD_GRID
+    assert f["convolve_noalloc"](None, p, p, 32, 24, 40, None) == _abi.EP_ERR_INVALID_ARG

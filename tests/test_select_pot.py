@@ -25,7 +25,11 @@ import pytest
 import eff_pot_gb300 as ep
 from eff_pot_gb300 import _abi
 
-SOURCE = "/root/reference/src/V_impur.f90"
+# The reference checkout: $EP_REFERENCE_ROOT, else a "reference" directory
+# beside this repository.  Tests that read its V_impur.f90 skip without it.
+REFERENCE_ROOT = os.environ.get("EP_REFERENCE_ROOT") or os.path.join(
+    os.path.dirname(os.path.dirname(os.path.dirname(os.path.abspath(__file__)))), "reference")
+SOURCE = os.path.join(REFERENCE_ROOT, "src", "V_impur.f90")
 BOHR_PATIL, K_PATIL = 0.529177249, 11604.448 * 27.211608
 
 
