@@ -1248,7 +1248,7 @@ __global__ void __launch_bounds__(EP_TX* EP_TY, sizeof(T) == 4 ? 3 : 2) k_correc
   extern __shared__ __align__(16) unsigned char smraw[];
   constexpr int NT = EP_TX * EP_TY;
   const HCoef<T> hc(ph);
-  Acc<T> acc[4];
+  Kahan<T> acc[4];
   // buffer scales folded into the method's coefficients once per thread:
   // p5 = (9 s3 po3 - s2o po2 + f3 (H + 2 s1 h1 - s2 h2)) / 8
   const T k3 = T(1.125) * bscale_of<T>(sc, sl.a), k2o = T(0.125) * bscale_of<T>(sc, sl.b), kH = T(0.125) * f3,
@@ -1273,7 +1273,9 @@ __global__ void __launch_bounds__(EP_TX* EP_TY, sizeof(T) == 4 ? 3 : 2) k_correc
       acc[3].add(c.x * c.x + c.y * c.y);
     }
   });
-  block_reduce_store_acc<4>(acc, partials);
+  // without STATS only the norm (q = 1) is reduced and finalised
+  constexpr unsigned QM = STATS ? 0xFu : 0x2u;
+  block_reduce_store_acc<4, QM>(acc, partials);
   // The last block to finish sums all partials (no block waits for another).
   __shared__ bool last;
   const int tid = threadIdx.x + blockDim.x * threadIdx.y;
@@ -1285,7 +1287,7 @@ __global__ void __launch_bounds__(EP_TX* EP_TY, sizeof(T) == 4 ? 3 : 2) k_correc
   __syncthreads();
   if (last) {
     __threadfence();
-    finalize_block(partials, (int)nb, 4, sc, 0, 1, (double)g.N, ph.dxyz, n4, renorm, STATS ? 1 : 0);
+    finalize_block(partials, (int)nb, 4, sc, 0, 1, (double)g.N, ph.dxyz, n4, renorm, STATS ? 1 : 0, QM);
     if (tid == 0) {
       // renormalise lazily: every logical state value is multiplied by s;
       // the buffers written here restart their scale at s

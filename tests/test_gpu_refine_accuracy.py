@@ -1,0 +1,42 @@
+"""FP32 + FP64 refinement against the plain FP64 path at 128^3.
+
+The single droplet + impurity workload (N=1000 on a 128^3 grid, h = 0.4 A,
+Morse impurity fixed at the centre, OTC, imaginary time, dt = 1e-4) runs
+5000 steps twice from the same seeded state: plain FP64 throughout, and
+4800 FP32 steps followed by 200 FP64 refinement sweeps.  The pure droplet
+(no impurity) is run the same two ways.  At equal imaginary time the two
+paths must agree to 1e-8 relative in the total energy, and the impurity
+solvation energy E(droplet + X) - E(droplet) (energy.f90:146-165; the
+effective-potential scan's quantity) to 1e-4 K.  The FP64 path itself is
+checked against the oracle on this geometry in test_gpu_parity_configs.py.
+"""
+import pytest
+
+import eff_pot_gb300 as ep
+from eff_pot_gb300 import scan
+from eff_pot_gb300.build import build
+
+pytestmark = pytest.mark.gpu
+
+STEPS, REFINE, DT = 5000, 200, 1e-4
+
+
+def test_fp32_refine_matches_fp64_at_equal_imaginary_time():
+    build()
+    ep.load_library()
+    inst = [(scan.PURE, None), ("X", 0.0)]
+    psi = ep.woods_saxon_psi(128, 128, 128, 25.6, 25.6, 25.6, 1000.0, seed=1)
+    kw = dict(dt=DT, pot=ep.morse(10.0, 4.5, 1.2), make_batch=ep.Batch,
+              cfg_of=lambda z, p: scan.scan_config(z, p))
+    e32 = scan.run_instances(inst, psi, precision="fp32", steps32=STEPS - REFINE, steps64=REFINE, **kw)
+    e64 = scan.run_instances(inst, psi, precision="fp64", steps32=STEPS - REFINE, steps64=REFINE, **kw)
+    rel = {k: abs(e32[k]["etot"] - e64[k]["etot"]) / abs(e64[k]["etot"]) for k in e64}
+    solv32 = e32["X"]["etot"] - e32[scan.PURE]["etot"]
+    solv64 = e64["X"]["etot"] - e64[scan.PURE]["etot"]
+    print(f"REFINE128 E_X fp64 {e64['X']['etot']:.12f} fp32+refine {e32['X']['etot']:.12f} rel {rel['X']:.2e}; "
+          f"E_pure fp64 {e64[scan.PURE]['etot']:.12f} fp32+refine {e32[scan.PURE]['etot']:.12f} "
+          f"rel {rel[scan.PURE]:.2e}; solvation fp64 {solv64:.9f} K fp32+refine {solv32:.9f} K "
+          f"diff {solv32 - solv64:.3e} K")
+    for k, v in rel.items():
+        assert v < 1e-8, (k, v)
+    assert abs(solv32 - solv64) < 1e-4
