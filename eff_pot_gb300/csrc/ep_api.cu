@@ -6,6 +6,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <array>
 #include <cmath>
 #include <cstring>
 #include <string>
@@ -25,6 +26,10 @@ struct StepGraph {
   std::vector<const void*> engine;
   std::vector<int> gen;
   std::vector<long long> launches;  // kernels per replay, per context
+  // multi-step graphs: steps per replay, and each context's next-step
+  // buffers when the capture began (the replay is valid at that phase only)
+  int nsteps = 1;
+  std::vector<std::array<const void*, 7>> sig0;
   void reset() {
     if (exec) cudaGraphExecDestroy(exec);
     if (graph) cudaGraphDestroy(graph);
@@ -34,11 +39,14 @@ struct StepGraph {
     engine.clear();
     gen.clear();
     launches.clear();
+    sig0.clear();
+    nsteps = 1;
   }
 };
 
 struct ep_ctx {
   StepGraph graph;
+  StepGraph graphk;  // one rotation period of steps
   bool use_graphs = true;
   ep_config cfg{};
   cudaStream_t st = nullptr;
@@ -53,6 +61,7 @@ struct ep_ctx {
 
 struct ep_batch {
   StepGraph graph;
+  StepGraph graphk;  // one rotation period of steps
   bool use_graphs = true;
   std::vector<ep_ctx*> ctx;
   cudaStream_t st = nullptr;
@@ -204,6 +213,123 @@ int replay_step(StepGraph& G, const std::vector<ep_ctx*>& cs, cudaStream_t st, d
   return cudaGraphLaunch(G.exec, st) == cudaSuccess ? EP_OK : EP_ERR_CUDA;
 }
 
+// ---------------------------------------------------------------------------
+// Multi-step graphs.  The buffers a step reads and writes repeat after a
+// fixed number of steps (the history rotation: 10 for steppc), so that many
+// consecutive steps of every context are captured once and replayed with no
+// node updates at all; after a replay the host applies the same number of
+// buffer rotations.  A replay is valid only at the phase of the rotation
+// where it was captured; single steps realign the phase.
+std::array<const void*, 7> signature_of(ep_ctx* c) {
+  std::array<const void*, 7> a{};
+  dispatch(c, [&](auto& e) -> int {
+    const void* s[7];
+    e.step_signature(s);
+    for (int k = 0; k < 7; ++k) a[k] = s[k];
+    return EP_OK;
+  });
+  return a;
+}
+int common_period(const std::vector<ep_ctx*>& cs) {
+  int P = 0;
+  for (ep_ctx* c : cs) {
+    const int p = dispatch(c, [](auto& e) -> int { return e.rotation_period(); });
+    if (p <= 0) return 0;
+    if (P == 0) P = p;
+    else if (P != p) return 0;
+  }
+  return P;
+}
+bool at_phase(const StepGraph& G, const std::vector<ep_ctx*>& cs) {
+  if (G.sig0.size() != cs.size()) return false;
+  for (size_t i = 0; i < cs.size(); ++i)
+    if (signature_of(cs[i]) != G.sig0[i]) return false;
+  return true;
+}
+int capture_steps(StepGraph& G, const std::vector<ep_ctx*>& cs, cudaStream_t st, ep_batch* b, double dt, int P) {
+  G.reset();
+  const size_t n = cs.size();
+  G.engine.assign(n, nullptr);
+  G.gen.assign(n, 0);
+  G.launches.assign(n, 0);
+  G.sig0.resize(n);
+  for (size_t i = 0; i < n; ++i) G.sig0[i] = signature_of(cs[i]);
+  if (cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal) != cudaSuccess) return EP_ERR_CUDA;
+  if (b) batch_fork(b);
+  int r = EP_OK;
+  for (int p = 0; p < P && !r; ++p) {  // step-major: the contexts' kernels overlap
+    for (size_t i = 0; i < n && !r; ++i) {
+      ep_ctx* c = cs[i];
+      const long long l0 = c->prof.launches;
+      r = dispatch(c, [&](auto& e) -> int { return e.steppc(dt, nullptr); });
+      G.launches[i] += c->prof.launches - l0;
+    }
+  }
+  for (size_t i = 0; i < n; ++i) {
+    G.engine[i] = engine_of(cs[i]);
+    G.gen[i] = gen_of(cs[i]);
+  }
+  if (b && !r) batch_join(b);
+  cudaGraph_t graph = nullptr;
+  const cudaError_t e = cudaStreamEndCapture(st, &graph);
+  if (r || e != cudaSuccess || !graph) {
+    if (graph) cudaGraphDestroy(graph);
+    G.reset();
+    cudaGetLastError();
+    return r ? r : EP_ERR_CUDA;
+  }
+  G.graph = graph;
+  if (cudaGraphInstantiate(&G.exec, graph, 0) != cudaSuccess) {
+    G.exec = nullptr;
+    G.reset();
+    return EP_ERR_CUDA;
+  }
+  G.nsteps = P;
+  return cudaGraphLaunch(G.exec, st) == cudaSuccess ? EP_OK : EP_ERR_CUDA;
+}
+int replay_steps(StepGraph& G, const std::vector<ep_ctx*>& cs, cudaStream_t st) {
+  if (cudaGraphLaunch(G.exec, st) != cudaSuccess) return EP_ERR_CUDA;
+  for (size_t i = 0; i < cs.size(); ++i) {
+    dispatch(cs[i], [&](auto& e) -> int {
+      for (int p = 0; p < G.nsteps; ++p) e.rotate_step();
+      return EP_OK;
+    });
+    cs[i]->prof.launches += G.launches[i];
+  }
+  return EP_OK;
+}
+
+// ng graph-eligible steps of every context of cs: whole rotation periods
+// from the multi-step graph Gk (captured at the first phase that needs it),
+// the rest -- realignment and remainder -- as single replayed steps of G1.
+int graph_steps(StepGraph& G1, StepGraph& Gk, const std::vector<ep_ctx*>& cs, cudaStream_t st, ep_batch* b,
+                double dt, int ng) {
+  int s = 0, r;
+  auto single = [&]() -> int {
+    if (!graph_valid(G1, cs)) return capture_step(G1, cs, st, b, dt);
+    return replay_step(G1, cs, st, dt);
+  };
+  const int P = common_period(cs);
+  if (P >= 2 && ng >= P) {
+    if (graph_valid(Gk, cs))
+      while (s < ng && !at_phase(Gk, cs)) {
+        if ((r = single())) return r;
+        ++s;
+      }
+    if (ng - s >= P) {
+      if (!graph_valid(Gk, cs) || !at_phase(Gk, cs)) {
+        if ((r = capture_steps(Gk, cs, st, b, dt, P))) return r;
+        s += P;
+      }
+      for (; ng - s >= P; s += P)
+        if ((r = replay_steps(Gk, cs, st))) return r;
+    }
+  }
+  for (; s < ng; ++s)
+    if ((r = single())) return r;
+  return EP_OK;
+}
+
 }  // namespace
 
 extern "C" {
@@ -311,6 +437,7 @@ int ep_destroy(ep_ctx* c) {
   cudaSetDevice(c->cfg.device);
   if (c->st) cudaStreamSynchronize(c->st);
   c->graph.reset();
+  c->graphk.reset();
   if (c->e64) { c->e64->release(); delete c->e64; }
   if (c->e32) { c->e32->release(); delete c->e32; }
   if (c->imp.d_potpi) cudaFree(c->imp.d_potpi);
@@ -579,12 +706,8 @@ int ep_run(ep_ctx* c, int nsteps, double dt, ep_run_stats* stats) {
   if (ng >= 2 && graph_eligible(c)) {
     std::vector<ep_ctx*> one{c};
     int r;
-    if (!graph_valid(c->graph, one)) {
-      if ((r = capture_step(c->graph, one, c->st, nullptr, dt))) return r;
-      s0 = 1;
-    }
-    for (; s0 < ng; ++s0)
-      if ((r = replay_step(c->graph, one, c->st, dt))) return r;
+    if ((r = graph_steps(c->graph, c->graphk, one, c->st, nullptr, dt, ng))) return r;
+    s0 = ng;
   }
   return dispatch(c, [&](auto& e) -> int {
     ep_step_errors se{};
@@ -674,6 +797,7 @@ int ep_batch_destroy(ep_batch* b) {
   if (!b) return EP_ERR_INVALID_ARG;
   if (b->st) cudaStreamSynchronize(b->st);
   b->graph.reset();
+  b->graphk.reset();
   for (ep_ctx* c : b->ctx) ep_destroy(c);
   cudaSetDevice(b->device);
   for (cudaEvent_t e : b->join) if (e) cudaEventDestroy(e);
@@ -701,12 +825,8 @@ int ep_batch_run(ep_batch* b, int nsteps, double dt, ep_run_stats* stats) {
   for (ep_ctx* c : b->ctx) eligible = eligible && graph_eligible(c);
   if (eligible) {
     int r;
-    if (!graph_valid(b->graph, b->ctx)) {
-      if ((r = capture_step(b->graph, b->ctx, b->st, b, dt))) return r;
-      s0 = 1;
-    }
-    for (; s0 < ng; ++s0)
-      if ((r = replay_step(b->graph, b->ctx, b->st, dt))) return r;
+    if ((r = graph_steps(b->graph, b->graphk, b->ctx, b->st, b, dt, ng))) return r;
+    s0 = ng;
   }
   batch_fork(b);
   // step-major interleaving so the instances' kernels overlap

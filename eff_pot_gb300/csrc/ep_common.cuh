@@ -21,6 +21,19 @@ EP_HD float2 operator-(float2 a, float2 b) { return make_float2(a.x - b.x, a.y -
 EP_HD float2 operator*(float s, float2 a) { return make_float2(s * a.x, s * a.y); }
 
 template <class T> EP_HD C2<T> cmk(T a, T b) { C2<T> r; r.x = a; r.y = b; return r; }
+
+// Complex (re, im) arithmetic as one vector operation: on sm_100+ an FP32
+// pair is one paired instruction (FADD2 / FMUL2 / FFMA2), half the issue
+// slots of two scalar ones; FP64 pairs are two scalar operations with the
+// same rounding as the contracted scalar expressions (s*a + c -> fma).
+EP_DEV float2 vadd(float2 a, float2 b) { return __fadd2_rn(a, b); }
+EP_DEV float2 vsub(float2 a, float2 b) { return __ffma2_rn(b, make_float2(-1.f, -1.f), a); }
+EP_DEV float2 vmul(float s, float2 a) { return __fmul2_rn(make_float2(s, s), a); }
+EP_DEV float2 vfma(float s, float2 a, float2 c) { return __ffma2_rn(make_float2(s, s), a, c); }
+EP_DEV double2 vadd(double2 a, double2 b) { return make_double2(a.x + b.x, a.y + b.y); }
+EP_DEV double2 vsub(double2 a, double2 b) { return make_double2(a.x - b.x, a.y - b.y); }
+EP_DEV double2 vmul(double s, double2 a) { return make_double2(s * a.x, s * a.y); }
+EP_DEV double2 vfma(double s, double2 a, double2 c) { return make_double2(fma(s, a.x, c.x), fma(s, a.y, c.y)); }
 template <class T2> EP_HD T2 cmul(T2 a, T2 b) {
   T2 r; r.x = a.x * b.x - a.y * b.y; r.y = a.x * b.y + a.y * b.x; return r;
 }

@@ -76,7 +76,7 @@ class Engine {
   ImpState* imp = nullptr;
   std::string* err = nullptr;
   int dev_sm = 0;
-  int zc_pc = 16, zc_rk = 16, zc_d1 = 16;  // z planes per CTA of the stencil marches
+  int zc_pc = 16, zc_pr = 16, zc_rk = 16, zc_d1 = 16;  // z planes per CTA of the stencil marches
   T* dyz = nullptr;                         // dy(gy) + dz(gz) of term_alfa
   T* sigdel = nullptr;                      // Sig_Del of the D state (vpi holds Pi_Del)
   int d1march(int mode, const T* f, const T* f2, T* o0, T* o1, T* o2);
@@ -92,6 +92,45 @@ class Engine {
   int launch_march(const void* fn, dim3 grid, dim3 blk, size_t smem, void** args, const char* name, int which);
   int steppc_update(double dt, cudaGraphExec_t x, cudaGraphNode_t np, cudaGraphNode_t nc);
   bool graph_ok() const { return cfg.impurity != EP_IMPURITY_MOVING && !prof->on; }
+  // Multi-step graphs.  The buffers the next steppc's predictor and corrector
+  // read and write (psi, spare, psiold in age order, hpsiold in age order),
+  // the steps after which they repeat, and the host half of one steppc with
+  // a fixed (or no) impurity -- the buffer rotation of lap_predict and
+  // lap_correct, nothing launched -- applied for each step of a replayed
+  // multi-step graph.
+  void step_signature(const void* (&sig)[7]) const {
+    sig[0] = psi; sig[1] = spare;
+    sig[2] = po[ioldp[0]]; sig[3] = po[ioldp[1]]; sig[4] = po[ioldp[2]];
+    sig[5] = ph[ioldh[0]]; sig[6] = ph[ioldh[1]];
+  }
+  void rotate_step() {
+    std::swap(psi, po[ioldp[2]]);
+    std::swap(ioldh[0], ioldh[1]);
+    std::swap(psi, spare);
+    const int t = ioldp[2];
+    ioldp[2] = ioldp[1];
+    ioldp[1] = ioldp[0];
+    ioldp[0] = t;
+    if (cfg.time_mode == EP_IMAGINARY_TIME && cfg.renormalize) lazy = true;
+  }
+  int rotation_period() const {
+    Engine<T> e;  // host copy of the rotation state only
+    e.cfg = cfg;
+    e.psi = psi; e.spare = spare;
+    for (int k = 0; k < 3; ++k) { e.po[k] = po[k]; e.ioldp[k] = ioldp[k]; }
+    for (int k = 0; k < 2; ++k) { e.ph[k] = ph[k]; e.ioldh[k] = ioldh[k]; }
+    const void* s0[7];
+    step_signature(s0);
+    for (int n = 1; n <= 64; ++n) {
+      e.rotate_step();
+      const void* s[7];
+      e.step_signature(s);
+      bool same = true;
+      for (int k = 0; k < 7; ++k) same = same && s[k] == s0[k];
+      if (same) return n;
+    }
+    return 0;
+  }
   int march_zchunk(int blocks_per_sm, int tile_x = EP_TX) const;
   long long bytes = 0;
   Phys phys{};

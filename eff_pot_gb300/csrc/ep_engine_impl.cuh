@@ -282,23 +282,25 @@ int Engine<T>::init(const ep_config& c, cudaStream_t s, Prof* p, ImpState* im, s
 #undef EP_ATTR
   {
     // z-chunk lengths of the stencil marches from their resident blocks per SM
-    int occ_pc = 0, occ_rk = 0, occ_d1 = 0;
+    int occ_pc = 0, occ_pr = 0, occ_rk = 0, occ_d1 = 0;
     const int nt = EP_TX * EP_TY;
 #define EP_OCC(RR)                                                                                         \
   case RR:                                                                                                 \
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_pc, k_correct<T, RR, true>, nt, march_smem<T, RR, 5, 2>()); \
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_pr, k_predict<T, RR>, nt, march_smem<T, RR, 4, 2>());      \
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_rk, k_rkstage<T, RR>, nt, march_smem<T, RR, 1, 2>()); \
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_d1, k_d1march<T, RR, 0>, nt, 0);                    \
     break;
     switch (fd.R) { EP_OCC(1) EP_OCC(2) EP_OCC(3) EP_OCC(4) EP_OCC(5) EP_OCC(6) default: break; }
 #undef EP_OCC
     zc_pc = march_zchunk(occ_pc);
+    zc_pr = march_zchunk(occ_pr);
     zc_rk = march_zchunk(occ_rk);
     zc_d1 = march_zchunk(occ_d1, EP_D1_TX);
   }
   {
     const long long nxy = (long long)((c.nx + EP_TX - 1) / EP_TX) * ((c.ny + EP_TY - 1) / EP_TY);
-    const int zmin = std::min(zc_pc, zc_rk);
+    const int zmin = std::min(std::min(zc_pc, zc_pr), zc_rk);
     const long long nbs = nxy * ((c.nz + zmin - 1) / zmin);
     // block partials are compensated (hi, lo) pairs: the hi parts of a
     // reduction's nblocks*nq sums, then their lo parts
@@ -795,13 +797,13 @@ int Engine<T>::lap_predict(double dt) {
   CT* po3 = po[ioldp[2]];
   const CT* h1 = ph[ioldh[0]];
   CT* h2 = ph[ioldh[1]];
-  dim3 grid((g.nx + EP_TX - 1) / EP_TX, (g.ny + EP_TY - 1) / EP_TY, (g.nz + zc_pc - 1) / zc_pc);
+  dim3 grid((g.nx + EP_TX - 1) / EP_TX, (g.ny + EP_TY - 1) / EP_TY, (g.nz + zc_pr - 1) / zc_pr);
   dim3 blk(EP_TX, EP_TY);
   T f = (T)(c4o3 * dt), c1 = (T)c112;
   Slots sl{slot_of(psi), slot_of(po3), -1, slot_of(h1), slot_of(h2), slot_of(pc), -1};
   const CT* psic = psi;
   const T *pot4c = pot4, *uimpc = uimp;
-  int zc = zc_pc;
+  int zc = zc_pr;
   void* args[] = {&g, &fd, &phys, &zc, &psic, &pot4c, &uimpc, &po3, &h1, &h2, &pc, &den, &f, &c1, &sc, &sl};
   const void* fn = nullptr;
   size_t smem = 0;

@@ -150,6 +150,11 @@ template <class T> struct HCoef {
 };
 template <class T>
 EP_DEV C2<T> happly(const HCoef<T>& hc, C2<T> lap, C2<T> psi, T pot4, T uimp) {
+  if constexpr (sizeof(T) == 4) {  // paired FP32 instructions
+    const C2<T> L = vfma(hc.h, lap, vmul(-pot4, psi));
+    if (hc.real_time) return cmk<T>(-L.y + uimp * psi.y, L.x - uimp * psi.x);
+    return vfma(-uimp, psi, L);
+  }
   const T h = hc.h;
   C2<T> L = cmk<T>(lap.x * h - pot4 * psi.x, lap.y * h - pot4 * psi.y);
   if (hc.real_time) return cmk<T>(-L.y + uimp * psi.y, L.x - uimp * psi.x);
@@ -927,6 +932,7 @@ EP_DEV void lap_march_async(const Geo& g, const C2<T>* __restrict__ psi, const F
   const bool valid = (x < g.nx) && (y < g.ny);
   const int per = fd.periodic;
   const long long sxy = (long long)g.nx * g.ny;
+  const long long xy = x + (long long)g.nx * y;
   auto addr = [&](int xx, int yy, int zz) -> long long {
     if (xx < 0 || xx >= g.nx || yy < 0 || yy >= g.ny || zz < 0 || zz >= g.nz) {
       if (!per) return -1;
@@ -978,10 +984,13 @@ EP_DEV void lap_march_async(const Geo& g, const C2<T>* __restrict__ psi, const F
       }
     }
     if (valid) {
-      const long long aq = addr(x, y, z + R);
-      if (aq >= 0) cp_async<sizeof(CT)>(sq + buf * NT + tid, psi + aq);
+      // the z-queue element (x, y, z + R): only z can leave the box (z >= 0)
+      int zq = z + R;
+      const bool inq = zq < g.nz || per;
+      if (zq >= g.nz) zq -= g.nz;
+      if (inq) cp_async<sizeof(CT)>(sq + buf * NT + tid, psi + (xy + sxy * zq));
       else sq[buf * NT + tid] = cmk<T>(T(0), T(0));
-      const long long p = x + (long long)g.nx * y + sxy * z;
+      const long long p = xy + sxy * z;
 #pragma unroll
       for (int i = 0; i < NC; ++i) cp_async<sizeof(CT)>(sc_ + (buf * NC + i) * NT + tid, cin[i] + p);
 #pragma unroll
@@ -1009,15 +1018,15 @@ EP_DEV void lap_march_async(const Geo& g, const C2<T>* __restrict__ psi, const F
       q[2 * R] = sq[buf * NT + tid];
       const CT* row = sp + buf * PL + (ty + R) * W + (tx + R);
       const CT c = q[R];
-      CT lx = fd.w2[0][0] * c, ly = fd.w2[1][0] * c, lz = fd.w2[2][0] * c;
+      CT lx = vmul(fd.w2[0][0], c), ly = vmul(fd.w2[1][0], c), lz = vmul(fd.w2[2][0], c);
 #pragma unroll
       for (int k = 1; k <= R; ++k) {
-        lx = lx + fd.w2[0][k] * (row[-k] + row[k]);
-        ly = ly + fd.w2[1][k] * (row[-k * W] + row[k * W]);
-        lz = lz + fd.w2[2][k] * (q[R - k] + q[R + k]);
+        lx = vfma(fd.w2[0][k], vadd(row[-k], row[k]), lx);
+        ly = vfma(fd.w2[1][k], vadd(row[-k * W], row[k * W]), ly);
+        lz = vfma(fd.w2[2][k], vadd(q[R - k], q[R + k]), lz);
       }
-      f((long long)x + (long long)g.nx * y + sxy * z, scale * c, scale * ((lx + ly) + lz),
-        sc_ + buf * NC * NT + tid, sr + buf * NR * NT + tid);
+      f(xy + sxy * z, vmul(scale, c), vmul(scale, vadd(vadd(lx, ly), lz)), sc_ + buf * NC * NT + tid,
+        sr + buf * NR * NT + tid);
     }
 #pragma unroll
     for (int k = 0; k < 2 * R; ++k) q[k] = q[k + 1];
@@ -1210,8 +1219,14 @@ __global__ void __launch_bounds__(EP_TX* EP_TY, sizeof(T) == 4 ? 4 : 2) k_predic
       g, psi, fd, zc, smraw, cin, rin, bscale_of<T>(sc, sl.psi),
       [&](long long p, C2<T> c, C2<T> lap, const C2<T>* ic, const T* ir) {
         const C2<T> H = happly<T>(hc, lap, c, ir[0], ir[NT]);
-        const C2<T> pp = ((s3 * ic[0] + k2f * H) - kh1 * ic[NT]) + kh2 * ic[2 * NT];
-        const C2<T> pn = pp - kpc * ic[3 * NT];
+        C2<T> pp, pn;
+        if constexpr (sizeof(T) == 4) {
+          pp = vfma(kh2, ic[2 * NT], vfma(-kh1, ic[NT], vfma(k2f, H, vmul(s3, ic[0]))));
+          pn = vfma(-kpc, ic[3 * NT], pp);
+        } else {
+          pp = ((s3 * ic[0] + k2f * H) - kh1 * ic[NT]) + kh2 * ic[2 * NT];
+          pn = pp - kpc * ic[3 * NT];
+        }
         po3[p] = pn;
         pc[p] = pp;
         h2[p] = H;
@@ -1259,10 +1274,17 @@ __global__ void __launch_bounds__(EP_TX* EP_TY, sizeof(T) == 4 ? 3 : 2) k_correc
   lap_march_async<T, R, 5, 2>(g, psi, fd, zc, smraw, cin, rin, bscale_of<T>(sc, sl.psi),
                               [&](long long p, C2<T> c, C2<T> lap, const C2<T>* ic, const T* ir) {
     const C2<T> H = happly<T>(hc, lap, c, ir[0], ir[NT]);
-    const C2<T> p5 = (((k3 * ic[0] - k2o * ic[NT]) + kH * H) + k1 * ic[2 * NT]) - k2 * ic[3 * NT];
-    const C2<T> pcn = sp_ * ic[4 * NT] - p5;
+    C2<T> p5, pcn, po;
+    if constexpr (sizeof(T) == 4) {
+      p5 = vfma(-k2, ic[3 * NT], vfma(k1, ic[2 * NT], vfma(kH, H, vfma(-k2o, ic[NT], vmul(k3, ic[0])))));
+      pcn = vsub(vmul(sp_, ic[4 * NT]), p5);
+      po = vfma(c9, pcn, p5);
+    } else {
+      p5 = (((k3 * ic[0] - k2o * ic[NT]) + kH * H) + k1 * ic[2 * NT]) - k2 * ic[3 * NT];
+      pcn = sp_ * ic[4 * NT] - p5;
+      po = p5 + c9 * pcn;
+    }
     pc[p] = pcn;
-    const C2<T> po = p5 + c9 * pcn;
     out[p] = po;
     const T dn = po.x * po.x + po.y * po.y;
     den[p] = dn;

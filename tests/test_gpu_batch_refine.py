@@ -209,3 +209,31 @@ def test_fp32_fields_track_fp64_at_production_sizes(n):
         assert np.abs(f32[f] - f64[f]).max() < 2e-5 * scale, f
     for k in ("etot", "ekin4", "elj4", "ecor4", "ealphas", "eHeX"):
         assert abs(e32[k] - e64[k]) < 2e-5 * abs(e64["etot"]), k
+
+
+@pytest.mark.parametrize("prec", [_abi.EP_FP64, _abi.EP_FP32])
+def test_multi_step_graphs_match_direct_launches(prec):
+    """Runs long enough for whole rotation periods (10 steps) replay a
+    captured multi-step graph with no node updates; runs of other lengths
+    realign the phase with single replayed steps.  Same bits, same kernel
+    count as launching every kernel, for one context and for a batch."""
+    cfgs = [cfg_of(n=n, xmax=0.5 * n, precision=prec) for n in (32, 24)]
+    psis = [ep.woods_saxon_psi(c.nx, c.ny, c.nz, c.xmax, c.ymax, c.zmax, c.n4, seed=20 + i)
+            for i, c in enumerate(cfgs)]
+    runs = (25, 13, 31, 3, 10)
+    res = []
+    for graphs in (False, True):
+        with ep.Batch(cfgs) as b, ep.Solver(cfgs[0]) as s:
+            b.step_graphs(graphs)
+            s.step_graphs(graphs)
+            for inst, psi, z in zip(list(b) + [s], psis + [psis[0]], (0.0, 0.7, 0.3)):
+                prepare(inst, psi, (0.0, 0.0, z))
+            for _ in range(3):
+                b.steprk(5e-4)
+                s.steprk(5e-4)
+            stats = [b.run(k, 5e-4) for k in runs] + [s.run(k, 5e-4) for k in runs]
+            res.append(([x.psi() for x in b] + [s.psi()], stats, b.kernel_launches(), s.kernel_launches()))
+    for a, c in zip(res[0][0], res[1][0]):
+        assert np.array_equal(a, c)
+    assert res[0][1] == res[1][1]
+    assert res[0][2] == res[1][2] and res[0][3] == res[1][3]
