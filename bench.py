@@ -262,6 +262,7 @@ def run_ours(args):
     zs = [1.25 * (rank + world * k) / world for k in range(args.batch)]
     cfgs = [make_cfg("fp32", z, device=local) for z in zs]
     b = ep.Batch(cfgs)
+    b.step_graphs(args.step_graphs)
     for s, z in zip(b, zs):
         prepare(s, psi, z)
     b.autotune()
@@ -305,6 +306,7 @@ def run_ours(args):
     host[...] = np.asfortranarray(psi).ravel(order="F").view(np.float64).reshape(-1, 2)
     psi_host = host.view(np.complex128).reshape((N_GRID,) * 3, order="F")
     b = ep.Batch(cfgs)
+    b.step_graphs(args.step_graphs)
     for s, z in zip(b, zs):
         pot = ep.morse(10.0, 4.5, 1.2)
         s.set_impurity_potentials(pot, pot, pot)
@@ -372,6 +374,7 @@ def run_ours(args):
                                "OTC, imaginary time, dt=1e-4",
                    "instances": args.batch, "grid": [N_GRID] * 3, "fp32_steps": k32, "fp64_refine_steps": k64,
                    "parallelism": "one stream per instance" + (f", {world} GPUs x {args.batch}" if world > 1 else ""),
+                   "step_graphs": args.step_graphs,
                    "l2": "inputs larger than L2 (%.1f GB of state)" % (args.batch * 0.39 + args.batch * 0.77)},
         "fp64_single_steps_per_s": K / (ms64 / 1e3),
         "fp32_single_steps_per_s": K / (ms32 / 1e3),
@@ -411,6 +414,9 @@ def main():
     ap.add_argument("--batch", type=int, default=32)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--step-graphs", type=int, default=1, choices=[0, 1, 2],
+                    help="batch steps: 0 direct launches, 1 one replayed graph per step (default), "
+                         "2 one graph per 10-step rotation period")
     ap.add_argument("--clocks-dir", default=None, help="where the nvidia-smi samples of the timed region go "
                                                       "(default: the temporary directory)")
     args = ap.parse_args()

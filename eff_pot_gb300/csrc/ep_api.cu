@@ -47,7 +47,7 @@ struct StepGraph {
 struct ep_ctx {
   StepGraph graph;
   StepGraph graphk;  // one rotation period of steps
-  bool use_graphs = true;
+  int use_graphs = 1;  // 0 direct launches, 1 step graphs, 2 multi-step graphs
   ep_config cfg{};
   cudaStream_t st = nullptr;
   Prof prof;
@@ -62,7 +62,7 @@ struct ep_ctx {
 struct ep_batch {
   StepGraph graph;
   StepGraph graphk;  // one rotation period of steps
-  bool use_graphs = true;
+  int use_graphs = 1;  // 0 direct launches, 1 step graphs, 2 multi-step graphs
   std::vector<ep_ctx*> ctx;
   cudaStream_t st = nullptr;
   cudaEvent_t fork = nullptr;
@@ -134,7 +134,7 @@ int gen_of(ep_ctx* c) {
   return dispatch(c, [](auto& e) -> int { return e.shapes_gen; });
 }
 bool graph_eligible(ep_ctx* c) {
-  return c->use_graphs && dispatch(c, [](auto& e) -> int { return e.graph_ok() ? 1 : 0; }) == 1;
+  return c->use_graphs > 0 && dispatch(c, [](auto& e) -> int { return e.graph_ok() ? 1 : 0; }) == 1;
 }
 bool graph_valid(const StepGraph& G, const std::vector<ep_ctx*>& cs) {
   if (!G.exec || G.engine.size() != cs.size()) return false;
@@ -303,13 +303,13 @@ int replay_steps(StepGraph& G, const std::vector<ep_ctx*>& cs, cudaStream_t st) 
 // from the multi-step graph Gk (captured at the first phase that needs it),
 // the rest -- realignment and remainder -- as single replayed steps of G1.
 int graph_steps(StepGraph& G1, StepGraph& Gk, const std::vector<ep_ctx*>& cs, cudaStream_t st, ep_batch* b,
-                double dt, int ng) {
+                double dt, int ng, int mode) {
   int s = 0, r;
   auto single = [&]() -> int {
     if (!graph_valid(G1, cs)) return capture_step(G1, cs, st, b, dt);
     return replay_step(G1, cs, st, dt);
   };
-  const int P = common_period(cs);
+  const int P = mode >= 2 ? common_period(cs) : 0;
   if (P >= 2 && ng >= P) {
     if (graph_valid(Gk, cs))
       while (s < ng && !at_phase(Gk, cs)) {
@@ -706,7 +706,7 @@ int ep_run(ep_ctx* c, int nsteps, double dt, ep_run_stats* stats) {
   if (ng >= 2 && graph_eligible(c)) {
     std::vector<ep_ctx*> one{c};
     int r;
-    if ((r = graph_steps(c->graph, c->graphk, one, c->st, nullptr, dt, ng))) return r;
+    if ((r = graph_steps(c->graph, c->graphk, one, c->st, nullptr, dt, ng, c->use_graphs))) return r;
     s0 = ng;
   }
   return dispatch(c, [&](auto& e) -> int {
@@ -821,11 +821,11 @@ int ep_batch_run(ep_batch* b, int nsteps, double dt, ep_run_stats* stats) {
   batch_join(b);  // work the caller left on the instance streams comes first
   int s0 = 0;
   const int ng = nsteps - (stats ? 1 : 0);
-  bool eligible = b->use_graphs && ng >= 2;
+  bool eligible = b->use_graphs > 0 && ng >= 2;
   for (ep_ctx* c : b->ctx) eligible = eligible && graph_eligible(c);
   if (eligible) {
     int r;
-    if ((r = graph_steps(b->graph, b->graphk, b->ctx, b->st, b, dt, ng))) return r;
+    if ((r = graph_steps(b->graph, b->graphk, b->ctx, b->st, b, dt, ng, b->use_graphs))) return r;
     s0 = ng;
   }
   batch_fork(b);
@@ -1025,14 +1025,14 @@ long long ep_kernel_launches(const ep_ctx* c) { return c ? c->prof.launches : 0;
 
 int ep_set_step_graphs(ep_ctx* c, int on) {
   if (!c) return EP_ERR_INVALID_ARG;
-  c->use_graphs = on != 0;
+  c->use_graphs = on < 0 ? 0 : on > 2 ? 2 : on;
   return EP_OK;
 }
 
 int ep_batch_set_step_graphs(ep_batch* b, int on) {
   if (!b) return EP_ERR_INVALID_ARG;
-  b->use_graphs = on != 0;
-  for (ep_ctx* c : b->ctx) c->use_graphs = on != 0;
+  b->use_graphs = on < 0 ? 0 : on > 2 ? 2 : on;
+  for (ep_ctx* c : b->ctx) c->use_graphs = b->use_graphs;
   return EP_OK;
 }
 

@@ -331,9 +331,10 @@ class Solver:
         self._check(self._f["profile_enable"](self._h, 1 if on else 0), "profile_enable")
 
     def step_graphs(self, on=True):
-        """Replay run() steps from a captured CUDA graph (default) or launch
-        every kernel directly."""
-        self._check(self._f["set_step_graphs"](self._h, 1 if on else 0), "set_step_graphs")
+        """Replay run() steps from a captured CUDA graph (True or 1, the
+        default), whole rotation periods of steps from one graph (2), or
+        launch every kernel directly (False or 0)."""
+        self._check(self._f["set_step_graphs"](self._h, int(on)), "set_step_graphs")
 
     def profile_read(self):
         cap, maxn = 4096, 64
@@ -417,7 +418,8 @@ class Batch:
         return int(self._f["batch_kernel_launches"](self._h))
 
     def step_graphs(self, on=True):
-        self._check(self._f["batch_set_step_graphs"](self._h, 1 if on else 0), "batch_set_step_graphs")
+        """As Solver.step_graphs, for every instance of the batch."""
+        self._check(self._f["batch_set_step_graphs"](self._h, int(on)), "batch_set_step_graphs")
 
     def close(self):
         if getattr(self, "_h", None):

@@ -352,12 +352,15 @@ int ep_event_elapsed(ep_ctx* ctx, int slot_a, int slot_b, double* ms);
 /* Kernel launches made by this context since creation (kernels replayed
  * from step graphs included). */
 long long ep_kernel_launches(const ep_ctx* ctx);
-/* Step graphs (default on): ep_run / ep_batch_run capture one steppc of a
- * context (or of every context of a batch) with a fixed or no impurity into
- * a CUDA graph once and replay it, updating only the predictor / corrector
- * nodes to the rotated history buffers.  Results are bit-identical to direct
- * launches.  No reference counterpart (the reference loop calls steppc per
- * step, DFT4He3d.f90). */
+/* Step graphs (default on = 1): ep_run / ep_batch_run capture one steppc
+ * of a context (or of every context of a batch) with a fixed or no impurity
+ * into a CUDA graph once and replay it, updating only the predictor /
+ * corrector nodes to the rotated history buffers.  on = 2: whole periods of
+ * the history rotation (10 steps) are captured once more and replayed with
+ * no node updates (single steps realign the phase and take the remainder).
+ * on = 0: every kernel is launched directly.  Results are bit-identical in
+ * all three modes.  No reference counterpart (the reference loop calls
+ * steppc per step, DFT4He3d.f90). */
 int ep_set_step_graphs(ep_ctx* ctx, int on);
 int ep_batch_set_step_graphs(ep_batch* b, int on);
 /* Per-kernel-class event timing of every launch made while enabled. */
