@@ -126,7 +126,8 @@ def make_cfg(precision, z=0.0, device=0):
     return ep.make_config(nx=N_GRID, ny=N_GRID, nz=N_GRID, xmax=XMAX, ymax=XMAX, zmax=XMAX,
                           icon=_abi.EP_ICON_PERIODIC, core="OTC", n4=N4, impurity=_abi.EP_IMPURITY_FIXED,
                           time_mode=_abi.EP_IMAGINARY_TIME, renormalize=1,
-                          precision=_abi.EP_FP32 if precision == "fp32" else _abi.EP_FP64, device=device)
+                          precision={"fp32": _abi.EP_FP32, "fp64": _abi.EP_FP64, "dfloat": _abi.EP_DFLOAT}[precision],
+                          device=device)
 
 
 def prepare(s, psi, z):
@@ -254,6 +255,7 @@ def run_ours(args):
     # --- single instance: plain FP64 path, FP32 path with per-kernel events
     ms64, _, prof64, tuned64 = time_single("fp64", psi, K, args.warmup, local, profile=True)
     ms32, l32, prof, tuned32 = time_single("fp32", psi, K, args.warmup, local, profile=True)
+    msdd, _, profdd, tuneddd = time_single("dfloat", psi, K, args.warmup, local, profile=True)
 
     # --- the batched scan, FP32 then FP64 refinement
     # N ranks scan the same z range N times more finely: rank r takes every
@@ -272,7 +274,7 @@ def run_ours(args):
     # warm-up, including one precision round trip (allocates the FP64 buffers,
     # whose launch shapes are tuned too)
     b.run(args.warmup, DT)
-    b.set_precision("fp64")
+    b.set_precision(args.refine)
     b.autotune()
     b.run(1, DT)
     b.set_precision("fp32")
@@ -283,7 +285,7 @@ def run_ours(args):
     with ClockSampler(local, "batch", args.clocks_dir) as clk:
         b.event_record(0)
         b.run(k32, DT, wait=False)
-        b.set_precision("fp64")
+        b.set_precision(args.refine)
         b.run(k64, DT, wait=False)
         b.event_record(1)
         ms_b = b.event_elapsed(0, 1)
@@ -311,7 +313,7 @@ def run_ours(args):
         pot = ep.morse(10.0, 4.5, 1.2)
         s.set_impurity_potentials(pot, pot, pot)
         s.set_impurity(rimp=(0.0, 0.0, z), invar=np.zeros(10, dtype=np.complex128))
-    b.set_precision("fp64")
+    b.set_precision(args.refine)
     b.set_precision("fp32")
     b.synchronize()
     barrier(dist)
@@ -324,7 +326,7 @@ def run_ours(args):
     b.steprk(DT)
     b.steprk(DT)
     b.run(k32, DT, wait=False)
-    b.set_precision("fp64")
+    b.set_precision(args.refine)
     b.run(k64, DT)
     # the final fields of every instance first (their kernels overlap on the
     # instance streams), then energies and psi into page-locked memory
@@ -369,14 +371,15 @@ def run_ours(args):
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": K, "warmup": args.warmup,
         "ms_per_step": ms_b / K, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-        "dtype": "f32+f64", "data": "synthetic (seeded Woods-Saxon droplets, seed 1)",
+        "dtype": "f32+f64" if args.refine == "fp64" else "f32+dfloat", "data": "synthetic (seeded Woods-Saxon droplets, seed 1)",
         "config": {"workload": f"{args.batch} droplets N=1000 + Morse impurity at z=0..{zs[-1]} A, 128^3, h=0.4 A, "
                                "OTC, imaginary time, dt=1e-4",
                    "instances": args.batch, "grid": [N_GRID] * 3, "fp32_steps": k32, "fp64_refine_steps": k64,
                    "parallelism": "one stream per instance" + (f", {world} GPUs x {args.batch}" if world > 1 else ""),
-                   "step_graphs": args.step_graphs,
+                   "step_graphs": args.step_graphs, "refine": args.refine,
                    "l2": "inputs larger than L2 (%.1f GB of state)" % (args.batch * 0.39 + args.batch * 0.77)},
         "fp64_single_steps_per_s": K / (ms64 / 1e3),
+        "dfloat_single_steps_per_s": K / (msdd / 1e3),
         "fp32_single_steps_per_s": K / (ms32 / 1e3),
         "speedup_vs_fp64_single": value / (world * K / (ms64 / 1e3)),
         "hbm_gbs_batch": batch_bytes / (ms_b / 1e3) / 1e9,
@@ -386,6 +389,8 @@ def run_ours(args):
                      "measured_on": "single FP32 instance, kernels timed alone (burst peak)",
                      "peak_source": "MEASURED_PEAKS.json hbm_gbs (of measured)" if "hbm_gbs" in peaks else "fallback"},
         "kernels_ms_per_step_fp32_single": {k: round(v, 4) for k, v in sorted(per_step.items(), key=lambda t: -t[1])},
+        "kernels_ms_per_step_dfloat_single": {k: round(v[0] / K, 4)
+                                              for k, v in sorted(profdd.items(), key=lambda t: -t[1][0])},
         "kernels_ms_per_step_fp64_single": {k: round(v[0] / K, 4)
                                             for k, v in sorted(prof64.items(), key=lambda t: -t[1][0])},
         "autotune": {"fp32": tuned32, "fp64": tuned64},
@@ -414,6 +419,8 @@ def main():
     ap.add_argument("--batch", type=int, default=32)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--refine", default="fp64", choices=["fp64", "dfloat"],
+                    help="arithmetic of the refinement sweeps: FP64, or double-float (FP64-class on the FP32 pipes)")
     ap.add_argument("--step-graphs", type=int, default=1, choices=[0, 1, 2],
                     help="batch steps: 0 direct launches, 1 one replayed graph per step (default), "
                          "2 one graph per 10-step rotation period")

@@ -17,7 +17,7 @@ STATUS_NAMES = {
 EP_CORE_OT, EP_CORE_OTC, EP_CORE_OP = 0, 1, 2
 EP_IMAGINARY_TIME, EP_REAL_TIME = 0, 1
 EP_IMPURITY_NONE, EP_IMPURITY_FIXED, EP_IMPURITY_MOVING = 0, 1, 2
-EP_FP64, EP_FP32 = 0, 1
+EP_FP64, EP_FP32, EP_DFLOAT = 0, 1, 2
 EP_ICON_PERIODIC, EP_ICON_ZERO_OUTSIDE = 8, 13
 EP_STATE_P, EP_STATE_D = 0, 1
 EP_POT_NULL, EP_POT_MORSE, EP_POT_KOUTSELOS = 0, 1, 2

@@ -10,6 +10,7 @@
 #include <cmath>
 #include <cstring>
 #include <string>
+#include <type_traits>
 #include <vector>
 
 #include "../../include/eff_pot.h"
@@ -55,6 +56,7 @@ struct ep_ctx {
   std::string err;
   Engine<double>* e64 = nullptr;
   Engine<float>* e32 = nullptr;
+  Engine<dfloat>* edd = nullptr;
   int active = EP_FP64;
   cudaEvent_t ev[16] = {};
 };
@@ -118,6 +120,7 @@ int dispatch(ep_ctx* c, F f) {
   if (!c) return EP_ERR_INVALID_ARG;
   if (c->active == EP_FP64 && c->e64) return f(*c->e64);
   if (c->active == EP_FP32 && c->e32) return f(*c->e32);
+  if (c->active == EP_DFLOAT && c->edd) return f(*c->edd);
   return fail(c, EP_ERR_STATE, "context has no engine");
 }
 
@@ -128,7 +131,8 @@ int dispatch(ep_ctx* c, F f) {
 // of a batch on their forked streams) is captured once; later steps update
 // the two march nodes per context and launch the graph.
 const void* engine_of(ep_ctx* c) {
-  return c->active == EP_FP64 ? (const void*)c->e64 : (const void*)c->e32;
+  return c->active == EP_FP64 ? (const void*)c->e64
+         : c->active == EP_FP32 ? (const void*)c->e32 : (const void*)c->edd;
 }
 int gen_of(ep_ctx* c) {
   return dispatch(c, [](auto& e) -> int { return e.shapes_gen; });
@@ -332,6 +336,47 @@ int graph_steps(StepGraph& G1, StepGraph& Gk, const std::vector<ep_ctx*>& cs, cu
 
 }  // namespace
 
+namespace {
+
+// The engine of precision T of c, created on first use.
+template <class T> Engine<T>*& engine_slot(ep_ctx* c);
+template <> Engine<double>*& engine_slot<double>(ep_ctx* c) { return c->e64; }
+template <> Engine<float>*& engine_slot<float>(ep_ctx* c) { return c->e32; }
+template <> Engine<dfloat>*& engine_slot<dfloat>(ep_ctx* c) { return c->edd; }
+
+// The active engine's state converted into the engine of precision T.
+template <class T>
+int switch_to(ep_ctx* c, int precision) {
+  Engine<T>*& e = engine_slot<T>(c);
+  int r;
+  if (!e) {
+    ep_config cfg = c->cfg;
+    cfg.precision = precision;
+    e = new Engine<T>();
+    if ((r = e->init(cfg, c->st, &c->prof, &c->imp, &c->err))) { e->release(); delete e; e = nullptr; return r; }
+  }
+  r = dispatch(c, [&](auto& src) -> int {
+    typedef typename std::remove_reference<decltype(src)>::type Src;
+    if constexpr (std::is_same<Src, Engine<T>>::value) {
+      return EP_OK;
+    } else {
+      int q = src.ensure_materialized();
+      return q ? q : e->import_state(src);
+    }
+  });
+  if (r) return r;
+  // an FP64-class engine recomputes the impurity field from the tables and
+  // the impurity state instead of widening its FP32 copy: a fixed impurity's
+  // field is never refreshed, so the refinement sweeps would otherwise carry
+  // its FP32 rounding to the end
+  if (!std::is_same<T, float>::value && c->cfg.impurity != EP_IMPURITY_NONE && c->imp.have_tables &&
+      (r = e->potenimp()))
+    return r;
+  return EP_OK;
+}
+
+}  // namespace
+
 extern "C" {
 
 int ep_config_init(ep_config* c) {
@@ -397,7 +442,10 @@ int ep_create(const ep_config* cfg, ep_ctx** out) {
     g_create_error = "a moving impurity needs mimpur > 0";
     return EP_ERR_INVALID_ARG;
   }
-  if (c.precision != EP_FP64 && c.precision != EP_FP32) { g_create_error = "unknown precision"; return EP_ERR_INVALID_ARG; }
+  if (c.precision != EP_FP64 && c.precision != EP_FP32 && c.precision != EP_DFLOAT) {
+    g_create_error = "unknown precision";
+    return EP_ERR_INVALID_ARG;
+  }
   if (c.state != EP_STATE_P && c.state != EP_STATE_D) { g_create_error = "state must be P or D"; return EP_ERR_INVALID_ARG; }
   int ndev = 0;
   if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) {
@@ -419,6 +467,9 @@ int ep_create(const ep_config* cfg, ep_ctx** out) {
   if (c.precision == EP_FP64) {
     x->e64 = new Engine<double>();
     r = x->e64->init(c, x->st, &x->prof, &x->imp, &x->err);
+  } else if (c.precision == EP_DFLOAT) {
+    x->edd = new Engine<dfloat>();
+    r = x->edd->init(c, x->st, &x->prof, &x->imp, &x->err);
   } else {
     x->e32 = new Engine<float>();
     r = x->e32->init(c, x->st, &x->prof, &x->imp, &x->err);
@@ -440,6 +491,7 @@ int ep_destroy(ep_ctx* c) {
   c->graphk.reset();
   if (c->e64) { c->e64->release(); delete c->e64; }
   if (c->e32) { c->e32->release(); delete c->e32; }
+  if (c->edd) { c->edd->release(); delete c->edd; }
   if (c->imp.d_potpi) cudaFree(c->imp.d_potpi);
   if (c->imp.d_potdel) cudaFree(c->imp.d_potdel);
   if (c->imp.d_potsigdel) cudaFree(c->imp.d_potsigdel);
@@ -733,32 +785,13 @@ int ep_renormalize(ep_ctx* c, double* norm_before) {
 }
 
 int ep_set_precision(ep_ctx* c, int precision) {
-  if (!c || (precision != EP_FP64 && precision != EP_FP32)) return EP_ERR_INVALID_ARG;
+  if (!c || (precision != EP_FP64 && precision != EP_FP32 && precision != EP_DFLOAT)) return EP_ERR_INVALID_ARG;
   if (precision == c->active) return EP_OK;
   cudaSetDevice(c->cfg.device);
-  ep_config cfg = c->cfg;
-  cfg.precision = precision;
-  int r;
-  if (precision == EP_FP64) {
-    if (!c->e64) {
-      c->e64 = new Engine<double>();
-      if ((r = c->e64->init(cfg, c->st, &c->prof, &c->imp, &c->err))) { c->e64->release(); delete c->e64; c->e64 = nullptr; return r; }
-    }
-    if ((r = c->e32->ensure_materialized())) return r;
-    if ((r = c->e64->import_state(*c->e32))) return r;
-    // the impurity field is recomputed in FP64 from the tables and the
-    // impurity state, not widened from its FP32 copy: a fixed impurity's
-    // field is never refreshed, so the refinement sweeps would otherwise
-    // carry its FP32 rounding to the end
-    if (c->cfg.impurity != EP_IMPURITY_NONE && c->imp.have_tables && (r = c->e64->potenimp())) return r;
-  } else {
-    if (!c->e32) {
-      c->e32 = new Engine<float>();
-      if ((r = c->e32->init(cfg, c->st, &c->prof, &c->imp, &c->err))) { c->e32->release(); delete c->e32; c->e32 = nullptr; return r; }
-    }
-    if ((r = c->e64->ensure_materialized())) return r;
-    if ((r = c->e32->import_state(*c->e64))) return r;
-  }
+  const int r = precision == EP_FP64   ? switch_to<double>(c, precision)
+                : precision == EP_FP32 ? switch_to<float>(c, precision)
+                                       : switch_to<dfloat>(c, precision);
+  if (r) return r;
   c->active = precision;
   c->cfg.precision = precision;
   return EP_OK;
@@ -954,10 +987,10 @@ int ep_autotune(ep_ctx* c, char* report, int cap) {
 
 int ep_get_launch_shapes(const ep_ctx* c, int* s) {
   if (!c || !s) return EP_ERR_INVALID_ARG;
-  if (c->active == EP_FP64 && c->e64) shapes_out(*c->e64, s);
-  else if (c->e32) shapes_out(*c->e32, s);
-  else return EP_ERR_STATE;
-  return EP_OK;
+  return dispatch(const_cast<ep_ctx*>(c), [&](auto& e) -> int {
+    shapes_out(e, s);
+    return EP_OK;
+  });
 }
 
 int ep_set_launch_shapes(ep_ctx* c, const int* s) {
@@ -965,10 +998,11 @@ int ep_set_launch_shapes(ep_ctx* c, const int* s) {
   Shapes sh;
   for (int k = 0; k < 4; ++k) { sh.xnl[k] = s[0]; sh.xthr[k] = s[1]; }
   sh.ylt = s[2]; sh.ythr = s[3]; sh.zlt = s[4]; sh.zthr = s[5];
-  if (c->active == EP_FP64 && c->e64) { c->e64->shp = sh; ++c->e64->shapes_gen; }
-  else if (c->e32) { c->e32->shp = sh; ++c->e32->shapes_gen; }
-  else return EP_ERR_STATE;
-  return EP_OK;
+  return dispatch(c, [&](auto& e) -> int {
+    e.shp = sh;
+    ++e.shapes_gen;
+    return EP_OK;
+  });
 }
 
 int ep_batch_autotune(ep_batch* b) {
@@ -989,6 +1023,7 @@ int ep_batch_autotune(ep_batch* b) {
         if (j != i) {
           if (ci_->active == EP_FP64 && ci_->e64 && cj_->e64) { cj_->e64->shp = ci_->e64->shp; ++cj_->e64->shapes_gen; }
           if (ci_->active == EP_FP32 && ci_->e32 && cj_->e32) { cj_->e32->shp = ci_->e32->shp; ++cj_->e32->shapes_gen; }
+          if (ci_->active == EP_DFLOAT && ci_->edd && cj_->edd) { cj_->edd->shp = ci_->edd->shp; ++cj_->edd->shapes_gen; }
         }
         done[j] = 1;
       }
@@ -1066,7 +1101,7 @@ int ep_profile_read(ep_ctx* c, char* names, int cap, double* ms, long long* laun
 
 long long ep_device_bytes(const ep_ctx* c) {
   if (!c) return 0;
-  return (c->e64 ? c->e64->bytes : 0) + (c->e32 ? c->e32->bytes : 0);
+  return (c->e64 ? c->e64->bytes : 0) + (c->e32 ? c->e32->bytes : 0) + (c->edd ? c->edd->bytes : 0);
 }
 
 }  // extern "C"

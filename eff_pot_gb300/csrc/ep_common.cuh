@@ -6,11 +6,14 @@
 #define EP_DEV __device__ __forceinline__
 #define EP_HD __host__ __device__ __forceinline__
 
+#include "ep_dd.cuh"
+
 // ---------------------------------------------------------------------------
 // Complex numbers as CUDA vector types (x = re, y = im).
 template <class T> struct cpx_traits;
 template <> struct cpx_traits<double> { typedef double2 type; };
 template <> struct cpx_traits<float> { typedef float2 type; };
+template <> struct cpx_traits<dfloat> { typedef dfloat2 type; };
 template <class T> using C2 = typename cpx_traits<T>::type;
 
 EP_HD double2 operator+(double2 a, double2 b) { return make_double2(a.x + b.x, a.y + b.y); }
@@ -21,6 +24,11 @@ EP_HD float2 operator-(float2 a, float2 b) { return make_float2(a.x - b.x, a.y -
 EP_HD float2 operator*(float s, float2 a) { return make_float2(s * a.x, s * a.y); }
 
 template <class T> EP_HD C2<T> cmk(T a, T b) { C2<T> r; r.x = a; r.y = b; return r; }
+
+// A value of any field precision as an FP64 number.
+EP_HD double dbl(double v) { return v; }
+EP_HD double dbl(float v) { return v; }
+EP_HD double dbl(dfloat v) { return (double)v; }
 
 // Complex (re, im) arithmetic as one vector operation: on sm_100+ an FP32
 // pair is one paired instruction (FADD2 / FMUL2 / FFMA2), half the issue
@@ -34,6 +42,10 @@ EP_DEV double2 vadd(double2 a, double2 b) { return make_double2(a.x + b.x, a.y +
 EP_DEV double2 vsub(double2 a, double2 b) { return make_double2(a.x - b.x, a.y - b.y); }
 EP_DEV double2 vmul(double s, double2 a) { return make_double2(s * a.x, s * a.y); }
 EP_DEV double2 vfma(double s, double2 a, double2 c) { return make_double2(fma(s, a.x, c.x), fma(s, a.y, c.y)); }
+EP_DEV dfloat2 vadd(dfloat2 a, dfloat2 b) { return a + b; }
+EP_DEV dfloat2 vsub(dfloat2 a, dfloat2 b) { return a - b; }
+EP_DEV dfloat2 vmul(dfloat s, dfloat2 a) { return s * a; }
+EP_DEV dfloat2 vfma(dfloat s, dfloat2 a, dfloat2 c) { return s * a + c; }
 template <class T2> EP_HD T2 cmul(T2 a, T2 b) {
   T2 r; r.x = a.x * b.x - a.y * b.y; r.y = a.x * b.y + a.y * b.x; return r;
 }

@@ -1,0 +1,130 @@
+// ep_dd.cuh - double-float arithmetic: a real number as the unevaluated sum
+// hi + lo of two FP32 values (|lo| <= ulp(hi)/2), about 48 significant bits.
+//
+// The FP64 pipe of this part runs at 1/64 of the FP32 rate; a double-float
+// operation costs 4-11 FP32 instructions, so the FP64-class engine computed in
+// double-float (Engine<dfloat>) runs on the FP32 pipes.  The operations follow
+// the published error-free transformations: Knuth's TwoSum for the sum of two
+// FP32 values, the FMA product error (a*b - fl(a*b) = fma(a, b, -fl(a*b))),
+// Dekker's Fast2Sum for the renormalisation, and the "sloppy" double-float
+// sum (one TwoSum of the high parts, the low parts added, one Fast2Sum), whose
+// error is bounded by about 2^-44 (|a| + |b|); the product's by about 2^-45
+// |a b|.  The FP32 range applies (normal values down to 1.2e-38; below about
+// 1e-31 the low part is subnormal or zero and the relative precision falls
+// towards FP32's).  Every step that must be rounded on its own is written
+// with the _rn intrinsics, which the compiler never contracts into an FMA.
+#pragma once
+#include <cuda_runtime.h>
+
+#ifndef EP_HD
+#define EP_HD __host__ __device__ __forceinline__
+#endif
+
+struct __align__(8) dfloat {
+  float hi, lo;
+  dfloat() = default;
+  EP_HD constexpr dfloat(float h, float l) : hi(h), lo(l) {}
+  EP_HD constexpr dfloat(double d) : hi((float)d), lo((float)(d - (double)(float)d)) {}
+  EP_HD constexpr dfloat(float f) : hi(f), lo(0.0f) {}
+  EP_HD constexpr dfloat(int i) : dfloat((double)i) {}
+  EP_HD explicit constexpr operator double() const { return (double)hi + (double)lo; }
+  EP_HD explicit constexpr operator float() const { return hi + lo; }
+};
+
+struct __align__(16) dfloat2 {
+  dfloat x, y;
+};
+
+#if defined(__CUDA_ARCH__)
+#define EP_DD_ADD(a, b) __fadd_rn(a, b)
+#define EP_DD_SUB(a, b) __fsub_rn(a, b)
+#define EP_DD_MUL(a, b) __fmul_rn(a, b)
+#define EP_DD_FMA(a, b, c) __fmaf_rn(a, b, c)
+#else
+#define EP_DD_ADD(a, b) ((a) + (b))
+#define EP_DD_SUB(a, b) ((a) - (b))
+#define EP_DD_MUL(a, b) ((a) * (b))
+#define EP_DD_FMA(a, b, c) fmaf(a, b, c)
+#endif
+
+// Fast2Sum (|a| >= |b|): s + e == a + b exactly.
+EP_HD dfloat dd_fast2sum(float a, float b) {
+  const float s = EP_DD_ADD(a, b);
+  return dfloat(s, EP_DD_SUB(b, EP_DD_SUB(s, a)));
+}
+
+EP_HD dfloat operator-(dfloat a) { return dfloat(-a.hi, -a.lo); }
+
+EP_HD dfloat operator+(dfloat a, dfloat b) {
+  const float s = EP_DD_ADD(a.hi, b.hi);
+  const float bb = EP_DD_SUB(s, a.hi);
+  float e = EP_DD_ADD(EP_DD_SUB(a.hi, EP_DD_SUB(s, bb)), EP_DD_SUB(b.hi, bb));
+  e = EP_DD_ADD(e, EP_DD_ADD(a.lo, b.lo));
+  return dd_fast2sum(s, e);
+}
+EP_HD dfloat operator-(dfloat a, dfloat b) { return a + (-b); }
+
+EP_HD dfloat operator*(dfloat a, dfloat b) {
+  const float p = EP_DD_MUL(a.hi, b.hi);
+  float e = EP_DD_FMA(a.hi, b.hi, -p);
+  e = EP_DD_FMA(a.hi, b.lo, e);
+  e = EP_DD_FMA(a.lo, b.hi, e);
+  return dd_fast2sum(p, e);
+}
+
+// a / b: one FP32 quotient, its remainder in double-float, one correction.
+EP_HD dfloat operator/(dfloat a, dfloat b) {
+  const float q1 = a.hi / b.hi;
+  const dfloat r = a - b * dfloat(q1);
+  const float q2 = r.hi / b.hi;
+  return dd_fast2sum(q1, q2);
+}
+
+EP_HD dfloat& operator+=(dfloat& a, dfloat b) { return a = a + b; }
+EP_HD dfloat& operator-=(dfloat& a, dfloat b) { return a = a - b; }
+EP_HD dfloat& operator*=(dfloat& a, dfloat b) { return a = a * b; }
+
+EP_HD bool operator<(dfloat a, dfloat b) { return a.hi < b.hi || (a.hi == b.hi && a.lo < b.lo); }
+EP_HD bool operator>(dfloat a, dfloat b) { return b < a; }
+EP_HD bool operator<=(dfloat a, dfloat b) { return !(b < a); }
+EP_HD bool operator>=(dfloat a, dfloat b) { return !(a < b); }
+EP_HD bool operator==(dfloat a, dfloat b) { return a.hi == b.hi && a.lo == b.lo; }
+EP_HD bool operator!=(dfloat a, dfloat b) { return !(a == b); }
+
+EP_HD dfloat fabs(dfloat a) { return a.hi < 0.0f ? -a : a; }
+EP_HD dfloat fma(dfloat a, dfloat b, dfloat c) { return a * b + c; }
+EP_HD dfloat fmin(dfloat a, dfloat b) { return b < a ? b : a; }
+EP_HD dfloat fmax(dfloat a, dfloat b) { return a < b ? b : a; }
+EP_HD bool isfinite(dfloat a) { return isfinite(a.hi); }
+// sqrt: the FP32 root and one Newton correction in double-float.
+EP_HD dfloat sqrt(dfloat a) {
+  if (!(a.hi > 0.0f)) return dfloat(sqrtf(a.hi), 0.0f);
+  const float r = sqrtf(a.hi);
+  const dfloat d = a - dfloat(r) * dfloat(r);
+  return dd_fast2sum(r, d.hi / (2.0f * r));
+}
+
+#if defined(__CUDACC__)
+__device__ __forceinline__ dfloat __shfl_sync(unsigned m, dfloat v, int src) {
+  return dfloat(__shfl_sync(m, v.hi, src), __shfl_sync(m, v.lo, src));
+}
+__device__ __forceinline__ dfloat __shfl_down_sync(unsigned m, dfloat v, unsigned d) {
+  return dfloat(__shfl_down_sync(m, v.hi, d), __shfl_down_sync(m, v.lo, d));
+}
+__device__ __forceinline__ dfloat __shfl_xor_sync(unsigned m, dfloat v, int d) {
+  return dfloat(__shfl_xor_sync(m, v.hi, d), __shfl_xor_sync(m, v.lo, d));
+}
+__device__ __forceinline__ dfloat __ldg(const dfloat* p) {
+  const float2 v = __ldg(reinterpret_cast<const float2*>(p));
+  return dfloat(v.x, v.y);
+}
+__device__ __forceinline__ dfloat __ldcg(const dfloat* p) {
+  const float2 v = __ldcg(reinterpret_cast<const float2*>(p));
+  return dfloat(v.x, v.y);
+}
+#endif
+
+// Complex double-float.
+EP_HD dfloat2 operator+(dfloat2 a, dfloat2 b) { return dfloat2{a.x + b.x, a.y + b.y}; }
+EP_HD dfloat2 operator-(dfloat2 a, dfloat2 b) { return dfloat2{a.x - b.x, a.y - b.y}; }
+EP_HD dfloat2 operator*(dfloat s, dfloat2 a) { return dfloat2{s * a.x, s * a.y}; }

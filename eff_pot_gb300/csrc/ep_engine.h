@@ -132,6 +132,14 @@ class Engine {
     return 0;
   }
   int march_zchunk(int blocks_per_sm, int tile_x = EP_TX) const;
+  // kernel attributes (dynamic shared memory) and the march z-chunk lengths,
+  // set up by init
+  int x_attrs();
+  int fft_attrs();
+  int x_pass(int which, bool otc);
+  template <int N2> int x_launch(int which, bool otc);
+  template <int N2> int x_attrs_n2();
+  int march_setup();
   long long bytes = 0;
   Phys phys{};
   FdW<T> fd{};

@@ -23,21 +23,24 @@
     if (_e != cudaSuccess) return cuda_ok(_e, name);                  \
   } while (0)
 
-// Launch an X kernel template KER<T, N2> with N2 = the register-transform
-// length of this grid (0: general engine).
-#define EP_XLAUNCH(name, KER, grid, block, smem, ...)                  \
-  do {                                                                 \
-    switch (x_reg_n2<T>(g.nx / 2)) {                                   \
-      case 16: { auto k = KER<T, 16>; EP_LAUNCH(name, k, grid, block, smem, __VA_ARGS__); } break;   \
-      case 32: { auto k = KER<T, 32>; EP_LAUNCH(name, k, grid, block, smem, __VA_ARGS__); } break;   \
-      case 64: { auto k = KER<T, 64>; EP_LAUNCH(name, k, grid, block, smem, __VA_ARGS__); } break;   \
-      case 128: { auto k = KER<T, 128>; EP_LAUNCH(name, k, grid, block, smem, __VA_ARGS__); } break; \
-      case 48: if constexpr (sizeof(T) == 4) { auto k = KER<T, 48>; EP_LAUNCH(name, k, grid, block, smem, __VA_ARGS__); } break; \
-      case 80: if constexpr (sizeof(T) == 4) { auto k = KER<T, 80>; EP_LAUNCH(name, k, grid, block, smem, __VA_ARGS__); } break; \
-      case 96: if constexpr (sizeof(T) == 4) { auto k = KER<T, 96>; EP_LAUNCH(name, k, grid, block, smem, __VA_ARGS__); } break; \
-      default: { auto k = KER<T, 0>; EP_LAUNCH(name, k, grid, block, smem, __VA_ARGS__); } break;    \
-    }                                                                  \
-  } while (0)
+
+// Stencil radii built per precision: every npd = 3..13 (R = 1..6) in FP64
+// and FP32; in double-float only the 13-point stencils (R = 6: npd = 13, the
+// reference default and every benchmark workload), whose kernels are several
+// times larger than the FP64 ones.
+// Parts of the engine's member definitions: a translation unit that defines
+// EP_ENGINE_PARTS compiles only those parts (the large double-float engine
+// is built from several units in parallel); the default is all of them.
+#define EP_PART_REST 1
+#define EP_PART_X 2
+#define EP_PART_FFT 4
+#define EP_PART_MARCH 8
+#define EP_PART_XK 16
+#ifndef EP_ENGINE_PARTS
+#define EP_ENGINE_PARTS 31
+#endif
+
+template <class T> constexpr bool r_built(int R) { return !std::is_same<T, dfloat>::value || R == 6; }
 
 namespace {
 
@@ -88,6 +91,7 @@ inline void twiddles(int n, std::vector<CT>& tw) {
 
 }  // namespace
 
+#if EP_ENGINE_PARTS & EP_PART_REST
 template <class T>
 int Engine<T>::cuda_ok(cudaError_t e, const char* what) {
   if (e == cudaSuccess) return EP_OK;
@@ -136,6 +140,10 @@ int Engine<T>::init(const ep_config& c, cudaStream_t s, Prof* p, ImpState* im, s
   prof = p;
   imp = im;
   err = e;
+  if (!r_built<T>(c.npd / 2)) {
+    *err = "double-float fields are built for npd = 13 only";
+    return EP_ERR_UNSUPPORTED;
+  }
   g.nx = c.nx; g.ny = c.ny; g.nz = c.nz; g.nxh = c.nx / 2 + 1;
   g.N = (long long)c.nx * c.ny * c.nz;
   g.Nh = (long long)g.nxh * c.ny * c.nz;
@@ -175,6 +183,9 @@ int Engine<T>::init(const ep_config& c, cudaStream_t s, Prof* p, ImpState* im, s
   phl.f = PhysF{(float)phl.cp4, (float)phl.cpp4, (float)phl.a0, (float)phl.a1, (float)phl.rden0s,
                 (float)phl.h2o2m4, (float)phl.alphas, (float)phl.C, (float)phl.beta, (float)phl.den_m,
                 (float)phl.renor};
+  phl.d = PhysD{dfloat(phl.cp4), dfloat(phl.cpp4), dfloat(phl.a0), dfloat(phl.a1), dfloat(phl.rden0s),
+                dfloat(phl.h2o2m4), dfloat(phl.alphas), dfloat(phl.C), dfloat(phl.beta), dfloat(phl.den_m),
+                dfloat(phl.renor)};
   phys = phl;
 
   const size_t N = (size_t)g.N, Nh = (size_t)g.Nh;
@@ -247,57 +258,13 @@ int Engine<T>::init(const ep_config& c, cudaStream_t s, Prof* p, ImpState* im, s
     cudaStreamSynchronize(st);
     cudaFree(dpg);
   }
-  const int big = 220 * 1024;
-#define EP_XATTR(NN)                                                                \
-  cudaFuncSetAttribute(k_x1<T, NN>, cudaFuncAttributeMaxDynamicSharedMemorySize, big); \
-  cudaFuncSetAttribute(k_x2<T, NN>, cudaFuncAttributeMaxDynamicSharedMemorySize, big); \
-  cudaFuncSetAttribute(k_x3<T, NN>, cudaFuncAttributeMaxDynamicSharedMemorySize, big); \
-  cudaFuncSetAttribute(k_x4<T, NN>, cudaFuncAttributeMaxDynamicSharedMemorySize, big);
-  EP_XATTR(0) EP_XATTR(16) EP_XATTR(32) EP_XATTR(64) EP_XATTR(128)
-  if constexpr (sizeof(T) == 4) { EP_XATTR(48) EP_XATTR(80) EP_XATTR(96) }
-#undef EP_XATTR
-  cudaFuncSetAttribute(k_c2c<T, -1>, cudaFuncAttributeMaxDynamicSharedMemorySize, big);
-  cudaFuncSetAttribute(k_c2c<T, +1>, cudaFuncAttributeMaxDynamicSharedMemorySize, big);
-  cudaFuncSetAttribute(k_zconv<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, big);
-#define EP_RFFT_ATTR(NN)                                                                                  \
-  cudaFuncSetAttribute(k_c2c_r<T, NN, -1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)rfft::smem_bytes<T, NN>()); \
-  cudaFuncSetAttribute(k_c2c_r<T, NN, +1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)rfft::smem_bytes<T, NN>()); \
-  cudaFuncSetAttribute(k_zconv_r<T, NN, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)rfft::smem_bytes<T, NN>()); \
-  cudaFuncSetAttribute(k_zconv_r<T, NN, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)rfft::smem_bytes<T, NN>());
-  EP_RFFT_ATTR(32) EP_RFFT_ATTR(64) EP_RFFT_ATTR(128) EP_RFFT_ATTR(256)
-  if constexpr (sizeof(T) == 4) { EP_RFFT_ATTR(96) EP_RFFT_ATTR(192) }
-#undef EP_RFFT_ATTR
   {
     int dev = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&dev_sm, cudaDevAttrMultiProcessorCount, dev);
     if (dev_sm <= 0) dev_sm = 152;
   }
-#define EP_ATTR(RR)                                                                                      \
-  cudaFuncSetAttribute(k_predict<T, RR>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)march_smem<T, RR, 4, 2>()); \
-  cudaFuncSetAttribute(k_correct<T, RR, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)march_smem<T, RR, 5, 2>()); \
-  cudaFuncSetAttribute(k_correct<T, RR, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)march_smem<T, RR, 5, 2>()); \
-  cudaFuncSetAttribute(k_rkstage<T, RR>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)march_smem<T, RR, 1, 2>());
-  EP_ATTR(1) EP_ATTR(2) EP_ATTR(3) EP_ATTR(4) EP_ATTR(5) EP_ATTR(6)
-#undef EP_ATTR
-  {
-    // z-chunk lengths of the stencil marches from their resident blocks per SM
-    int occ_pc = 0, occ_pr = 0, occ_rk = 0, occ_d1 = 0;
-    const int nt = EP_TX * EP_TY;
-#define EP_OCC(RR)                                                                                         \
-  case RR:                                                                                                 \
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_pc, k_correct<T, RR, true>, nt, march_smem<T, RR, 5, 2>()); \
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_pr, k_predict<T, RR>, nt, march_smem<T, RR, 4, 2>());      \
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_rk, k_rkstage<T, RR>, nt, march_smem<T, RR, 1, 2>()); \
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_d1, k_d1march<T, RR, 0>, nt, 0);                    \
-    break;
-    switch (fd.R) { EP_OCC(1) EP_OCC(2) EP_OCC(3) EP_OCC(4) EP_OCC(5) EP_OCC(6) default: break; }
-#undef EP_OCC
-    zc_pc = march_zchunk(occ_pc);
-    zc_pr = march_zchunk(occ_pr);
-    zc_rk = march_zchunk(occ_rk);
-    zc_d1 = march_zchunk(occ_d1, EP_D1_TX);
-  }
+  if ((r = x_attrs()) || (r = fft_attrs()) || (r = march_setup())) return r;
   {
     const long long nxy = (long long)((c.nx + EP_TX - 1) / EP_TX) * ((c.ny + EP_TY - 1) / EP_TY);
     const int zmin = std::min(std::min(zc_pc, zc_pr), zc_rk);
@@ -331,6 +298,8 @@ void Engine<T>::release() {
 
 // ---------------------------------------------------------------------------
 // Register-resident transforms (ep_rfft.cuh) of lines of length N.
+#endif
+#if EP_ENGINE_PARTS & EP_PART_FFT
 template <class T>
 template <int N>
 int Engine<T>::rfft_y(const Arr8<T>& a, int n, const LineSet& ls, int dir) {
@@ -415,13 +384,18 @@ int Engine<T>::zconv(const CT* const* in, CT* const (*out)[3], const T* const (*
 }
 
 // First-derivative marches (k_d1march): mode 0 = grad f, mode 1 = dy f + dz f2.
+#endif
+#if EP_ENGINE_PARTS & EP_PART_MARCH
 template <class T>
 int Engine<T>::d1march(int mode, const T* f, const T* f2, T* o0, T* o1, T* o2) {
   dim3 grid((g.nx + EP_D1_TX - 1) / EP_D1_TX, (g.ny + EP_TY - 1) / EP_TY, (g.nz + zc_d1 - 1) / zc_d1);
   dim3 blk(EP_TX, EP_TY);
 #define EP_D1(RR)                                                                                  \
   case RR:                                                                                         \
-    if (mode == 0) {                                                                               \
+    if constexpr (!r_built<T>(RR)) {                                                               \
+      *err = "double-float fields are built for npd = 13 only";                                    \
+      return EP_ERR_UNSUPPORTED;                                                                   \
+    } else if (mode == 0) {                                                                        \
       auto k = k_d1march<T, RR, 0>;                                                                \
       EP_LAUNCH("grad_march", k, grid, blk, 0, g, fd, zc_d1, f, f2, o0, o1, o2);                  \
     } else {                                                                                       \
@@ -438,17 +412,14 @@ int Engine<T>::d1march(int mode, const T* f, const T* f2, T* o0, T* o1, T* o2) {
 }
 
 // poten() + derden() + term_alfa() (poten.f90:5-131, term_alfa.f90:5-109).
+#endif
+#if EP_ENGINE_PARTS & EP_PART_X
 template <class T>
 int Engine<T>::poten() {
   const bool otc = cfg.core == EP_CORE_OTC;
   const bool grad = otc || cfg.impurity != EP_IMPURITY_NONE;
-  const long long nlines = (long long)g.ny * g.nz;
   int r;
-  {
-    const int nl = x_lines(0, 0);
-    EP_XLAUNCH("x1_r2c_den", k_x1, (unsigned)((nlines + nl - 1) / nl), shp.xthr[0], x_smem(nl, 0), g, den, S[0], p2, twx,
-               nl);
-  }
+  if ((r = x_pass(1, otc))) return r;
   if (grad && (r = d1march(0, den, nullptr, dxd, dyd, dzd))) return r;
   CT* a1[1] = {S[0]};
   if ((r = fft_y(a1, 1, -1))) return r;
@@ -461,11 +432,7 @@ int Engine<T>::poten() {
   }
   CT* b3[3] = {Tb[0], Tb[1], Tb[2]};
   if ((r = fft_y(b3, otc ? 3 : 2, +1))) return r;
-  {
-    const int nl = x_lines(1, otc ? 3 : 2);
-    EP_XLAUNCH("x2_c2r_r2c", k_x2, (unsigned)((nlines + nl - 1) / nl), shp.xthr[1], x_smem(nl, otc ? 3 : 2), g, phys, Tb[0],
-              Tb[1], Tb[2], den, dxd, dyd, dzd, dencg, delj4, pot4, falfs, S[0], S[1], S[2], S[3], p2, twx, nl);
-  }
+  if ((r = x_pass(2, otc))) return r;
   CT* c4[4] = {S[0], S[1], S[2], S[3]};
   if ((r = fft_y(c4, otc ? 4 : 1, -1))) return r;
   {
@@ -477,12 +444,7 @@ int Engine<T>::poten() {
   }
   CT* d4[4] = {Tb[0], Tb[1], Tb[2], Tb[3]};
   if ((r = fft_y(d4, otc ? 4 : 1, +1))) return r;
-  {
-    const int nl = x_lines(2, otc ? 4 : 1);
-    EP_XLAUNCH("x3_c2r_r2c", k_x3, (unsigned)((nlines + nl - 1) / nl), shp.xthr[2], x_smem(nl, otc ? 4 : 1), g, phys, fd,
-              Tb[0], Tb[1], Tb[2], Tb[3], den, dxd, dyd, dzd, falfs, pot4, intx, inty, intz, gy, gz, dgx, S[0], p2,
-              twx, nl);
-  }
+  if ((r = x_pass(3, otc))) return r;
   if (otc) {
     if ((r = d1march(1, gy, gz, dyz, nullptr, nullptr))) return r;
     if ((r = fft_y(a1, 1, -1))) return r;
@@ -493,14 +455,14 @@ int Engine<T>::poten() {
     if ((r = zconv(in, out, ker, no, 1))) return r;
     CT* e1[1] = {Tb[0]};
     if ((r = fft_y(e1, 1, +1))) return r;
-    const int nl = x_lines(3, 1);
-    EP_XLAUNCH("x4_c2r_ualpha", k_x4, (unsigned)((nlines + nl - 1) / nl), shp.xthr[3], x_smem(nl, 1), g, phys, Tb[0], den,
-              dgx, dyz, pot4, ualphas, p2, twx, nl);
+    if ((r = x_pass(4, otc))) return r;
   }
   have_field = true;
   return EP_OK;
 }
 
+#endif
+#if EP_ENGINE_PARTS & EP_PART_REST
 template <class T>
 int Engine<T>::potenimp() {
   if (cfg.impurity == EP_IMPURITY_NONE) return cuda_ok(cudaMemsetAsync(uimp, 0, g.N * sizeof(T), st), "uimp");
@@ -756,6 +718,8 @@ int Engine<T>::refresh() {
 // Launch of a stencil-march kernel, or -- while a step graph is replayed --
 // an update of its captured node (which = 0 predictor, 1 corrector).  While
 // a step is captured the node just recorded is remembered for the updates.
+#endif
+#if EP_ENGINE_PARTS & EP_PART_MARCH
 template <class T>
 int Engine<T>::launch_march(const void* fn, dim3 grid, dim3 blk, size_t smem, void** args, const char* name,
                             int which) {
@@ -807,13 +771,19 @@ int Engine<T>::lap_predict(double dt) {
   void* args[] = {&g, &fd, &phys, &zc, &psic, &pot4c, &uimpc, &po3, &h1, &h2, &pc, &den, &f, &c1, &sc, &sl};
   const void* fn = nullptr;
   size_t smem = 0;
-#define EP_PRED(RR) \
-  case RR: fn = (const void*)k_predict<T, RR>; smem = march_smem<T, RR, 4, 2>(); break;
+#define EP_PRED(RR)                                                                   \
+  case RR:                                                                            \
+    if constexpr (r_built<T>(RR)) {                                                   \
+      fn = (const void*)k_predict<T, RR>;                                             \
+      smem = march_smem<T, RR, 4, 2>();                                               \
+    }                                                                                 \
+    break;
   switch (fd.R) {
     EP_PRED(1) EP_PRED(2) EP_PRED(3) EP_PRED(4) EP_PRED(5) EP_PRED(6)
     default: *err = "npd > 13 not built"; return EP_ERR_UNSUPPORTED;
   }
 #undef EP_PRED
+  if (!fn) { *err = "npd not built in this precision"; return EP_ERR_UNSUPPORTED; }
   int r;
   if ((r = launch_march(fn, grid, blk, smem, args, "predict", 0))) return r;
   std::swap(psi, po[ioldp[2]]);
@@ -843,14 +813,17 @@ int Engine<T>::lap_correct(double dt, bool want) {
   size_t smem = 0;
 #define EP_CORR(RR)                                                                                   \
   case RR:                                                                                            \
-    fn = want ? (const void*)k_correct<T, RR, true> : (const void*)k_correct<T, RR, false>;           \
-    smem = march_smem<T, RR, 5, 2>();                                                                 \
+    if constexpr (r_built<T>(RR)) {                                                                   \
+      fn = want ? (const void*)k_correct<T, RR, true> : (const void*)k_correct<T, RR, false>;         \
+      smem = march_smem<T, RR, 5, 2>();                                                               \
+    }                                                                                                 \
     break;
   switch (fd.R) {
     EP_CORR(1) EP_CORR(2) EP_CORR(3) EP_CORR(4) EP_CORR(5) EP_CORR(6)
     default: *err = "npd > 13 not built"; return EP_ERR_UNSUPPORTED;
   }
 #undef EP_CORR
+  if (!fn) { *err = "npd not built in this precision"; return EP_ERR_UNSUPPORTED; }
   int r;
   if ((r = launch_march(fn, grid, blk, smem, args, "correct", 1))) return r;
   std::swap(psi, spare);
@@ -889,11 +862,13 @@ int Engine<T>::rk_stage(int jr, double dt) {
   dim3 blk(EP_TX, EP_TY);
   const T a = (T)arun[jr], b = (T)brun[jr], cr = (T)crun[jr], d = (T)dt;
 #define EP_RK(RR)                                                                                              \
-  case RR: {                                                                                                   \
-    auto k = k_rkstage<T, RR>;                                                                                 \
-    EP_LAUNCH("rkstage", k, grid, blk, (march_smem<T, RR, 1, 2>()), g, fd, phys, zc_rk, psi, pot4, uimp, q, out, hout, \
-              den, a, b, cr, d, sc);                                                                           \
-  } break;
+  case RR:                                                                                                     \
+    if constexpr (r_built<T>(RR)) {                                                                            \
+      auto k = k_rkstage<T, RR>;                                                                               \
+      EP_LAUNCH("rkstage", k, grid, blk, (march_smem<T, RR, 1, 2>()), g, fd, phys, zc_rk, psi, pot4, uimp, q, out, \
+                hout, den, a, b, cr, d, sc);                                                                   \
+    }                                                                                                          \
+    break;
   switch (fd.R) {
     EP_RK(1) EP_RK(2) EP_RK(3) EP_RK(4) EP_RK(5) EP_RK(6)
     default: *err = "npd > 13 not built"; return EP_ERR_UNSUPPORTED;
@@ -917,6 +892,8 @@ int Engine<T>::rk_stage(int jr, double dt) {
 }
 
 // steprk (steprk.f90:1-191).
+#endif
+#if EP_ENGINE_PARTS & EP_PART_REST
 template <class T>
 int Engine<T>::steprk(double dt, bool wait) {
   if (!have_field) { *err = "poten() must run before steprk()"; return EP_ERR_STATE; }
@@ -1324,3 +1301,129 @@ done:
   cudaEventDestroy(b);
   return r;
 }
+
+#endif
+#if EP_ENGINE_PARTS & EP_PART_X
+template <class T>
+int Engine<T>::x_attrs() {
+  int r;
+  if ((r = x_attrs_n2<0>()) || (r = x_attrs_n2<16>()) || (r = x_attrs_n2<32>()) || (r = x_attrs_n2<64>()) ||
+      (r = x_attrs_n2<128>()))
+    return r;
+  if constexpr (sizeof(T) == 4) {
+    if ((r = x_attrs_n2<48>()) || (r = x_attrs_n2<80>()) || (r = x_attrs_n2<96>())) return r;
+  }
+  return EP_OK;
+}
+
+// X pass `which` (1..4) of poten on the register transform of this grid's
+// half-lines (N2 = 0: the general engine).
+template <class T>
+int Engine<T>::x_pass(int which, bool otc) {
+  switch (x_reg_n2<T>(g.nx / 2)) {
+    case 16: return x_launch<16>(which, otc);
+    case 32: return x_launch<32>(which, otc);
+    case 64: return x_launch<64>(which, otc);
+    case 128: return x_launch<128>(which, otc);
+    case 48: if constexpr (sizeof(T) == 4) return x_launch<48>(which, otc); break;
+    case 80: if constexpr (sizeof(T) == 4) return x_launch<80>(which, otc); break;
+    case 96: if constexpr (sizeof(T) == 4) return x_launch<96>(which, otc); break;
+    default: break;
+  }
+  return x_launch<0>(which, otc);
+}
+#endif
+
+#if EP_ENGINE_PARTS & EP_PART_XK
+template <class T>
+template <int N2>
+int Engine<T>::x_attrs_n2() {
+  const int big = 220 * 1024;
+  cudaFuncSetAttribute(k_x1<T, N2>, cudaFuncAttributeMaxDynamicSharedMemorySize, big);
+  cudaFuncSetAttribute(k_x2<T, N2>, cudaFuncAttributeMaxDynamicSharedMemorySize, big);
+  cudaFuncSetAttribute(k_x3<T, N2>, cudaFuncAttributeMaxDynamicSharedMemorySize, big);
+  cudaFuncSetAttribute(k_x4<T, N2>, cudaFuncAttributeMaxDynamicSharedMemorySize, big);
+  return EP_OK;
+}
+
+template <class T>
+template <int N2>
+int Engine<T>::x_launch(int which, bool otc) {
+  const long long nlines = (long long)g.ny * g.nz;
+  if (which == 1) {
+    const int nl = x_lines(0, 0);
+    auto k = k_x1<T, N2>;
+    EP_LAUNCH("x1_r2c_den", k, (unsigned)((nlines + nl - 1) / nl), shp.xthr[0], x_smem(nl, 0), g, den, S[0], p2, twx, nl);
+  } else if (which == 2) {
+    const int nl = x_lines(1, otc ? 3 : 2);
+    auto k = k_x2<T, N2>;
+    EP_LAUNCH("x2_c2r_r2c", k, (unsigned)((nlines + nl - 1) / nl), shp.xthr[1], x_smem(nl, otc ? 3 : 2), g, phys, Tb[0],
+              Tb[1], Tb[2], den, dxd, dyd, dzd, dencg, delj4, pot4, falfs, S[0], S[1], S[2], S[3], p2, twx, nl);
+  } else if (which == 3) {
+    const int nl = x_lines(2, otc ? 4 : 1);
+    auto k = k_x3<T, N2>;
+    EP_LAUNCH("x3_c2r_r2c", k, (unsigned)((nlines + nl - 1) / nl), shp.xthr[2], x_smem(nl, otc ? 4 : 1), g, phys, fd,
+              Tb[0], Tb[1], Tb[2], Tb[3], den, dxd, dyd, dzd, falfs, pot4, intx, inty, intz, gy, gz, dgx, S[0], p2, twx,
+              nl);
+  } else {
+    const int nl = x_lines(3, 1);
+    auto k = k_x4<T, N2>;
+    EP_LAUNCH("x4_c2r_ualpha", k, (unsigned)((nlines + nl - 1) / nl), shp.xthr[3], x_smem(nl, 1), g, phys, Tb[0], den,
+              dgx, dyz, pot4, ualphas, p2, twx, nl);
+  }
+  return EP_OK;
+}
+#endif
+
+#if EP_ENGINE_PARTS & EP_PART_FFT
+template <class T>
+int Engine<T>::fft_attrs() {
+  const int big = 220 * 1024;
+  cudaFuncSetAttribute(k_c2c<T, -1>, cudaFuncAttributeMaxDynamicSharedMemorySize, big);
+  cudaFuncSetAttribute(k_c2c<T, +1>, cudaFuncAttributeMaxDynamicSharedMemorySize, big);
+  cudaFuncSetAttribute(k_zconv<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, big);
+#define EP_RFFT_ATTR(NN)                                                                                  \
+  cudaFuncSetAttribute(k_c2c_r<T, NN, -1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)rfft::smem_bytes<T, NN>()); \
+  cudaFuncSetAttribute(k_c2c_r<T, NN, +1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)rfft::smem_bytes<T, NN>()); \
+  cudaFuncSetAttribute(k_zconv_r<T, NN, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)rfft::smem_bytes<T, NN>()); \
+  cudaFuncSetAttribute(k_zconv_r<T, NN, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)rfft::smem_bytes<T, NN>());
+  EP_RFFT_ATTR(32) EP_RFFT_ATTR(64) EP_RFFT_ATTR(128) EP_RFFT_ATTR(256)
+  if constexpr (sizeof(T) == 4) { EP_RFFT_ATTR(96) EP_RFFT_ATTR(192) }
+#undef EP_RFFT_ATTR
+  return EP_OK;
+}
+#endif
+
+#if EP_ENGINE_PARTS & EP_PART_MARCH
+template <class T>
+int Engine<T>::march_setup() {
+#define EP_ATTR(RR)                                                                                      \
+  if constexpr (r_built<T>(RR)) {                                                                        \
+  cudaFuncSetAttribute(k_predict<T, RR>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)march_smem<T, RR, 4, 2>()); \
+  cudaFuncSetAttribute(k_correct<T, RR, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)march_smem<T, RR, 5, 2>()); \
+  cudaFuncSetAttribute(k_correct<T, RR, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)march_smem<T, RR, 5, 2>()); \
+  cudaFuncSetAttribute(k_rkstage<T, RR>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)march_smem<T, RR, 1, 2>()); }
+  EP_ATTR(1) EP_ATTR(2) EP_ATTR(3) EP_ATTR(4) EP_ATTR(5) EP_ATTR(6)
+#undef EP_ATTR
+  {
+    // z-chunk lengths of the stencil marches from their resident blocks per SM
+    int occ_pc = 0, occ_pr = 0, occ_rk = 0, occ_d1 = 0;
+    const int nt = EP_TX * EP_TY;
+#define EP_OCC(RR)                                                                                         \
+  case RR:                                                                                                 \
+    if constexpr (r_built<T>(RR)) {                                                                        \
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_pc, k_correct<T, RR, true>, nt, march_smem<T, RR, 5, 2>()); \
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_pr, k_predict<T, RR>, nt, march_smem<T, RR, 4, 2>());      \
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_rk, k_rkstage<T, RR>, nt, march_smem<T, RR, 1, 2>()); \
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_d1, k_d1march<T, RR, 0>, nt, 0); }                  \
+    break;
+    switch (fd.R) { EP_OCC(1) EP_OCC(2) EP_OCC(3) EP_OCC(4) EP_OCC(5) EP_OCC(6) default: break; }
+#undef EP_OCC
+    zc_pc = march_zchunk(occ_pc);
+    zc_pr = march_zchunk(occ_pr);
+    zc_rk = march_zchunk(occ_rk);
+    zc_d1 = march_zchunk(occ_d1, EP_D1_TX);
+  }
+  return EP_OK;
+}
+#endif

@@ -29,6 +29,15 @@ template <> struct K<double> {
   static constexpr double s52 = 0.58778525229247312916870595463907;  // sin(4pi/5)
   static constexpr double r2 = 0.70710678118654752440084436210485;   // 1/sqrt(2)
 };
+template <> struct K<dfloat> {
+  static constexpr dfloat half = dfloat(0.5);
+  static constexpr dfloat s3 = dfloat(0.86602540378443864676372317075294);
+  static constexpr dfloat c51 = dfloat(0.30901699437494742410229341718282);
+  static constexpr dfloat c52 = dfloat(-0.80901699437494742410229341718282);
+  static constexpr dfloat s51 = dfloat(0.95105651629515357211643933337938);
+  static constexpr dfloat s52 = dfloat(0.58778525229247312916870595463907);
+  static constexpr dfloat r2 = dfloat(0.70710678118654752440084436210485);
+};
 template <> struct K<float> {
   static constexpr float half = 0.5f;
   static constexpr float s3 = 0.86602540378443864676372317075294f;
@@ -107,6 +116,11 @@ template <> struct K16<double> {
   static constexpr double c = 0.92387953251128675612818318939678829;  // cos(pi/8)
   static constexpr double s = 0.38268343236508977172845998403039887;  // sin(pi/8)
   static constexpr double r = 0.70710678118654752440084436210484904;  // 1/sqrt(2)
+};
+template <> struct K16<dfloat> {
+  static constexpr dfloat c = dfloat(0.92387953251128675612818318939678829);
+  static constexpr dfloat s = dfloat(0.38268343236508977172845998403039887);
+  static constexpr dfloat r = dfloat(0.70710678118654752440084436210484904);
 };
 template <> struct K16<float> {
   static constexpr float c = 0.92387953251128675612818318939678829f;

@@ -1,6 +1,7 @@
 // ep_kernels.cuh - device kernels of the eff_pot hot path, templated on the
 // field precision T (double or float).  Reductions always accumulate in FP64.
 #pragma once
+#include <type_traits>
 #include "ep_common.cuh"
 #include "ep_fft.cuh"
 #include "ep_reduce.cuh"
@@ -19,6 +20,11 @@ template <class T> struct FdW {
 struct PhysF {
   float cp4, cpp4, a0, a1, rden0s, h2o2m4, alphas, C, beta, den_m, renor;
 };
+// The same constants split into double-float pairs on the host, for the
+// double-float kernels.
+struct PhysD {
+  dfloat cp4, cpp4, a0, a1, rden0s, h2o2m4, alphas, C, beta, den_m, renor;
+};
 struct Phys {
   double cp4, cpp4, a0, a1, den0s, h2o2m4, alphas, C, beta, den_m;
   double renor, dxyz;
@@ -26,6 +32,7 @@ struct Phys {
   int core;               // EP_CORE_*
   int time_mode;          // 0 imaginary, 1 real
   PhysF f;                // the same constants for the FP32 kernels
+  PhysD d;                // and for the double-float kernels
 };
 
 // Phys in the field precision T.  FP32 kernels take the host-rounded copies:
@@ -39,6 +46,12 @@ template <> struct PConst<double> {
       : cp4(p.cp4), cpp4(p.cpp4), a0(p.a0), a1(p.a1), rden0s(p.rden0s), h2o2m4(p.h2o2m4), alphas(p.alphas),
         C(p.C), beta(p.beta), den_m(p.den_m), renor(p.renor) {}
 };
+template <> struct PConst<dfloat> {
+  dfloat cp4, cpp4, a0, a1, rden0s, h2o2m4, alphas, C, beta, den_m, renor;
+  EP_DEV explicit PConst(const Phys& p)
+      : cp4(p.d.cp4), cpp4(p.d.cpp4), a0(p.d.a0), a1(p.d.a1), rden0s(p.d.rden0s), h2o2m4(p.d.h2o2m4),
+        alphas(p.d.alphas), C(p.d.C), beta(p.d.beta), den_m(p.d.den_m), renor(p.d.renor) {}
+};
 template <> struct PConst<float> {
   float cp4, cpp4, a0, a1, rden0s, h2o2m4, alphas, C, beta, den_m, renor;
   EP_DEV explicit PConst(const Phys& p)
@@ -50,6 +63,7 @@ template <> struct PConst<float> {
 template <class T> EP_DEV T bscale_of(const DevScalars* sc, int k);
 template <> EP_DEV double bscale_of<double>(const DevScalars* sc, int k) { return sc->bscale[k]; }
 template <> EP_DEV float bscale_of<float>(const DevScalars* sc, int k) { return sc->bscale_f[k]; }
+template <> EP_DEV dfloat bscale_of<dfloat>(const DevScalars* sc, int k) { return dfloat(sc->bscale[k]); }
 
 // Lines of a strided pass: element k of line L lives at
 //   (L % Mi) + (L / Mi) * So + k * Sa.
@@ -138,6 +152,13 @@ EP_DEV float penalty_of(const Pen<float>& pn, float den) {
   const float omt2 = 4.0f * e / ((1.0f + e) * (1.0f + e));
   return pn.C * (onept + pn.beta * den * omt2);
 }
+// Double-float fields: the penalty in FP32 (at the densities of a liquid it
+// is below 1e-7 K, and a density near den_m is far outside the method).
+template <> struct Pen<dfloat> {
+  Pen<float> f;
+  EP_DEV explicit Pen(const Phys& ph) : f(ph) {}
+};
+EP_DEV dfloat penalty_of(const Pen<dfloat>& pn, dfloat den) { return dfloat(penalty_of(pn.f, den.hi)); }
 
 // H-apply of steppc.f90:53 / steprk.f90:74-75:
 //   imaginary time: (lap*h2o2m4 - pot4*psi) - uimp*psi
@@ -407,6 +428,9 @@ EP_DEV Pack<T, K> ldk(const T* p) {
   } else if constexpr (sizeof(T) == 4) {
     const float4 q = *reinterpret_cast<const float4*>(p);
     r.v[0] = q.x; r.v[1] = q.y; r.v[2] = q.z; r.v[3] = q.w;
+  } else if constexpr (std::is_same<T, dfloat>::value) {
+    const float4 q = *reinterpret_cast<const float4*>(p);
+    r.v[0] = dfloat(q.x, q.y); r.v[1] = dfloat(q.z, q.w);
   } else {
     const double2 q = *reinterpret_cast<const double2*>(p);
     r.v[0] = q.x; r.v[1] = q.y;
@@ -419,6 +443,8 @@ EP_DEV void stk(T* p, const Pack<T, K>& r) {
     *p = r.v[0];
   } else if constexpr (sizeof(T) == 4) {
     *reinterpret_cast<float4*>(p) = make_float4(r.v[0], r.v[1], r.v[2], r.v[3]);
+  } else if constexpr (std::is_same<T, dfloat>::value) {
+    *reinterpret_cast<float4*>(p) = make_float4(r.v[0].hi, r.v[0].lo, r.v[1].hi, r.v[1].lo);
   } else {
     *reinterpret_cast<double2*>(p) = make_double2(r.v[0], r.v[1]);
   }
@@ -1497,6 +1523,11 @@ template <> EP_HD float2 conv<float2, double2>(double2 a) { return make_float2((
 template <> EP_HD double2 conv<double2, float2>(float2 a) { return make_double2(a.x, a.y); }
 template <> EP_HD double2 conv<double2, double2>(double2 a) { return a; }
 template <> EP_HD float2 conv<float2, float2>(float2 a) { return a; }
+template <> EP_HD dfloat2 conv<dfloat2, double2>(double2 a) { return dfloat2{dfloat(a.x), dfloat(a.y)}; }
+template <> EP_HD double2 conv<double2, dfloat2>(dfloat2 a) { return make_double2((double)a.x, (double)a.y); }
+template <> EP_HD dfloat2 conv<dfloat2, float2>(float2 a) { return dfloat2{dfloat(a.x), dfloat(a.y)}; }
+template <> EP_HD float2 conv<float2, dfloat2>(dfloat2 a) { return make_float2((float)a.x, (float)a.y); }
+template <> EP_HD dfloat2 conv<dfloat2, dfloat2>(dfloat2 a) { return a; }
 template <class A, class B>
 __global__ void k_convert(const A* __restrict__ in, B* __restrict__ out, long long n) {
   for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)

@@ -151,12 +151,12 @@ __global__ void k_impmoments_d(Geo g, const T* __restrict__ den, const T* __rest
   for (long long p = blockIdx.x * (long long)blockDim.x + threadIdx.x; p < g.N; p += (long long)gridDim.x * blockDim.x) {
     int ix, iy, iz;
     idx3(g, p, ix, iy, iz);
-    const double u = uimp[p];
+    const double u = dbl(uimp[p]);
     acc[0].add((double)dxd[p] * u);
     acc[1].add((double)dyd[p] * u);
     if (iz >= izlo && iz < izhi) acc[2].add((double)dzd[p] * u);
     const double xx = coord(xmax, hx, ix) - r0, yy = coord(ymax, hy, iy) - r1, zz = coord(zmax, hz, iz) - r2;
-    const double rho = den[p];
+    const double rho = dbl(den[p]);
     const double dvd = (double)delta[p] * rho, dv1 = (double)pidel[p] * rho, dv2 = (double)sigdel[p] * rho;
     double a[5], P[15];
     dstate_factors(xx, yy, zz, a, P);
@@ -245,7 +245,7 @@ __global__ void k_normsum(const C2<T>* __restrict__ psi, long long N, double* __
   Acc<double> acc[1];
   for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < N; i += (long long)gridDim.x * blockDim.x) {
     const C2<T> v = psi[i];
-    acc[0].add((double)v.x * v.x + (double)v.y * v.y);
+    acc[0].add(dbl(v.x) * dbl(v.x) + dbl(v.y) * dbl(v.y));
   }
   block_reduce_store_acc<1>(acc, partials);
 }
@@ -284,13 +284,13 @@ __global__ void k_energy(Geo g, FdW<T> fd, Phys ph, const C2<T>* __restrict__ ps
     const C2<T> dx = d1c_global(psi, p, ix, g.nx, 1, fd.w1[0], fd.R, fd.periodic);
     const C2<T> dy = d1c_global(psi, p, iy, g.ny, (long long)g.nx, fd.w1[1], fd.R, fd.periodic);
     const C2<T> dz = d1c_global(psi, p, iz, g.nz, (long long)g.nx * g.ny, fd.w1[2], fd.R, fd.periodic);
-    const double dn = den[p], cg = dencg[p];
-    acc[0].add(((double)dx.x * dx.x + (double)dx.y * dx.y) + ((double)dy.x * dy.x + (double)dy.y * dy.y) +
-               ((double)dz.x * dz.x + (double)dz.y * dz.y));
+    const double dn = dbl(den[p]), cg = dbl(dencg[p]);
+    acc[0].add((dbl(dx.x) * dbl(dx.x) + dbl(dx.y) * dbl(dx.y)) + (dbl(dy.x) * dbl(dy.x) + dbl(dy.y) * dbl(dy.y)) +
+               (dbl(dz.x) * dbl(dz.x) + dbl(dz.y) * dbl(dz.y)));
     acc[1].add((double)delj4[p] * dn);
     acc[2].add(dn * (cg * cg) * (aux1 + aux2 * cg));
     if (otc)
-      acc[3].add((double)falfs[p] * ((double)dxd[p] * ix_[p] + (double)dyd[p] * iy_[p] + (double)dzd[p] * iz_[p]));
+      acc[3].add(dbl(falfs[p]) * (dbl(dxd[p]) * dbl(ix_[p]) + dbl(dyd[p]) * dbl(iy_[p]) + dbl(dzd[p]) * dbl(iz_[p])));
     acc[4].add(dn * (1.0 + tanh(ph.beta * (dn - ph.den_m))));
     if (impurity) {
       const double a = r0 - coord(xmax, hx, ix), b = r1 - coord(ymax, hy, iy), c = r2 - coord(zmax, hz, iz);
@@ -315,12 +315,12 @@ __global__ void k_impmoments(Geo g, const T* __restrict__ den, const T* __restri
   for (long long p = blockIdx.x * (long long)blockDim.x + threadIdx.x; p < g.N; p += (long long)gridDim.x * blockDim.x) {
     int ix, iy, iz;
     idx3(g, p, ix, iy, iz);
-    const double u = uimp[p];
+    const double u = dbl(uimp[p]);
     acc[0].add((double)dxd[p] * u);
     acc[1].add((double)dyd[p] * u);
     if (iz >= izlo && iz < izhi) acc[2].add((double)dzd[p] * u);
     const double xx = coord(xmax, hx, ix) - r0, yy = coord(ymax, hy, iy) - r1, zz = coord(zmax, hz, iz) - r2;
-    const double a1 = den[p], a2 = delta[p], a3 = vpi[p];
+    const double a1 = dbl(den[p]), a2 = dbl(delta[p]), a3 = dbl(vpi[p]);
     acc[3].add(a1 * (a2 * xx * xx + a3));
     acc[4].add(a1 * a2 * xx * yy);
     acc[5].add(a1 * a2 * xx * zz);

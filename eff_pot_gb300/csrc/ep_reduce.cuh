@@ -67,9 +67,26 @@ template <class T> struct Kahan {
   EP_DEV T lo() const { return -c; }
   EP_DEV double get() const { return (double)s - (double)c; }
 };
-// The accumulator of sums of T values: Neumaier in FP64, Kahan in FP32.
+// Double-float terms: Kahan in FP32 on the high parts, the low parts summed
+// apart (value s - c + l); the block reduction carries FP32 pairs.
+template <> struct Kahan<dfloat> {
+  typedef float value_type;
+  float s = 0.0f, c = 0.0f, l = 0.0f;
+  EP_DEV void add(dfloat v) {
+    const float y = v.hi - c;
+    const float t = s + y;
+    c = (t - s) - y;
+    s = t;
+    l += v.lo;
+  }
+  EP_DEV float lo() const { return l - c; }
+  EP_DEV double get() const { return (double)s - (double)c + (double)l; }
+};
+// The accumulator of sums of T values: Neumaier in FP64, Kahan in FP32 and
+// double-float.
 template <class T> struct AccOf { typedef Neumaier<T> type; };
 template <> struct AccOf<float> { typedef Kahan<float> type; };
+template <> struct AccOf<dfloat> { typedef Kahan<dfloat> type; };
 template <class T> using Acc = typename AccOf<T>::type;
 
 template <class F>

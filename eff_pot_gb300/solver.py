@@ -18,6 +18,8 @@ from . import _abi
 from .config import make_config, config_dict, MP_U
 
 _HERE = os.path.dirname(os.path.abspath(__file__))
+PRECISIONS = {"fp64": _abi.EP_FP64, "fp32": _abi.EP_FP32, "dfloat": _abi.EP_DFLOAT}
+PRECISION_NAMES = {v: k for k, v in PRECISIONS.items()}
 LIBPATH = os.path.join(_HERE, "_build", "libeffpot.so")
 _lib = None
 _funcs = None
@@ -292,12 +294,12 @@ class Solver:
         return n.value
 
     def set_precision(self, precision):
-        """'fp32'/'fp64' (or EP_FP32/EP_FP64): convert the state and go on."""
-        p = {"fp32": _abi.EP_FP32, "fp64": _abi.EP_FP64}.get(precision, precision)
-        self._check(self._f["set_precision"](self._h, p), "set_precision")
+        """'fp32' / 'fp64' / 'dfloat' (or EP_FP32 / EP_FP64 / EP_DFLOAT):
+        convert the state and go on in that arithmetic."""
+        self._check(self._f["set_precision"](self._h, PRECISIONS.get(precision, precision)), "set_precision")
 
     def precision(self):
-        return "fp32" if self._f["get_precision"](self._h) == _abi.EP_FP32 else "fp64"
+        return PRECISION_NAMES[self._f["get_precision"](self._h)]
 
     def autotune(self):
         """Pick the FFT-pass launch shapes for this grid (needs a density)."""
@@ -397,8 +399,8 @@ class Batch:
         return [dict(errHe=s.errHe, mu=s.mu, norm=s.norm, steps_done=s.steps_done) for s in stats]
 
     def set_precision(self, precision):
-        p = {"fp32": _abi.EP_FP32, "fp64": _abi.EP_FP64}.get(precision, precision)
-        self._check(self._f["batch_set_precision"](self._h, p), "batch_set_precision")
+        self._check(self._f["batch_set_precision"](self._h, PRECISIONS.get(precision, precision)),
+                    "batch_set_precision")
 
     def autotune(self):
         self._check(self._f["batch_autotune"](self._h), "batch_autotune")

@@ -41,7 +41,10 @@ enum { EP_IMAGINARY_TIME = 0, EP_REAL_TIME = 1 };
 /* ---- impurity treatment ------------------------------------------------- */
 enum { EP_IMPURITY_NONE = 0, EP_IMPURITY_FIXED = 1, EP_IMPURITY_MOVING = 2 };
 /* ---- arithmetic of the bulk field updates ------------------------------ */
-enum { EP_FP64 = 0, EP_FP32 = 1 };
+/* Field arithmetic: FP64; FP32; double-float (each real an unevaluated sum
+ * of two FP32 values, about 48 significant bits, computed on the FP32 pipes:
+ * the FP64-class path that is not bound by the FP64 pipe). */
+enum { EP_FP64 = 0, EP_FP32 = 1, EP_DFLOAT = 2 };
 /* ---- boundary modes of the finite differences (newder.f ICON) ---------- */
 enum { EP_ICON_PERIODIC = 8, EP_ICON_ZERO_OUTSIDE = 13 };
 /* ---- electronic state of the impurity (Lstate, modules.f90:303) -------- */
@@ -73,7 +76,7 @@ typedef struct ep_config {
   double als_p;              /* spin-orbit splitting, P state               */
   double ev0;                /* phase reference of potinvar                 */
   double z_exciplex_exclusion;
-  int precision;             /* EP_FP64 / EP_FP32                           */
+  int precision;             /* EP_FP64 / EP_FP32 / EP_DFLOAT               */
   int device;                /* CUDA device ordinal                         */
   int state;                 /* Lstate: EP_STATE_P (default) / EP_STATE_D   */
   double als_d;              /* spin-orbit splitting, D state (Als_D)       */
@@ -298,11 +301,12 @@ int ep_run(ep_ctx* ctx, int nsteps, double deltat, ep_run_stats* stats);
 /* Renormalise psi to n4 now (imaginary time). */
 int ep_renormalize(ep_ctx* ctx, double* norm_before);
 
-/* Switch the arithmetic of the bulk fields between EP_FP32 and EP_FP64,
- * keeping the state: psi, the multistep history (psiold, hpsiold, pc, q)
- * and every field are converted and the next steps run in the new
- * precision.  FP32 -> FP64 starts the FP64 refinement sweeps of a FP32 run;
- * the first switch allocates the FP64 buffers. */
+/* Switch the arithmetic of the bulk fields between EP_FP32, EP_FP64 and
+ * EP_DFLOAT, keeping the state: psi, the multistep history (psiold,
+ * hpsiold, pc, q) and every field are converted and the next steps run in
+ * the new precision.  FP32 -> FP64 (or -> EP_DFLOAT) starts the refinement
+ * sweeps of a FP32 run; the first switch to a precision allocates its
+ * buffers. */
 int ep_set_precision(ep_ctx* ctx, int precision);
 int ep_get_precision(const ep_ctx* ctx);
 

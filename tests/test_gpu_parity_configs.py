@@ -18,10 +18,11 @@ every transform length they run is checked against the oracle:
   real time (the large real-time configuration, on its full grid): X
   half-lines of 128, Y lines of 256, Z lines of 320.
 
-Gates: FP64 -- the drop-in bar, 1e-10 relative in the total energy and the
-chemical potential and 1e-9 A^-3 max-abs in the density, fields 1e-11
-relative, psi 1e-10 relative; FP32 -- 2e-5 relative in fields and energies,
-1e-4 relative in psi, 1e-6 A^-3 max-abs in the density.
+Gates: FP64 and double-float -- the drop-in bar, 1e-10 relative in the
+total energy and the chemical potential and 1e-9 A^-3 max-abs in the
+density, fields 1e-11 relative, psi 1e-10 relative; FP32 -- 2e-5 relative
+in fields and energies, 1e-4 relative in psi, 1e-6 A^-3 max-abs in the
+density.
 """
 import numpy as np
 import pytest
@@ -111,13 +112,14 @@ def oracle_result(oracle, name):
     return _ORACLE[name]
 
 
-@pytest.mark.parametrize("prec", [_abi.EP_FP64, _abi.EP_FP32], ids=["fp64", "fp32"])
+@pytest.mark.parametrize("prec", [_abi.EP_FP64, _abi.EP_FP32, _abi.EP_DFLOAT], ids=["fp64", "fp32", "dfloat"])
 @pytest.mark.parametrize("name", list(CASES))
 def test_benchmark_geometry_matches_oracle(oracle, name, prec):
     case = CASES[name]
     o = oracle_result(oracle, name)
     g = evolve(ep.Solver, case, prec)
-    fp64 = prec == _abi.EP_FP64
+    # the double-float path is gated like FP64 (the drop-in bar)
+    fp64 = prec in (_abi.EP_FP64, _abi.EP_DFLOAT)
     ftol, etol, ptol, dtol = (1e-11, 1e-10, 1e-10, 1e-9) if fp64 else (2e-5, 2e-5, 1e-4, 1e-6)
     report = {}
     for f in FIELDS_OTC:
@@ -137,7 +139,7 @@ def test_benchmark_geometry_matches_oracle(oracle, name, prec):
         for k in ("rimp", "vimp", "aimp"):
             report[f"imp.{k}"] = float(np.max(np.abs(g["imp"][k] - o["imp"][k]))) / max(
                 1.0, float(np.max(np.abs(o["imp"][k]))))
-    print(f"PARITY {name} {'fp64' if fp64 else 'fp32'} " +
+    print(f"PARITY {name} {({_abi.EP_FP64: 'fp64', _abi.EP_FP32: 'fp32', _abi.EP_DFLOAT: 'dfloat'})[prec]} " +
           " ".join(f"{k}={v:.2e}" for k, v in report.items()))
     for f in FIELDS_OTC:
         if f in report:
