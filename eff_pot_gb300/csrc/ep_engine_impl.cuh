@@ -1069,7 +1069,7 @@ template <class T>
 int Engine<T>::upload_psi(const double* h) {
   int r;
   if ((r = ensure_materialized())) return r;
-  if (sizeof(T) == sizeof(double)) {
+  if (std::is_same<T, double>::value) {
     if ((r = cuda_ok(cudaMemcpyAsync(psi, h, g.N * sizeof(CT), cudaMemcpyHostToDevice, st), "upload psi"))) return r;
   } else {
     double2* tmp = nullptr;
@@ -1102,7 +1102,7 @@ int Engine<T>::download_c(int which, double* h) {
     default: *err = "unknown complex field"; return EP_ERR_INVALID_ARG;
   }
   int r;
-  if (sizeof(T) == sizeof(double)) {
+  if (std::is_same<T, double>::value) {
     if ((r = cuda_ok(cudaMemcpyAsync(h, src, g.N * sizeof(CT), cudaMemcpyDeviceToHost, st), "download"))) return r;
   } else {
     double2* tmp = nullptr;
@@ -1144,7 +1144,7 @@ int Engine<T>::download_r(int which, double* h) {
     default: *err = "unknown field"; return EP_ERR_INVALID_ARG;
   }
   int r;
-  if (sizeof(T) == sizeof(double)) {
+  if (std::is_same<T, double>::value) {
     if ((r = cuda_ok(cudaMemcpyAsync(h, src, g.N * sizeof(T), cudaMemcpyDeviceToHost, st), "download"))) return r;
   } else {
     double* tmp = nullptr;
