@@ -20,7 +20,7 @@ from .solver import Solver
 
 def main(argv=None):
     ap = argparse.ArgumentParser()
-    ap.add_argument("--precision", default="fp32", choices=["fp32", "fp64"])
+    ap.add_argument("--precision", default="fp32", choices=["fp32", "fp64", "dfloat"])
     ap.add_argument("--steps", type=int, default=6)
     ap.add_argument("--n", type=int, default=128)
     a = ap.parse_args(argv)
@@ -28,7 +28,7 @@ def main(argv=None):
     n, xmax = a.n, 0.2 * a.n
     cfg = make_config(nx=n, ny=n, nz=n, xmax=xmax, ymax=xmax, zmax=xmax, icon=_abi.EP_ICON_PERIODIC,
                       core="OTC", n4=1000.0, impurity=_abi.EP_IMPURITY_FIXED,
-                      precision=_abi.EP_FP32 if a.precision == "fp32" else _abi.EP_FP64)
+                      precision={"fp32": _abi.EP_FP32, "fp64": _abi.EP_FP64, "dfloat": _abi.EP_DFLOAT}[a.precision])
     with Solver(cfg) as s:
         pot = morse(10.0, 4.5, 1.2)
         s.set_impurity_potentials(pot, pot, pot)
