@@ -67,20 +67,23 @@ template <class T> struct Kahan {
   EP_DEV T lo() const { return -c; }
   EP_DEV double get() const { return (double)s - (double)c; }
 };
-// Double-float terms: Kahan in FP32 on the high parts, the low parts summed
-// apart (value s - c + l); the block reduction carries FP32 pairs.
+// Double-float terms: the pair (s, c) of FP32 values, each high part added
+// to s with the error-free TwoSum and its rounding error and the low part
+// collected in c (Ogita, Rump and Oishi's Sum2 kept as a pair: the error is
+// about n u^2 of the magnitudes, where Kahan's s - c in FP32 keeps an error
+// of up to 2u of the sum -- enough to move the renormalisation factor of the
+// double-float path by 1e-12 a step).
 template <> struct Kahan<dfloat> {
   typedef float value_type;
-  float s = 0.0f, c = 0.0f, l = 0.0f;
+  float s = 0.0f, c = 0.0f;
   EP_DEV void add(dfloat v) {
-    const float y = v.hi - c;
-    const float t = s + y;
-    c = (t - s) - y;
+    const float t = s + v.hi;
+    const float bb = t - s;
+    c += ((s - (t - bb)) + (v.hi - bb)) + v.lo;
     s = t;
-    l += v.lo;
   }
-  EP_DEV float lo() const { return l - c; }
-  EP_DEV double get() const { return (double)s - (double)c + (double)l; }
+  EP_DEV float lo() const { return c; }
+  EP_DEV double get() const { return (double)s + (double)c; }
 };
 // The accumulator of sums of T values: Neumaier in FP64, Kahan in FP32 and
 // double-float.
