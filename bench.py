@@ -5,9 +5,12 @@ N=1000 helium droplet on a periodic 128^3 grid (h = 0.4 A, Orsay-Trento with
 the alpha_s term, 'OTC') with a Morse He-X impurity (De=10 K, re=4.5 A,
 alpha=1.2/A) fixed at z = 0, 1.25, ..., 38.75 A on the x=y=0 axis, advanced
 together in imaginary time (dt = 1e-4 1/K, renormalised after every step):
-FP32 bulk steps then FP64 refinement sweeps in the scan's 4000:200 ratio.
+FP32 bulk steps then FP64-class refinement sweeps in the scan's 4000:200
+ratio -- by default in double-float arithmetic (pairs of FP32 values, the
+engine that matches the FP64 oracle to the FP64 gates on the FP32 pipes;
+--refine fp64 for native FP64), with the other arithmetic timed beside it.
 A "step" is one steppc of every instance; value = instance-steps/s.
-Beside it: the plain FP64 path and the FP32 path on one instance (the
+Beside it: the plain FP64, double-float and FP32 paths on one instance (the
 configuration of a single droplet + impurity at 128^3), the per-kernel
 roofline of the FP32 instance, the end-to-end rate through the C ABI with
 host buffers, and the C++ FP64 oracle on the host cores.  Inputs are seeded
@@ -31,7 +34,7 @@ sys.path.insert(0, ROOT)
 
 N_GRID, XMAX, N4, DT, SEED = 128, 25.6, 1000.0, 1e-4, 1
 REFINE_RATIO = 200.0 / 4200.0
-METRIC = ("time-steps/s at 128^3: batched (32 droplets + Morse impurity scan) FP32 + FP64-refine, "
+METRIC = ("time-steps/s at 128^3: batched (32 droplets + Morse impurity scan) FP32 + FP64-class refine, "
           "instance-steps/s")
 UNIT = "instance-steps/s"
 
@@ -291,6 +294,20 @@ def run_ours(args):
         ms_b = b.event_elapsed(0, 1)
     launches = b.kernel_launches() - l0
     stats = b.run(1, DT)
+    # the same K steps with the other refinement arithmetic, for comparison
+    other = "fp64" if args.refine == "dfloat" else "dfloat"
+    b.set_precision(other)
+    b.autotune()
+    b.run(1, DT)
+    b.set_precision("fp32")
+    b.run(1, DT)
+    b.synchronize()
+    b.event_record(2)
+    b.run(k32, DT, wait=False)
+    b.set_precision(other)
+    b.run(k64, DT, wait=False)
+    b.event_record(3)
+    ms_other = max_over_ranks(dist, b.event_elapsed(2, 3))
     b.close()
     ms_b = max_over_ranks(dist, ms_b)
     value = world * args.batch * K / (ms_b / 1e3)
@@ -382,6 +399,7 @@ def run_ours(args):
         "dfloat_single_steps_per_s": K / (msdd / 1e3),
         "fp32_single_steps_per_s": K / (ms32 / 1e3),
         "speedup_vs_fp64_single": value / (world * K / (ms64 / 1e3)),
+        f"batch_{other}_refine_instance_steps_per_s": world * args.batch * K / (ms_other / 1e3),
         "hbm_gbs_batch": batch_bytes / (ms_b / 1e3) / 1e9,
         "fp64_flop_roofline": fp64_flop_roofline(K / (ms64 / 1e3)),
         "roofline": {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": peak, "unit": "GB/s",
@@ -419,7 +437,7 @@ def main():
     ap.add_argument("--batch", type=int, default=32)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu", action="store_true")
-    ap.add_argument("--refine", default="fp64", choices=["fp64", "dfloat"],
+    ap.add_argument("--refine", default="dfloat", choices=["fp64", "dfloat"],
                     help="arithmetic of the refinement sweeps: FP64, or double-float (FP64-class on the FP32 pipes)")
     ap.add_argument("--step-graphs", type=int, default=1, choices=[0, 1, 2],
                     help="batch steps: 0 direct launches, 1 one replayed graph per step (default), "

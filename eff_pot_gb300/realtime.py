@@ -67,7 +67,7 @@ def kicked_run(psi, precision, nsteps, sample=100, dims=DIMS, h=H, n4=N4, dt_fs=
     Returns the samples and the wall time of the evolution."""
     dt = dt_fs * 1e-3 / KTOPS                      # fs -> ps -> hbar/k_B units
     v = kick * 1e10 / 1e12 * KTOPS                 # m/s -> A/ps -> A per hbar/k_B
-    prec = _abi.EP_FP32 if precision == "fp32" else _abi.EP_FP64
+    prec = {"fp32": _abi.EP_FP32, "fp64": _abi.EP_FP64, "dfloat": _abi.EP_DFLOAT}[precision]
     s = Solver(config(prec, _abi.EP_REAL_TIME, _abi.EP_IMPURITY_MOVING, dims, h, n4))
     out = []
     try:
@@ -122,6 +122,7 @@ def main(argv=None):
     ap = argparse.ArgumentParser(description=__doc__.splitlines()[0])
     ap.add_argument("--fp32-steps", type=int, default=20000)
     ap.add_argument("--fp64-steps", type=int, default=2000)
+    ap.add_argument("--dfloat-steps", type=int, default=0, help="also the double-float path")
     ap.add_argument("--ground-fp32", type=int, default=2000)
     ap.add_argument("--ground-fp64", type=int, default=300)
     ap.add_argument("--sample", type=int, default=100)
@@ -133,13 +134,18 @@ def main(argv=None):
     t_gs = time.perf_counter() - t0
     r32, w32 = kicked_run(psi, "fp32", a.fp32_steps, a.sample)
     r64, w64 = kicked_run(psi, "fp64", a.fp64_steps, a.sample) if a.fp64_steps else ([], 0.0)
+    rdd, wdd = kicked_run(psi, "dfloat", a.dfloat_steps, a.sample) if a.dfloat_steps else ([], 0.0)
     print(json.dumps({"workload": "N=10000 droplet + Morse impurity kicked at 50 m/s along z, 256x256x320, "
                                   "h=0.4 A, OTC, real time, dt=0.5 fs, impurity mass 40 u",
                       "ground_state": {"fp32_steps": a.ground_fp32, "fp64_steps": a.ground_fp64, "wall_s": t_gs},
                       "fp32": {"steps": a.fp32_steps, "wall_s": w32, "steps_per_s": a.fp32_steps / w32},
                       "fp64": {"steps": a.fp64_steps, "wall_s": w64,
                                "steps_per_s": a.fp64_steps / w64 if w64 else None},
-                      "drift": drift_report(r32, r64), "samples_fp32": r32, "samples_fp64": r64}))
+                      "dfloat": {"steps": a.dfloat_steps, "wall_s": wdd,
+                                 "steps_per_s": a.dfloat_steps / wdd if wdd else None},
+                      "drift": drift_report(r32, r64),
+                      "drift_dfloat": drift_report(rdd, r64) if rdd else None,
+                      "samples_fp32": r32, "samples_fp64": r64, "samples_dfloat": rdd}))
 
 
 if __name__ == "__main__":

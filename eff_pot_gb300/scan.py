@@ -6,8 +6,8 @@ impurity, then subtracting the total energies printed by energy.f90
 (energy.f90:146-165, collected by loop.sh / get_impurity_energy.sh).  Here
 every instance -- the pure droplet and the droplet with the impurity fixed
 at each z on the x = y = 0 axis -- advances together in one Batch: FP32
-steps, then FP64 refinement sweeps, then poten + energy of each instance in
-FP64.  With reference=True the same instances are also run on the plain FP64
+steps, then FP64-class refinement sweeps (double-float by default, or FP64),
+then poten + energy of each instance.  With reference=True the same instances are also run on the plain FP64
 path to the same imaginary time, and every V_eff(z) carries its difference
 from the FP64 result.
 
@@ -55,10 +55,12 @@ def _prepare(s, psi, z, pot):
     s.start(psi)
 
 
-def run_instances(mine, psi, *, precision, steps32, steps64, dt, pot, make_batch, cfg_of, rk_steps=3, tune=True):
+def run_instances(mine, psi, *, precision, steps32, steps64, dt, pot, make_batch, cfg_of, rk_steps=3, tune=True,
+                  refine="fp64"):
     """Advance this rank's instances as one batch and return {key: energies}.
 
-    precision 'fp32': steps32 FP32 steps, then steps64 FP64 refinement sweeps;
+    precision 'fp32': steps32 FP32 steps, then steps64 refinement sweeps in
+    `refine` arithmetic ('fp64', or 'dfloat': the double-float engine);
     'fp64': steps32 + steps64 plain FP64 steps (the same imaginary time).
     Start: density, potenimp, poten, rk_steps Runge-Kutta-Gill steps."""
     if not mine:
@@ -75,7 +77,7 @@ def run_instances(mine, psi, *, precision, steps32, steps64, dt, pot, make_batch
         if precision == "fp32":
             if steps32:
                 b.run(steps32, dt, wait=False)
-            b.set_precision("fp64")
+            b.set_precision(refine)
             if steps64:
                 b.run(steps64, dt, wait=False)
         else:
@@ -121,7 +123,7 @@ def veff_table(zs, e32, e64=None):
 
 
 def veff_scan(zs, *, steps32=4000, steps64=200, dt=1e-4, n=128, h=0.4, n4=1000.0, seed=1, reference=False,
-              pot=None, rank=0, world=1, dist=None, device=0, make_batch=Batch, tune=True):
+              pot=None, rank=0, world=1, dist=None, device=0, make_batch=Batch, tune=True, refine="dfloat"):
     """V_eff(z) for the impurity positions zs (A, on the x = y = 0 axis).
 
     Returns (on rank 0) a dict with the pure droplet's energy and one row
@@ -136,7 +138,7 @@ def veff_scan(zs, *, steps32=4000, steps64=200, dt=1e-4, n=128, h=0.4, n4=1000.0
 
     kw = dict(steps32=steps32, steps64=steps64, dt=dt, pot=pot, make_batch=make_batch, cfg_of=cfg_of, tune=tune)
     t0 = time.perf_counter()
-    e32 = gather(dist, run_instances(mine, psi, precision="fp32", **kw))
+    e32 = gather(dist, run_instances(mine, psi, precision="fp32", refine=refine, **kw))
     t32 = time.perf_counter() - t0
     e64, t64 = None, None
     if reference:
@@ -146,7 +148,8 @@ def veff_scan(zs, *, steps32=4000, steps64=200, dt=1e-4, n=128, h=0.4, n4=1000.0
     if e32 is None:
         return None
     res = {"E_pure": e32[PURE]["etot"], "rows": veff_table(zs, e32, e64), "wall_s_fp32_refine": t32,
-           "steps": {"fp32": steps32, "fp64_refine": steps64, "dt": dt}, "instances": len(zs) + 1,
+           "steps": {"fp32": steps32, "refine": steps64, "refine_arithmetic": refine, "dt": dt},
+           "instances": len(zs) + 1,
            "ranks": world}
     if e64 is not None:
         res["E_pure_fp64"] = e64[PURE]["etot"]
@@ -163,6 +166,8 @@ def main(argv=None):
     ap.add_argument("--fp32-steps", type=int, default=4000)
     ap.add_argument("--fp64-steps", type=int, default=200)
     ap.add_argument("--reference", action="store_true", help="also run the plain FP64 path (per-point error)")
+    ap.add_argument("--refine", default="dfloat", choices=["dfloat", "fp64"],
+                    help="arithmetic of the refinement sweeps (default: double-float)")
     a = ap.parse_args(argv)
     import os
     from .build import build
@@ -178,7 +183,7 @@ def main(argv=None):
         dist.barrier()
     zs = [a.dz * k for k in range(a.points)]
     res = veff_scan(zs, steps32=a.fp32_steps, steps64=a.fp64_steps, reference=a.reference, rank=rank,
-                    world=world, dist=dist, device=local)
+                    world=world, dist=dist, device=local, refine=a.refine)
     if rank == 0:
         print(json.dumps(res))
     if dist is not None:

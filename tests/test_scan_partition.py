@@ -18,7 +18,7 @@ import pytest
 
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 ZS = [0.0, 1.25, 2.5, 3.75, 5.0]
-KW = dict(steps32=3, steps64=2, dt=5e-4, n=16, h=1.0, n4=60.0, seed=1, reference=True, tune=False)
+KW = dict(steps32=3, steps64=2, dt=5e-4, n=16, h=1.0, n4=60.0, seed=1, reference=True, tune=False, refine="fp64")
 
 
 class OracleBatch:
