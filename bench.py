@@ -17,7 +17,8 @@ host buffers, and the C++ FP64 oracle on the host cores.  Inputs are seeded
 Woods-Saxon droplets; every working set is far larger than L2.
 
 python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
-                [--batch B] [--no-cpu]
+                [--batch B] [--no-cpu] [--refine dfloat|fp64] [--step-graphs 0|1|2]
+                [--workload scan|pure64|impurity128|uneven|realtime]
 """
 import argparse
 import ctypes as C
@@ -429,6 +430,186 @@ def run_ours(args):
     return 0
 
 
+# ---------------------------------------------------------------------------
+# The other workloads of the benchmark configurations, one JSON line each
+# (--workload): bounded samples of their step counts, device-timed steps/s
+# of every engine, the HBM fraction of the algorithmic step bytes, and the
+# C++ FP64 oracle on the host cores for the CPU column.
+
+def _wl_cfg(dims, h, n4, impurity, precision, real_time=False, device=0):
+    import eff_pot_gb300 as ep
+    from eff_pot_gb300 import _abi
+    nx, ny, nz = dims
+    kw = dict(nx=nx, ny=ny, nz=nz, xmax=nx * h / 2, ymax=ny * h / 2, zmax=nz * h / 2, icon=_abi.EP_ICON_PERIODIC,
+              core="OTC", n4=n4, impurity=impurity, device=device,
+              time_mode=_abi.EP_REAL_TIME if real_time else _abi.EP_IMAGINARY_TIME, renormalize=0 if real_time else 1,
+              precision={"fp32": _abi.EP_FP32, "fp64": _abi.EP_FP64, "dfloat": _abi.EP_DFLOAT}[precision])
+    if impurity == _abi.EP_IMPURITY_MOVING:
+        kw.update(mimpur=40.0, fix_lambda=1)
+    return ep.make_config(**kw)
+
+
+def _wl_prepare(s, psi, rimp, pot, vimp=None):
+    import numpy as np
+    import eff_pot_gb300 as ep
+    p = pot if pot is not None else ep.null_potential()
+    s.set_impurity_potentials(p, p, p)
+    s.set_impurity(rimp=rimp, vimp=vimp, invar=np.zeros(10, dtype=np.complex128))
+    s.start(psi)
+
+
+def _wl_timed(obj, steps, dt, batch=False):
+    f, h = obj._f, obj._h
+    rec = f["batch_event_record"] if batch else f["event_record"]
+    ela = f["batch_event_elapsed"] if batch else f["event_elapsed"]
+    rec(h, 0)
+    obj.run(steps, dt, wait=False)
+    rec(h, 1)
+    ms = C.c_double()
+    ela(h, 0, 1, C.byref(ms))
+    return ms.value
+
+
+def _wl_single(cfg, psi, rimp, pot, steps, warmup, dt, rk=3, vimp=None):
+    import eff_pot_gb300 as ep
+    with ep.Solver(cfg) as s:
+        _wl_prepare(s, psi, rimp, pot, vimp)
+        s.autotune()
+        for _ in range(rk):
+            s.steprk(dt)
+        s.run(warmup, dt)
+        s.synchronize()
+        ms = _wl_timed(s, steps, dt)
+    return steps / (ms / 1e3)
+
+
+def _wl_cpu(cfg, psi, rimp, pot, steps, dt, rk=3, vimp=None):
+    from oracle import pyoracle
+    threads = os.cpu_count() or 1
+    pyoracle.set_threads(threads)
+    s = pyoracle.OracleSolver(cfg)
+    _wl_prepare(s, psi, rimp, pot, vimp)
+    for _ in range(rk):
+        s.steprk(dt)
+    s.steppc(dt)
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        s.steppc(dt, wait=False)
+        if cfg.time_mode == 0:
+            s.renormalize()
+    el = time.perf_counter() - t0
+    s.close()
+    return {"value": steps / el, "unit": "steps/s", "cores": threads, "kind": "port",
+            "sample": f"{steps} steppc steps after start-up; C++ FP64 oracle, {threads} OpenMP threads"}
+
+
+def _peak_gbs():
+    try:
+        return float(json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))["hbm_gbs"])
+    except Exception:
+        return 6800.0
+
+
+def _wl_frac(dims, steps_per_s, s):
+    from eff_pot_gb300.roofline import step_bytes
+    b = sum(step_bytes(*dims, otc=True, grad=True, s=s, renorm=False).values())
+    return b * steps_per_s / 1e9 / _peak_gbs()
+
+
+def run_workload(args):
+    """One of the benchmark configurations other than the scan."""
+    import numpy as np
+    import eff_pot_gb300 as ep
+    from eff_pot_gb300 import _abi
+    from eff_pot_gb300.build import build
+    build()
+    wl = args.workload
+    line = {"workload": wl, "unit": "steps/s", "data": "synthetic (seeded Woods-Saxon droplets)"}
+    if wl in ("pure64", "impurity128"):
+        if wl == "pure64":
+            dims, h, n4, seed, imp, pot = (64,) * 3, 0.8, 500.0, 0, _abi.EP_IMPURITY_NONE, None
+            line["config"] = "pure N=500 droplet, 64^3, h=0.8 A, OTC, imaginary time, dt=1e-4"
+            n64, n32, ncpu = 200, 400, 40
+        else:
+            dims, h, n4, seed, imp, pot = (128,) * 3, 0.4, 1000.0, 1, _abi.EP_IMPURITY_FIXED, ep.morse(10.0, 4.5, 1.2)
+            line["config"] = "N=1000 droplet + Morse impurity at the centre, 128^3, h=0.4 A, OTC, imaginary time"
+            n64, n32, ncpu = 100, 400, 20
+        psi = ep.woods_saxon_psi(*dims, dims[0] * h / 2, dims[1] * h / 2, dims[2] * h / 2, n4, seed=seed)
+        z = (0.0, 0.0, 0.0)
+        for prec, n in (("fp64", n64), ("dfloat", n64 * 2), ("fp32", n32)):
+            v = _wl_single(_wl_cfg(dims, h, n4, imp, prec), psi, z, pot, n, 5, 1e-4)
+            line[f"gpu_{prec}_steps_per_s"] = v
+            line[f"hbm_frac_{prec}"] = _wl_frac(dims, v, 4 if prec == "fp32" else 8)
+        r = 200.0 / 5000.0
+        line["gpu_fp32_dfloat_refine_steps_per_s"] = 1.0 / ((1 - r) / line["gpu_fp32_steps_per_s"] +
+                                                          r / line["gpu_dfloat_steps_per_s"])
+        if not args.no_cpu:
+            line["cpu_baseline"] = _wl_cpu(_wl_cfg(dims, h, n4, imp, "fp64"), psi, z, pot, ncpu, 1e-4)
+    elif wl == "uneven":
+        rng = np.random.default_rng(2)
+        ns = rng.choice([300, 1000, 2000, 5000], size=64)
+        grid_of = {300: 96, 1000: 128, 2000: 160, 5000: 192}
+        cfgs, psis, rimps, has = [], [], [], []
+        for i, nn in enumerate(ns):
+            g = grid_of[int(nn)]
+            imp = i % 2 == 0
+            c = _wl_cfg((g,) * 3, 0.4, float(nn), _abi.EP_IMPURITY_FIXED if imp else _abi.EP_IMPURITY_NONE, "fp32")
+            R = 2.22 * float(nn) ** (1.0 / 3.0)
+            cfgs.append(c)
+            psis.append(ep.woods_saxon_psi(g, g, g, c.xmax, c.ymax, c.zmax, float(nn), seed=100 + i))
+            rimps.append((0.0, 0.0, rng.uniform(0.0, R) if imp else 0.0))
+            has.append(imp)
+        steps, k64 = 20, 1
+        with ep.Batch(cfgs) as b:
+            for s, psi, r, imp in zip(b, psis, rimps, has):
+                _wl_prepare(s, psi, r, ep.morse(10.0, 4.5, 1.2) if imp else None)
+            b.autotune()
+            for _ in range(3):
+                b.steprk(1e-4)
+            b.run(3, 1e-4)
+            for prec in ("fp64", "dfloat"):
+                b.set_precision(prec)
+                b.autotune()
+                b.run(1, 1e-4)
+            b.set_precision("fp32")
+            b.synchronize()
+            ms32 = _wl_timed(b, steps - k64, 1e-4, batch=True)
+            out = {}
+            for prec in ("dfloat", "fp64"):
+                b.set_precision(prec)
+                out[prec] = _wl_timed(b, k64, 1e-4, batch=True)
+                b.set_precision("fp32")
+        from eff_pot_gb300.roofline import step_bytes
+        pts = sum(c.nx * c.ny * c.nz for c in cfgs)
+        b32 = sum(sum(step_bytes(c.nx, c.ny, c.nz, s=4, renorm=False).values()) for c in cfgs)
+        line.update(config="64 droplets, N in {300,1000,2000,5000} (seed 2), grids 96..192^3 at h=0.4 A, "
+                           "half with the Morse impurity", unit="instance-steps/s", grid_points_total=pts,
+                    batch_fp32_instance_steps_per_s=64 * (steps - k64) / (ms32 / 1e3),
+                    batch_dfloat_instance_steps_per_s=64 * k64 / (out["dfloat"] / 1e3),
+                    batch_fp64_instance_steps_per_s=64 * k64 / (out["fp64"] / 1e3),
+                    batch_fp32_dfloat_refine_instance_steps_per_s=64 * steps / ((ms32 + out["dfloat"]) / 1e3),
+                    hbm_frac_fp32=b32 * (steps - k64) / (ms32 / 1e3) / 1e9 / _peak_gbs(),
+                    sample=f"{steps - k64} FP32 steps, then one refinement step in each FP64-class arithmetic")
+    elif wl == "realtime":
+        dims, h, n4 = (256, 256, 320), 0.4, 10000.0
+        psi = ep.woods_saxon_psi(*dims, dims[0] * h / 2, dims[1] * h / 2, dims[2] * h / 2, n4, seed=4)
+        dt = 0.5e-3 / ep.KTOPS
+        v = (0.0, 0.0, 50.0 * 1e10 / 1e12 * ep.KTOPS)
+        pot = ep.morse(10.0, 4.5, 1.2)
+        line["config"] = ("N=10000 + Morse impurity kicked at 50 m/s, 256x256x320, h=0.4 A, real time, dt=0.5 fs "
+                          "(steady-state steps; the drift run is eff_pot_gb300.realtime)")
+        for prec, n in (("fp32", 30), ("dfloat", 10), ("fp64", 6)):
+            r = _wl_single(_wl_cfg(dims, h, n4, _abi.EP_IMPURITY_MOVING, prec, real_time=True), psi, (0.0, 0.0, 0.0),
+                           pot, n, 2, dt, rk=4, vimp=v)
+            line[f"gpu_{prec}_steps_per_s"] = r
+            line[f"hbm_frac_{prec}"] = _wl_frac(dims, r, 4 if prec == "fp32" else 8)
+        if not args.no_cpu:
+            line["cpu_baseline"] = _wl_cpu(_wl_cfg(dims, h, n4, _abi.EP_IMPURITY_MOVING, "fp64", real_time=True),
+                                           psi, (0.0, 0.0, 0.0), pot, 3, dt, rk=4, vimp=v)
+    print(json.dumps(line))
+    return 0
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -437,6 +618,8 @@ def main():
     ap.add_argument("--batch", type=int, default=32)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--workload", default="scan", choices=["scan", "pure64", "impurity128", "uneven", "realtime"],
+                    help="scan (default): the headline batch; the others: one line per benchmark configuration")
     ap.add_argument("--refine", default="dfloat", choices=["fp64", "dfloat"],
                     help="arithmetic of the refinement sweeps: FP64, or double-float (FP64-class on the FP32 pipes)")
     ap.add_argument("--step-graphs", type=int, default=1, choices=[0, 1, 2],
@@ -448,6 +631,8 @@ def main():
     args.warmup = max(args.warmup, 3)
     if args.impl == "reference":
         return run_reference(args)
+    if args.workload != "scan":
+        return run_workload(args)
     return run_ours(args)
 
 
