@@ -131,7 +131,64 @@ __device__ __forceinline__ dfloat __ldcg(const dfloat* p) {
 }
 #endif
 
-// Complex double-float.
-EP_HD dfloat2 operator+(dfloat2 a, dfloat2 b) { return dfloat2{a.x + b.x, a.y + b.y}; }
-EP_HD dfloat2 operator-(dfloat2 a, dfloat2 b) { return dfloat2{a.x - b.x, a.y - b.y}; }
-EP_HD dfloat2 operator*(dfloat s, dfloat2 a) { return dfloat2{s * a.x, s * a.y}; }
+// Complex double-float.  On the device the real and imaginary parts go
+// through the same error-free steps side by side as FP32 pairs (FADD2 /
+// FMUL2 / FFMA2: one instruction for both parts; x * -1 + y is the exact
+// y - x).  The host forms are the scalar operators.
+#if defined(__CUDA_ARCH__)
+__device__ __forceinline__ float2 dd_neg2(float2 a) { return make_float2(-a.x, -a.y); }
+// (h, l) pairs of the two parts: hi parts in h, lo parts in l.
+__device__ __forceinline__ dfloat2 dd_pack(float2 h, float2 l) {
+  return dfloat2{dfloat(h.x, l.x), dfloat(h.y, l.y)};
+}
+__device__ __forceinline__ dfloat2 dd_add2(float2 ah, float2 al, float2 bh, float2 bl) {
+  const float2 m1 = make_float2(-1.0f, -1.0f);
+  const float2 s = __fadd2_rn(ah, bh);
+  const float2 bb = __ffma2_rn(ah, m1, s);                    // s - a
+  const float2 e1 = __ffma2_rn(__ffma2_rn(bb, m1, s), m1, ah);  // a - (s - bb)
+  const float2 e2 = __ffma2_rn(bb, m1, bh);                   // b - bb
+  const float2 e = __fadd2_rn(__fadd2_rn(e1, e2), __fadd2_rn(al, bl));
+  const float2 h = __fadd2_rn(s, e);
+  return dd_pack(h, __ffma2_rn(__ffma2_rn(s, m1, h), m1, e));   // e - (h - s)
+}
+__device__ __forceinline__ dfloat2 operator+(dfloat2 a, dfloat2 b) {
+  return dd_add2(make_float2(a.x.hi, a.y.hi), make_float2(a.x.lo, a.y.lo), make_float2(b.x.hi, b.y.hi),
+                 make_float2(b.x.lo, b.y.lo));
+}
+__device__ __forceinline__ dfloat2 operator-(dfloat2 a, dfloat2 b) {
+  return dd_add2(make_float2(a.x.hi, a.y.hi), make_float2(a.x.lo, a.y.lo), make_float2(-b.x.hi, -b.y.hi),
+                 make_float2(-b.x.lo, -b.y.lo));
+}
+// s * (ah + al) for a double-float s: the FMA product error of both parts.
+__device__ __forceinline__ void dd_scale2(dfloat s, float2 ah, float2 al, float2& ph, float2& pe) {
+  const float2 sh = make_float2(s.hi, s.hi), sl = make_float2(s.lo, s.lo);
+  ph = __fmul2_rn(sh, ah);
+  float2 e = __ffma2_rn(sh, ah, dd_neg2(ph));
+  e = __ffma2_rn(sh, al, e);
+  pe = __ffma2_rn(sl, ah, e);
+}
+__device__ __forceinline__ dfloat2 operator*(dfloat s, dfloat2 a) {
+  float2 p, e;
+  dd_scale2(s, make_float2(a.x.hi, a.y.hi), make_float2(a.x.lo, a.y.lo), p, e);
+  const float2 h = __fadd2_rn(p, e);
+  return dd_pack(h, __ffma2_rn(__ffma2_rn(p, make_float2(-1.0f, -1.0f), h), make_float2(-1.0f, -1.0f), e));
+}
+// Complex products: the two real-by-complex products side by side, then one
+// complex sum (a * b and a * conj(b)).
+__device__ __forceinline__ dfloat2 cmul(dfloat2 a, dfloat2 b) {
+  float2 tp, te, up, ue;
+  dd_scale2(a.x, make_float2(b.x.hi, b.y.hi), make_float2(b.x.lo, b.y.lo), tp, te);
+  dd_scale2(a.y, make_float2(-b.y.hi, b.x.hi), make_float2(-b.y.lo, b.x.lo), up, ue);
+  return dd_add2(tp, te, up, ue);
+}
+__device__ __forceinline__ dfloat2 cmulc(dfloat2 a, dfloat2 b) {
+  float2 tp, te, up, ue;
+  dd_scale2(a.x, make_float2(b.x.hi, -b.y.hi), make_float2(b.x.lo, -b.y.lo), tp, te);
+  dd_scale2(a.y, make_float2(b.y.hi, b.x.hi), make_float2(b.y.lo, b.x.lo), up, ue);
+  return dd_add2(tp, te, up, ue);
+}
+#else
+inline dfloat2 operator+(dfloat2 a, dfloat2 b) { return dfloat2{a.x + b.x, a.y + b.y}; }
+inline dfloat2 operator-(dfloat2 a, dfloat2 b) { return dfloat2{a.x - b.x, a.y - b.y}; }
+inline dfloat2 operator*(dfloat s, dfloat2 a) { return dfloat2{s * a.x, s * a.y}; }
+#endif
