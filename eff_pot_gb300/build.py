@@ -13,8 +13,8 @@ LIB = os.path.join(BUILD, "libeffpot.so")
 DRIVER = os.path.join(BUILD, "ep_dft4he3d")
 DRIVER_SRC = ["ep_fortran_io.cpp", "ep_dft4he3d.cpp"]
 UNITS = ["ep_engine_fp64.cu", "ep_engine_fp32.cu", "ep_engine_dd.cu", "ep_engine_dd_x.cu", "ep_engine_dd_xk0.cu",
-         "ep_engine_dd_xk32.cu", "ep_engine_dd_xk128.cu", "ep_engine_dd_fft.cu", "ep_engine_dd_march.cu",
-         "ep_common.cu", "ep_api.cu", "ep_noalloc.cu", "ep_select_pot.cu"]
+         "ep_engine_dd_fft.cu", "ep_engine_dd_march.cu", "ep_common.cu", "ep_api.cu", "ep_noalloc.cu",
+         "ep_select_pot.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-Xcompiler", "-O2",
          "-I" + os.path.join(ROOT, "include")]

@@ -1307,8 +1307,9 @@ done:
 template <class T>
 int Engine<T>::x_attrs() {
   int r;
-  if ((r = x_attrs_n2<0>()) || (r = x_attrs_n2<16>()) || (r = x_attrs_n2<32>()) || (r = x_attrs_n2<64>()) ||
-      (r = x_attrs_n2<128>()))
+  if ((r = x_attrs_n2<0>())) return r;
+  if constexpr (std::is_same<T, dfloat>::value) return EP_OK;  // general engine only
+  if ((r = x_attrs_n2<16>()) || (r = x_attrs_n2<32>()) || (r = x_attrs_n2<64>()) || (r = x_attrs_n2<128>()))
     return r;
   if constexpr (sizeof(T) == 4) {
     if ((r = x_attrs_n2<48>()) || (r = x_attrs_n2<80>()) || (r = x_attrs_n2<96>())) return r;
@@ -1320,6 +1321,7 @@ int Engine<T>::x_attrs() {
 // half-lines (N2 = 0: the general engine).
 template <class T>
 int Engine<T>::x_pass(int which, bool otc) {
+  if constexpr (std::is_same<T, dfloat>::value) return x_launch<0>(which, otc);
   switch (x_reg_n2<T>(g.nx / 2)) {
     case 16: return x_launch<16>(which, otc);
     case 32: return x_launch<32>(which, otc);

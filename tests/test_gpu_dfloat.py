@@ -130,3 +130,41 @@ def test_dfloat_builds_the_13_point_stencils_only():
     with pytest.raises(ep.EffPotError) as ei:
         ep.Solver(cfg)
     assert ei.value.status == _abi.EP_ERR_UNSUPPORTED
+
+
+def test_dfloat_batch_and_step_graphs_equal_independent_direct_launches():
+    """The refinement sweeps of the batched scan run in double-float: a
+    batch that switches FP32 -> double-float gives every instance the bits
+    of the same instance run alone with every kernel launched directly."""
+    cfgs = [ep.make_config(nx=n, ny=n, nz=n, xmax=0.5 * n, ymax=0.5 * n, zmax=0.5 * n, icon=_abi.EP_ICON_PERIODIC,
+                           core="OTC", n4=200.0, impurity=_abi.EP_IMPURITY_FIXED, precision=_abi.EP_FP32)
+            for n in (32, 24)]
+    psis = [ep.woods_saxon_psi(c.nx, c.ny, c.nz, c.xmax, c.ymax, c.zmax, c.n4, seed=30 + i) for i, c in enumerate(cfgs)]
+    zs = (0.0, 0.6)
+
+    def prep(s, psi, z):
+        pot = ep.morse()
+        s.set_impurity_potentials(pot, pot, pot)
+        s.set_impurity(rimp=(0.0, 0.0, z), invar=np.zeros(10, dtype=np.complex128))
+        s.start(psi)
+
+    with ep.Batch(cfgs) as b:
+        for s, psi, z in zip(b, psis, zs):
+            prep(s, psi, z)
+        for _ in range(3):
+            b.steprk(5e-4)
+        b.run(12, 5e-4)
+        b.set_precision("dfloat")
+        stats = b.run(13, 5e-4)
+        got = [s.psi() for s in b]
+    for cfg, psi, z, g, st in zip(cfgs, psis, zs, got, stats):
+        with ep.Solver(cfg) as s:
+            s.step_graphs(False)
+            prep(s, psi, z)
+            for _ in range(3):
+                s.steprk(5e-4)
+            s.run(12, 5e-4)
+            s.set_precision("dfloat")
+            ref = s.run(13, 5e-4)
+            assert np.array_equal(g, s.psi())
+            assert st["mu"] == ref["mu"]
