@@ -19,9 +19,29 @@ template <class T> using C2 = typename cpx_traits<T>::type;
 EP_HD double2 operator+(double2 a, double2 b) { return make_double2(a.x + b.x, a.y + b.y); }
 EP_HD double2 operator-(double2 a, double2 b) { return make_double2(a.x - b.x, a.y - b.y); }
 EP_HD double2 operator*(double s, double2 a) { return make_double2(s * a.x, s * a.y); }
-EP_HD float2 operator+(float2 a, float2 b) { return make_float2(a.x + b.x, a.y + b.y); }
-EP_HD float2 operator-(float2 a, float2 b) { return make_float2(a.x - b.x, a.y - b.y); }
-EP_HD float2 operator*(float s, float2 a) { return make_float2(s * a.x, s * a.y); }
+// FP32 complex sums and scalings are paired instructions on the device (the
+// same rounding as the two scalar ones: a - b is b * -1 + a, exact).
+EP_HD float2 operator+(float2 a, float2 b) {
+#if defined(__CUDA_ARCH__)
+  return __fadd2_rn(a, b);
+#else
+  return make_float2(a.x + b.x, a.y + b.y);
+#endif
+}
+EP_HD float2 operator-(float2 a, float2 b) {
+#if defined(__CUDA_ARCH__)
+  return __ffma2_rn(b, make_float2(-1.0f, -1.0f), a);
+#else
+  return make_float2(a.x - b.x, a.y - b.y);
+#endif
+}
+EP_HD float2 operator*(float s, float2 a) {
+#if defined(__CUDA_ARCH__)
+  return __fmul2_rn(make_float2(s, s), a);
+#else
+  return make_float2(s * a.x, s * a.y);
+#endif
+}
 
 template <class T> EP_HD C2<T> cmk(T a, T b) { C2<T> r; r.x = a; r.y = b; return r; }
 
