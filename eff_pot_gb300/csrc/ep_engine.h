@@ -77,6 +77,7 @@ class Engine {
   std::string* err = nullptr;
   int dev_sm = 0;
   int zc_pc = 16, zc_pr = 16, zc_rk = 16, zc_d1 = 16;  // z planes per CTA of the stencil marches
+  bool pairs = false;  // predictor / corrector with two points per thread (FP32, even R and nx)
   T* dyz = nullptr;                         // dy(gy) + dz(gz) of term_alfa
   T* sigdel = nullptr;                      // Sig_Del of the D state (vpi holds Pi_Del)
   int d1march(int mode, const T* f, const T* f2, T* o0, T* o1, T* o2);

@@ -2,6 +2,7 @@
 #pragma once
 #include <algorithm>
 #include <cmath>
+#include <cstdlib>
 #include <cstring>
 
 #include "ep_dstate.h"
@@ -41,6 +42,8 @@
 #endif
 
 template <class T> constexpr bool r_built(int R) { return !std::is_same<T, dfloat>::value || R == 6; }
+// the two-points-per-thread predictor / corrector: FP32 fields, even R
+template <class T> constexpr bool pair_built(int R) { return std::is_same<T, float>::value && R % 2 == 0; }
 
 namespace {
 
@@ -267,8 +270,9 @@ int Engine<T>::init(const ep_config& c, cudaStream_t s, Prof* p, ImpState* im, s
   if ((r = x_attrs()) || (r = fft_attrs()) || (r = march_setup())) return r;
   {
     const long long nxy = (long long)((c.nx + EP_TX - 1) / EP_TX) * ((c.ny + EP_TY - 1) / EP_TY);
+    const long long nxy2 = (long long)((c.nx + EP_PX - 1) / EP_PX) * ((c.ny + EP_TY - 1) / EP_TY);
     const int zmin = std::min(std::min(zc_pc, zc_pr), zc_rk);
-    const long long nbs = nxy * ((c.nz + zmin - 1) / zmin);
+    const long long nbs = std::max(nxy, nxy2) * ((c.nz + zmin - 1) / zmin);
     // block partials are compensated (hi, lo) pairs: the hi parts of a
     // reduction's nblocks*nq sums, then their lo parts
     npartials = 2 * std::max(nbs * 4, (long long)EP_RED_BLOCKS * 18);
@@ -761,7 +765,8 @@ int Engine<T>::lap_predict(double dt) {
   CT* po3 = po[ioldp[2]];
   const CT* h1 = ph[ioldh[0]];
   CT* h2 = ph[ioldh[1]];
-  dim3 grid((g.nx + EP_TX - 1) / EP_TX, (g.ny + EP_TY - 1) / EP_TY, (g.nz + zc_pr - 1) / zc_pr);
+  const int tile_x = pairs ? EP_PX : EP_TX;
+  dim3 grid((g.nx + tile_x - 1) / tile_x, (g.ny + EP_TY - 1) / EP_TY, (g.nz + zc_pr - 1) / zc_pr);
   dim3 blk(EP_TX, EP_TY);
   T f = (T)(c4o3 * dt), c1 = (T)c112;
   Slots sl{slot_of(psi), slot_of(po3), -1, slot_of(h1), slot_of(h2), slot_of(pc), -1};
@@ -773,8 +778,15 @@ int Engine<T>::lap_predict(double dt) {
   size_t smem = 0;
 #define EP_PRED(RR)                                                                   \
   case RR:                                                                            \
+    if constexpr (pair_built<T>(RR)) {                                                \
+      if (pairs) {                                                                    \
+        fn = (const void*)k_predict<T, RR, true>;                                     \
+        smem = march_pair_smem<RR, 4, 2>();                                           \
+        break;                                                                        \
+      }                                                                               \
+    }                                                                                 \
     if constexpr (r_built<T>(RR)) {                                                   \
-      fn = (const void*)k_predict<T, RR>;                                             \
+      fn = (const void*)k_predict<T, RR, false>;                                      \
       smem = march_smem<T, RR, 4, 2>();                                               \
     }                                                                                 \
     break;
@@ -798,7 +810,8 @@ int Engine<T>::lap_correct(double dt, bool want) {
   const CT* po2 = po[ioldp[1]];
   const CT* h1 = ph[ioldh[0]];
   const CT* h2 = ph[ioldh[1]];
-  dim3 grid((g.nx + EP_TX - 1) / EP_TX, (g.ny + EP_TY - 1) / EP_TY, (g.nz + zc_pc - 1) / zc_pc);
+  const int tile_x = pairs ? EP_PX : EP_TX;
+  dim3 grid((g.nx + tile_x - 1) / tile_x, (g.ny + EP_TY - 1) / EP_TY, (g.nz + zc_pc - 1) / zc_pc);
   dim3 blk(EP_TX, EP_TY);
   T f3 = (T)(3.0 * dt), cc = (T)c9;
   int renorm = (cfg.time_mode == EP_IMAGINARY_TIME && cfg.renormalize) ? 1 : 0;
@@ -813,8 +826,15 @@ int Engine<T>::lap_correct(double dt, bool want) {
   size_t smem = 0;
 #define EP_CORR(RR)                                                                                   \
   case RR:                                                                                            \
+    if constexpr (pair_built<T>(RR)) {                                                                \
+      if (pairs) {                                                                                    \
+        fn = want ? (const void*)k_correct<T, RR, true, true> : (const void*)k_correct<T, RR, false, true>; \
+        smem = march_pair_smem<RR, 5, 2>();                                                           \
+        break;                                                                                        \
+      }                                                                                               \
+    }                                                                                                 \
     if constexpr (r_built<T>(RR)) {                                                                   \
-      fn = want ? (const void*)k_correct<T, RR, true> : (const void*)k_correct<T, RR, false>;         \
+      fn = want ? (const void*)k_correct<T, RR, true, false> : (const void*)k_correct<T, RR, false, false>; \
       smem = march_smem<T, RR, 5, 2>();                                                               \
     }                                                                                                 \
     break;
@@ -1401,12 +1421,29 @@ template <class T>
 int Engine<T>::march_setup() {
 #define EP_ATTR(RR)                                                                                      \
   if constexpr (r_built<T>(RR)) {                                                                        \
-  cudaFuncSetAttribute(k_predict<T, RR>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)march_smem<T, RR, 4, 2>()); \
-  cudaFuncSetAttribute(k_correct<T, RR, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)march_smem<T, RR, 5, 2>()); \
-  cudaFuncSetAttribute(k_correct<T, RR, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)march_smem<T, RR, 5, 2>()); \
-  cudaFuncSetAttribute(k_rkstage<T, RR>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)march_smem<T, RR, 1, 2>()); }
+  cudaFuncSetAttribute(k_predict<T, RR, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)march_smem<T, RR, 4, 2>()); \
+  cudaFuncSetAttribute(k_correct<T, RR, true, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)march_smem<T, RR, 5, 2>()); \
+  cudaFuncSetAttribute(k_correct<T, RR, false, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)march_smem<T, RR, 5, 2>()); \
+  cudaFuncSetAttribute(k_rkstage<T, RR>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)march_smem<T, RR, 1, 2>()); } \
+  if constexpr (pair_built<T>(RR)) {                                                                     \
+  cudaFuncSetAttribute(k_predict<T, RR, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)march_pair_smem<RR, 4, 2>()); \
+  cudaFuncSetAttribute(k_correct<T, RR, true, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)march_pair_smem<RR, 5, 2>()); \
+  cudaFuncSetAttribute(k_correct<T, RR, false, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)march_pair_smem<RR, 5, 2>()); }
   EP_ATTR(1) EP_ATTR(2) EP_ATTR(3) EP_ATTR(4) EP_ATTR(5) EP_ATTR(6)
 #undef EP_ATTR
+  {
+    // the pair form needs an even stencil radius and even nx (a pair never
+    // straddles the box edge); EP_MARCH_PAIRS=0 keeps the one-point form
+    const char* ev = getenv("EP_MARCH_PAIRS");
+    bool can = g.nx % 2 == 0 && !(ev && ev[0] == '0');
+    switch (fd.R) {
+      case 2: can = can && pair_built<T>(2); break;
+      case 4: can = can && pair_built<T>(4); break;
+      case 6: can = can && pair_built<T>(6); break;
+      default: can = false;
+    }
+    pairs = can;
+  }
   {
     // z-chunk lengths of the stencil marches from their resident blocks per SM
     int occ_pc = 0, occ_pr = 0, occ_rk = 0, occ_d1 = 0;
@@ -1414,15 +1451,20 @@ int Engine<T>::march_setup() {
 #define EP_OCC(RR)                                                                                         \
   case RR:                                                                                                 \
     if constexpr (r_built<T>(RR)) {                                                                        \
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_pc, k_correct<T, RR, true>, nt, march_smem<T, RR, 5, 2>()); \
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_pr, k_predict<T, RR>, nt, march_smem<T, RR, 4, 2>());      \
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_pc, k_correct<T, RR, true, false>, nt, march_smem<T, RR, 5, 2>()); \
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_pr, k_predict<T, RR, false>, nt, march_smem<T, RR, 4, 2>());      \
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_rk, k_rkstage<T, RR>, nt, march_smem<T, RR, 1, 2>()); \
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_d1, k_d1march<T, RR, 0>, nt, 0); }                  \
+    if constexpr (pair_built<T>(RR)) {                                                                     \
+    if (pairs) {                                                                                           \
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_pc, k_correct<T, RR, true, true>, nt, march_pair_smem<RR, 5, 2>()); \
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_pr, k_predict<T, RR, true>, nt, march_pair_smem<RR, 4, 2>()); } } \
     break;
     switch (fd.R) { EP_OCC(1) EP_OCC(2) EP_OCC(3) EP_OCC(4) EP_OCC(5) EP_OCC(6) default: break; }
 #undef EP_OCC
-    zc_pc = march_zchunk(occ_pc);
-    zc_pr = march_zchunk(occ_pr);
+    const int tile_x = pairs ? EP_PX : EP_TX;
+    zc_pc = march_zchunk(occ_pc, tile_x);
+    zc_pr = march_zchunk(occ_pr, tile_x);
     zc_rk = march_zchunk(occ_rk);
     zc_d1 = march_zchunk(occ_d1, EP_D1_TX);
   }

@@ -1063,6 +1063,136 @@ EP_DEV void lap_march_async(const Geo& g, const C2<T>* __restrict__ psi, const F
   }
 }
 
+// The same march with two points per thread (FP32 fields, even R, even nx):
+// thread (tx, ty) owns the x-neighbouring points 2 tx and 2 tx + 1 of a tile
+// EP_PX = 2 EP_TX points wide.  Every plane element, z-queue element and
+// complex input moves as a 16-byte pair of complex values (real inputs as
+// 8-byte pairs), so a point costs half the shared-memory loads, copy and
+// address instructions and barriers of the one-point form: the x-neighbours
+// of a pair are R + 1 pairs of its row, the y-neighbours 2R pairs of its
+// column.  Each point's Laplacian is summed in the one-point form's order,
+// so both forms give the same bits.  f(p, psi, lap, ic, ir) gets the pair at
+// the even index p, its inputs as ic[i * NT] / ir[i * NT].
+#define EP_PX (2 * EP_TX)
+
+template <int R, int NC, int NR>
+constexpr size_t march_pair_smem() {
+  return (size_t)2 * ((EP_PX + 2 * R) / 2) * (EP_TY + 2 * R) * sizeof(float4) +
+         (size_t)2 * EP_TX * EP_TY * sizeof(float4) + (size_t)2 * NC * EP_TX * EP_TY * sizeof(float4) +
+         (size_t)2 * NR * EP_TX * EP_TY * sizeof(float2) + (size_t)((EP_PX + 2 * R) / 2) * (EP_TY + 2 * R) * sizeof(int);
+}
+
+EP_DEV float2 lo2(float4 v) { return make_float2(v.x, v.y); }
+EP_DEV float2 hi2(float4 v) { return make_float2(v.z, v.w); }
+EP_DEV float4 cat2(float2 a, float2 b) { return make_float4(a.x, a.y, b.x, b.y); }
+
+template <int R, int NC, int NR, class F>
+EP_DEV void lap_march_pair(const Geo& g, const float2* __restrict__ psi, const FdW<float>& fd, int zc,
+                           unsigned char* smem, const float2* const* cin, const float* const* rin, float scale,
+                           F&& f) {
+  static_assert(R % 2 == 0, "the pair march needs an even stencil radius");
+  constexpr int W2 = (EP_PX + 2 * R) / 2, H = EP_TY + 2 * R, PL = W2 * H, NT = EP_TX * EP_TY, RH = R / 2;
+  float4* sp = reinterpret_cast<float4*>(smem);
+  float4* sq = sp + 2 * PL;
+  float4* sc_ = sq + 2 * NT;
+  float2* sr = reinterpret_cast<float2*>(sc_ + 2 * NC * NT);
+  int* soff = reinterpret_cast<int*>(sr + 2 * NR * NT);
+  const int tx = threadIdx.x, ty = threadIdx.y, tid = ty * EP_TX + tx;
+  const int x = blockIdx.x * EP_PX + 2 * tx, y = blockIdx.y * EP_TY + ty;
+  const int z0 = blockIdx.z * zc, z1 = min(z0 + zc, g.nz);
+  const bool valid = (x < g.nx) && (y < g.ny);
+  const int per = fd.periodic;
+  const long long sxy = (long long)g.nx * g.ny;
+  const long long xy = x + (long long)g.nx * y;
+  // pair offsets of the halo plane (x even, so a pair never straddles the
+  // wrap or the box edge); -1 outside a zero-boundary box
+  for (int e = tid; e < PL; e += NT) {
+    const int r = e / W2, c = e - r * W2;
+    const int xx = blockIdx.x * EP_PX - R + 2 * c, yy = blockIdx.y * EP_TY - R + r;
+    int o = -1;
+    if (xx >= 0 && xx < g.nx && yy >= 0 && yy < g.ny) o = xx + g.nx * yy;
+    else if (per) o = wrapi(xx, g.nx) + g.nx * wrapi(yy, g.ny);
+    soff[e] = o;
+  }
+  __syncthreads();
+  const float4 zero4 = make_float4(0.f, 0.f, 0.f, 0.f);
+  auto zplane = [&](int zz) -> int {
+    if (zz < 0 || zz >= g.nz) return per ? wrapi(zz, g.nz) : -1;
+    return zz;
+  };
+  auto prefetch = [&](int z, int buf) {
+    float4* P = sp + buf * PL;
+    const int zz = zplane(z);
+    const float2* pz = psi + sxy * (zz < 0 ? 0 : zz);
+    for (int e = tid; e < PL; e += NT) {
+      const int o = zz < 0 ? -1 : soff[e];
+      if (o >= 0) cp_async<16>(P + e, pz + o);
+      else P[e] = zero4;
+    }
+    if (valid) {
+      const int zq = zplane(z + R);
+      if (zq >= 0) cp_async<16>(sq + buf * NT + tid, psi + (xy + sxy * zq));
+      else sq[buf * NT + tid] = zero4;
+      const long long p = xy + sxy * z;
+#pragma unroll
+      for (int i = 0; i < NC; ++i) cp_async<16>(sc_ + (buf * NC + i) * NT + tid, cin[i] + p);
+#pragma unroll
+      for (int i = 0; i < NR; ++i) cp_async<8>(sr + (buf * NR + i) * NT + tid, rin[i] + p);
+    }
+    cp_commit();
+  };
+  float4 q[2 * R + 1];
+#pragma unroll
+  for (int k = 0; k < 2 * R; ++k) {
+    const int zz = zplane(z0 - R + k);
+    q[k] = (valid && zz >= 0) ? __ldg(reinterpret_cast<const float4*>(psi + (xy + sxy * zz))) : zero4;
+  }
+  prefetch(z0, 0);
+  for (int z = z0; z < z1; ++z) {
+    const int buf = (z - z0) & 1;
+    if (z + 1 < z1) {
+      prefetch(z + 1, buf ^ 1);
+      cp_wait<1>();
+    } else {
+      cp_wait<0>();
+    }
+    __syncthreads();
+    if (valid) {
+      q[2 * R] = sq[buf * NT + tid];
+      // elements 2tx .. 2tx + 2R + 1 of the halo row (x - R .. x + 1 + R)
+      const float4* rowp = sp + buf * PL + (ty + R) * W2 + tx;
+      float2 e[2 * R + 2];
+#pragma unroll
+      for (int j = 0; j <= R; ++j) {
+        const float4 v = rowp[j];
+        e[2 * j] = lo2(v);
+        e[2 * j + 1] = hi2(v);
+      }
+      const float4* colp = rowp + RH;
+      const float2 ca = lo2(q[R]), cb = hi2(q[R]);
+      float2 lxa = vmul(fd.w2[0][0], ca), lya = vmul(fd.w2[1][0], ca), lza = vmul(fd.w2[2][0], ca);
+      float2 lxb = vmul(fd.w2[0][0], cb), lyb = vmul(fd.w2[1][0], cb), lzb = vmul(fd.w2[2][0], cb);
+#pragma unroll
+      for (int k = 1; k <= R; ++k) {
+        lxa = vfma(fd.w2[0][k], vadd(e[R - k], e[R + k]), lxa);
+        lxb = vfma(fd.w2[0][k], vadd(e[R + 1 - k], e[R + 1 + k]), lxb);
+        const float4 yn = colp[-k * W2], yp = colp[k * W2];
+        lya = vfma(fd.w2[1][k], vadd(lo2(yn), lo2(yp)), lya);
+        lyb = vfma(fd.w2[1][k], vadd(hi2(yn), hi2(yp)), lyb);
+        const float4 zn = q[R - k], zp = q[R + k];
+        lza = vfma(fd.w2[2][k], vadd(lo2(zn), lo2(zp)), lza);
+        lzb = vfma(fd.w2[2][k], vadd(hi2(zn), hi2(zp)), lzb);
+      }
+      f(xy + sxy * z, cat2(vmul(scale, ca), vmul(scale, cb)),
+        cat2(vmul(scale, vadd(vadd(lxa, lya), lza)), vmul(scale, vadd(vadd(lxb, lyb), lzb))),
+        sc_ + buf * NC * NT + tid, sr + buf * NR * NT + tid);
+    }
+#pragma unroll
+    for (int k = 0; k < 2 * R; ++k) q[k] = q[k + 1];
+    __syncthreads();
+  }
+}
+
 // First derivatives of real fields by a 2.5-D march, software-pipelined like
 // lap_march_async (13-point derivnd stencils, init_deriv_parallel.f90, with
 // the boundary handling and summation order of d1_global):
@@ -1228,8 +1358,8 @@ EP_DEV bool last_block(unsigned int* counter) {
 // Predictor + modifier of steppc.f90:53-64.  The new psi is written over
 // psiold(ioldp(3)) (read here point-wise), so the host swaps buffers instead
 // of copying.
-template <class T, int R>
-__global__ void __launch_bounds__(EP_TX* EP_TY, sizeof(T) == 4 ? 4 : 2) k_predict(Geo g, FdW<T> fd, Phys ph, int zc,
+template <class T, int R, bool PAIR>
+__global__ void __launch_bounds__(EP_TX* EP_TY, PAIR ? 2 : (sizeof(T) == 4 ? 4 : 2)) k_predict(Geo g, FdW<T> fd, Phys ph, int zc,
                                                          const C2<T>* __restrict__ psi, const T* __restrict__ pot4,
                                                          const T* __restrict__ uimp, C2<T>* po3,
                                                          const C2<T>* __restrict__ h1, C2<T>* h2, C2<T>* pc,
@@ -1244,23 +1374,46 @@ __global__ void __launch_bounds__(EP_TX* EP_TY, sizeof(T) == 4 ? 4 : 2) k_predic
           kh2 = (T(2) * f) * bscale_of<T>(sc, sl.h2), kpc = c112 * bscale_of<T>(sc, sl.pc);
   const C2<T>* cin[4] = {po3, h1, h2, pc};
   const T* rin[2] = {pot4, uimp};
-  lap_march_async<T, R, 4, 2>(
-      g, psi, fd, zc, smraw, cin, rin, bscale_of<T>(sc, sl.psi),
-      [&](long long p, C2<T> c, C2<T> lap, const C2<T>* ic, const T* ir) {
-        const C2<T> H = happly<T>(hc, lap, c, ir[0], ir[NT]);
-        C2<T> pp, pn;
-        if constexpr (sizeof(T) == 4) {
-          pp = vfma(kh2, ic[2 * NT], vfma(-kh1, ic[NT], vfma(k2f, H, vmul(s3, ic[0]))));
-          pn = vfma(-kpc, ic[3 * NT], pp);
-        } else {
-          pp = ((s3 * ic[0] + k2f * H) - kh1 * ic[NT]) + kh2 * ic[2 * NT];
-          pn = pp - kpc * ic[3 * NT];
-        }
-        po3[p] = pn;
-        pc[p] = pp;
-        h2[p] = H;
-        den[p] = pn.x * pn.x + pn.y * pn.y;
-      });
+  // one point: H psi, the predictor pp and the modified value pn, from psi,
+  // its Laplacian, po3, h1, h2, pc, pot4 and uimp
+  auto point = [&](C2<T> c, C2<T> lap, C2<T> a3, C2<T> b1, C2<T> b2, C2<T> opc, T v, T u, C2<T>& H, C2<T>& pp,
+                   C2<T>& pn) {
+    H = happly<T>(hc, lap, c, v, u);
+    if constexpr (sizeof(T) == 4) {
+      pp = vfma(kh2, b2, vfma(-kh1, b1, vfma(k2f, H, vmul(s3, a3))));
+      pn = vfma(-kpc, opc, pp);
+    } else {
+      pp = ((s3 * a3 + k2f * H) - kh1 * b1) + kh2 * b2;
+      pn = pp - kpc * opc;
+    }
+  };
+  if constexpr (PAIR) {
+    lap_march_pair<R, 4, 2>(
+        g, psi, fd, zc, smraw, cin, rin, bscale_of<T>(sc, sl.psi),
+        [&](long long p, float4 c, float4 lap, const float4* ic, const float2* ir) {
+          float2 Ha, ppa, pna, Hb, ppb, pnb;
+          point(lo2(c), lo2(lap), lo2(ic[0]), lo2(ic[NT]), lo2(ic[2 * NT]), lo2(ic[3 * NT]), ir[0].x, ir[NT].x, Ha,
+                ppa, pna);
+          point(hi2(c), hi2(lap), hi2(ic[0]), hi2(ic[NT]), hi2(ic[2 * NT]), hi2(ic[3 * NT]), ir[0].y, ir[NT].y, Hb,
+                ppb, pnb);
+          *reinterpret_cast<float4*>(po3 + p) = cat2(pna, pnb);
+          *reinterpret_cast<float4*>(pc + p) = cat2(ppa, ppb);
+          *reinterpret_cast<float4*>(h2 + p) = cat2(Ha, Hb);
+          *reinterpret_cast<float2*>(den + p) =
+              make_float2(pna.x * pna.x + pna.y * pna.y, pnb.x * pnb.x + pnb.y * pnb.y);
+        });
+  } else {
+    lap_march_async<T, R, 4, 2>(
+        g, psi, fd, zc, smraw, cin, rin, bscale_of<T>(sc, sl.psi),
+        [&](long long p, C2<T> c, C2<T> lap, const C2<T>* ic, const T* ir) {
+          C2<T> H, pp, pn;
+          point(c, lap, ic[0], ic[NT], ic[2 * NT], ic[3 * NT], ir[0], ir[NT], H, pp, pn);
+          po3[p] = pn;
+          pc[p] = pp;
+          h2[p] = H;
+          den[p] = pn.x * pn.x + pn.y * pn.y;
+        });
+  }
   if (last_block(&sc->counter2)) {
     if (threadIdx.x == 0 && threadIdx.y == 0) {
       sc->bscale[sl.a] = 1.0;
@@ -1278,8 +1431,8 @@ __global__ void __launch_bounds__(EP_TX* EP_TY, sizeof(T) == 4 ? 4 : 2) k_predic
 // Corrector + final value of steppc.f90:135-151 with fused reductions:
 // sum |pc|, sum |psi|^2 (new), <psi|H|psi> and sum |psi|^2 of the modified
 // psi (chemical potential).
-template <class T, int R, bool STATS>
-__global__ void __launch_bounds__(EP_TX* EP_TY, sizeof(T) == 4 ? 3 : 2) k_correct(Geo g, FdW<T> fd, Phys ph, int zc,
+template <class T, int R, bool STATS, bool PAIR>
+__global__ void __launch_bounds__(EP_TX* EP_TY, PAIR ? 2 : (sizeof(T) == 4 ? 3 : 2)) k_correct(Geo g, FdW<T> fd, Phys ph, int zc,
                                                          const C2<T>* __restrict__ psi, const T* __restrict__ pot4,
                                                          const T* __restrict__ uimp,
                                                          const C2<T>* __restrict__ po3,
@@ -1300,30 +1453,52 @@ __global__ void __launch_bounds__(EP_TX* EP_TY, sizeof(T) == 4 ? 3 : 2) k_correc
           sp_ = bscale_of<T>(sc, sl.pc);
   const C2<T>* cin[5] = {po3, po2, h1, h2, pc};
   const T* rin[2] = {pot4, uimp};
-  lap_march_async<T, R, 5, 2>(g, psi, fd, zc, smraw, cin, rin, bscale_of<T>(sc, sl.psi),
-                              [&](long long p, C2<T> c, C2<T> lap, const C2<T>* ic, const T* ir) {
-    const C2<T> H = happly<T>(hc, lap, c, ir[0], ir[NT]);
-    C2<T> p5, pcn, po;
+  // one point: the corrected pc and the final psi from psi, its Laplacian,
+  // po3, po2, h1, h2, pc, pot4 and uimp; returns |psi|^2 and adds the point
+  // to the reductions
+  auto point = [&](C2<T> c, C2<T> lap, C2<T> a3, C2<T> a2, C2<T> b1, C2<T> b2, C2<T> opc, T v, T u, C2<T>& pcn,
+                   C2<T>& po) -> T {
+    const C2<T> H = happly<T>(hc, lap, c, v, u);
+    C2<T> p5;
     if constexpr (sizeof(T) == 4) {
-      p5 = vfma(-k2, ic[3 * NT], vfma(k1, ic[2 * NT], vfma(kH, H, vfma(-k2o, ic[NT], vmul(k3, ic[0])))));
-      pcn = vsub(vmul(sp_, ic[4 * NT]), p5);
+      p5 = vfma(-k2, b2, vfma(k1, b1, vfma(kH, H, vfma(-k2o, a2, vmul(k3, a3)))));
+      pcn = vsub(vmul(sp_, opc), p5);
       po = vfma(c9, pcn, p5);
     } else {
-      p5 = (((k3 * ic[0] - k2o * ic[NT]) + kH * H) + k1 * ic[2 * NT]) - k2 * ic[3 * NT];
-      pcn = sp_ * ic[4 * NT] - p5;
+      p5 = (((k3 * a3 - k2o * a2) + kH * H) + k1 * b1) - k2 * b2;
+      pcn = sp_ * opc - p5;
       po = p5 + c9 * pcn;
     }
-    pc[p] = pcn;
-    out[p] = po;
     const T dn = po.x * po.x + po.y * po.y;
-    den[p] = dn;
     acc[1].add(dn);
     if (STATS) {  // errHe and mu are read only when the caller asks for them
       acc[0].add(sqrt(pcn.x * pcn.x + pcn.y * pcn.y));
       acc[2].add(hexp_t<T>(ph, c, H));
       acc[3].add(c.x * c.x + c.y * c.y);
     }
-  });
+    return dn;
+  };
+  if constexpr (PAIR) {
+    lap_march_pair<R, 5, 2>(g, psi, fd, zc, smraw, cin, rin, bscale_of<T>(sc, sl.psi),
+                            [&](long long p, float4 c, float4 lap, const float4* ic, const float2* ir) {
+      float2 pca, poa, pcb, pob;
+      const float da = point(lo2(c), lo2(lap), lo2(ic[0]), lo2(ic[NT]), lo2(ic[2 * NT]), lo2(ic[3 * NT]),
+                             lo2(ic[4 * NT]), ir[0].x, ir[NT].x, pca, poa);
+      const float db = point(hi2(c), hi2(lap), hi2(ic[0]), hi2(ic[NT]), hi2(ic[2 * NT]), hi2(ic[3 * NT]),
+                             hi2(ic[4 * NT]), ir[0].y, ir[NT].y, pcb, pob);
+      *reinterpret_cast<float4*>(pc + p) = cat2(pca, pcb);
+      *reinterpret_cast<float4*>(out + p) = cat2(poa, pob);
+      *reinterpret_cast<float2*>(den + p) = make_float2(da, db);
+    });
+  } else {
+    lap_march_async<T, R, 5, 2>(g, psi, fd, zc, smraw, cin, rin, bscale_of<T>(sc, sl.psi),
+                                [&](long long p, C2<T> c, C2<T> lap, const C2<T>* ic, const T* ir) {
+      C2<T> pcn, po;
+      den[p] = point(c, lap, ic[0], ic[NT], ic[2 * NT], ic[3 * NT], ic[4 * NT], ir[0], ir[NT], pcn, po);
+      pc[p] = pcn;
+      out[p] = po;
+    });
+  }
   // without STATS only the norm (q = 1) is reduced and finalised
   constexpr unsigned QM = STATS ? 0xFu : 0x2u;
   block_reduce_store_acc<4, QM>(acc, partials);
