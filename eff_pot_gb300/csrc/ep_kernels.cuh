@@ -1036,13 +1036,11 @@ EP_DEV void lap_march_async(const Geo& g, const C2<T>* __restrict__ psi, const F
   prefetch(z0, 0);
   for (int z = z0; z < z1; ++z) {
     const int buf = (z - z0) & 1;
-    if (z + 1 < z1) {
-      prefetch(z + 1, buf ^ 1);
-      cp_wait<1>();
-    } else {
-      cp_wait<0>();
-    }
+    // one barrier per plane: it publishes plane z and, as every thread has
+    // finished plane z - 1, frees the other buffer for plane z + 1
+    cp_wait<0>();
     __syncthreads();
+    if (z + 1 < z1) prefetch(z + 1, buf ^ 1);
     if (valid) {
       q[2 * R] = sq[buf * NT + tid];
       const CT* row = sp + buf * PL + (ty + R) * W + (tx + R);
@@ -1059,7 +1057,6 @@ EP_DEV void lap_march_async(const Geo& g, const C2<T>* __restrict__ psi, const F
     }
 #pragma unroll
     for (int k = 0; k < 2 * R; ++k) q[k] = q[k + 1];
-    __syncthreads();
   }
 }
 
@@ -1150,13 +1147,11 @@ EP_DEV void lap_march_pair(const Geo& g, const float2* __restrict__ psi, const F
   prefetch(z0, 0);
   for (int z = z0; z < z1; ++z) {
     const int buf = (z - z0) & 1;
-    if (z + 1 < z1) {
-      prefetch(z + 1, buf ^ 1);
-      cp_wait<1>();
-    } else {
-      cp_wait<0>();
-    }
+    // one barrier per plane: it publishes plane z and, as every thread has
+    // finished plane z - 1, frees the other buffer for plane z + 1
+    cp_wait<0>();
     __syncthreads();
+    if (z + 1 < z1) prefetch(z + 1, buf ^ 1);
     if (valid) {
       q[2 * R] = sq[buf * NT + tid];
       // elements 2tx .. 2tx + 2R + 1 of the halo row (x - R .. x + 1 + R)
@@ -1189,7 +1184,6 @@ EP_DEV void lap_march_pair(const Geo& g, const float2* __restrict__ psi, const F
     }
 #pragma unroll
     for (int k = 0; k < 2 * R; ++k) q[k] = q[k + 1];
-    __syncthreads();
   }
 }
 
@@ -1200,8 +1194,8 @@ EP_DEV void lap_march_pair(const Geo& g, const float2* __restrict__ psi, const F
 //   MODE 1: o0 = d/dy f + d/dz f2                (term_alfa.f90:220-230)
 // Each thread computes two x-neighbouring points (x even), so every
 // neighbour in shared memory, the z-queue and every store move as pairs
-// (8-byte FP32 / 16-byte FP64 accesses): the march is bound by its
-// load/store instructions, not its arithmetic.
+// (8-byte FP32 / 16-byte FP64 accesses), and the y and z sums of the pair
+// are paired FP32 instructions (each point summed in the scalar order).
 #define EP_D1_TX (2 * EP_TX)  // x points of a CTA row
 template <class T, int R, int MODE>
 __global__ void __launch_bounds__(EP_TX* EP_TY) k_d1march(Geo g, const __grid_constant__ FdW<T> fd, int zc,
@@ -1282,13 +1276,9 @@ __global__ void __launch_bounds__(EP_TX* EP_TY) k_d1march(Geo g, const __grid_co
   prefetch(z0, 0);
   for (int z = z0; z < z1; ++z) {
     const int buf = (z - z0) & 1;
-    if (z + 1 < z1) {
-      prefetch(z + 1, buf ^ 1);
-      cp_wait<1>();
-    } else {
-      cp_wait<0>();
-    }
+    cp_wait<0>();  // one barrier per plane, as in lap_march_async
     __syncthreads();
+    if (z + 1 < z1) prefetch(z + 1, buf ^ 1);
     if (valid) {
       q[2 * R] = sq[buf][tid];
       // row element x of this thread (even offset: W, HX and 2 tx are even)
@@ -1297,16 +1287,9 @@ __global__ void __launch_bounds__(EP_TX* EP_TY) k_d1march(Geo g, const __grid_co
       const long long p = pxy + sxy * z;
       PT dy = cmk<T>(T(0), T(0)), dz = cmk<T>(T(0), T(0));
 #pragma unroll
-      for (int k = 1; k <= R; ++k) {
-        const PT a = rowp[k * WP], b = rowp[-k * WP];
-        dy.x += fd.w1[1][k] * (a.x - b.x);
-        dy.y += fd.w1[1][k] * (a.y - b.y);
-      }
+      for (int k = 1; k <= R; ++k) dy = vfma(fd.w1[1][k], vsub(rowp[k * WP], rowp[-k * WP]), dy);
 #pragma unroll
-      for (int k = 1; k <= R; ++k) {
-        dz.x += fd.w1[2][k] * (q[R + k].x - q[R - k].x);
-        dz.y += fd.w1[2][k] * (q[R + k].y - q[R - k].y);
-      }
+      for (int k = 1; k <= R; ++k) dz = vfma(fd.w1[2][k], vsub(q[R + k], q[R - k]), dz);
       if (MODE == 0) {
         // elements x + JLO*2 .. x + 2*JHI + 1 of the row, as pairs
         T e[NE];
@@ -1331,7 +1314,6 @@ __global__ void __launch_bounds__(EP_TX* EP_TY) k_d1march(Geo g, const __grid_co
     }
 #pragma unroll
     for (int k = 0; k < 2 * R; ++k) q[k] = q[k + 1];
-    __syncthreads();
   }
 }
 
