@@ -99,7 +99,9 @@ struct DevScalars {
   float bscale_f[8];
 };
 #define EP_NSLOTS 8
-enum { EP_FLAG_NONFINITE = 1u, EP_FLAG_DEN_NONPOS = 2u };
+// EP_FLAG_TIMEOUT: a bounded wait on a TMA copy ran out (the block stopped
+// its march and the host reports EP_ERR_TIMEOUT).
+enum { EP_FLAG_NONFINITE = 1u, EP_FLAG_DEN_NONPOS = 2u, EP_FLAG_TIMEOUT = 4u };
 
 // ---------------------------------------------------------------------------
 // 1-D FFT plan: length and radix sequence (radices 8,4,2,3,5).

@@ -77,7 +77,22 @@ class Engine {
   std::string* err = nullptr;
   int dev_sm = 0;
   int zc_pc = 16, zc_pr = 16, zc_rk = 16, zc_d1 = 16;  // z planes per CTA of the stencil marches
-  bool pairs = false;  // predictor / corrector with two points per thread (FP32, even R and nx)
+  // predictor / corrector form: 0 one point per thread, 1 two points per
+  // thread staged by cp.async (FP32, even R and nx), 2 the same staged by TMA
+  // boxes (also nx % 64 == 0 and ny % 8 == 0)
+  int pmode = 0;
+  // TMA boxes of each rotating complex buffer ({128 x R}, {128 x EP_TYT},
+  // {16 x R}, {16 x EP_TYT} floats x rows) and of pot4 / uimp
+  // ({64 x EP_TYT})
+  struct BufMaps {
+    const void* buf;
+    CUtensorMap m[4];
+  };
+  std::vector<BufMaps> cmaps;
+  CUtensorMap rmaps[2];
+  int build_march_maps();
+  const CUtensorMap* maps_of(const void* buf) const;
+  bool march_maps(MarchMaps& mm, const CT* marched, const CT* const* cin, int nc) const;
   T* dyz = nullptr;                         // dy(gy) + dz(gz) of term_alfa
   T* sigdel = nullptr;                      // Sig_Del of the D state (vpi holds Pi_Del)
   int d1march(int mode, const T* f, const T* f2, T* o0, T* o1, T* o2);
@@ -132,7 +147,7 @@ class Engine {
     }
     return 0;
   }
-  int march_zchunk(int blocks_per_sm, int tile_x = EP_TX) const;
+  int march_zchunk(int blocks_per_sm, int tile_x = EP_TX, int tile_y = EP_TY) const;
   // kernel attributes (dynamic shared memory) and the march z-chunk lengths,
   // set up by init
   int x_attrs();

@@ -282,8 +282,8 @@ int Engine<T>::init(const ep_config& c, cudaStream_t s, Prof* p, ImpState* im, s
 }
 
 template <class T>
-int Engine<T>::march_zchunk(int blocks_per_sm, int tile_x) const {
-  const long long nxy = (long long)((g.nx + tile_x - 1) / tile_x) * ((g.ny + EP_TY - 1) / EP_TY);
+int Engine<T>::march_zchunk(int blocks_per_sm, int tile_x, int tile_y) const {
+  const long long nxy = (long long)((g.nx + tile_x - 1) / tile_x) * ((g.ny + tile_y - 1) / tile_y);
   const long long slots = (long long)dev_sm * std::max(1, blocks_per_sm);
   return march_chunk(nxy, g.nz, slots, fd.R);
 }
@@ -765,28 +765,38 @@ int Engine<T>::lap_predict(double dt) {
   CT* po3 = po[ioldp[2]];
   const CT* h1 = ph[ioldh[0]];
   CT* h2 = ph[ioldh[1]];
-  const int tile_x = pairs ? EP_PX : EP_TX;
-  dim3 grid((g.nx + tile_x - 1) / tile_x, (g.ny + EP_TY - 1) / EP_TY, (g.nz + zc_pr - 1) / zc_pr);
-  dim3 blk(EP_TX, EP_TY);
+  const int tile_x = pmode ? EP_PX : EP_TX, tile_y = pmode == 2 ? EP_TYT : EP_TY;
+  dim3 grid((g.nx + tile_x - 1) / tile_x, (g.ny + tile_y - 1) / tile_y, (g.nz + zc_pr - 1) / zc_pr);
+  dim3 blk(EP_TX, tile_y);
   T f = (T)(c4o3 * dt), c1 = (T)c112;
   Slots sl{slot_of(psi), slot_of(po3), -1, slot_of(h1), slot_of(h2), slot_of(pc), -1};
   const CT* psic = psi;
   const T *pot4c = pot4, *uimpc = uimp;
   int zc = zc_pr;
-  void* args[] = {&g, &fd, &phys, &zc, &psic, &pot4c, &uimpc, &po3, &h1, &h2, &pc, &den, &f, &c1, &sc, &sl};
+  NoMaps nomaps{0};
+  MarchMaps mm;
+  if (pmode == 2) {
+    const CT* cin[4] = {po3, h1, h2, pc};
+    if (!march_maps(mm, psi, cin, 4)) {
+      *err = "predictor: a buffer without tensor maps";
+      return EP_ERR_STATE;
+    }
+  }
+  void* args[] = {&g,  &fd, &phys, &zc, &psic, &pot4c, &uimpc, &po3, &h1, &h2,
+                  &pc, &den, &f,   &c1, &sc,   &sl,    pmode == 2 ? (void*)&mm : (void*)&nomaps};
   const void* fn = nullptr;
   size_t smem = 0;
 #define EP_PRED(RR)                                                                   \
   case RR:                                                                            \
     if constexpr (pair_built<T>(RR)) {                                                \
-      if (pairs) {                                                                    \
-        fn = (const void*)k_predict<T, RR, true>;                                     \
-        smem = march_pair_smem<RR, 4, 2>();                                           \
+      if (pmode) {                                                                    \
+        fn = pmode == 2 ? (const void*)k_predict<T, RR, 2> : (const void*)k_predict<T, RR, 1>; \
+        smem = pmode == 2 ? march_tma_smem<RR, 4, 2>() : march_pair_smem<RR, 4, 2>(); \
         break;                                                                        \
       }                                                                               \
     }                                                                                 \
     if constexpr (r_built<T>(RR)) {                                                   \
-      fn = (const void*)k_predict<T, RR, false>;                                      \
+      fn = (const void*)k_predict<T, RR, 0>;                                          \
       smem = march_smem<T, RR, 4, 2>();                                               \
     }                                                                                 \
     break;
@@ -810,9 +820,9 @@ int Engine<T>::lap_correct(double dt, bool want) {
   const CT* po2 = po[ioldp[1]];
   const CT* h1 = ph[ioldh[0]];
   const CT* h2 = ph[ioldh[1]];
-  const int tile_x = pairs ? EP_PX : EP_TX;
-  dim3 grid((g.nx + tile_x - 1) / tile_x, (g.ny + EP_TY - 1) / EP_TY, (g.nz + zc_pc - 1) / zc_pc);
-  dim3 blk(EP_TX, EP_TY);
+  const int tile_x = pmode ? EP_PX : EP_TX, tile_y = pmode == 2 ? EP_TYT : EP_TY;
+  dim3 grid((g.nx + tile_x - 1) / tile_x, (g.ny + tile_y - 1) / tile_y, (g.nz + zc_pc - 1) / zc_pc);
+  dim3 blk(EP_TX, tile_y);
   T f3 = (T)(3.0 * dt), cc = (T)c9;
   int renorm = (cfg.time_mode == EP_IMAGINARY_TIME && cfg.renormalize) ? 1 : 0;
   Slots sl{slot_of(psi), slot_of(po3), slot_of(po2), slot_of(h1), slot_of(h2), slot_of(pc), slot_of(spare)};
@@ -820,21 +830,36 @@ int Engine<T>::lap_correct(double dt, bool want) {
   const T *pot4c = pot4, *uimpc = uimp;
   int zc = zc_pc;
   double n4 = cfg.n4;
+  NoMaps nomaps{0};
+  MarchMaps mm;
+  if (pmode == 2) {
+    const CT* cin[5] = {po3, po2, h1, h2, pc};
+    if (!march_maps(mm, psi, cin, 5)) {
+      *err = "corrector: a buffer without tensor maps";
+      return EP_ERR_STATE;
+    }
+  }
   void* args[] = {&g,  &fd,  &phys, &zc,  &psic, &pot4c, &uimpc,   &po3, &po2, &h1, &h2,
-                  &pc, &spare, &den, &f3, &cc,   &partials, &sc,   &renorm, &n4, &sl};
+                  &pc, &spare, &den, &f3, &cc,   &partials, &sc,   &renorm, &n4, &sl,
+                  pmode == 2 ? (void*)&mm : (void*)&nomaps};
   const void* fn = nullptr;
   size_t smem = 0;
 #define EP_CORR(RR)                                                                                   \
   case RR:                                                                                            \
     if constexpr (pair_built<T>(RR)) {                                                                \
-      if (pairs) {                                                                                    \
-        fn = want ? (const void*)k_correct<T, RR, true, true> : (const void*)k_correct<T, RR, false, true>; \
+      if (pmode == 2) {                                                                               \
+        fn = want ? (const void*)k_correct<T, RR, true, 2> : (const void*)k_correct<T, RR, false, 2>; \
+        smem = march_tma_smem<RR, 5, 2>();                                                            \
+        break;                                                                                        \
+      }                                                                                               \
+      if (pmode == 1) {                                                                               \
+        fn = want ? (const void*)k_correct<T, RR, true, 1> : (const void*)k_correct<T, RR, false, 1>; \
         smem = march_pair_smem<RR, 5, 2>();                                                           \
         break;                                                                                        \
       }                                                                                               \
     }                                                                                                 \
     if constexpr (r_built<T>(RR)) {                                                                   \
-      fn = want ? (const void*)k_correct<T, RR, true, false> : (const void*)k_correct<T, RR, false, false>; \
+      fn = want ? (const void*)k_correct<T, RR, true, 0> : (const void*)k_correct<T, RR, false, 0>;   \
       smem = march_smem<T, RR, 5, 2>();                                                               \
     }                                                                                                 \
     break;
@@ -1079,6 +1104,10 @@ int Engine<T>::check_flags() {
   if ((r = cuda_ok(cudaStreamSynchronize(st), "flags"))) return r;
   if (f) {
     cudaMemsetAsync(&sc->flags, 0, sizeof(unsigned), st);
+    if (f & EP_FLAG_TIMEOUT) {
+      *err = "a stencil march gave up waiting for its TMA copies";
+      return EP_ERR_TIMEOUT;
+    }
     *err = (f & EP_FLAG_DEN_NONPOS) ? "density not positive (steprk trap)" : "non-finite value in a reduction";
     return EP_ERR_NONFINITE;
   }
@@ -1417,24 +1446,101 @@ int Engine<T>::fft_attrs() {
 #endif
 
 #if EP_ENGINE_PARTS & EP_PART_MARCH
+// TMA tensor maps of the pair march.  A complex field is a float tensor of
+// 2 nx x ny x nz (row pitch 8 nx bytes, a multiple of 16 for even nx);
+// boxes reaching outside it read zeros.
+template <class T>
+int Engine<T>::build_march_maps() {
+  typedef CUresult (*EncodeTiled)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*, const cuuint64_t*,
+                                  const cuuint64_t*, const cuuint32_t*, const cuuint32_t*, CUtensorMapInterleave,
+                                  CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+  void* fp = nullptr;
+  cudaDriverEntryPointQueryResult qres{};
+  if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &fp, 12000, cudaEnableDefault, &qres) !=
+          cudaSuccess ||
+      qres != cudaDriverEntryPointSuccess || !fp) {
+    cudaGetLastError();
+    *err = "cuTensorMapEncodeTiled is not available";
+    return EP_ERR_CUDA;
+  }
+  EncodeTiled encode = reinterpret_cast<EncodeTiled>(fp);
+  auto make = [&](CUtensorMap* m, const void* base, int xfloats, int bx, int by) -> bool {
+    const cuuint64_t dim[3] = {(cuuint64_t)xfloats, (cuuint64_t)g.ny, (cuuint64_t)g.nz};
+    const cuuint64_t str[2] = {(cuuint64_t)xfloats * 4, (cuuint64_t)xfloats * 4 * g.ny};
+    const cuuint32_t box[3] = {(cuuint32_t)bx, (cuuint32_t)by, 1};
+    const cuuint32_t est[3] = {1, 1, 1};
+    return encode(m, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 3, const_cast<void*>(base), dim, str, box, est,
+                  CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+                  CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+  };
+  const void* cb[] = {psi, spare, po[0], po[1], po[2], ph[0], ph[1], pc, q};
+  cmaps.clear();
+  for (const void* b : cb) {
+    BufMaps bm{};
+    bm.buf = b;
+    if (!make(&bm.m[0], b, 2 * g.nx, 2 * EP_PX, fd.R) || !make(&bm.m[1], b, 2 * g.nx, 2 * EP_PX, EP_TYT) ||
+        !make(&bm.m[2], b, 2 * g.nx, 16, fd.R) || !make(&bm.m[3], b, 2 * g.nx, 16, EP_TYT)) {
+      *err = "tensor map of a complex field refused";
+      return EP_ERR_CUDA;
+    }
+    cmaps.push_back(bm);
+  }
+  if (!make(&rmaps[0], pot4, g.nx, EP_PX, EP_TYT) || !make(&rmaps[1], uimp, g.nx, EP_PX, EP_TYT)) {
+    *err = "tensor map of a real field refused";
+    return EP_ERR_CUDA;
+  }
+  return EP_OK;
+}
+
+template <class T>
+const CUtensorMap* Engine<T>::maps_of(const void* buf) const {
+  for (const BufMaps& b : cmaps)
+    if (b.buf == buf) return b.m;
+  return nullptr;
+}
+
+// The maps of one predictor / corrector launch: the marched field's four
+// boxes, the {128 x EP_TYT} box of each complex input, pot4 and uimp.
+template <class T>
+bool Engine<T>::march_maps(MarchMaps& mm, const CT* marched, const CT* const* cin, int nc) const {
+  memset(&mm, 0, sizeof(mm));
+  const CUtensorMap* m = maps_of(marched);
+  if (!m) return false;
+  for (int k = 0; k < 4; ++k) mm.halo[k] = m[k];
+  for (int i = 0; i < nc; ++i) {
+    const CUtensorMap* mi = maps_of(cin[i]);
+    if (!mi) return false;
+    mm.cin[i] = mi[1];
+  }
+  mm.rin[0] = rmaps[0];
+  mm.rin[1] = rmaps[1];
+  return true;
+}
+
 template <class T>
 int Engine<T>::march_setup() {
 #define EP_ATTR(RR)                                                                                      \
   if constexpr (r_built<T>(RR)) {                                                                        \
-  cudaFuncSetAttribute(k_predict<T, RR, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)march_smem<T, RR, 4, 2>()); \
-  cudaFuncSetAttribute(k_correct<T, RR, true, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)march_smem<T, RR, 5, 2>()); \
-  cudaFuncSetAttribute(k_correct<T, RR, false, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)march_smem<T, RR, 5, 2>()); \
+  cudaFuncSetAttribute(k_predict<T, RR, 0>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)march_smem<T, RR, 4, 2>()); \
+  cudaFuncSetAttribute(k_correct<T, RR, true, 0>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)march_smem<T, RR, 5, 2>()); \
+  cudaFuncSetAttribute(k_correct<T, RR, false, 0>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)march_smem<T, RR, 5, 2>()); \
   cudaFuncSetAttribute(k_rkstage<T, RR>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)march_smem<T, RR, 1, 2>()); } \
   if constexpr (pair_built<T>(RR)) {                                                                     \
-  cudaFuncSetAttribute(k_predict<T, RR, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)march_pair_smem<RR, 4, 2>()); \
-  cudaFuncSetAttribute(k_correct<T, RR, true, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)march_pair_smem<RR, 5, 2>()); \
-  cudaFuncSetAttribute(k_correct<T, RR, false, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)march_pair_smem<RR, 5, 2>()); }
+  cudaFuncSetAttribute(k_predict<T, RR, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)march_pair_smem<RR, 4, 2>()); \
+  cudaFuncSetAttribute(k_correct<T, RR, true, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)march_pair_smem<RR, 5, 2>()); \
+  cudaFuncSetAttribute(k_correct<T, RR, false, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)march_pair_smem<RR, 5, 2>()); \
+  cudaFuncSetAttribute(k_predict<T, RR, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)march_tma_smem<RR, 4, 2>()); \
+  cudaFuncSetAttribute(k_correct<T, RR, true, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)march_tma_smem<RR, 5, 2>()); \
+  cudaFuncSetAttribute(k_correct<T, RR, false, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)march_tma_smem<RR, 5, 2>()); }
   EP_ATTR(1) EP_ATTR(2) EP_ATTR(3) EP_ATTR(4) EP_ATTR(5) EP_ATTR(6)
 #undef EP_ATTR
   {
-    // the pair form needs an even stencil radius and even nx (a pair never
-    // straddles the box edge); EP_MARCH_PAIRS=0 keeps the one-point form
+    // the pair forms need an even stencil radius and even nx (a pair never
+    // straddles the box edge), the TMA form whole 64 x 16 tiles as well;
+    // EP_MARCH_PAIRS=0 keeps the one-point form, EP_MARCH_TMA=0 the cp.async
+    // staging
     const char* ev = getenv("EP_MARCH_PAIRS");
+    const char* et = getenv("EP_MARCH_TMA");
     bool can = g.nx % 2 == 0 && !(ev && ev[0] == '0');
     switch (fd.R) {
       case 2: can = can && pair_built<T>(2); break;
@@ -1442,7 +1548,12 @@ int Engine<T>::march_setup() {
       case 6: can = can && pair_built<T>(6); break;
       default: can = false;
     }
-    pairs = can;
+    const bool tma = can && g.nx % EP_PX == 0 && g.ny % EP_TYT == 0 && !(et && et[0] == '0');
+    pmode = tma ? 2 : (can ? 1 : 0);
+    if (pmode == 2) {
+      int r = build_march_maps();
+      if (r) return r;
+    }
   }
   {
     // z-chunk lengths of the stencil marches from their resident blocks per SM
@@ -1451,20 +1562,23 @@ int Engine<T>::march_setup() {
 #define EP_OCC(RR)                                                                                         \
   case RR:                                                                                                 \
     if constexpr (r_built<T>(RR)) {                                                                        \
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_pc, k_correct<T, RR, true, false>, nt, march_smem<T, RR, 5, 2>()); \
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_pr, k_predict<T, RR, false>, nt, march_smem<T, RR, 4, 2>());      \
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_pc, k_correct<T, RR, true, 0>, nt, march_smem<T, RR, 5, 2>()); \
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_pr, k_predict<T, RR, 0>, nt, march_smem<T, RR, 4, 2>());      \
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_rk, k_rkstage<T, RR>, nt, march_smem<T, RR, 1, 2>()); \
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_d1, k_d1march<T, RR, 0>, nt, 0); }                  \
     if constexpr (pair_built<T>(RR)) {                                                                     \
-    if (pairs) {                                                                                           \
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_pc, k_correct<T, RR, true, true>, nt, march_pair_smem<RR, 5, 2>()); \
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_pr, k_predict<T, RR, true>, nt, march_pair_smem<RR, 4, 2>()); } } \
+    if (pmode == 1) {                                                                                      \
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_pc, k_correct<T, RR, true, 1>, nt, march_pair_smem<RR, 5, 2>()); \
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_pr, k_predict<T, RR, 1>, nt, march_pair_smem<RR, 4, 2>()); } \
+    if (pmode == 2) {                                                                                      \
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_pc, k_correct<T, RR, true, 2>, EP_TX * EP_TYT, march_tma_smem<RR, 5, 2>()); \
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_pr, k_predict<T, RR, 2>, EP_TX * EP_TYT, march_tma_smem<RR, 4, 2>()); } } \
     break;
     switch (fd.R) { EP_OCC(1) EP_OCC(2) EP_OCC(3) EP_OCC(4) EP_OCC(5) EP_OCC(6) default: break; }
 #undef EP_OCC
-    const int tile_x = pairs ? EP_PX : EP_TX;
-    zc_pc = march_zchunk(occ_pc, tile_x);
-    zc_pr = march_zchunk(occ_pr, tile_x);
+    const int tile_x = pmode ? EP_PX : EP_TX, tile_y = pmode == 2 ? EP_TYT : EP_TY;
+    zc_pc = march_zchunk(occ_pc, tile_x, tile_y);
+    zc_pr = march_zchunk(occ_pr, tile_x, tile_y);
     zc_rk = march_zchunk(occ_rk);
     zc_d1 = march_zchunk(occ_d1, EP_D1_TX);
   }

@@ -6,6 +6,7 @@
 #include "ep_fft.cuh"
 #include "ep_reduce.cuh"
 #include "ep_pairpot.h"
+#include "ep_tma.cuh"
 
 // ---------------------------------------------------------------------------
 // Kernel parameter blocks.
@@ -1083,6 +1084,30 @@ EP_DEV float2 lo2(float4 v) { return make_float2(v.x, v.y); }
 EP_DEV float2 hi2(float4 v) { return make_float2(v.z, v.w); }
 EP_DEV float4 cat2(float2 a, float2 b) { return make_float4(a.x, a.y, b.x, b.y); }
 
+// The pair's Laplacian: e[] holds its row's elements x - R .. x + 1 + R,
+// colp its column (rows R apart by pitch PITCH float4), q its z-queue.  Each
+// point is summed in the order of the one-point march.
+template <int R, int PITCH>
+EP_DEV void pair_lap(const FdW<float>& fd, const float2* e, const float4* colp, const float4* q, float scale,
+                     float4& c, float4& lap) {
+  const float2 ca = lo2(q[R]), cb = hi2(q[R]);
+  float2 lxa = vmul(fd.w2[0][0], ca), lya = vmul(fd.w2[1][0], ca), lza = vmul(fd.w2[2][0], ca);
+  float2 lxb = vmul(fd.w2[0][0], cb), lyb = vmul(fd.w2[1][0], cb), lzb = vmul(fd.w2[2][0], cb);
+#pragma unroll
+  for (int k = 1; k <= R; ++k) {
+    lxa = vfma(fd.w2[0][k], vadd(e[R - k], e[R + k]), lxa);
+    lxb = vfma(fd.w2[0][k], vadd(e[R + 1 - k], e[R + 1 + k]), lxb);
+    const float4 yn = colp[-k * PITCH], yp = colp[k * PITCH];
+    lya = vfma(fd.w2[1][k], vadd(lo2(yn), lo2(yp)), lya);
+    lyb = vfma(fd.w2[1][k], vadd(hi2(yn), hi2(yp)), lyb);
+    const float4 zn = q[R - k], zp = q[R + k];
+    lza = vfma(fd.w2[2][k], vadd(lo2(zn), lo2(zp)), lza);
+    lzb = vfma(fd.w2[2][k], vadd(hi2(zn), hi2(zp)), lzb);
+  }
+  c = cat2(vmul(scale, ca), vmul(scale, cb));
+  lap = cat2(vmul(scale, vadd(vadd(lxa, lya), lza)), vmul(scale, vadd(vadd(lxb, lyb), lzb)));
+}
+
 template <int R, int NC, int NR, class F>
 EP_DEV void lap_march_pair(const Geo& g, const float2* __restrict__ psi, const FdW<float>& fd, int zc,
                            unsigned char* smem, const float2* const* cin, const float* const* rin, float scale,
@@ -1163,27 +1188,185 @@ EP_DEV void lap_march_pair(const Geo& g, const float2* __restrict__ psi, const F
         e[2 * j] = lo2(v);
         e[2 * j + 1] = hi2(v);
       }
-      const float4* colp = rowp + RH;
-      const float2 ca = lo2(q[R]), cb = hi2(q[R]);
-      float2 lxa = vmul(fd.w2[0][0], ca), lya = vmul(fd.w2[1][0], ca), lza = vmul(fd.w2[2][0], ca);
-      float2 lxb = vmul(fd.w2[0][0], cb), lyb = vmul(fd.w2[1][0], cb), lzb = vmul(fd.w2[2][0], cb);
-#pragma unroll
-      for (int k = 1; k <= R; ++k) {
-        lxa = vfma(fd.w2[0][k], vadd(e[R - k], e[R + k]), lxa);
-        lxb = vfma(fd.w2[0][k], vadd(e[R + 1 - k], e[R + 1 + k]), lxb);
-        const float4 yn = colp[-k * W2], yp = colp[k * W2];
-        lya = vfma(fd.w2[1][k], vadd(lo2(yn), lo2(yp)), lya);
-        lyb = vfma(fd.w2[1][k], vadd(hi2(yn), hi2(yp)), lyb);
-        const float4 zn = q[R - k], zp = q[R + k];
-        lza = vfma(fd.w2[2][k], vadd(lo2(zn), lo2(zp)), lza);
-        lzb = vfma(fd.w2[2][k], vadd(hi2(zn), hi2(zp)), lzb);
-      }
-      f(xy + sxy * z, cat2(vmul(scale, ca), vmul(scale, cb)),
-        cat2(vmul(scale, vadd(vadd(lxa, lya), lza)), vmul(scale, vadd(vadd(lxb, lyb), lzb))),
-        sc_ + buf * NC * NT + tid, sr + buf * NR * NT + tid);
+      float4 c, lap;
+      pair_lap<R, W2>(fd, e, rowp + RH, q, scale, c, lap);
+      f(xy + sxy * z, c, lap, sc_ + buf * NC * NT + tid, sr + buf * NR * NT + tid);
     }
 #pragma unroll
     for (int k = 0; k < 2 * R; ++k) q[k] = q[k + 1];
+  }
+}
+
+// Tensor maps of one TMA pair march (x in floats: a complex field is a
+// float tensor of 2 nx x ny x nz): the marched field's boxes {128 x R},
+// {128 x EP_TYT}, {16 x R} and {16 x EP_TYT} (floats x rows), a
+// {128 x EP_TYT} box of each complex input and a {64 x EP_TYT} box of each
+// real input.
+struct MarchMaps {
+  CUtensorMap halo[4];
+  CUtensorMap cin[5];
+  CUtensorMap rin[2];
+};
+
+// Kernel parameter of the predictor / corrector: the TMA form (PM = 2) takes
+// its tensor maps, the other forms an empty placeholder.
+struct NoMaps {
+  int unused;
+};
+template <int PM> struct MapsOf { typedef NoMaps type; };
+template <> struct MapsOf<2> { typedef MarchMaps type; };
+
+// Polls of a bounded mbarrier wait (a few tens of milliseconds at least; a
+// copy lands in microseconds).
+#define EP_MBAR_POLLS (1u << 22)
+
+// The TMA form's tile: EP_PX x EP_TYT points, 32 x EP_TYT threads (one CTA
+// per SM), EP_MSTAGES plane buffers in flight.
+#define EP_TYT 16
+#define EP_MSTAGES 3
+
+// Shared memory of the TMA pair march: per buffer the plane's centre columns
+// (2R + EP_TYT rows of 64 points), its left and right columns (8 points
+// each), the z-queue tile and the NC complex / NR real input tiles;
+// EP_MSTAGES buffers, a 128-byte alignment pad and one mbarrier per buffer.
+template <int R, int NC, int NR>
+__host__ __device__ constexpr int march_tma_buf() {
+  return (2 * R + EP_TYT) * EP_PX * 8 + 2 * (2 * R + EP_TYT) * 8 * 8 + (1 + NC) * EP_TX * EP_TYT * 16 +
+         NR * EP_TX * EP_TYT * 8;
+}
+template <int R, int NC, int NR>
+constexpr size_t march_tma_smem() {
+  return 128 + EP_MSTAGES * (size_t)march_tma_buf<R, NC, NR>() + 8 * EP_MSTAGES;
+}
+
+// The pair march with every plane, z-queue tile and input tile brought in by
+// TMA boxes that one thread issues (grids with nx a multiple of 64 and ny a
+// multiple of EP_TYT): the plane's periodic halo is nine boxes -- left halo,
+// centre and right halo columns by top halo, centre and bottom halo rows,
+// each starting at its wrapped coordinate (in a zero-boundary box the boxes
+// outside the tensor read zeros).  The row parts stack in shared memory; the
+// left and right columns land in their own arrays and each thread keeps the
+// shared-memory offsets of its R + 1 x-neighbour pairs.  Planes z + 1 and
+// z + 2 are in flight while plane z is computed; one mbarrier per buffer
+// counts the bytes, and a bounded wait that runs out raises EP_FLAG_TIMEOUT
+// and ends the march of the block.
+template <int R, int NC, int NR, class F>
+EP_DEV void lap_march_pair_tma(const Geo& g, const float2* __restrict__ psi, const FdW<float>& fd, int zc,
+                               unsigned char* smraw, const MarchMaps& mm, DevScalars* sc, float scale, F&& f) {
+  static_assert(R % 2 == 0 && R <= 8, "the pair march needs an even stencil radius of at most 8");
+  constexpr int TY = EP_TYT, NT = EP_TX * TY, RH = R / 2, HR = 2 * R + TY, S = EP_MSTAGES;
+  constexpr int CB = HR * EP_PX * 8, LB = HR * 8 * 8, QB = NT * 16, IB = NT * 16, JB = NT * 8;
+  constexpr int BUF = march_tma_buf<R, NC, NR>();
+  unsigned char* smem =
+      smraw + ((128u - (smem_u32(smraw) & 127u)) & 127u);  // 128-byte aligned TMA destinations
+  uint64_t* bars = reinterpret_cast<uint64_t*>(smem + S * BUF);
+  const int tx = threadIdx.x, ty = threadIdx.y, tid = ty * EP_TX + tx;
+  const int bx = blockIdx.x * EP_PX, by = blockIdx.y * TY;
+  const int x = bx + 2 * tx, y = by + ty;
+  const int z0 = blockIdx.z * zc, z1 = min(z0 + zc, g.nz);
+  const int per = fd.periodic;
+  const long long sxy = (long long)g.nx * g.ny;
+  const long long xy = x + (long long)g.nx * y;
+  // float4 offsets (within a buffer) of the x-pairs tx .. tx + R of the
+  // thread's extended row: left columns, centre columns, right columns
+  int xo[R + 1];
+  {
+    const int r = ty + R;
+#pragma unroll
+    for (int i = 0; i <= R; ++i) {
+      const int c = tx + i;
+      xo[i] = c < RH ? HR * 32 + r * 4 + (4 - RH + c)
+                     : (c < 32 + RH ? r * 32 + (c - RH) : HR * 36 + r * 4 + (c - 32 - RH));
+    }
+  }
+  int xl = bx - 8, xr = bx + EP_PX, yt = by - R, yb = by + TY;
+  if (per) {
+    xl = wrapi(xl, g.nx);
+    xr = wrapi(xr, g.nx);
+    yt = wrapi(yt, g.ny);
+    yb = wrapi(yb, g.ny);
+  }
+  auto issue = [&](int z, int b) {
+    unsigned char* B = smem + b * BUF;
+    uint64_t* bar = bars + b;
+    fence_proxy_async();
+    mbar_expect_tx(bar, (uint32_t)BUF);
+    const int zq = per ? wrapi(z + R, g.nz) : z + R;  // beyond a zero-boundary box: zeros
+    tma_load_3d(B, &mm.halo[0], 2 * bx, yt, z, bar);
+    tma_load_3d(B + R * EP_PX * 8, &mm.halo[1], 2 * bx, by, z, bar);
+    tma_load_3d(B + (R + TY) * EP_PX * 8, &mm.halo[0], 2 * bx, yb, z, bar);
+#pragma unroll
+    for (int s = 0; s < 2; ++s) {
+      unsigned char* L = B + CB + s * LB;
+      const int xs = 2 * (s ? xr : xl);
+      tma_load_3d(L, &mm.halo[2], xs, yt, z, bar);
+      tma_load_3d(L + R * 64, &mm.halo[3], xs, by, z, bar);
+      tma_load_3d(L + (R + TY) * 64, &mm.halo[2], xs, yb, z, bar);
+    }
+    tma_load_3d(B + CB + 2 * LB, &mm.halo[1], 2 * bx, by, zq, bar);
+#pragma unroll
+    for (int i = 0; i < NC; ++i) tma_load_3d(B + CB + 2 * LB + QB + i * IB, &mm.cin[i], 2 * bx, by, z, bar);
+#pragma unroll
+    for (int i = 0; i < NR; ++i) tma_load_3d(B + CB + 2 * LB + QB + NC * IB + i * JB, &mm.rin[i], bx, by, z, bar);
+  };
+  if (tid == 0) {
+#pragma unroll
+    for (int b = 0; b < S; ++b) mbar_init(bars + b, 1);
+    mbar_fence_init();
+  }
+  __syncthreads();
+  const float4 zero4 = make_float4(0.f, 0.f, 0.f, 0.f);
+  constexpr int Q = 2 * R + 1;
+  float4 q[Q];
+#pragma unroll
+  for (int k = 0; k < 2 * R; ++k) {
+    int zz = z0 - R + k;
+    if (zz < 0 || zz >= g.nz) zz = per ? wrapi(zz, g.nz) : -1;
+    q[k] = zz >= 0 ? __ldg(reinterpret_cast<const float4*>(psi + (xy + sxy * zz))) : zero4;
+  }
+  if (tid == 0) {
+#pragma unroll
+    for (int b = 0; b < S - 1; ++b)
+      if (z0 + b < z1) issue(z0 + b, b);
+  }
+  int b = 0;
+  uint32_t par = 0;
+  for (int z = z0; z < z1; ++z) {
+    const bool ok = mbar_wait(bars + b, par, EP_MBAR_POLLS);
+    // one barrier per plane: every thread has finished plane z - 1, so its
+    // buffer takes plane z + S - 1
+    if (__syncthreads_or(!ok)) {
+      if (tid == 0) {
+        atomicOr(&sc->flags, (unsigned)EP_FLAG_TIMEOUT);
+        // the copies still in flight, once more each
+        for (int k = 0; k < S - 1 && z + k < z1; ++k) {
+          const int bk = (b + k) % S;
+          mbar_wait(bars + bk, par ^ (bk < b ? 1u : 0u), EP_MBAR_POLLS);
+        }
+      }
+      break;
+    }
+    if (tid == 0 && z + S - 1 < z1) issue(z + S - 1, (b + S - 1) % S);
+    const unsigned char* B = smem + b * BUF;
+    const float4* B4 = reinterpret_cast<const float4*>(B);
+    q[2 * R] = B4[(CB + 2 * LB) / 16 + tid];
+    float2 e[2 * R + 2];
+#pragma unroll
+    for (int i = 0; i <= R; ++i) {
+      const float4 v = B4[xo[i]];
+      e[2 * i] = lo2(v);
+      e[2 * i + 1] = hi2(v);
+    }
+    float4 c, lap;
+    pair_lap<R, 32>(fd, e, B4 + (ty + R) * 32 + tx, q, scale, c, lap);
+    f(xy + sxy * z, c, lap, reinterpret_cast<const float4*>(B + CB + 2 * LB + QB) + tid,
+      reinterpret_cast<const float2*>(B + CB + 2 * LB + QB + NC * IB) + tid);
+#pragma unroll
+    for (int k = 0; k < 2 * R; ++k) q[k] = q[k + 1];
+    if (++b == S) {
+      b = 0;
+      par ^= 1u;
+    }
   }
 }
 
@@ -1340,15 +1523,17 @@ EP_DEV bool last_block(unsigned int* counter) {
 // Predictor + modifier of steppc.f90:53-64.  The new psi is written over
 // psiold(ioldp(3)) (read here point-wise), so the host swaps buffers instead
 // of copying.
-template <class T, int R, bool PAIR>
-__global__ void __launch_bounds__(EP_TX* EP_TY, PAIR ? 2 : (sizeof(T) == 4 ? 4 : 2)) k_predict(Geo g, FdW<T> fd, Phys ph, int zc,
+// PM: 0 one point per thread, 1 two points per thread staged by cp.async,
+// 2 two points per thread staged by TMA boxes.
+template <class T, int R, int PM>
+__global__ void __launch_bounds__(PM == 2 ? EP_TX * EP_TYT : EP_TX * EP_TY, PM == 2 ? 1 : (PM ? 2 : (sizeof(T) == 4 ? 4 : 2))) k_predict(Geo g, FdW<T> fd, Phys ph, int zc,
                                                          const C2<T>* __restrict__ psi, const T* __restrict__ pot4,
                                                          const T* __restrict__ uimp, C2<T>* po3,
                                                          const C2<T>* __restrict__ h1, C2<T>* h2, C2<T>* pc,
                                                          T* __restrict__ den, T f, T c112, DevScalars* sc,
-                                                         Slots sl) {
+                                                         Slots sl, const __grid_constant__ typename MapsOf<PM>::type mm) {
   extern __shared__ __align__(16) unsigned char smraw[];
-  constexpr int NT = EP_TX * EP_TY;
+  constexpr int NT = EP_TX * (PM == 2 ? EP_TYT : EP_TY);
   const HCoef<T> hc(ph);
   // buffer scales folded into the method's coefficients once per thread:
   // pp = s3 po3 + f (2 H - s1 h1 + 2 s2 h2), pn = pp - c112 sp pc
@@ -1369,21 +1554,20 @@ __global__ void __launch_bounds__(EP_TX* EP_TY, PAIR ? 2 : (sizeof(T) == 4 ? 4 :
       pn = pp - kpc * opc;
     }
   };
-  if constexpr (PAIR) {
-    lap_march_pair<R, 4, 2>(
-        g, psi, fd, zc, smraw, cin, rin, bscale_of<T>(sc, sl.psi),
-        [&](long long p, float4 c, float4 lap, const float4* ic, const float2* ir) {
-          float2 Ha, ppa, pna, Hb, ppb, pnb;
-          point(lo2(c), lo2(lap), lo2(ic[0]), lo2(ic[NT]), lo2(ic[2 * NT]), lo2(ic[3 * NT]), ir[0].x, ir[NT].x, Ha,
-                ppa, pna);
-          point(hi2(c), hi2(lap), hi2(ic[0]), hi2(ic[NT]), hi2(ic[2 * NT]), hi2(ic[3 * NT]), ir[0].y, ir[NT].y, Hb,
-                ppb, pnb);
-          *reinterpret_cast<float4*>(po3 + p) = cat2(pna, pnb);
-          *reinterpret_cast<float4*>(pc + p) = cat2(ppa, ppb);
-          *reinterpret_cast<float4*>(h2 + p) = cat2(Ha, Hb);
-          *reinterpret_cast<float2*>(den + p) =
-              make_float2(pna.x * pna.x + pna.y * pna.y, pnb.x * pnb.x + pnb.y * pnb.y);
-        });
+  if constexpr (PM != 0) {
+    auto pairf = [&](long long p, float4 c, float4 lap, const float4* ic, const float2* ir) {
+      float2 Ha, ppa, pna, Hb, ppb, pnb;
+      point(lo2(c), lo2(lap), lo2(ic[0]), lo2(ic[NT]), lo2(ic[2 * NT]), lo2(ic[3 * NT]), ir[0].x, ir[NT].x, Ha, ppa,
+            pna);
+      point(hi2(c), hi2(lap), hi2(ic[0]), hi2(ic[NT]), hi2(ic[2 * NT]), hi2(ic[3 * NT]), ir[0].y, ir[NT].y, Hb, ppb,
+            pnb);
+      *reinterpret_cast<float4*>(po3 + p) = cat2(pna, pnb);
+      *reinterpret_cast<float4*>(pc + p) = cat2(ppa, ppb);
+      *reinterpret_cast<float4*>(h2 + p) = cat2(Ha, Hb);
+      *reinterpret_cast<float2*>(den + p) = make_float2(pna.x * pna.x + pna.y * pna.y, pnb.x * pnb.x + pnb.y * pnb.y);
+    };
+    if constexpr (PM == 2) lap_march_pair_tma<R, 4, 2>(g, psi, fd, zc, smraw, mm, sc, bscale_of<T>(sc, sl.psi), pairf);
+    else lap_march_pair<R, 4, 2>(g, psi, fd, zc, smraw, cin, rin, bscale_of<T>(sc, sl.psi), pairf);
   } else {
     lap_march_async<T, R, 4, 2>(
         g, psi, fd, zc, smraw, cin, rin, bscale_of<T>(sc, sl.psi),
@@ -1413,8 +1597,8 @@ __global__ void __launch_bounds__(EP_TX* EP_TY, PAIR ? 2 : (sizeof(T) == 4 ? 4 :
 // Corrector + final value of steppc.f90:135-151 with fused reductions:
 // sum |pc|, sum |psi|^2 (new), <psi|H|psi> and sum |psi|^2 of the modified
 // psi (chemical potential).
-template <class T, int R, bool STATS, bool PAIR>
-__global__ void __launch_bounds__(EP_TX* EP_TY, PAIR ? 2 : (sizeof(T) == 4 ? 3 : 2)) k_correct(Geo g, FdW<T> fd, Phys ph, int zc,
+template <class T, int R, bool STATS, int PM>
+__global__ void __launch_bounds__(PM == 2 ? EP_TX * EP_TYT : EP_TX * EP_TY, PM == 2 ? 1 : (PM ? 2 : (sizeof(T) == 4 ? 3 : 2))) k_correct(Geo g, FdW<T> fd, Phys ph, int zc,
                                                          const C2<T>* __restrict__ psi, const T* __restrict__ pot4,
                                                          const T* __restrict__ uimp,
                                                          const C2<T>* __restrict__ po3,
@@ -1423,9 +1607,10 @@ __global__ void __launch_bounds__(EP_TX* EP_TY, PAIR ? 2 : (sizeof(T) == 4 ? 3 :
                                                          const C2<T>* __restrict__ h2, C2<T>* pc,
                                                          C2<T>* __restrict__ out, T* __restrict__ den, T f3, T c9,
                                                          double* __restrict__ partials, DevScalars* sc, int renorm,
-                                                         double n4, Slots sl) {
+                                                         double n4, Slots sl,
+                                                         const __grid_constant__ typename MapsOf<PM>::type mm) {
   extern __shared__ __align__(16) unsigned char smraw[];
-  constexpr int NT = EP_TX * EP_TY;
+  constexpr int NT = EP_TX * (PM == 2 ? EP_TYT : EP_TY);
   const HCoef<T> hc(ph);
   Kahan<T> acc[4];
   // buffer scales folded into the method's coefficients once per thread:
@@ -1460,9 +1645,8 @@ __global__ void __launch_bounds__(EP_TX* EP_TY, PAIR ? 2 : (sizeof(T) == 4 ? 3 :
     }
     return dn;
   };
-  if constexpr (PAIR) {
-    lap_march_pair<R, 5, 2>(g, psi, fd, zc, smraw, cin, rin, bscale_of<T>(sc, sl.psi),
-                            [&](long long p, float4 c, float4 lap, const float4* ic, const float2* ir) {
+  if constexpr (PM != 0) {
+    auto pairf = [&](long long p, float4 c, float4 lap, const float4* ic, const float2* ir) {
       float2 pca, poa, pcb, pob;
       const float da = point(lo2(c), lo2(lap), lo2(ic[0]), lo2(ic[NT]), lo2(ic[2 * NT]), lo2(ic[3 * NT]),
                              lo2(ic[4 * NT]), ir[0].x, ir[NT].x, pca, poa);
@@ -1471,7 +1655,9 @@ __global__ void __launch_bounds__(EP_TX* EP_TY, PAIR ? 2 : (sizeof(T) == 4 ? 3 :
       *reinterpret_cast<float4*>(pc + p) = cat2(pca, pcb);
       *reinterpret_cast<float4*>(out + p) = cat2(poa, pob);
       *reinterpret_cast<float2*>(den + p) = make_float2(da, db);
-    });
+    };
+    if constexpr (PM == 2) lap_march_pair_tma<R, 5, 2>(g, psi, fd, zc, smraw, mm, sc, bscale_of<T>(sc, sl.psi), pairf);
+    else lap_march_pair<R, 5, 2>(g, psi, fd, zc, smraw, cin, rin, bscale_of<T>(sc, sl.psi), pairf);
   } else {
     lap_march_async<T, R, 5, 2>(g, psi, fd, zc, smraw, cin, rin, bscale_of<T>(sc, sl.psi),
                                 [&](long long p, C2<T> c, C2<T> lap, const C2<T>* ic, const T* ir) {

@@ -2,14 +2,18 @@
 
 The FP32 engine marches the predictor and the corrector (steppc.f90:53-64,
 135-151) with two x-neighbouring points per thread whenever the stencil radius
-and nx are even; EP_MARCH_PAIRS=0 at context creation keeps the one-point
-form.  Each point's Laplacian and update are summed in the same order in both
-forms, so the fields they write must agree bit for bit; only the order in
-which the block reductions meet differs (the norm, errHe and mu agree to the
-FP32 reductions' compensated accuracy).  The cases cover both boundary modes,
-tiles that the grid fills only partly (nx = 30, 96), the 5- and 9-point
-stencils, real time with a
-moving impurity, and the benchmark grid.
+and nx are even, staging its planes and inputs with TMA boxes when the grid
+is made of whole 64 x 16 tiles and with per-thread cp.async copies otherwise;
+EP_MARCH_TMA=0 at context creation keeps the cp.async staging,
+EP_MARCH_PAIRS=0 the one-point form.  Each point's Laplacian and update are
+summed in the same order in every form, so the fields they write must agree
+bit for bit; only the order in which the block reductions meet differs (the
+norm, errHe and mu agree to the FP32 reductions' compensated accuracy).  The
+runs do not renormalise, so no reduction feeds back into the fields.  The
+cases cover both boundary modes, tiles that the grid fills only partly
+(nx = 30, 96: cp.async staging), the 5- and 9-point stencils, real time with
+a moving impurity, the benchmark grid, and grids whose tiles all touch the
+periodic wrap (nx = 64, ny = 16) for the TMA boxes.
 """
 import os
 
@@ -30,7 +34,13 @@ CASES = {
     "64x24x32_periodic_5pt": dict(dims=(64, 24, 32), h=0.8, n4=200.0, icon=_abi.EP_ICON_PERIODIC, npd=5),
     "64cubed_realtime_moving": dict(dims=(64, 64, 64), h=0.6, n4=500.0, icon=_abi.EP_ICON_PERIODIC, npd=13,
                                     real_time=True),
+    "64x16x24_periodic": dict(dims=(64, 16, 24), h=0.8, n4=100.0, icon=_abi.EP_ICON_PERIODIC, npd=13),
+    "64x16x24_zero_outside": dict(dims=(64, 16, 24), h=0.8, n4=100.0, icon=_abi.EP_ICON_ZERO_OUTSIDE, npd=13),
+    "192x32x24_zero_outside_9pt": dict(dims=(192, 32, 24), h=0.6, n4=300.0, icon=_abi.EP_ICON_ZERO_OUTSIDE,
+                                       npd=9),
+    "128x16x20_periodic_5pt": dict(dims=(128, 16, 20), h=0.8, n4=100.0, icon=_abi.EP_ICON_PERIODIC, npd=5),
 }
+FORMS = {"tma": {}, "pairs": {"EP_MARCH_TMA": "0"}, "one": {"EP_MARCH_PAIRS": "0"}}
 
 
 @pytest.fixture(scope="module", autouse=True)
@@ -39,7 +49,7 @@ def _lib():
     ep.load_library()
 
 
-def run(case, pairs):
+def run(case, form):
     nx, ny, nz = case["dims"]
     h = case["h"]
     rt = case.get("real_time", False)
@@ -51,15 +61,16 @@ def run(case, pairs):
         kw.update(mimpur=40.0, fix_lambda=1)
     cfg = ep.make_config(**kw)
     psi = ep.woods_saxon_psi(nx, ny, nz, cfg.xmax, cfg.ymax, cfg.zmax, case["n4"], seed=7)
-    old = os.environ.get("EP_MARCH_PAIRS")
-    os.environ["EP_MARCH_PAIRS"] = "1" if pairs else "0"
+    keys = ("EP_MARCH_PAIRS", "EP_MARCH_TMA")
+    old = {k: os.environ.pop(k, None) for k in keys}
+    os.environ.update(FORMS[form])
     try:
         s = ep.Solver(cfg)
     finally:
-        if old is None:
-            del os.environ["EP_MARCH_PAIRS"]
-        else:
-            os.environ["EP_MARCH_PAIRS"] = old
+        for k in keys:
+            os.environ.pop(k, None)
+            if old[k] is not None:
+                os.environ[k] = old[k]
     with s:
         pot = ep.morse(10.0, 4.5, 1.2, r_cutoff=0.0, umax=1000.0)
         s.set_impurity_potentials(pot, pot, pot)
@@ -76,12 +87,13 @@ def run(case, pairs):
     return out
 
 
+@pytest.mark.parametrize("form", ["tma", "pairs"])
 @pytest.mark.parametrize("name", list(CASES))
-def test_pair_march_gives_the_one_point_bits(name):
-    a = run(CASES[name], pairs=True)
-    b = run(CASES[name], pairs=False)
+def test_pair_march_gives_the_one_point_bits(name, form):
+    a = run(CASES[name], form)
+    b = run(CASES[name], "one")
     for k in ("psi", "den", "pc", "psiold1", "psiold2", "psiold3", "hpsiold1", "hpsiold2"):
-        assert np.array_equal(a[k], b[k]), (name, k, float(np.max(np.abs(a[k] - b[k]))))
+        assert np.array_equal(a[k], b[k]), (name, form, k, float(np.max(np.abs(a[k] - b[k]))))
     for k in ("norm", "mu", "errHe"):
         ref = b["stats"][k]
-        assert abs(a["stats"][k] - ref) <= 1e-6 * max(1.0, abs(ref)), (name, k, a["stats"][k], ref)
+        assert abs(a["stats"][k] - ref) <= 1e-6 * max(1.0, abs(ref)), (name, form, k, a["stats"][k], ref)
