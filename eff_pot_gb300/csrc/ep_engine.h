@@ -89,6 +89,7 @@ class Engine {
     CUtensorMap m[4];
   };
   std::vector<BufMaps> cmaps;
+  bool tma_timeout_test = false;  // EP_TEST_TMA_TIMEOUT=1: every TMA wait runs out
   CUtensorMap rmaps[2];
   int build_march_maps();
   const CUtensorMap* maps_of(const void* buf) const;

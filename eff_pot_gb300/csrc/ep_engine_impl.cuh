@@ -1514,6 +1514,10 @@ bool Engine<T>::march_maps(MarchMaps& mm, const CT* marched, const CT* const* ci
   }
   mm.rin[0] = rmaps[0];
   mm.rin[1] = rmaps[1];
+  // the failure-detection test: bytes announced that no copy delivers, and a
+  // short wait limit
+  mm.polls = tma_timeout_test ? 4096u : EP_MBAR_POLLS;
+  mm.no_copies = tma_timeout_test ? 1u : 0u;
   return true;
 }
 
@@ -1541,6 +1545,8 @@ int Engine<T>::march_setup() {
     // staging
     const char* ev = getenv("EP_MARCH_PAIRS");
     const char* et = getenv("EP_MARCH_TMA");
+    const char* ex = getenv("EP_TEST_TMA_TIMEOUT");
+    tma_timeout_test = ex && ex[0] == '1';
     bool can = g.nx % 2 == 0 && !(ev && ev[0] == '0');
     switch (fd.R) {
       case 2: can = can && pair_built<T>(2); break;

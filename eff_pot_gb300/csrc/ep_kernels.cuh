@@ -1202,10 +1202,15 @@ EP_DEV void lap_march_pair(const Geo& g, const float2* __restrict__ psi, const F
 // {128 x EP_TYT}, {16 x R} and {16 x EP_TYT} (floats x rows), a
 // {128 x EP_TYT} box of each complex input and a {64 x EP_TYT} box of each
 // real input.
+// polls: the limit of each bounded mbarrier wait; no_copies: announce each
+// plane's bytes but issue no copy (0; a failure-detection test sets it, so
+// every wait runs out with nothing in flight).
 struct MarchMaps {
   CUtensorMap halo[4];
   CUtensorMap cin[5];
   CUtensorMap rin[2];
+  unsigned polls;
+  unsigned no_copies;
 };
 
 // Kernel parameter of the predictor / corrector: the TMA form (PM = 2) takes
@@ -1291,6 +1296,7 @@ EP_DEV void lap_march_pair_tma(const Geo& g, const float2* __restrict__ psi, con
     uint64_t* bar = bars + b;
     fence_proxy_async();
     mbar_expect_tx(bar, (uint32_t)BUF);
+    if (mm.no_copies) return;
     const int zq = per ? wrapi(z + R, g.nz) : z + R;  // beyond a zero-boundary box: zeros
     tma_load_3d(B, &mm.halo[0], 2 * bx, yt, z, bar);
     tma_load_3d(B + R * EP_PX * 8, &mm.halo[1], 2 * bx, by, z, bar);
@@ -1332,7 +1338,7 @@ EP_DEV void lap_march_pair_tma(const Geo& g, const float2* __restrict__ psi, con
   int b = 0;
   uint32_t par = 0;
   for (int z = z0; z < z1; ++z) {
-    const bool ok = mbar_wait(bars + b, par, EP_MBAR_POLLS);
+    const bool ok = mbar_wait(bars + b, par, mm.polls);
     // one barrier per plane: every thread has finished plane z - 1, so its
     // buffer takes plane z + S - 1
     if (__syncthreads_or(!ok)) {
@@ -1341,7 +1347,7 @@ EP_DEV void lap_march_pair_tma(const Geo& g, const float2* __restrict__ psi, con
         // the copies still in flight, once more each
         for (int k = 0; k < S - 1 && z + k < z1; ++k) {
           const int bk = (b + k) % S;
-          mbar_wait(bars + bk, par ^ (bk < b ? 1u : 0u), EP_MBAR_POLLS);
+          mbar_wait(bars + bk, par ^ (bk < b ? 1u : 0u), mm.polls);
         }
       }
       break;

@@ -97,3 +97,37 @@ def test_pair_march_gives_the_one_point_bits(name, form):
     for k in ("norm", "mu", "errHe"):
         ref = b["stats"][k]
         assert abs(a["stats"][k] - ref) <= 1e-6 * max(1.0, abs(ref)), (name, form, k, a["stats"][k], ref)
+
+
+def test_tma_wait_that_runs_out_reports_timeout():
+    """Failure detection of the TMA march: with EP_TEST_TMA_TIMEOUT=1 the
+    predictor and corrector announce each plane's bytes on the mbarrier but
+    issue no copy, so every bounded wait runs out (4096 polls); the blocks
+    end their march, raise EP_FLAG_TIMEOUT, and ep_run returns
+    EP_ERR_TIMEOUT.  Nothing is in flight and the context stays usable; a
+    context made afterwards without the switch runs normally."""
+    case = CASES["64x16x24_periodic"]
+    nx, ny, nz = case["dims"]
+    h = case["h"]
+    cfg = ep.make_config(nx=nx, ny=ny, nz=nz, xmax=nx * h / 2, ymax=ny * h / 2, zmax=nz * h / 2,
+                         icon=case["icon"], core="OTC", n4=case["n4"], precision=_abi.EP_FP32,
+                         impurity=_abi.EP_IMPURITY_NONE, renormalize=0)
+    psi = ep.woods_saxon_psi(nx, ny, nz, cfg.xmax, cfg.ymax, cfg.zmax, case["n4"], seed=7)
+    old = os.environ.pop("EP_TEST_TMA_TIMEOUT", None)
+    os.environ["EP_TEST_TMA_TIMEOUT"] = "1"
+    try:
+        s = ep.Solver(cfg)
+    finally:
+        os.environ.pop("EP_TEST_TMA_TIMEOUT", None)
+        if old is not None:
+            os.environ["EP_TEST_TMA_TIMEOUT"] = old
+    with s:
+        s.start(psi)
+        for _ in range(3):
+            s.steprk(1e-4)
+        with pytest.raises(ep.EffPotError) as ei:
+            s.run(2, 1e-4)
+        assert ei.value.status == _abi.EP_ERR_TIMEOUT, ei.value
+        s.synchronize()
+    out = run(case, "tma")
+    assert np.all(np.isfinite(out["psi"]))
