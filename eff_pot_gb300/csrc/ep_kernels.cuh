@@ -118,13 +118,6 @@ EP_DEV T d1_global(const T* __restrict__ f, long long p, int i, int n, long long
 template <class T>
 EP_DEV T d1_line(const T* __restrict__ line, int i, int n, const T* w, int R, int periodic) {
   T s = T(0);
-  if (R == 6 && i >= 6 && i < n - 6) {
-    // the 13-point stencil away from the line's ends: no wrap, unrolled (the
-    // same sum in the same order)
-#pragma unroll
-    for (int k = 1; k <= 6; ++k) s += w[k] * (line[i + k] - line[i - k]);
-    return s;
-  }
   for (int k = 1; k <= R; ++k) {
     int ip = i + k, im = i - k;
     T fp, fm;
