@@ -327,10 +327,10 @@ int Engine<T>::rfft_z(const ConvSpec<T>& cs, int nin, const LineSet& ls) {
   for (int i = 0; i < nin; ++i) one = one && cs.nout[i] == 1;
   if (one) {
     auto k = k_zconv_r<T, N, true>;
-    EP_LAUNCH("fft_z_conv", k, grid, blk, (rfft::smem_bytes<T, N>()), cs, ls, twz);
+    EP_LAUNCH("fft_z_conv", k, grid, blk, (rfft::conv_smem_bytes<T, N, true>()), cs, ls, twz);
   } else {
     auto k = k_zconv_r<T, N, false>;
-    EP_LAUNCH("fft_z_conv", k, grid, blk, (rfft::smem_bytes<T, N>()), cs, ls, twz);
+    EP_LAUNCH("fft_z_conv", k, grid, blk, (rfft::conv_smem_bytes<T, N, false>()), cs, ls, twz);
   }
   return EP_OK;
 }
@@ -1436,8 +1436,8 @@ int Engine<T>::fft_attrs() {
 #define EP_RFFT_ATTR(NN)                                                                                  \
   cudaFuncSetAttribute(k_c2c_r<T, NN, -1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)rfft::smem_bytes<T, NN>()); \
   cudaFuncSetAttribute(k_c2c_r<T, NN, +1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)rfft::smem_bytes<T, NN>()); \
-  cudaFuncSetAttribute(k_zconv_r<T, NN, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)rfft::smem_bytes<T, NN>()); \
-  cudaFuncSetAttribute(k_zconv_r<T, NN, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)rfft::smem_bytes<T, NN>());
+  cudaFuncSetAttribute(k_zconv_r<T, NN, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)rfft::conv_smem_bytes<T, NN, true>()); \
+  cudaFuncSetAttribute(k_zconv_r<T, NN, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)rfft::conv_smem_bytes<T, NN, false>());
   EP_RFFT_ATTR(32) EP_RFFT_ATTR(64) EP_RFFT_ATTR(128) EP_RFFT_ATTR(256)
   if constexpr (sizeof(T) == 4) { EP_RFFT_ATTR(96) EP_RFFT_ATTR(192) }
 #undef EP_RFFT_ATTR

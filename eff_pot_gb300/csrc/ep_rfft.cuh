@@ -75,6 +75,18 @@ template <class T, int N>
 constexpr size_t smem_bytes() {
   return (size_t)(32 * (N + 1) + N) * sizeof(C2<T>);
 }
+// The FP32 convolution pass up to 128-point lines stages each thread's
+// form-factor values of its line (one table, or up to three) in shared
+// memory while the forward transform runs; longer lines and wider types read
+// them after the transform (the staging would cost resident CTAs).
+template <class T, int N>
+__host__ __device__ constexpr bool conv_stage() {
+  return sizeof(T) == 4 && N <= 128;
+}
+template <class T, int N, bool ONE>
+constexpr size_t conv_smem_bytes() {
+  return smem_bytes<T, N>() + (conv_stage<T, N>() ? (size_t)(ONE ? 1 : 3) * 32 * N * sizeof(T) : 0);
+}
 
 
 // Line base address of line L of a LineSet-like description.
@@ -138,6 +150,28 @@ __global__ void __launch_bounds__(32 * rfft::Shape<N>::P, (ONE ? Occ<T, N>::conv
   const long long b = (valid ? rfft::line_base(L, ls.Mi, ls.So) : 0) + (long long)t * ls.Sa;
   const int stp = P * (int)ls.Sa;
   C2<T>* Srow = S + lane * (N + 1);
+  // the thread's form-factor values, copied in while the forward transform
+  // runs (each thread reads back only its own copies)
+  constexpr bool STAGE = rfft::conv_stage<T, N>();
+  constexpr int NT = 32 * P;
+  T* kb = reinterpret_cast<T*>(tw + N);
+  const int tid = t * 32 + lane;
+  auto kval = [&](int j, int m) -> T {
+    if (!valid) return T(0);
+    if constexpr (STAGE) return kb[(j * E + m) * NT + tid];
+    return cs.ker[which][j][b + (long long)m * stp];
+  };
+  if constexpr (STAGE) {
+    const int ntab = ONE ? 1 : cs.nout[which];
+    if (valid) {
+      for (int j = 0; j < ntab; ++j) {
+        const T* ker = cs.ker[which][j] + b;
+#pragma unroll
+        for (int m = 0; m < E; ++m) cp_async<sizeof(T)>(kb + (j * E + m) * NT + tid, ker + m * stp);
+      }
+    }
+    cp_commit();
+  }
   C2<T> v[E];
   {
     const C2<T>* in = cs.in[which] + b;
@@ -146,12 +180,12 @@ __global__ void __launch_bounds__(32 * rfft::Shape<N>::P, (ONE ? Occ<T, N>::conv
   }
   __syncthreads();  // tw complete
   rfft::lines<T, N, -1>(v, Srow, tw, t);
+  if constexpr (STAGE) cp_wait<0>();
   if (ONE) {
     // a single kernel table: the product overwrites the spectrum
-    const T* ker = cs.ker[which][0] + b;
 #pragma unroll
     for (int m = 0; m < E; ++m) {
-      const T kv = valid ? ker[m * stp] : T(0);
+      const T kv = kval(0, m);
       v[m] = cmk<T>(v[m].x * kv, v[m].y * kv);
     }
     rfft::lines<T, N, +1>(v, Srow, tw, t);
@@ -164,11 +198,10 @@ __global__ void __launch_bounds__(32 * rfft::Shape<N>::P, (ONE ? Occ<T, N>::conv
   }
   const int nout = cs.nout[which];
   for (int j = 0; j < nout; ++j) {
-    const T* ker = cs.ker[which][j] + b;
     C2<T> u[E];
 #pragma unroll
     for (int m = 0; m < E; ++m) {
-      const T kv = valid ? ker[m * stp] : T(0);
+      const T kv = kval(j, m);
       u[m] = cmk<T>(v[m].x * kv, v[m].y * kv);
     }
     rfft::lines<T, N, +1>(u, Srow, tw, t);
