@@ -75,13 +75,13 @@ template <class T, int N>
 constexpr size_t smem_bytes() {
   return (size_t)(32 * (N + 1) + N) * sizeof(C2<T>);
 }
-// The FP32 convolution pass up to 128-point lines stages each thread's
+// The convolution pass up to 128-point lines stages each thread's
 // form-factor values of its line (one table, or up to three) in shared
-// memory while the forward transform runs; longer lines and wider types read
-// them after the transform (the staging would cost resident CTAs).
+// memory while the forward transform runs; longer lines read them after the
+// transform (the staging would cost resident CTAs, or not fit).
 template <class T, int N>
 __host__ __device__ constexpr bool conv_stage() {
-  return sizeof(T) == 4 && N <= 128;
+  return N <= 128;
 }
 template <class T, int N, bool ONE>
 constexpr size_t conv_smem_bytes() {
