@@ -187,6 +187,49 @@ __device__ __forceinline__ dfloat2 cmulc(dfloat2 a, dfloat2 b) {
   dd_scale2(a.y, make_float2(b.y.hi, b.x.hi), make_float2(b.y.lo, b.x.lo), up, ue);
   return dd_add2(tp, te, up, ue);
 }
+// Stencil sums w_k (x_k + y_k) of complex double-float values as unnormalised
+// accumulators (Ogita, Rump and Oishi's Sum2 with the FMA product error): the
+// running sum is h + l with the error terms gathered in l by plain FP32 pair
+// additions and one Fast2Sum at the end, about 20 paired operations a term
+// against 27 for a normalised double-float product and sum.
+struct dd2_acc {
+  float2 h, l;
+};
+__device__ __forceinline__ void two_sum2(float2 a, float2 b, float2& s, float2& e) {
+  const float2 m1 = make_float2(-1.0f, -1.0f);
+  s = __fadd2_rn(a, b);
+  const float2 bb = __ffma2_rn(a, m1, s);                                            // s - a
+  e = __fadd2_rn(__ffma2_rn(__ffma2_rn(bb, m1, s), m1, a), __ffma2_rn(bb, m1, b));  // (a - (s - bb)) + (b - bb)
+}
+// w (x + y), unnormalised: the pair sum by TwoSum of the high parts, the
+// product's error by FMA
+__device__ __forceinline__ void dd2_wsum(dfloat w, dfloat2 x, dfloat2 y, float2& ph, float2& pl) {
+  float2 sh, se;
+  two_sum2(make_float2(x.x.hi, x.y.hi), make_float2(y.x.hi, y.y.hi), sh, se);
+  const float2 sl = __fadd2_rn(se, __fadd2_rn(make_float2(x.x.lo, x.y.lo), make_float2(y.x.lo, y.y.lo)));
+  const float2 wh = make_float2(w.hi, w.hi), wl = make_float2(w.lo, w.lo);
+  ph = __fmul2_rn(wh, sh);
+  pl = __ffma2_rn(wh, sl, __ffma2_rn(wl, sh, __ffma2_rn(wh, sh, dd_neg2(ph))));
+}
+// w c, unnormalised
+__device__ __forceinline__ dd2_acc dd2_start(dfloat w, dfloat2 c) {
+  const float2 wh = make_float2(w.hi, w.hi), wl = make_float2(w.lo, w.lo), ch = make_float2(c.x.hi, c.y.hi);
+  dd2_acc a;
+  a.h = __fmul2_rn(wh, ch);
+  a.l = __ffma2_rn(wh, make_float2(c.x.lo, c.y.lo), __ffma2_rn(wl, ch, __ffma2_rn(wh, ch, dd_neg2(a.h))));
+  return a;
+}
+__device__ __forceinline__ void dd2_add(dd2_acc& a, float2 ph, float2 pl) {
+  float2 s, e;
+  two_sum2(a.h, ph, s, e);
+  a.h = s;
+  a.l = __fadd2_rn(a.l, __fadd2_rn(e, pl));
+}
+__device__ __forceinline__ dfloat2 dd2_value(const dd2_acc& a) {
+  const float2 m1 = make_float2(-1.0f, -1.0f);
+  const float2 h = __fadd2_rn(a.h, a.l);
+  return dd_pack(h, __ffma2_rn(__ffma2_rn(a.h, m1, h), m1, a.l));  // l - (h - a.h)
+}
 #else
 inline dfloat2 operator+(dfloat2 a, dfloat2 b) { return dfloat2{a.x + b.x, a.y + b.y}; }
 inline dfloat2 operator-(dfloat2 a, dfloat2 b) { return dfloat2{a.x - b.x, a.y - b.y}; }

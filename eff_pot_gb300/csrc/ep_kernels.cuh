@@ -1046,15 +1046,38 @@ EP_DEV void lap_march_async(const Geo& g, const C2<T>* __restrict__ psi, const F
       q[2 * R] = sq[buf * NT + tid];
       const CT* row = sp + buf * PL + (ty + R) * W + (tx + R);
       const CT c = q[R];
-      CT lx = vmul(fd.w2[0][0], c), ly = vmul(fd.w2[1][0], c), lz = vmul(fd.w2[2][0], c);
+      CT lap;
+      if constexpr (std::is_same<T, dfloat>::value) {
+#if defined(__CUDA_ARCH__)
+        // unnormalised double-float accumulation, one sum per direction
+        dd2_acc ax = dd2_start(fd.w2[0][0], c), ay = dd2_start(fd.w2[1][0], c), az = dd2_start(fd.w2[2][0], c);
+        float2 ph, pl;
 #pragma unroll
-      for (int k = 1; k <= R; ++k) {
-        lx = vfma(fd.w2[0][k], vadd(row[-k], row[k]), lx);
-        ly = vfma(fd.w2[1][k], vadd(row[-k * W], row[k * W]), ly);
-        lz = vfma(fd.w2[2][k], vadd(q[R - k], q[R + k]), lz);
+        for (int k = 1; k <= R; ++k) {
+          dd2_wsum(fd.w2[0][k], row[-k], row[k], ph, pl);
+          dd2_add(ax, ph, pl);
+          dd2_wsum(fd.w2[1][k], row[-k * W], row[k * W], ph, pl);
+          dd2_add(ay, ph, pl);
+          dd2_wsum(fd.w2[2][k], q[R - k], q[R + k], ph, pl);
+          dd2_add(az, ph, pl);
+        }
+        dd2_add(ax, ay.h, ay.l);
+        dd2_add(ax, az.h, az.l);
+        lap = dd2_value(ax);
+#else
+        lap = c;  // the host pass compiles no kernel body
+#endif
+      } else {
+        CT lx = vmul(fd.w2[0][0], c), ly = vmul(fd.w2[1][0], c), lz = vmul(fd.w2[2][0], c);
+#pragma unroll
+        for (int k = 1; k <= R; ++k) {
+          lx = vfma(fd.w2[0][k], vadd(row[-k], row[k]), lx);
+          ly = vfma(fd.w2[1][k], vadd(row[-k * W], row[k * W]), ly);
+          lz = vfma(fd.w2[2][k], vadd(q[R - k], q[R + k]), lz);
+        }
+        lap = vadd(vadd(lx, ly), lz);
       }
-      f(xy + sxy * z, vmul(scale, c), vmul(scale, vadd(vadd(lx, ly), lz)), sc_ + buf * NC * NT + tid,
-        sr + buf * NR * NT + tid);
+      f(xy + sxy * z, vmul(scale, c), vmul(scale, lap), sc_ + buf * NC * NT + tid, sr + buf * NR * NT + tid);
     }
 #pragma unroll
     for (int k = 0; k < 2 * R; ++k) q[k] = q[k + 1];
