@@ -211,6 +211,10 @@ __device__ __forceinline__ void dd2_wsum(dfloat w, dfloat2 x, dfloat2 y, float2&
   ph = __fmul2_rn(wh, sh);
   pl = __ffma2_rn(wh, sl, __ffma2_rn(wl, sh, __ffma2_rn(wh, sh, dd_neg2(ph))));
 }
+// w (x - y), unnormalised
+__device__ __forceinline__ void dd2_wdiff(dfloat w, dfloat2 x, dfloat2 y, float2& ph, float2& pl) {
+  dd2_wsum(w, x, dfloat2{dfloat(-y.x.hi, -y.x.lo), dfloat(-y.y.hi, -y.y.lo)}, ph, pl);
+}
 // w c, unnormalised
 __device__ __forceinline__ dd2_acc dd2_start(dfloat w, dfloat2 c) {
   const float2 wh = make_float2(w.hi, w.hi), wl = make_float2(w.lo, w.lo), ch = make_float2(c.x.hi, c.y.hi);

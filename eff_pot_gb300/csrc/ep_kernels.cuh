@@ -1498,10 +1498,29 @@ __global__ void __launch_bounds__(EP_TX* EP_TY) k_d1march(Geo g, const __grid_co
       const PT* rowp = reinterpret_cast<const PT*>(rowe);
       const long long p = pxy + sxy * z;
       PT dy = cmk<T>(T(0), T(0)), dz = cmk<T>(T(0), T(0));
+      if constexpr (std::is_same<T, dfloat>::value) {
+#if defined(__CUDA_ARCH__)
+        // unnormalised double-float accumulation of the pair's y and z sums
+        dd2_acc ay, az;
+        dd2_wdiff(fd.w1[1][1], rowp[WP], rowp[-WP], ay.h, ay.l);
+        dd2_wdiff(fd.w1[2][1], q[R + 1], q[R - 1], az.h, az.l);
+        float2 ph, pl;
 #pragma unroll
-      for (int k = 1; k <= R; ++k) dy = vfma(fd.w1[1][k], vsub(rowp[k * WP], rowp[-k * WP]), dy);
+        for (int k = 2; k <= R; ++k) {
+          dd2_wdiff(fd.w1[1][k], rowp[k * WP], rowp[-k * WP], ph, pl);
+          dd2_add(ay, ph, pl);
+          dd2_wdiff(fd.w1[2][k], q[R + k], q[R - k], ph, pl);
+          dd2_add(az, ph, pl);
+        }
+        dy = dd2_value(ay);
+        dz = dd2_value(az);
+#endif
+      } else {
 #pragma unroll
-      for (int k = 1; k <= R; ++k) dz = vfma(fd.w1[2][k], vsub(q[R + k], q[R - k]), dz);
+        for (int k = 1; k <= R; ++k) dy = vfma(fd.w1[1][k], vsub(rowp[k * WP], rowp[-k * WP]), dy);
+#pragma unroll
+        for (int k = 1; k <= R; ++k) dz = vfma(fd.w1[2][k], vsub(q[R + k], q[R - k]), dz);
+      }
       if (MODE == 0) {
         // elements x + JLO*2 .. x + 2*JHI + 1 of the row, as pairs
         T e[NE];
